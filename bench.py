@@ -1,0 +1,299 @@
+"""Benchmark of the phase-space step (slope -> flux incl. IB wall -> Shakhov collision).
+
+Workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x64 trees,
+3 levels near the wall, 48^2 velocity roots on [-15,15]^2 adapted by 2 levels), seeded
+synthetic initial state; 61 M phase cells, so f is far larger than L2 between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+Metric: phase-cell updates/s of the mixed-precision form (FP32 f, compensated moments,
+FP64 conserved update), with the plain FP64 form, the roofline of the dominant kernel, the
+oracle CPU baseline and the end-to-end rate through the C-ABI with host buffers beside it.
+N > 1: independent replicas, one per GPU (the path has no exchange on one device).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "kitamr.jl_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+WORKLOAD = "cylinder_ma5_kn0.1_64x64_L3_v48x48_vsL2"
+METRIC = "phase-cell updates/s"
+UNIT = "updates/s"
+
+
+def make_problem(scale=1.0):
+    from kitgpu import cases
+    return cases.cylinder(scale=scale, nv=48, vs_levels=2)
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """dram bytes per flux_collide launch from the committed ncu summary (scaled to the
+    full workload there), or None."""
+    p = os.path.join(ROOT, "profiles", "flux_collide_kernel_cylinder.txt")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", open(p).read())
+    return float(m.group(1)) if m else None
+
+
+def pinned_empty(n, torch):
+    return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
+
+
+def run_ours(args, rank, world, dist):
+    import torch
+    from kitgpu import abi, mesh
+    from kitgpu.solver import GpuStep
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    from kitgpu import cases
+    prob = make_problem()
+    topo, state = cases.build(prob)
+    P = mesh.phase_cells(topo)
+    dt = prob.dt()
+    res = {}
+    launches_total = 0
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
+        prm = abi.make_params(prob, precision=prec, st_check_interval=100)
+        g = GpuStep(prm, topo, device=dev)
+        g.upload_state(state["f"], state["w"], state["prim"])
+        step = 0
+        for _ in range(args.warmup):
+            g.step(dt, step, 1)
+            step += 1
+        sampler = ClockSampler(dev) if form == "mixed" else None
+        barrier()
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        rep = g.step(dt, step, args.steps)
+        barrier()
+        clocks = sampler.stop() if sampler else None
+        step += args.steps
+        ms = rep.device_ms
+        if dist is not None:
+            t = torch.tensor([ms], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        res[form] = dict(ms_per_step=ms / args.steps, value=P * world * args.steps / (ms / 1e3),
+                         launches=rep.kernel_launches)
+        if form == "mixed":
+            launches_total = rep.kernel_launches
+            res[form]["clocks"] = clocks
+            # per-kernel device times (CUDA events on the handle's stream), separate pass
+            g.profile(True)
+            g.step(dt, step, 3)
+            step += 3
+            res[form]["kernels"] = g.profile_read()
+            g.profile(False)
+            # end to end through the C-ABI with pinned host buffers: every step uploads f, w,
+            # prim and downloads f, w, prim, qf
+            f_h = pinned_empty(state["f"].size, torch)
+            f_h[:] = state["f"]
+            w_h = pinned_empty(state["w"].size, torch); w_h[:] = state["w"]
+            p_h = pinned_empty(state["prim"].size, torch); p_h[:] = state["prim"]
+            q_h = pinned_empty(topo["n_cells"] * topo["dim"], torch)
+            import ctypes as C
+            e2e_steps = max(1, min(args.steps, 10))
+            barrier()
+            t0 = time.perf_counter()
+            for s in range(e2e_steps):
+                g.L.kg_upload_state(g.h, f_h.ctypes.data, w_h.ctypes.data, p_h.ctypes.data)
+                r = abi.KgStepReport()
+                g.L.kg_step(g.h, dt, step + s, 1, C.byref(r))
+                g.L.kg_download_state(g.h, f_h.ctypes.data, w_h.ctypes.data, p_h.ctypes.data, q_h.ctypes.data, None)
+            barrier()
+            el = time.perf_counter() - t0
+            if dist is not None:
+                t = torch.tensor([el], dtype=torch.float64)
+                dist.all_reduce(t, op=dist.ReduceOp.MAX)
+                el = float(t.item())
+            h2d = f_h.nbytes + w_h.nbytes + p_h.nbytes
+            d2h = f_h.nbytes + w_h.nbytes + p_h.nbytes + q_h.nbytes
+            res[form]["e2e"] = {"value": P * world * e2e_steps / el, "unit": UNIT,
+                                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+        g.close()
+    return P, res, launches_total
+
+
+def cpu_baseline(threads, budget_s=12.0):
+    import oracle as O
+    from kitgpu import abi, cases, mesh
+    prob = make_problem(scale=0.25)
+    topo, state = cases.build(prob)
+    P = mesh.phase_cells(topo)
+    st = O.OracleState(topo, state)
+    prm = abi.make_params(prob, st_check_interval=100)
+    st.run(prm, prob.dt(), 0, 1, nthreads=threads)  # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        st.run(prm, prob.dt(), 1 + n, 1, nthreads=threads)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > budget_s or n >= 40:
+            break
+    return {"value": P * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"cylinder at scale 0.25 (16x16 trees, same velocity grids), {P} phase cells, {n} steps, FP64"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+        dist_mod.init_process_group("gloo")
+        dist = dist_mod
+    threads = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        # The reference is Julia and cannot run on this machine; its CPU path is the oracle port.
+        if rank != 0:
+            return
+        import oracle as O
+        from kitgpu import abi, cases, mesh
+        prob = make_problem(scale=0.25)
+        topo, state = cases.build(prob)
+        P = mesh.phase_cells(topo)
+        st = O.OracleState(topo, state)
+        prm = abi.make_params(prob, st_check_interval=100)
+        for s in range(args.warmup):
+            st.run(prm, prob.dt(), s, 1, nthreads=threads)
+        t0 = time.perf_counter()
+        st.run(prm, prob.dt(), args.warmup, args.steps, nthreads=threads)
+        el = time.perf_counter() - t0
+        v = P * args.steps / el
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": {"workload": WORKLOAD + " (bounded CPU sample: scale 0.25)",
+                                                "parallelism": "host threads"},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                 "sample": f"cylinder at scale 0.25, {P} phase cells per step, FP64 oracle"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    P, res, launches = run_ours(args, rank, world, dist)
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    mixed = res["mixed"]
+    kern = mixed.get("kernels", {})
+    roof = None
+    if "flux_collide_kernel" in kern:
+        ms, cnt = kern["flux_collide_kernel"]
+        avg_s = ms / cnt / 1e3
+        b_alg = 2 * 2 * 4 * P          # 2 * NDF * sizeof(float) per phase cell (one read, one write of f)
+        ach = b_alg / avg_s / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "traffic": ncu_traffic_per_launch(), "kernel": "flux_collide_kernel",
+                "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg}
+    line = {
+        "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32-f/f64-moments",
+        "data": "synthetic (seeded cylinder_buffer_IC state on a generated forest)",
+        "config": {"workload": WORKLOAD, "phase_cells": P, "form": "mixed", "l2": "inputs > L2 (f is 488 MB FP32)",
+                   "parallelism": f"replicas{world}"},
+        "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
+                  "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
+        "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+        "roofline": roof,
+        "e2e": mixed.get("e2e"),
+        "gpu_launches": launches,
+        "clocks": mixed.get("clocks"),
+    }
+    if not args.no_cpu and world == 1:
+        line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

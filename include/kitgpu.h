@@ -1,0 +1,210 @@
+/*
+ * kitgpu.h -- C-ABI of libkitgpu.so, the GB300 (sm_103a) implementation of
+ * KitAMR.jl's per-step phase-space hot path:
+ *
+ *     slope!  ->  flux!  (domain faces, inner/hanging faces, immersed-boundary wall)
+ *             ->  iterate!  (CAIDVM_Marching / Euler: Shakhov g+ and implicit relaxation)
+ *
+ * The p4est forest, the AMR criteria, the IB geometry and all I/O stay with the
+ * caller.  After every adaptation the caller flattens its cell / neighbour / face
+ * objects into a kg_topology (plain arrays, described below) and uploads it; the
+ * library owns every device allocation.  All entry points return an int status
+ * (KG_OK == 0); nothing throws across the ABI.  One host thread per handle.
+ *
+ * Reference interfaces replaced (paths relative to the KitAMR.jl project):
+ *   slope!(p4est,ka)              src/Flux/Slope.jl:1047-1070
+ *   flux!(p4est,ka)               src/Flux/Flux.jl:458-488
+ *   iterate!(p4est,ka)            src/Theory/Iterate.jl:5-16 (the per-cell marching
+ *                                 kernels at :96-130 and :131-162)
+ *   calc_flux / calc_domain_flux  src/Flux/CAIDVM.jl:4-121, src/Flux/DVM.jl:1-99
+ *   update_solid_cell!            src/Boundary/Immersed_boundary.jl:122-146,207-213
+ *   update_solid_neighbor!        src/Boundary/Immersed_boundary.jl:436-500
+ *   residual_check!               src/Solver/Finalize.jl:5-11
+ */
+#ifndef KITGPU_H
+#define KITGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define KG_OK               0
+#define KG_ERR_ARG          1   /* bad argument / null pointer / size mismatch      */
+#define KG_ERR_TOPOLOGY     2   /* topology rejected (inconsistent or unsupported)  */
+#define KG_ERR_CUDA         3   /* CUDA runtime error                                */
+#define KG_ERR_NOMEM        4   /* device or host allocation failed                  */
+#define KG_ERR_NONFINITE    5   /* device status word: non-finite moment             */
+#define KG_ERR_NEGATIVE     6   /* device status word: rho <= 0 or lambda <= 0       */
+#define KG_ERR_STATE        7   /* call out of order (e.g. step before upload)      */
+#define KG_ERR_BUDGET       8   /* admission refused: HBM footprint over budget      */
+#define KG_ERR_TIMEOUT      9   /* bounded device wait gave up                       */
+
+/* ---- scheme selectors (src/Abstract/Types.jl:320-337) -------------------- */
+#define KG_FLUX_CAIDVM      0   /* CAIDVM: micro + macro flux, conserved w           */
+#define KG_FLUX_DVM         1   /* DVM: micro flux only                              */
+#define KG_MARCH_CAIDVM     0   /* iterate!(::Type{CAIDVM_Marching})  Iterate.jl:96  */
+#define KG_MARCH_EULER      1   /* iterate!(::Type{Euler})            Iterate.jl:131 */
+#define KG_PREC_FP64        0   /* f, sdf, fluxes in FP64 (plain form)               */
+#define KG_PREC_MIXED       1   /* f, sdf, micro fluxes in FP32; moments compensated;
+                                   w, prim, exponents, wall density in FP64          */
+
+/* ---- face / boundary kinds --------------------------------------------- */
+#define KG_FACE_INNER       0   /* FullFace, or one sub-face of a (Back)HangingFace  */
+#define KG_FACE_DOMAIN      1   /* DomainFace                                        */
+#define KG_BC_MAXWELL       0   /* Domain(Maxwellian,...)       CAIDVM.jl:4-25       */
+#define KG_BC_INFLOW        1   /* Domain(SuperSonicInflow,...) CAIDVM.jl:29-49      */
+#define KG_BC_OUTFLOW       2   /* Domain(UniformOutflow,...)   CAIDVM.jl:53-67      */
+#define KG_BC_INTERP        3   /* Domain(InterpolatedOutflow)  CAIDVM.jl:71-94 (2D) */
+
+/* neighbour reference encoding inside kg_topology.nbr_ref / face_there */
+#define KG_NBR_NONE   INT32_MIN /* `nothing` (domain boundary, state 0)             */
+#define KG_NBR_INSIDE (INT32_MIN + 1) /* InsideSolidData (no distribution function) */
+#define KG_WALL(w)    (-1 - (w))/* SolidNeighbor record w                            */
+
+/* ---- solver parameters (Gas, Solver, Status of src/Solver/Types.jl) ------ */
+typedef struct kg_params {
+    int32_t dim;                 /* 2 or 3                                          */
+    int32_t ndf;                 /* 2 in 2D (h, b); 1 in 3D                          */
+    int32_t flux;                /* KG_FLUX_*                                        */
+    int32_t marching;            /* KG_MARCH_*                                       */
+    int32_t precision;           /* KG_PREC_*                                        */
+    int32_t st_check_interval;   /* solver.ST_CHECK_INTERVAL (residual cadence)      */
+    double  gamma;               /* gas.γ                                            */
+    double  K;                   /* gas.K  (internal DOF)                            */
+    double  Pr;                  /* gas.Pr                                           */
+    double  omega;               /* gas.ω  (get_τ exponent, src/Gas/Model.jl:14)     */
+    double  mu_ref;              /* gas.μᵣ (as the caller computed it)               */
+} kg_params;
+
+/* ---- flattened topology (reference-shaped) ----------- *
+ * Arrays are read during kg_upload_topology only and never retained.
+ *
+ * Velocity grids.  Grid g owns velocity cells [grid_off[g], grid_off[g+1]) in the
+ * reference's depth-first leaf order (src/Velocity_space/Rebuild.jl:44-85).
+ * vs_midpoint for grid g is the column-major nv x dim block starting at
+ * grid_off[g]*dim (u of every cell, then v, then w) -- the memory of VsData.midpoint.
+ *
+ * Cells.  Every PsData that carries a distribution function: fluid cells
+ * (bound_enc == 0), IB donor cells (bound_enc > 0) and solid ghost cells
+ * (bound_enc < 0).  InsideSolidData carries none and is not listed.
+ *
+ * Neighbour lists.  For cell c and faceid k (0-based, 2*dim per cell, reference
+ * faceid k+1): state nbr_state[c*2*dim+k] in {0, 1, 2^(dim-1), -1}
+ * (src/Physical_space/Types.jl:6-9) and references
+ * nbr_ref[nbr_off[c*2*dim+k] .. nbr_off[c*2*dim+k+1]) in p4est order; a
+ * reference is a cell index, KG_WALL(w) for a SolidNeighbor, KG_NBR_INSIDE for
+ * an InsideSolidData, or KG_NBR_NONE.
+ *
+ * Faces.  The reference face list with every HangingFace / BackHangingFace
+ * expanded into its sub-faces (src/Flux/Flux.jl:37-59).  face_area is the signed
+ * value update_flux!/update_domain_flux! multiply by (rot * face_area / 2^(dim-1)
+ * for a HangingFace sub-face; Flux.jl:64-111).  face_there_midpoint is the
+ * midpoint of the across-face data as the face sees it (the shifted copy for a
+ * periodic face, Boundary/Period.jl / Solver/Initialize.jl:77-79).
+ */
+typedef struct kg_topology {
+    int32_t dim, ndf;
+    /* velocity grids */
+    int32_t        n_grids;
+    const int64_t *grid_off;         /* n_grids + 1                                  */
+    const int8_t  *vs_level;         /* grid_off[n_grids]                            */
+    const double  *vs_weight;        /* grid_off[n_grids]                            */
+    const double  *vs_midpoint;      /* grid_off[n_grids] * dim (per-grid col-major) */
+    /* cells */
+    int32_t        n_cells;
+    const int32_t *cell_bound_enc;   /* n_cells                                      */
+    const int32_t *cell_level;       /* n_cells: physical level (Slope.jl:825-829)   */
+    const int32_t *cell_grid;        /* n_cells: velocity grid id                    */
+    const double  *cell_midpoint;    /* n_cells * dim (row-major)                    */
+    const double  *cell_ds;          /* n_cells * dim                                */
+    /* neighbours */
+    const int8_t  *nbr_state;        /* n_cells * 2*dim                              */
+    const int32_t *nbr_off;          /* n_cells * 2*dim + 1                          */
+    const int32_t *nbr_ref;          /* nbr_off[n_cells*2*dim]                       */
+    /* immersed-boundary wall records (SolidNeighbor, Physical_space/Types.jl:28-48) */
+    int32_t        n_walls;
+    const int32_t *wall_donor;       /* donor cell (bound_enc > 0)                   */
+    const int32_t *wall_solid;       /* solid ghost cell                             */
+    const int32_t *wall_faceid;      /* 0-based faceid of the donor                  */
+    const double  *wall_aux_point;   /* n_walls * dim                                */
+    const double  *wall_normal;      /* n_walls * dim                                */
+    const double  *wall_bc;          /* n_walls * (dim+2): ib.bc at the aux point    */
+    const int32_t *wall_cut_off;     /* n_walls + 1: cut velocity cells (CuttedVelocityCells) */
+    const int32_t *wall_cut_index;   /* 0-based velocity index in the donor grid     */
+    const double  *wall_cut_gas_w;   /* gas_weights                                  */
+    const double  *wall_cut_solid_w; /* solid_weights                                */
+    /* faces */
+    int32_t        n_faces;
+    const int8_t  *face_kind;        /* KG_FACE_*                                    */
+    const int8_t  *face_dir;         /* 0-based normal direction                     */
+    const double  *face_rot;         /* +1 / -1                                      */
+    const double  *face_area;        /* signed area factor (see above)               */
+    const double  *face_midpoint;    /* n_faces * dim                                */
+    const int32_t *face_here;        /* cell index (always a local PsData)           */
+    const int32_t *face_there;       /* cell index or KG_WALL(w); unused for domain  */
+    const double  *face_there_midpoint; /* n_faces * dim; unused for domain          */
+    const int8_t  *face_bc_kind;     /* KG_BC_* for domain faces                     */
+    const double  *face_bc;          /* n_faces * (dim+2): bc prim for domain faces  */
+} kg_topology;
+
+/* Residual sums of residual_check! (Finalize.jl:5-11) for the last step of the
+ * call whose step counter was a multiple of st_check_interval.               */
+typedef struct kg_step_report {
+    int32_t status;              /* device status word mapped to KG_ERR_*        */
+    int32_t checked;             /* 1 if some step of the call was a check step  */
+    int64_t checked_step;        /* the step counter of that step                */
+    double  sum_res[5];          /* Σ (prim_c - prim_old)^2      (dim+2 used)   */
+    double  sum_avg[5];          /* Σ |prim_c|                                    */
+    double  device_ms;           /* device time of the whole call (CUDA events)  */
+    int64_t phase_cells;         /* Σ velocity cells over fluid + donor cells    */
+    int32_t kernel_launches;     /* kernels this call launched                   */
+} kg_step_report;
+
+typedef struct kg_handle kg_handle;
+
+/* Lifecycle.  kg_create selects device `device` (-1: current). */
+int kg_create(const kg_params *params, int device, kg_handle **out);
+int kg_destroy(kg_handle *h);
+
+/* Replaces the topology (after initialize / amr_recover!, Solver/AMR.jl:54-70).
+ * Device state is re-allocated and must be uploaded again.                  */
+int kg_upload_topology(kg_handle *h, const kg_topology *topo);
+
+/* State transfer.  f: concatenation over cells (in cell order) of the column-
+ * major nv x ndf block (VsData.df memory); w, prim: n_cells x (dim+2) row-major.
+ * kg_download_state: any output pointer may be NULL; qf is n_cells x dim; sdf is
+ * per cell the column-major nv x ndf x dim block (VsData.sdf memory).        */
+int kg_upload_state(kg_handle *h, const double *f, const double *w, const double *prim);
+int kg_download_state(kg_handle *h, double *f, double *w, double *prim, double *qf, double *sdf);
+
+/* Advance `nsteps` steps with time step dt; `step` is status.step before the
+ * first of them (drives the residual cadence).  One call = nsteps x
+ * (slope -> flux -> iterate).                                               */
+int kg_step(kg_handle *h, double dt, int64_t step, int32_t nsteps, kg_step_report *report);
+
+/* Optional per-kernel device timing (CUDA events on the handle's stream).
+ * kg_profile_read fills up to `cap` entries; names are static strings.       */
+int kg_profile_enable(kg_handle *h, int enable);
+int kg_profile_read(kg_handle *h, const char **names, double *total_ms, int64_t *launches,
+                    int32_t cap, int32_t *count);
+
+/* Device bytes held by the handle, and the bytes a topology would need.     */
+int kg_memory_footprint(const kg_handle *h, int64_t *bytes);
+int kg_topology_footprint(const kg_params *params, const kg_topology *topo, int64_t *bytes);
+
+/* Last error message of the handle (or of the last failed kg_create if h is NULL). */
+int kg_last_error(const kg_handle *h, char *buf, size_t cap);
+
+/* Capture the kg_step sequence of `nsteps` steps as a CUDA graph (step
+ * counter handling stays on the host); kg_step then replays it when called
+ * with the same nsteps and dt.                                               */
+int kg_use_graph(kg_handle *h, int enable);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* KITGPU_H */

@@ -1,0 +1,422 @@
+// kg_flatten.cpp -- host flattener: reference-shaped kg_topology -> gather form.
+//
+// The decisions the reference takes per cell and direction while it walks its
+// objects (slope dispatch on neighbour states, transverse projection flags, the
+// per-face upwind split, which side of a face is updated) depend only on topology,
+// so they are taken here once per adaptation and handed to the kernels as tables.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <utility>
+#include "kg_internal.h"
+
+namespace kg {
+namespace {
+
+struct Ctx {
+    const kg_topology* t;
+    int D, NDF;
+    Flat* F;
+    std::map<std::pair<int, int>, int> pairs;  // (my grid, other grid) -> id
+    std::string* err;
+};
+
+int grid_nv(const kg_topology& t, int g) { return (int)(t.grid_off[g + 1] - t.grid_off[g]); }
+
+// data index of a neighbour reference (cells first, then walls); -1 for none/inside
+int data_of(const Ctx& c, int32_t r) {
+    if (r == KG_NBR_NONE || r == KG_NBR_INSIDE) return -1;
+    if (r >= 0) return r;
+    return c.t->n_cells + (-1 - r);
+}
+
+// The reference's level merge walk (e.g. diff_vs!, Flux/Slope.jl:36-63) defines, for
+// every velocity cell i of grid A, the run of grid-B cells that overlap it: one cell
+// when B is as coarse or coarser, the whole covering run when B is finer.
+int pairing(Ctx& c, int ga, int gb) {
+    if (ga == gb) return -1;
+    auto key = std::make_pair(ga, gb);
+    auto it = c.pairs.find(key);
+    if (it != c.pairs.end()) return it->second;
+    const kg_topology& t = *c.t;
+    Flat& F = *c.F;
+    int na = grid_nv(t, ga), nb = grid_nv(t, gb);
+    const int8_t* la = t.vs_level + t.grid_off[ga];
+    const int8_t* lb = t.vs_level + t.grid_off[gb];
+    int id = (int)F.p_off.size() - 1;
+    int j = 0;
+    double flag = 0.0;
+    for (int i = 0; i < na; ++i) {
+        if (j >= nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
+        int li = la[i];
+        if (li == lb[j]) {
+            F.p_j0.push_back(j); F.p_cnt.push_back(1);
+            j += 1;
+        } else if (li < lb[j]) {
+            int j0 = j, cnt = 0;
+            while (flag != 1.0) {
+                if (j >= nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
+                flag += 1.0 / std::ldexp(1.0, c.D * (lb[j] - li));
+                j += 1; cnt += 1;
+            }
+            flag = 0.0;
+            F.p_j0.push_back(j0); F.p_cnt.push_back(cnt);
+        } else {
+            F.p_j0.push_back(j); F.p_cnt.push_back(1);
+            flag += 1.0 / std::ldexp(1.0, c.D * (li - lb[j]));
+            if (flag == 1.0) { j += 1; flag = 0.0; }
+        }
+    }
+    if (j != nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
+    F.p_off.push_back((int64_t)F.p_j0.size());
+    c.pairs[key] = id;
+    return id;
+}
+
+const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
+
+}  // namespace
+
+int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& err) {
+    F = Flat();
+    if (t.dim != 2 && t.dim != 3) { err = "dim must be 2 or 3"; return KG_ERR_ARG; }
+    if (t.ndf != (t.dim == 2 ? 2 : 1)) { err = "ndf must be 2 in 2D and 1 in 3D"; return KG_ERR_ARG; }
+    if (prm.dim != t.dim || prm.ndf != t.ndf) { err = "params and topology disagree on dim/ndf"; return KG_ERR_ARG; }
+    if (prm.st_check_interval <= 0) { err = "st_check_interval must be positive"; return KG_ERR_ARG; }
+    if (t.n_grids <= 0 || t.n_cells <= 0) { err = "empty topology"; return KG_ERR_TOPOLOGY; }
+    if (!t.grid_off || !t.vs_level || !t.vs_weight || !t.vs_midpoint || !t.cell_bound_enc || !t.cell_level ||
+        !t.cell_grid || !t.cell_midpoint || !t.cell_ds || !t.nbr_state || !t.nbr_off || !t.nbr_ref ||
+        (t.n_faces > 0 && (!t.face_kind || !t.face_dir || !t.face_rot || !t.face_area || !t.face_midpoint ||
+                           !t.face_here || !t.face_there || !t.face_there_midpoint || !t.face_bc_kind || !t.face_bc)) ||
+        (t.n_walls > 0 && (!t.wall_donor || !t.wall_solid || !t.wall_faceid || !t.wall_aux_point ||
+                           !t.wall_normal || !t.wall_bc || !t.wall_cut_off)))
+        { err = "null topology array"; return KG_ERR_ARG; }
+    const int D = t.dim, NDF = t.ndf, NC = t.n_cells, NWL = t.n_walls;
+    F.dim = D; F.ndf = NDF; F.n_cells = NC; F.n_walls = NWL; F.n_data = NC + NWL;
+    Ctx c{&t, D, NDF, &F, {}, &err};
+    F.p_off.push_back(0);
+
+    // ---- velocity grids ------------------------------------------------------
+    int64_t PG = t.grid_off[t.n_grids];
+    if (t.grid_off[0] != 0 || PG <= 0) { err = "grid_off must start at 0"; return KG_ERR_TOPOLOGY; }
+    for (int g = 0; g < t.n_grids; ++g) {
+        if (t.grid_off[g + 1] <= t.grid_off[g]) { err = "empty velocity grid"; return KG_ERR_TOPOLOGY; }
+        F.max_nv = std::max(F.max_nv, grid_nv(t, g));
+    }
+    F.g_off.assign(t.grid_off, t.grid_off + t.n_grids + 1);
+    F.vlev.assign(t.vs_level, t.vs_level + PG);
+    F.vw.assign(t.vs_weight, t.vs_weight + PG);
+    F.vu.assign((size_t)D * PG, 0.0);
+    for (int g = 0; g < t.n_grids; ++g) {
+        int nv = grid_nv(t, g);
+        const double* m = t.vs_midpoint + t.grid_off[g] * D;
+        for (int d = 0; d < D; ++d)
+            for (int i = 0; i < nv; ++i) F.vu[(size_t)d * PG + t.grid_off[g] + i] = m[(size_t)d * nv + i];
+        // v = 0 must lie on a root corner (check_vs_setting, Solver/Types.jl:335-353):
+        // no midpoint may have a zero component, or the upwind split would be ambiguous
+        for (int d = 0; d < D; ++d)
+            for (int i = 0; i < nv; ++i)
+                if (m[(size_t)d * nv + i] == 0.0) { err = "a velocity midpoint lies on u_d = 0 (v = 0 must be a root corner)"; return KG_ERR_TOPOLOGY; }
+    }
+
+    // ---- data table: cells then walls -------------------------------------------
+    F.foff.assign(F.n_data + 1, 0);
+    F.dgrid.resize(F.n_data); F.dbe.resize(F.n_data);
+    F.dmid.assign((size_t)F.n_data * MAXD, 0.0); F.dds.assign((size_t)F.n_data * MAXD, 0.0);
+    for (int i = 0; i < NC; ++i) {
+        int g = t.cell_grid[i];
+        if (g < 0 || g >= t.n_grids) { err = "cell_grid out of range"; return KG_ERR_TOPOLOGY; }
+        F.dgrid[i] = g; F.dbe[i] = t.cell_bound_enc[i];
+        for (int d = 0; d < D; ++d) { F.dmid[(size_t)i * MAXD + d] = t.cell_midpoint[(size_t)i * D + d]; F.dds[(size_t)i * MAXD + d] = t.cell_ds[(size_t)i * D + d]; }
+    }
+    for (int w = 0; w < NWL; ++w) {
+        int dn = t.wall_donor[w], sc = t.wall_solid[w];
+        if (dn < 0 || dn >= NC || sc < 0 || sc >= NC) { err = "wall donor/solid out of range"; return KG_ERR_TOPOLOGY; }
+        if (t.cell_bound_enc[dn] <= 0 || t.cell_bound_enc[sc] >= 0) { err = "wall donor must have bound_enc > 0 and solid bound_enc < 0"; return KG_ERR_TOPOLOGY; }
+        int i = NC + w;
+        F.dgrid[i] = t.cell_grid[dn];              // SolidNeighbor shares the donor's grid
+        F.dbe[i] = t.cell_bound_enc[sc];           // and the solid cell's bound_enc, midpoint, ds
+        for (int d = 0; d < D; ++d) { F.dmid[(size_t)i * MAXD + d] = t.cell_midpoint[(size_t)sc * D + d]; F.dds[(size_t)i * MAXD + d] = t.cell_ds[(size_t)sc * D + d]; }
+    }
+    for (int i = 0; i < F.n_data; ++i) F.foff[i + 1] = F.foff[i] + (int64_t)grid_nv(t, F.dgrid[i]) * NDF;
+
+    // ---- neighbour access helpers ---------------------------------------------------
+    const int NF = 2 * D;
+    int64_t nref = t.nbr_off[NC * NF];
+    for (int i = 0; i < NC * NF; ++i)
+        if (t.nbr_off[i + 1] < t.nbr_off[i] || (t.nbr_off[i + 1] == t.nbr_off[i])) { err = "empty neighbour list (a boundary list holds one KG_NBR_NONE)"; return KG_ERR_TOPOLOGY; }
+    for (int64_t r = 0; r < nref; ++r) {
+        int32_t v = t.nbr_ref[r];
+        if (v >= NC || (v < 0 && v != KG_NBR_NONE && v != KG_NBR_INSIDE && (-1 - v) >= NWL)) { err = "nbr_ref out of range"; return KG_ERR_TOPOLOGY; }
+    }
+    auto st = [&](int cell, int k) { return (int)t.nbr_state[cell * NF + k]; };
+    auto lst = [&](int cell, int k) { return t.nbr_ref + t.nbr_off[cell * NF + k]; };
+    auto cnt = [&](int cell, int k) { return (int)(t.nbr_off[cell * NF + k + 1] - t.nbr_off[cell * NF + k]); };
+    auto be_of = [&](int data) { return F.dbe[data]; };
+
+    // ---- slope ops (slope!, Flux/Slope.jl:458-1070) ------------------------------------
+    int Lmin = INT32_MAX, Lmax = 0;
+    for (int i = 0; i < NC; ++i) {
+        if (t.cell_bound_enc[i] < 0) continue;
+        F.n_fluid++;
+        F.phase_cells += grid_nv(t, t.cell_grid[i]);
+        Lmin = std::min(Lmin, t.cell_level[i]);
+        Lmax = std::max(Lmax, t.cell_level[i]);
+    }
+    if (F.n_fluid == 0) { err = "no fluid cells"; return KG_ERR_TOPOLOGY; }
+    const int half = 1 << (D - 1);
+    auto add_list = [&](int cell, int k, int& off, int& n) -> int {
+        off = (int)F.slope_nbr.size();
+        n = cnt(cell, k);
+        for (int j = 0; j < n; ++j) {
+            int dn = data_of(c, lst(cell, k)[j]);
+            if (dn < 0) { err = "slope list references nothing / inside-solid data"; return KG_ERR_TOPOLOGY; }
+            int p = pairing(c, t.cell_grid[cell], F.dgrid[dn]);
+            if (p == -2) return KG_ERR_TOPOLOGY;
+            F.slope_nbr.push_back(NbrRef{dn, p});
+        }
+        return KG_OK;
+    };
+    auto first_data = [&](int cell, int k) { return data_of(c, lst(cell, k)[0]); };
+    auto has_offset = [&](int cell, int k) {  // _ps_has_transverse_offset (Slope.jl:177-199)
+        int dir = k / 2, n = cnt(cell, k);
+        if (n == 0) return false;
+        for (int tt = 0; tt < D; ++tt) {
+            if (tt == dir) continue;
+            double avg = 0.0;
+            for (int j = 0; j < n; ++j) avg += dmid(c, data_of(c, lst(cell, k)[j]))[tt];
+            avg /= n;
+            if (avg != t.cell_midpoint[(size_t)cell * D + tt]) return true;
+        }
+        return false;
+    };
+    auto op_one = [&](SlopeOp& op, int cell, int k, double ds, bool proj) -> int {
+        op.kind = SLOPE_ONE; op.inv_dsA = 1.0 / ds; op.projA = proj;
+        return add_list(cell, k, op.listA, op.cntA);
+    };
+    auto op_two = [&](SlopeOp& op, int cell, double dsL, double dsR, bool pL, bool pR, int dir) -> int {
+        op.kind = SLOPE_TWO; op.inv_dsA = 1.0 / dsL; op.inv_dsB = 1.0 / dsR; op.projA = pL; op.projB = pR;
+        int rc = add_list(cell, 2 * dir, op.listA, op.cntA);
+        if (rc) return rc;
+        return add_list(cell, 2 * dir + 1, op.listB, op.cntB);
+    };
+    // the neighbour-state dispatcher update_slope!(Val(sL), Val(sR)) (Slope.jl:458-771)
+    auto dispatch = [&](SlopeOp& op, int cell, int dir) -> int {
+        int kL = 2 * dir, kR = 2 * dir + 1;
+        int sL = st(cell, kL), sR = st(cell, kR);
+        const double* pm = t.cell_midpoint + (size_t)cell * D;
+        double ds = t.cell_ds[(size_t)cell * D + dir];
+        if (sL == 1 && sR == 1) {
+            bool Ls = be_of(first_data(cell, kL)) < 0, Rs = be_of(first_data(cell, kR)) < 0;
+            if (Ls && Rs) { op.kind = SLOPE_ZERO; return KG_OK; }
+            if (Ls) return op_one(op, cell, kR, pm[dir] - dmid(c, first_data(cell, kR))[dir], false);
+            if (Rs) return op_one(op, cell, kL, pm[dir] - dmid(c, first_data(cell, kL))[dir], false);
+            return op_two(op, cell, ds, -ds, false, false, dir);
+        }
+        if (sL == 0 || sR == 0) {
+            if (sL == 0 && sR == 0) { err = "a fluid cell has domain boundaries on both sides of a direction (no reference method)"; return KG_ERR_TOPOLOGY; }
+            int k = sL == 0 ? kR : kL;
+            return op_one(op, cell, k, pm[dir] - dmid(c, first_data(cell, k))[dir], false);
+        }
+        auto fac = [&](int s) { return s == 1 ? 1.0 : (s == half ? 0.75 : 1.5); };
+        if ((sL != 1 && sL != half && sL != -1) || (sR != 1 && sR != half && sR != -1)) { err = "invalid neighbour state"; return KG_ERR_TOPOLOGY; }
+        return op_two(op, cell, fac(sL) * ds, -fac(sR) * ds, false, false, dir);
+    };
+    // transverse correction (update_slope_transverse_level! step 2, Slope.jl:908-941)
+    auto transverse = [&](SlopeOp& op, int cell, int dir) -> int {
+        int kL = 2 * dir, kR = 2 * dir + 1;
+        int sL = st(cell, kL), sR = st(cell, kR);
+        const double* pm = t.cell_midpoint + (size_t)cell * D;
+        if (sL != 0 && sR != 0) {
+            double dsL = pm[dir] - dmid(c, first_data(cell, kL))[dir];
+            double dsR = pm[dir] - dmid(c, first_data(cell, kR))[dir];
+            if (be_of(first_data(cell, kL)) < 0) return op_one(op, cell, kR, dsR, true);
+            if (be_of(first_data(cell, kR)) < 0) return op_one(op, cell, kL, dsL, true);
+            return op_two(op, cell, dsL, dsR, has_offset(cell, kL), has_offset(cell, kR), dir);
+        }
+        if (sR == 0 && sL == -1) {
+            if (be_of(first_data(cell, kL)) < 0) { op.kind = SLOPE_SKIP; return KG_OK; }
+            return op_one(op, cell, kL, pm[dir] - dmid(c, first_data(cell, kL))[dir], true);
+        }
+        if (sL == 0 && sR == -1) {
+            if (be_of(first_data(cell, kR)) < 0) { op.kind = SLOPE_SKIP; return KG_OK; }
+            return op_one(op, cell, kR, pm[dir] - dmid(c, first_data(cell, kR))[dir], true);
+        }
+        op.kind = SLOPE_SKIP;
+        return KG_OK;
+    };
+    if (Lmin == INT32_MAX) Lmin = 0;
+    F.pass_off.push_back(0);
+    F.pass_cells_off.push_back(0);
+    for (int L = Lmin; L <= Lmax; ++L) {
+        for (int i = 0; i < NC; ++i) {
+            if (t.cell_bound_enc[i] < 0 || t.cell_level[i] != L) continue;
+            F.pass_cells.push_back(i);
+            F.cell_slope_op.push_back((int32_t)F.slope_ops.size());
+            for (int dir = 0; dir < D; ++dir) {
+                SlopeOp op{};
+                op.cell = i; op.dir = (int8_t)dir;
+                op.kind = SLOPE_SKIP;
+                int sL = st(i, 2 * dir), sR = st(i, 2 * dir + 1);
+                int rc;
+                if (L == Lmin || !(sL == -1 || sR == -1)) rc = dispatch(op, i, dir);
+                else rc = transverse(op, i, dir);
+                if (rc) return rc;
+                F.slope_ops.push_back(op);
+            }
+        }
+        F.pass_off.push_back((int32_t)F.slope_ops.size());
+        F.pass_cells_off.push_back((int32_t)F.pass_cells.size());
+    }
+
+    // ---- flux incidences (flux!, Flux/Flux.jl:19-111,458-503) -----------------------------
+    std::vector<std::vector<Incidence>> per(NC);
+    for (int fi = 0; fi < t.n_faces; ++fi) {
+        Incidence a{};
+        int dir = t.face_dir[fi];
+        if (dir < 0 || dir >= D) { err = "face_dir out of range"; return KG_ERR_TOPOLOGY; }
+        int here = t.face_here[fi];
+        if (here < 0 || here >= NC || t.cell_bound_enc[here] < 0) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
+        double rot = t.face_rot[fi], area = t.face_area[fi];
+        for (int d = 0; d < D; ++d) { a.fmid[d] = t.face_midpoint[(size_t)fi * D + d]; a.my_mid[d] = t.cell_midpoint[(size_t)here * D + d]; }
+        a.dir = (int8_t)dir;
+        if (t.face_kind[fi] == KG_FACE_DOMAIN) {
+            int bk = t.face_bc_kind[fi];
+            if (bk < KG_BC_MAXWELL || bk > KG_BC_INTERP) { err = "unknown domain boundary kind"; return KG_ERR_TOPOLOGY; }
+            if (bk == KG_BC_MAXWELL && prm.flux == KG_FLUX_DVM) { err = "DVM Maxwellian domain flux is undefined in the reference (DVM.jl:3,12)"; return KG_ERR_TOPOLOGY; }
+            if (bk == KG_BC_INTERP && D != 2) { err = "InterpolatedOutflow is 2D only in the reference"; return KG_ERR_TOPOLOGY; }
+            a.kind = INC_DOMAIN; a.bc_kind = (int8_t)bk; a.other = -1; a.pair = -1; a.here_side = 1;
+            a.orient = rot; a.sarea = area;
+            a.bc = (int32_t)(F.bc_prim.size() / MAXW);
+            for (int e = 0; e < MAXW; ++e) F.bc_prim.push_back(e < D + 2 ? t.face_bc[(size_t)fi * (D + 2) + e] : 0.0);
+            per[here].push_back(a);
+            continue;
+        }
+        int od = data_of(c, t.face_there[fi]);
+        if (od < 0) { err = "inner face without a there side"; return KG_ERR_TOPOLOGY; }
+        bool solid = F.dbe[od] < 0;
+        a.kind = solid ? INC_SOLID : INC_INNER;
+        a.other = od; a.here_side = 1; a.orient = rot; a.sarea = area;
+        for (int d = 0; d < D; ++d) { a.ot_mid[d] = t.face_there_midpoint[(size_t)fi * D + d]; a.ot_ds[d] = F.dds[(size_t)od * MAXD + d]; }
+        a.pair = pairing(c, t.cell_grid[here], F.dgrid[od]);
+        if (a.pair == -2) return KG_ERR_TOPOLOGY;
+        if (solid && od >= NC && F.dgrid[od] != t.cell_grid[here]) { err = "wall grid differs from donor grid"; return KG_ERR_TOPOLOGY; }
+        per[here].push_back(a);
+        if (!solid && od < NC) {
+            // the there side receives the same flux with the opposite sign
+            Incidence b{};
+            b.kind = INC_INNER; b.dir = (int8_t)dir; b.other = here; b.here_side = 0;
+            b.orient = -rot; b.sarea = -area;
+            for (int d = 0; d < D; ++d) {
+                b.fmid[d] = a.fmid[d];
+                b.my_mid[d] = a.ot_mid[d];                // the (possibly periodic-shifted) copy
+                b.ot_mid[d] = a.my_mid[d];
+                b.ot_ds[d] = t.cell_ds[(size_t)here * D + d];
+            }
+            b.pair = pairing(c, t.cell_grid[od], t.cell_grid[here]);
+            if (b.pair == -2) return KG_ERR_TOPOLOGY;
+            per[od].push_back(b);
+        }
+    }
+    F.inc_off.push_back(0);
+    for (int i = 0; i < NC; ++i) {
+        if (t.cell_bound_enc[i] < 0) continue;
+        F.fluid_cells.push_back(i);
+        for (auto& a : per[i]) F.inc.push_back(a);
+        F.max_inc = std::max(F.max_inc, (int)per[i].size());
+        F.inc_off.push_back((int32_t)F.inc.size());
+    }
+
+    // ---- immersed boundary (Boundary/Immersed_boundary.jl:122-146,367-500) -----------------
+    auto fluid_sources = [&](int cell, const double* target, std::vector<int>& srcs) {
+        for (int k = 0; k < NF; ++k) {
+            int32_t r = lst(cell, k)[0];
+            if (r >= 0 && t.cell_bound_enc[r] >= 0) srcs.push_back(r);
+        }
+        (void)target;
+    };
+    auto push_sources = [&](int tgt_grid, const std::vector<int>& srcs, const double* target) -> int {
+        for (int s : srcs) {
+            int p = pairing(c, tgt_grid, t.cell_grid[s]);
+            if (p == -2) return KG_ERR_TOPOLOGY;
+            F.ib_nbr.push_back(NbrRef{s, p});
+            for (int d = 0; d < MAXD; ++d) F.ib_dx.push_back(d < D ? target[d] - t.cell_midpoint[(size_t)s * D + d] : 0.0);
+        }
+        return KG_OK;
+    };
+    for (int i = 0; i < NC; ++i) {
+        if (t.cell_bound_enc[i] >= 0) continue;
+        std::vector<int> srcs;
+        const double* tm = t.cell_midpoint + (size_t)i * D;
+        fluid_sources(i, tm, srcs);
+        SolidOp so{};
+        so.cell = i; so.list = (int32_t)F.ib_nbr.size(); so.cnt = (int32_t)srcs.size();
+        if (srcs.empty()) { err = "solid cell without fluid neighbours"; return KG_ERR_TOPOLOGY; }
+        int rc = push_sources(t.cell_grid[i], srcs, tm);
+        if (rc) return rc;
+        F.solid_ops.push_back(so);
+    }
+    for (int w = 0; w < NWL; ++w) {
+        WallOp wo{};
+        int dn = t.wall_donor[w], sc = t.wall_solid[w];
+        int k = t.wall_faceid[w];
+        if (k < 0 || k >= NF) { err = "wall faceid out of range"; return KG_ERR_TOPOLOGY; }
+        wo.donor = dn; wo.solid = sc; wo.data = NC + w; wo.dir = k / 2;
+        for (int d = 0; d < D; ++d) {
+            wo.aux[d] = t.wall_aux_point[(size_t)w * D + d];
+            wo.normal[d] = t.wall_normal[(size_t)w * D + d];
+            wo.ib_point[d] = wo.aux[d] + t.cell_midpoint[(size_t)dn * D + d] - t.cell_midpoint[(size_t)sc * D + d];
+        }
+        for (int e = 0; e < D + 2; ++e) wo.bc[e] = t.wall_bc[(size_t)w * (D + 2) + e];
+        int dir = wo.dir;
+        wo.dxf = wo.ib_point[dir] - t.cell_midpoint[(size_t)dn * D + dir];
+        wo.dxs = t.cell_midpoint[(size_t)dn * D + dir] - t.cell_midpoint[(size_t)sc * D + dir];
+        wo.dxL = wo.aux[dir] - wo.ib_point[dir];
+        std::vector<int> srcs;
+        fluid_sources(dn, wo.ib_point, srcs);
+        srcs.push_back(dn);  // image_df appends the donor itself (Immersed_boundary.jl:373)
+        wo.list = (int32_t)F.ib_nbr.size(); wo.cnt = (int32_t)srcs.size();
+        int rc = push_sources(t.cell_grid[dn], srcs, wo.ib_point);
+        if (rc) return rc;
+        wo.spair = pairing(c, t.cell_grid[dn], t.cell_grid[sc]);
+        if (wo.spair == -2) return KG_ERR_TOPOLOGY;
+        int c0 = t.wall_cut_off[w], c1 = t.wall_cut_off[w + 1];
+        if (c1 < c0) { err = "wall_cut_off must be non-decreasing"; return KG_ERR_TOPOLOGY; }
+        wo.cut_off = (int32_t)F.cut_idx.size(); wo.cut_cnt = c1 - c0;
+        int nv = grid_nv(t, t.cell_grid[dn]);
+        wo.cvcw_off = (int64_t)F.cvcw.size();
+        const double* wt = t.vs_weight + t.grid_off[t.cell_grid[dn]];
+        size_t base = F.cvcw.size();
+        F.cvcw.insert(F.cvcw.end(), wt, wt + nv);
+        for (int a = c0; a < c1; ++a) {
+            int idx = t.wall_cut_index[a];
+            if (idx < 0 || idx >= nv) { err = "wall_cut_index out of range"; return KG_ERR_TOPOLOGY; }
+            F.cut_idx.push_back(idx); F.cut_gw.push_back(t.wall_cut_gas_w[a]); F.cut_sw.push_back(t.wall_cut_solid_w[a]);
+            F.cvcw[base + idx] = 0.0;
+        }
+        // the donor's neighbour entry for this face must be this wall record
+        if (lst(dn, k)[0] != KG_WALL(w)) { err = "donor neighbour entry does not reference its wall record"; return KG_ERR_TOPOLOGY; }
+        F.wall_ops.push_back(wo);
+    }
+    if (F.p_j0.empty()) { F.p_j0.push_back(0); F.p_cnt.push_back(0); }
+    return KG_OK;
+}
+
+int64_t device_bytes(const Flat& F, int precision) {
+    int64_t s = precision == KG_PREC_FP64 ? 8 : 4;
+    int64_t nf = F.foff.back();
+    int64_t b = 0;
+    b += 2 * nf * s;                       // f ping-pong
+    b += nf * F.dim * s;                   // sdf
+    b += (int64_t)F.n_data * (MAXW * 8) * 3;  // w, prim, qf
+    b += (int64_t)F.vu.size() * 8 + (int64_t)F.vw.size() * 8 + (int64_t)F.vlev.size();
+    b += (int64_t)(F.p_j0.size() + F.p_cnt.size()) * 4;
+    b += (int64_t)F.slope_ops.size() * sizeof(SlopeOp) + (int64_t)F.slope_nbr.size() * sizeof(NbrRef);
+    b += (int64_t)F.inc.size() * sizeof(Incidence);
+    b += (int64_t)F.wall_ops.size() * sizeof(WallOp) + (int64_t)F.cvcw.size() * 8;
+    b += (int64_t)F.n_data * 64;
+    return b;
+}
+
+}  // namespace kg

@@ -1,0 +1,116 @@
+// kg_internal.h -- device-side layout of libkitgpu.so.
+//
+// The reference-shaped kg_topology (scatter form: a face list whose faces update
+// both adjacent cells) is flattened on the host into a gather form: every cell
+// owns the list of (sub-)faces it receives fluxes through ("incidences"), its
+// slope operations per direction, and the velocity pairing tables that replace
+// the reference's level merge walks.  Each cell is then advanced by one CTA that
+// writes only its own data, so no atomics are needed and results are
+// deterministic.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+#include "../../include/kitgpu.h"
+
+namespace kg {
+
+constexpr int MAXD = 3;
+constexpr int MAXW = MAXD + 2;
+
+// ---- slope operations (one per fluid cell and direction) -------------------
+enum SlopeKind : int8_t { SLOPE_ZERO = 0, SLOPE_SKIP = 1, SLOPE_ONE = 2, SLOPE_TWO = 3 };
+
+struct SlopeOp {            // 48 bytes
+    double inv_dsA, inv_dsB;   // 1/ds of list A, list B
+    int32_t listA, cntA;       // into slope_nbr
+    int32_t listB, cntB;
+    int8_t kind, projA, projB, dir;
+    int32_t cell;
+};
+
+struct NbrRef {             // neighbour in a slope / extrapolation list
+    int32_t data;           // data index (cell, or n_cells + wall)
+    int32_t pair;           // velocity pairing id (my grid <- its grid), -1 = identity
+};
+
+// ---- flux incidences ------------------------------------------------------
+enum IncKind : int8_t { INC_INNER = 0, INC_DOMAIN = 1, INC_SOLID = 2 };
+// INC_SOLID: the across-face data has bound_enc < 0 (SolidNeighbor wall record or a
+// solid PsData); the reference reconstructs the here side without the positivity
+// limiter and (CAIDVM) takes the there side unreconstructed.
+
+struct Incidence {          // 128 bytes
+    double fmid[MAXD];      // face (sub-face) midpoint
+    double my_mid[MAXD];    // centre used for this cell's reconstruction
+    double ot_mid[MAXD];    // centre used for the other side's reconstruction
+    double orient;          // +rot if this cell is the face's here side, -rot otherwise
+    double sarea;           // +area (here) / -area (there): factor of the received flux
+    double ot_ds[MAXD];     // other side's ds (positivity limiter)
+    int32_t other;          // data index of the other side (-1 for a domain face)
+    int32_t pair;           // pairing (my grid <- other's grid), -1 identity
+    int8_t kind, dir, bc_kind, here_side;
+    int32_t bc;             // index into bc_prim (domain faces)
+};
+
+// ---- immersed boundary ----------------------------------------------------
+struct SolidOp {            // update_solid_cell! for one solid cell
+    int32_t cell, list, cnt, pad;
+};
+struct WallOp {             // update_solid_neighbor! for one SolidNeighbor
+    double ib_point[MAXD], aux[MAXD], normal[MAXD], bc[MAXW];
+    double dxf, dxs, dxL;
+    int32_t donor, solid, data, dir;
+    int32_t list, cnt;      // image_df sources (fluid neighbours + donor) in ib_nbr
+    int32_t spair;          // pairing (donor grid <- solid grid) for boundary_slope!
+    int32_t cut_off, cut_cnt;
+    int64_t cvcw_off;       // dense cut-cell weight vector (weight with cut cells zeroed)
+};
+
+// ---- flattened topology (host copy, then mirrored to device) ------------------
+struct Flat {
+    int dim = 2, ndf = 2;
+    int n_cells = 0, n_walls = 0, n_data = 0;
+    int n_fluid = 0;              // cells with bound_enc >= 0
+    int64_t phase_cells = 0;      // Σ nv over fluid cells
+    int max_nv = 0;
+    // velocity grids
+    std::vector<int64_t> g_off;   // n_grids + 1
+    std::vector<int8_t> vlev;
+    std::vector<double> vw;
+    std::vector<double> vu;       // [dim][P_g] (dimension-major)
+    // data table
+    std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)
+    std::vector<int32_t> dgrid, dbe;
+    std::vector<double> dmid, dds; // n_data * MAXD
+    // pairing tables
+    std::vector<int64_t> p_off;    // n_pairs + 1 (offsets into p_j0 / p_cnt)
+    std::vector<int32_t> p_j0, p_cnt;
+    // slope: passes (levels) and ops
+    std::vector<int32_t> pass_off;   // n_passes + 1 into slope_ops (grouped by pass)
+    std::vector<SlopeOp> slope_ops;  // ordered by pass, then cell, then dir
+    std::vector<int32_t> pass_cells_off;  // per pass: cells [pass_cells_off[p], ...) in pass_cells
+    std::vector<int32_t> pass_cells;
+    std::vector<int32_t> cell_slope_op;   // per pass-cell entry: first op index (dim ops each)
+    std::vector<NbrRef> slope_nbr;
+    // flux incidences, per fluid cell
+    std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
+    std::vector<int32_t> inc_off;         // n_fluid + 1
+    std::vector<Incidence> inc;
+    std::vector<double> bc_prim;          // domain-face bc prim, MAXW per entry
+    // immersed boundary
+    std::vector<SolidOp> solid_ops;
+    std::vector<WallOp> wall_ops;
+    std::vector<NbrRef> ib_nbr;
+    std::vector<double> ib_dx;            // per ib_nbr entry: dx[MAXD] (target - source centre)
+    std::vector<int32_t> cut_idx;
+    std::vector<double> cut_gw, cut_sw;
+    std::vector<double> cvcw;
+    int max_inc = 0;
+};
+
+// Builds the gather form; returns KG_OK or an error code with a message.
+int flatten(const kg_params& prm, const kg_topology& t, Flat& out, std::string& err);
+int64_t device_bytes(const Flat& f, int precision);
+
+}  // namespace kg

@@ -1,0 +1,818 @@
+// kg_kernels.cu -- sm_103a kernels of the phase-space step.
+//
+//   slope_kernel          slope! level pass (Flux/Slope.jl:458-1019)
+//   solid_kernel          update_solid_cell!  (Boundary/Immersed_boundary.jl:98-146)
+//   wall_kernel           update_solid_neighbor! (Immersed_boundary.jl:367-483)
+//   flux_collide_kernel   flux! (gather form of Flux.jl:19-344, CAIDVM.jl, DVM.jl) fused with
+//                         iterate!(CAIDVM_Marching | Euler) (Theory/Iterate.jl:96-162)
+//   residual_kernel       Σ over cells of the residual_check! terms (Solver/Finalize.jl:5-11)
+//
+// Layout: f of data d is the column-major nv x ndf block at foff[d] (velocity fastest, the
+// memory of VsData.df); sdf of d is the nv x ndf x dim block at foff[d]*dim.  One CTA works
+// on one physical cell with threads striding its velocity cells, so every global access to
+// f / sdf / velocity metadata is coalesced along the velocity index.
+//
+// T is the storage type of f / sdf (double: plain form; float: mixed form).  In the mixed
+// form the per-velocity arithmetic runs in FP32 while the exponent of the Maxwellian, the
+// conserved update, the primitive recovery and the wall-density solve stay in FP64, and
+// moment sums use compensated (two-sum) FP32 accumulation before an FP64 block reduction.
+#include <cuda_runtime.h>
+#include "kg_device.cuh"
+
+namespace kg {
+
+template <typename T> struct Arith { using type = double; };
+template <> struct Arith<float> { using type = float; };
+
+// Compensated accumulator: plain FP64 sum for double, Neumaier two-sum for float.
+template <typename A> struct Acc {
+    A s = 0, c = 0;
+    __device__ __forceinline__ void add(A x) {
+        A t = s + x;
+        if (fabs((double)s) >= fabs((double)x)) c += (s - t) + x; else c += (x - t) + s;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+template <> struct Acc<double> {
+    double s = 0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+struct VGridView {
+    int64_t goff;
+    int nv;
+    const double* vu;
+    int64_t PG;
+    __device__ __forceinline__ double u(int i, int d) const { return vu[(int64_t)d * PG + goff + i]; }
+};
+
+__device__ __forceinline__ VGridView grid_view(const Dev& P, int data) {
+    VGridView g;
+    int gr = P.dgrid[data];
+    g.goff = P.g_off[gr];
+    g.nv = (int)(P.g_off[gr + 1] - g.goff);
+    g.vu = P.vu;
+    g.PG = P.PG;
+    return g;
+}
+
+// =============================================================================
+// slope
+// =============================================================================
+template <int D, int NDF, typename T>
+__device__ __forceinline__ void slope_side(const Dev& P, int cell, int dir, int i, int li, const double* fc,
+                                           int list, int cnt, double inv_ds, bool proj, double* s) {
+    using A = typename Arith<T>::type;
+    const T* f = (const T*)P.f_in;
+    const T* sdf = (const T*)P.sdf;
+    A acc[NDF];
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) acc[k] = 0;
+    const double* cm = P.dmid + (int64_t)cell * MAXD;
+    for (int n = 0; n < cnt; ++n) {
+        NbrRef r = P.slope_nbr[list + n];
+        const int64_t fo = P.foff[r.data];
+        const int nvn = (int)((P.foff[r.data + 1] - fo) / NDF);
+        const T* fn = f + fo;
+        const T* sn = sdf + fo * D;
+        A dm[D];
+#pragma unroll
+        for (int t = 0; t < D; ++t) dm[t] = (proj && t != dir) ? (A)(cm[t] - P.dmid[(int64_t)r.data * MAXD + t]) : (A)0;
+        int j0 = i, jc = 1;
+        int64_t gn = 0;
+        if (r.pair >= 0) {
+            int64_t po = P.p_off[r.pair] + i;
+            j0 = P.p_j0[po];
+            jc = P.p_cnt[po];
+            gn = P.g_off[P.dgrid[r.data]];
+        }
+        for (int j = j0; j < j0 + jc; ++j) {
+            A sc = 1;
+            if (r.pair >= 0) sc = (A)merge_inv_scale<D>(li, P.vlev[gn + j]);
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                A p = (A)fn[(int64_t)k * nvn + j];
+#pragma unroll
+                for (int t = 0; t < D; ++t)
+                    if (dm[t] != (A)0) p += dm[t] * (A)sn[((int64_t)t * NDF + k) * nvn + j];
+                acc[k] += ((A)fc[k] - p) * sc * (A)inv_ds;
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) s[k] = (double)(acc[k] / (A)cnt);
+}
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
+    using A = typename Arith<T>::type;
+    const int pc = pc_base + blockIdx.x;
+    const int cell = P.pass_cells[pc];
+    const int op0 = P.cell_slope_op[pc];
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const int64_t fo = P.foff[cell];
+    const T* fcell = (const T*)P.f_in + fo;
+    T* scell = (T*)P.sdf + fo * D;
+    __shared__ SlopeOp ops[MAXD];
+    if (threadIdx.x < D) ops[threadIdx.x] = P.slope_ops[op0 + threadIdx.x];
+    __syncthreads();
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const int li = P.vlev[g.goff + i];
+        double fc[NDF];
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) fc[k] = (double)fcell[(int64_t)k * nv + i];
+#pragma unroll
+        for (int dir = 0; dir < D; ++dir) {
+            const SlopeOp& op = ops[dir];
+            if (op.kind == SLOPE_SKIP) continue;
+            double out[NDF];
+            if (op.kind == SLOPE_ZERO) {
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) out[k] = 0.0;
+            } else {
+                double sA[NDF];
+                slope_side<D, NDF, T>(P, cell, dir, i, li, fc, op.listA, op.cntA, op.inv_dsA, op.projA, sA);
+                if (op.kind == SLOPE_ONE) {
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) out[k] = sA[k];
+                } else {
+                    double sB[NDF];
+                    slope_side<D, NDF, T>(P, cell, dir, i, li, fc, op.listB, op.cntB, op.inv_dsB, op.projB, sB);
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) out[k] = (double)minmod((A)sA[k], (A)sB[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) scell[((int64_t)dir * NDF + k) * nv + i] = (T)out[k];
+        }
+    }
+}
+
+// =============================================================================
+// immersed boundary
+// =============================================================================
+// Σ_n weight_n(u) * merge_n(f_n + sdf_n . dx_n) over a source list, for target velocity i
+// (vs_extrapolate! with the directional weights of update_solid_cell! / image_df).
+template <int D, int NDF, typename T>
+__device__ __forceinline__ void extrapolate(const Dev& P, const VGridView& g, int i, int li, int list, int cnt,
+                                            double* out) {
+    using A = typename Arith<T>::type;
+    const T* f = (const T*)P.f_in;
+    const T* sdf = (const T*)P.sdf;
+    double u[D], un = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) { u[d] = g.u(i, d); un += u[d] * u[d]; }
+    un = sqrt(un);
+    double W[2 * MAXD + 1];
+    double wsum = 0.0;
+    for (int n = 0; n < cnt; ++n) {
+        const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
+        double nl = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) nl += dx[d] * dx[d];
+        nl = sqrt(nl);
+        double ul = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) ul += u[d] * (dx[d] / nl);
+        double v = fmax(0.0, ul / un);
+        W[n] = v * v;
+        wsum += W[n];
+    }
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) out[k] = 0.0;
+    for (int n = 0; n < cnt; ++n) {
+        const double wi = wsum == 0.0 ? 1.0 / cnt : W[n] / wsum;
+        NbrRef r = P.ib_nbr[list + n];
+        const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
+        const int64_t fo = P.foff[r.data];
+        const int nvn = (int)((P.foff[r.data + 1] - fo) / NDF);
+        const T* fn = f + fo;
+        const T* sn = sdf + fo * D;
+        int j0 = i, jc = 1;
+        int64_t gn = 0;
+        if (r.pair >= 0) {
+            int64_t po = P.p_off[r.pair] + i;
+            j0 = P.p_j0[po];
+            jc = P.p_cnt[po];
+            gn = P.g_off[P.dgrid[r.data]];
+        }
+        for (int j = j0; j < j0 + jc; ++j) {
+            double sc = r.pair >= 0 ? merge_inv_scale<D>(li, P.vlev[gn + j]) : 1.0;
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                A v = (A)fn[(int64_t)k * nvn + j];
+                A s = 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) s += (A)sn[((int64_t)d * NDF + k) * nvn + j] * (A)dx[d];
+                out[k] += (double)(v + s) * sc * wi;
+            }
+        }
+    }
+}
+
+template <int D, int NDF>
+__device__ __forceinline__ void moments_add(const VGridView& g, const double wgt, int i, const double* fv, double* m) {
+    // micro_to_macro_2D2F / 3D1F terms of one velocity cell
+    double u2 = 0.0;
+    m[0] += wgt * fv[0];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { double u = g.u(i, d); m[1 + d] += wgt * u * fv[0]; u2 += u * u; }
+    if (NDF == 2) m[D + 1] += 0.5 * wgt * (u2 * fv[0] + fv[NDF - 1]);
+    else m[D + 1] += 0.5 * wgt * u2 * fv[0];
+}
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) solid_kernel(Dev P) {
+    __shared__ double sred[(D + 2) * (BLOCK / 32)];
+    const SolidOp op = P.solid_ops[blockIdx.x];
+    const VGridView g = grid_view(P, op.cell);
+    const int nv = g.nv;
+    const int64_t fo = P.foff[op.cell];
+    T* fa = (T*)P.f_in + fo;
+    T* fb = (T*)P.f_out + fo;
+    const double* vw = P.vw + g.goff;
+    double m[D + 2];
+#pragma unroll
+    for (int e = 0; e < D + 2; ++e) m[e] = 0.0;
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const int li = P.vlev[g.goff + i];
+        double v[NDF];
+        extrapolate<D, NDF, T>(P, g, i, li, op.list, op.cnt, v);
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) { fa[(int64_t)k * nv + i] = (T)v[k]; fb[(int64_t)k * nv + i] = (T)v[k]; }
+        moments_add<D, NDF>(g, vw[i], i, v, m);
+    }
+    block_sum<D + 2>(m, sred);
+    if (threadIdx.x == 0) {
+        double* w = P.w + (int64_t)op.cell * MAXW;
+        double* pr = P.prim + (int64_t)op.cell * MAXW;
+#pragma unroll
+        for (int e = 0; e < D + 2; ++e) w[e] = m[e];
+        get_prim<D>(m, P.gamma, pr);
+    }
+}
+
+template <int D>
+__device__ __forceinline__ double maxwell_h(const VGridView& g, int i, const double* prim) {
+    // h of discrete_maxwell_2D2F / M of discrete_maxwell_3D1F (FP64 exponent)
+    double c2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) { double cu = g.u(i, d) - prim[1 + d]; c2 += cu * cu; }
+    const double lam = prim[D + 1];
+    const double pre = D == 2 ? lam / PI : pow(lam / PI, 1.5);
+    return prim[0] * pre * exp(-lam * c2);
+}
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
+    extern __shared__ double sh[];
+    double* aux = sh;                          // NDF * nv
+    __shared__ double sred[2 * (BLOCK / 32)];
+    const WallOp op = P.wall_ops[blockIdx.x];
+    const VGridView g = grid_view(P, op.donor);
+    const VGridView gs = grid_view(P, op.solid);
+    const int nv = g.nv, nvs = gs.nv;
+    const T* fc = (const T*)P.f_in + P.foff[op.donor];
+    const T* fsol = (const T*)P.f_in + P.foff[op.solid];
+    const int64_t wo = P.foff[op.data];
+    T* wsdf = (T*)P.sdf + wo * D;
+    const double* cvcw = P.cvcw + op.cvcw_off;
+    const int dir = op.dir;
+    double prim1[MAXW];
+#pragma unroll
+    for (int e = 0; e < D + 2; ++e) prim1[e] = op.bc[e];
+    prim1[0] = 1.0;
+    double red[2] = {0.0, 0.0};  // MuR, SF
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const int li = P.vlev[g.goff + i];
+        double vn = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) vn += g.u(i, d) * op.normal[d];
+        const double theta = vn >= 0.0 ? 1.0 : 0.0;
+        double ib[NDF];
+        extrapolate<D, NDF, T>(P, g, i, li, op.list, op.cnt, ib);
+        // boundary_slope! (Immersed_boundary.jl:396-435)
+        double sL[NDF];
+        int j0 = i, jc = 1;
+        if (op.spair >= 0) {
+            int64_t po = P.p_off[op.spair] + i;
+            j0 = P.p_j0[po];
+            jc = P.p_cnt[po];
+        }
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) sL[k] = 0.0;
+        for (int j = j0; j < j0 + jc; ++j) {
+            double sc = op.spair >= 0 ? merge_inv_scale<D>(li, P.vlev[gs.goff + j]) : 1.0;
+#pragma unroll
+            for (int k = 0; k < NDF; ++k)
+                sL[k] += ((double)fc[(int64_t)k * nv + i] - (double)fsol[(int64_t)k * nvs + j]) * sc / op.dxs;
+        }
+        double a0 = 0.0;
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            double fck = (double)fc[(int64_t)k * nv + i];
+            double ss = minmod(sL[k], (ib[k] - fck) / op.dxf);
+            ss = fmin(fabs((ib[k] - JL_EPS) / (ss * op.dxL + JL_EPS)), 1.0) * ss;
+            wsdf[((int64_t)dir * NDF + k) * nv + i] = (T)ss;
+            double a = ib[k] + ss * op.dxL;
+            aux[(int64_t)k * nv + i] = a;
+            if (k == 0) a0 = a;
+        }
+        const double mh = maxwell_h<D>(g, i, prim1);
+        red[0] += cvcw[i] * vn * mh * theta;
+        red[1] += cvcw[i] * vn * a0 * (1.0 - theta);
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
+        const int idx = P.cut_idx[op.cut_off + a];
+        double vn = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) vn += g.u(idx, d) * op.normal[d];
+        const double mh = maxwell_h<D>(g, idx, prim1);
+        red[0] += P.cut_sw[op.cut_off + a] * vn * mh;
+        red[1] += P.cut_gw[op.cut_off + a] * vn * aux[idx];
+    }
+    block_sum<2>(red, sred);
+    const double rho_w = -red[1] / red[0];
+    T* wa = (T*)P.f_in + wo;
+    T* wb = (T*)P.f_out + wo;
+    const double lam = prim1[D + 1];
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        double vn = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) vn += g.u(i, d) * op.normal[d];
+        if (vn >= 0.0) {
+            const double mh = maxwell_h<D>(g, i, prim1);
+            double mv[NDF];
+            mv[0] = mh;
+            if (NDF == 2) mv[NDF - 1] = mh * P.K / (2.0 * lam);
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) { T v = (T)(mv[k] * rho_w); wa[(int64_t)k * nv + i] = v; wb[(int64_t)k * nv + i] = v; }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) { T v = (T)aux[(int64_t)k * nv + i]; wa[(int64_t)k * nv + i] = v; wb[(int64_t)k * nv + i] = v; }
+        }
+    }
+    __syncthreads();
+    for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
+        const int idx = P.cut_idx[op.cut_off + a];
+        const double gw = P.cut_gw[op.cut_off + a], sw = P.cut_sw[op.cut_off + a];
+        const double mh = maxwell_h<D>(g, idx, prim1);
+        double mv[NDF];
+        mv[0] = mh;
+        if (NDF == 2) mv[NDF - 1] = mh * P.K / (2.0 * lam);
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            T v = (T)((gw * aux[(int64_t)k * nv + idx] + sw * (mv[k] * rho_w)) / (gw + sw));
+            wa[(int64_t)k * nv + idx] = v;
+            wb[(int64_t)k * nv + idx] = v;
+        }
+    }
+}
+
+// =============================================================================
+// flux + collision
+// =============================================================================
+template <int D, typename A>
+__device__ __forceinline__ A pp_recon(A f, const A* s, const double* ds, const A* dx) {
+    // positivity_preserving_reconstruct (Flux/CAIDVM.jl:127-142)
+    A sabs = 0, sdx = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) sabs += (A)ds[d] * fabs(s[d]);
+#pragma unroll
+    for (int d = 0; d < D; ++d) sdx += dx[d] * s[d];
+    A th = fabs((f - (A)JL_EPS) / ((A)0.5 * sabs + (A)EPS_REF));
+    th = th < (A)1 ? th : (A)1;
+    return f + th * sdx;
+}
+template <int D, typename A>
+__device__ __forceinline__ A plain_recon(A f, const A* s, const A* dx) {
+    A sdx = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) sdx += dx[d] * s[d];
+    return f + sdx;
+}
+
+// micro flux leaving data `dat` (velocity j of grid gv) through a face; mode 0 = positivity
+// reconstruction, 1 = plain reconstruction, 2 = unreconstructed
+template <int D, int NDF, typename T>
+__device__ __forceinline__ void side_micro(const Dev& P, int dat, int64_t fo, int nvd, const VGridView& gv, int j,
+                                           const double* fmid, const double* cmid, const double* ds, double dt, int dir,
+                                           int mode, typename Arith<T>::type* out) {
+    using A = typename Arith<T>::type;
+    const T* f = (const T*)P.f_in + fo;
+    const T* sdf = (const T*)P.sdf + fo * D;
+    A dx[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dx[d] = (A)(fmid[d] - gv.u(j, d) * dt - cmid[d]);
+    const A vn = (A)gv.u(j, dir);
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) {
+        A fk = (A)f[(int64_t)k * nvd + j];
+        if (mode == 2) { out[k] = fk * vn; continue; }
+        A s[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) s[d] = (A)sdf[((int64_t)d * NDF + k) * nvd + j];
+        out[k] = (mode == 0 ? pp_recon<D, A>(fk, s, ds, dx) : plain_recon<D, A>(fk, s, dx)) * vn;
+    }
+}
+
+template <int D, int NDF>
+__device__ __forceinline__ void psi_add(double* m, double wgt, const double* u, const double* v) {
+    // weight * ψ * micro, ψ = (1, u, |u|²/2 with b) as in micro_to_macro_*
+    double u2 = 0.0;
+    m[0] += wgt * v[0];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { m[1 + d] += wgt * u[d] * v[0]; u2 += u[d] * u[d]; }
+    if (NDF == 2) m[D + 1] += 0.5 * wgt * (u2 * v[0] + v[NDF - 1]);
+    else m[D + 1] += 0.5 * wgt * u2 * v[0];
+}
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, int64_t step, int check_interval) {
+    using A = typename Arith<T>::type;
+    extern __shared__ double sh[];
+    __shared__ Incidence sinc[MAX_INC];
+    __shared__ double srho[MAX_INC];
+    __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
+    __shared__ double sscal[4 * MAXW];
+    const int fcx = blockIdx.x;
+    const int cell = P.fluid_cells[fcx];
+    const int i0 = P.inc_off[fcx], ninc = P.inc_off[fcx + 1] - i0;
+    for (int e = threadIdx.x; e < ninc; e += BLOCK) sinc[e] = P.inc[i0 + e];
+    __syncthreads();
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const int64_t fo = P.foff[cell];
+    const T* fcell = (const T*)P.f_in + fo;
+    T* fnew = (T*)P.f_out + fo;
+    const double* vw = P.vw + g.goff;
+    const double* cds = P.dds + (int64_t)cell * MAXD;
+    double V = cds[0];
+#pragma unroll
+    for (int d = 1; d < D; ++d) V *= cds[d];
+    const double s_dt = dt / V;
+    double* fst = sh;                       // NDF * nv : convected f (then corrected f)
+    const bool caidvm = P.flux == KG_FLUX_CAIDVM;
+
+    // ---- 0. wall density of Maxwellian domain faces (calc_ρw, Theory/Math.jl:251-282) --
+    for (int e = 0; e < ninc; ++e) {
+        const Incidence& I = sinc[e];
+        if (!(I.kind == INC_DOMAIN && I.bc_kind == KG_BC_MAXWELL)) continue;
+        const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
+        double red[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            const double ud = g.u(i, I.dir);
+            if (I.orient * ud <= 0.0) {
+                // SF = Σ w u_n h_reconstructed over the outgoing half
+                A fk = (A)fcell[i];
+                A s[D], dx[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    s[d] = (A)((const T*)P.sdf)[(fo * D) + (int64_t)d * NDF * nv + i];
+                    dx[d] = (A)(I.fmid[d] - g.u(i, d) * dt - I.my_mid[d]);
+                }
+                red[0] += vw[i] * ud * (double)plain_recon<D, A>(fk, s, dx);
+            } else {
+                double c2 = 0.0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) { double cu = g.u(i, d) - bc[1 + d]; c2 += cu * cu; }
+                red[1] += vw[i] * ud * exp(-bc[D + 1] * c2);
+            }
+        }
+        block_sum<2>(red, sred);
+        if (threadIdx.x == 0) {
+            const double lam = bc[D + 1];
+            const double SG = (D == 2 ? lam / PI : pow(lam / PI, 1.5)) * red[1];
+            srho[e] = -red[0] / SG;
+        }
+        __syncthreads();
+    }
+
+    // ---- 1. fluxes gathered over the incidences; convected f into shared memory ----
+    double wacc[D + 2], wfc[D + 2];
+#pragma unroll
+    for (int e = 0; e < D + 2; ++e) { wacc[e] = 0.0; wfc[e] = 0.0; }
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const int li = P.vlev[g.goff + i];
+        double u[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) u[d] = g.u(i, d);
+        const double wi = vw[i];
+        double acc[NDF];
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) acc[k] = 0.0;
+        for (int e = 0; e < ninc; ++e) {
+            const Incidence& I = sinc[e];
+            const double ud = u[I.dir];
+            double mic[NDF];
+            if (I.orient * ud <= 0.0) {
+                // outgoing from this cell: its own reconstruction
+                A m[NDF];
+                int mode;
+                if (I.kind == INC_DOMAIN) mode = (I.bc_kind == KG_BC_OUTFLOW) ? 2 : 1;
+                else mode = (I.kind == INC_SOLID) ? 1 : 0;
+                side_micro<D, NDF, T>(P, cell, fo, nv, g, i, I.fmid, I.my_mid, cds, dt, I.dir, mode, m);
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
+                if (caidvm) {
+                    double t[D + 2];
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
+                    psi_add<D, NDF>(t, wi, u, mic);
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+                }
+            } else if (I.kind == INC_DOMAIN) {
+                const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
+                if (I.bc_kind == KG_BC_MAXWELL || I.bc_kind == KG_BC_INFLOW) {
+                    double pr[MAXW];
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) pr[q] = bc[q];
+                    if (I.bc_kind == KG_BC_MAXWELL) pr[0] = srho[e];
+                    const double mh = maxwell_h<D>(g, i, pr);
+                    mic[0] = mh * ud;
+                    if (NDF == 2) mic[NDF - 1] = mh * P.K / (2.0 * pr[D + 1]) * ud;
+                } else if (I.bc_kind == KG_BC_OUTFLOW) {
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) mic[k] = (double)fcell[(int64_t)k * nv + i] * ud;
+                } else {  // interpolated outflow (CAIDVM.jl:71-94)
+                    const T* sc = (const T*)P.sdf + fo * D;
+                    double tpm[D];
+#pragma unroll
+                    for (int d = 0; d < D; ++d) tpm[d] = 2.0 * I.fmid[d] - I.my_mid[d];
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) {
+                        double s[D];
+#pragma unroll
+                        for (int d = 0; d < D; ++d) s[d] = (double)sc[((int64_t)d * NDF + k) * nv + i];
+                        double tdf = (double)fcell[(int64_t)k * nv + i] + (tpm[I.dir] - I.my_mid[I.dir]) * s[I.dir];
+                        double sdx = 0.0;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) sdx += (I.fmid[d] - u[d] * dt - tpm[d]) * s[d];
+                        mic[k] = (tdf + sdx) * ud;
+                    }
+                }
+                if (caidvm) {
+                    double t[D + 2];
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
+                    psi_add<D, NDF>(t, wi, u, mic);
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+                }
+            } else {
+                // incoming: the other side's micro flux mapped onto this grid
+                const int od = I.other;
+                const int64_t ofo = P.foff[od];
+                const int onv = (int)((P.foff[od + 1] - ofo) / NDF);
+                int mode;
+                if (I.kind == INC_SOLID) mode = caidvm ? 2 : 1;
+                else mode = 0;
+                if (I.pair < 0) {
+                    A m[NDF];
+                    side_micro<D, NDF, T>(P, od, ofo, onv, g, i, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
+                    if (caidvm) {
+                        double t[D + 2];
+#pragma unroll
+                        for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
+                        psi_add<D, NDF>(t, wi, u, mic);
+#pragma unroll
+                        for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+                    }
+                } else {
+                    const VGridView go = grid_view(P, od);
+                    const int64_t po = P.p_off[I.pair] + i;
+                    const int j0 = P.p_j0[po], jc = P.p_cnt[po];
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) mic[k] = 0.0;
+                    for (int j = j0; j < j0 + jc; ++j) {
+                        A m[NDF];
+                        side_micro<D, NDF, T>(P, od, ofo, onv, go, j, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
+                        const double sc = merge_inv_scale<D>(li, P.vlev[go.goff + j]);
+#pragma unroll
+                        for (int k = 0; k < NDF; ++k) mic[k] += (double)m[k] * sc;
+                    }
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) acc[k] += I.sarea * mic[k];
+        }
+        double fv[NDF], fs[NDF];
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            fv[k] = (double)fcell[(int64_t)k * nv + i];
+            fs[k] = fv[k] + s_dt * acc[k];
+            fst[(int64_t)k * nv + i] = fs[k];
+        }
+        // CAIDVM: moments of the convected f; Euler+DVM: moments of f before convection
+        if (P.marching == KG_MARCH_CAIDVM) moments_add<D, NDF>(g, wi, i, fs, wfc);
+        else moments_add<D, NDF>(g, wi, i, fv, wfc);
+    }
+    // macro flux of incoming halves whose grid differs (moments on the other side's grid)
+    if (caidvm) {
+        for (int e = 0; e < ninc; ++e) {
+            const Incidence& I = sinc[e];
+            if (I.kind == INC_DOMAIN || I.pair < 0) continue;
+            const int od = I.other;
+            const VGridView go = grid_view(P, od);
+            const int64_t ofo = P.foff[od];
+            const int onv = go.nv;
+            const int mode = I.kind == INC_SOLID ? 2 : 0;
+            for (int j = threadIdx.x; j < onv; j += BLOCK) {
+                const double ud = go.u(j, I.dir);
+                if (I.orient * ud <= 0.0) continue;   // not leaving the other side towards us
+                A m[NDF];
+                side_micro<D, NDF, T>(P, od, ofo, onv, go, j, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
+                double mic[NDF], uo[D], t[D + 2];
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
+#pragma unroll
+                for (int d = 0; d < D; ++d) uo[d] = go.u(j, d);
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
+                psi_add<D, NDF>(t, P.vw[go.goff + j], uo, mic);
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+            }
+        }
+    }
+    // ---- 2. cell scalars ---------------------------------------------------------
+    {
+        double red[2 * (D + 2)];
+#pragma unroll
+        for (int q = 0; q < D + 2; ++q) { red[q] = wacc[q]; red[D + 2 + q] = wfc[q]; }
+        block_sum<2 * (D + 2)>(red, sred);
+        if (threadIdx.x == 0) {
+            double* w = P.w + (int64_t)cell * MAXW;
+            double wn[MAXW], pc[MAXW], pn[MAXW];
+            if (P.marching == KG_MARCH_CAIDVM) {
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
+                get_prim<D>(wn, P.gamma, pc);
+                double wf[MAXW];
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) wf[q] = red[D + 2 + q];
+                get_prim<D>(wf, P.gamma, pn);
+            } else {
+                if (P.flux == KG_FLUX_DVM) {
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) wn[q] = red[D + 2 + q];
+                } else {
+#pragma unroll
+                    for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
+                }
+                get_prim<D>(wn, P.gamma, pc);
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) pn[q] = pc[q];
+            }
+#pragma unroll
+            for (int q = 0; q < D + 2; ++q) { w[q] = wn[q]; sscal[q] = pc[q]; sscal[MAXW + q] = pn[q]; }
+            const double tau = P.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - P.omega) / pc[0];
+            sscal[2 * MAXW] = tau;
+            int bad = 0;
+            for (int q = 0; q < D + 2; ++q) if (!isfinite(pc[q])) bad |= ST_NONFINITE;
+            if (!(pc[0] > 0.0) || !(pc[D + 1] > 0.0)) bad |= ST_NEGATIVE;
+            if (bad) atomicOr(P.status, bad);
+        }
+        __syncthreads();
+    }
+    double pc[MAXW], pn[MAXW];
+#pragma unroll
+    for (int q = 0; q < D + 2; ++q) { pc[q] = sscal[q]; pn[q] = sscal[MAXW + q]; }
+    const double tau = sscal[2 * MAXW];
+    // ---- 3. conservation correction and heat flux --------------------------------
+    double qv[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) qv[d] = 0.0;
+    const double lamc = pc[D + 1];
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        double fv[NDF];
+        if (P.marching == KG_MARCH_CAIDVM) {
+            const double mc = maxwell_h<D>(g, i, pc);
+            const double mn = maxwell_h<D>(g, i, pn);
+            fv[0] = fst[i] + (mc - mn);
+            if (NDF == 2) fv[NDF - 1] = fst[nv + i] + (mc * P.K / (2.0 * lamc) - mn * P.K / (2.0 * pn[D + 1]));
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fst[(int64_t)k * nv + i] = fv[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fv[k] = (double)fcell[(int64_t)k * nv + i];
+        }
+        // heat_flux_2D2F / 3D1F (lib/KitCore/2D2F.jl:68-88, 3D1F.jl:41-72)
+        double c[D], c2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { c[d] = g.u(i, d) - pc[1 + d]; c2 += c[d] * c[d]; }
+        const double wi = vw[i];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            if (NDF == 2) qv[d] += wi * c[d] * (c2 * fv[0] + fv[NDF - 1]);
+            else qv[d] += wi * c[d] * c2 * fv[0];
+        }
+    }
+    block_sum<D>(qv, sred);
+#pragma unroll
+    for (int d = 0; d < D; ++d) qv[d] *= 0.5;
+    // ---- 4. Shakhov g+ and implicit relaxation -------------------------------------
+    const double r1 = tau / (tau + dt), r2 = dt / (tau + dt);
+    const double sk = 0.8 * (1.0 - P.Pr) * lamc * lamc / pc[0];
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const double mc = maxwell_h<D>(g, i, pc);
+        double c[D], c2 = 0.0, cq = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { c[d] = g.u(i, d) - pc[1 + d]; c2 += c[d] * c[d]; cq += c[d] * qv[d]; }
+        double gp[NDF];
+        if (NDF == 2) {
+            const double mb = mc * P.K / (2.0 * lamc);
+            gp[0] = mc + sk * cq * (2.0 * lamc * c2 + P.K - 5.0) * mc;
+            gp[NDF - 1] = mb + sk * cq * (2.0 * lamc * c2 + P.K - 3.0) * mb;
+        } else {
+            gp[0] = mc + sk * cq * (2.0 * lamc * c2 - 5.0) * mc;
+        }
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            double v;
+            if (P.marching == KG_MARCH_CAIDVM) v = fst[(int64_t)k * nv + i] * r1 + r2 * gp[k];
+            else v = fst[(int64_t)k * nv + i] * tau / (tau + dt) + r2 * gp[k];
+            fnew[(int64_t)k * nv + i] = (T)v;
+        }
+    }
+    // ---- 5. per-cell outputs and residual terms ------------------------------------
+    if (threadIdx.x == 0) {
+        double* pr = P.prim + (int64_t)cell * MAXW;
+        double* res = P.cell_res + (int64_t)fcx * 2 * MAXW;
+        const bool chk = (step % check_interval) == 0;
+#pragma unroll
+        for (int q = 0; q < D + 2; ++q) {
+            const double dl = pc[q] - pr[q];
+            res[q] = chk ? dl * dl : 0.0;
+            res[MAXW + q] = chk ? fabs(pc[q]) : 0.0;
+            pr[q] = pc[q];
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d) P.qf[(int64_t)cell * MAXD + d] = qv[d];
+    }
+}
+
+// Deterministic Σ of the per-cell residual terms (one CTA).
+__global__ void __launch_bounds__(BLOCK) residual_kernel(const double* cell_res, int n, double* out) {
+    __shared__ double sred[2 * MAXW * (BLOCK / 32)];
+    double v[2 * MAXW];
+#pragma unroll
+    for (int q = 0; q < 2 * MAXW; ++q) v[q] = 0.0;
+    for (int c = threadIdx.x; c < n; c += BLOCK)
+#pragma unroll
+        for (int q = 0; q < 2 * MAXW; ++q) v[q] += cell_res[(int64_t)c * 2 * MAXW + q];
+    block_sum<2 * MAXW>(v, sred);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < 2 * MAXW; ++q) out[q] = v[q];
+}
+
+// ---- launchers ------------------------------------------------------------------
+template <int D, int NDF, typename T>
+struct Launch {
+    static cudaError_t slope(const Dev& P, int pc_base, int n, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, pc_base);
+        return cudaGetLastError();
+    }
+    static cudaError_t solid(const Dev& P, int n, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        solid_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P);
+        return cudaGetLastError();
+    }
+    static cudaError_t wall(const Dev& P, int n, int max_nv, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        size_t smem = (size_t)NDF * max_nv * sizeof(double);
+        cudaError_t e = cudaFuncSetAttribute(wall_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        wall_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
+        return cudaGetLastError();
+    }
+    static cudaError_t flux(const Dev& P, int n, int max_nv, double dt, int64_t step, int check, cudaStream_t s) {
+        size_t smem = (size_t)NDF * max_nv * sizeof(double);
+        cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, dt, step, check);
+        return cudaGetLastError();
+    }
+};
+
+cudaError_t launch_residual(const double* cell_res, int n, double* out, cudaStream_t s) {
+    residual_kernel<<<1, BLOCK, 0, s>>>(cell_res, n, out);
+    return cudaGetLastError();
+}
+
+// explicit instantiations: 2D two-distribution and 3D one-distribution, plain and mixed
+template struct Launch<2, 2, double>;
+template struct Launch<3, 1, double>;
+template struct Launch<2, 2, float>;
+template struct Launch<3, 1, float>;
+
+}  // namespace kg

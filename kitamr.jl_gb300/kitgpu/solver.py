@@ -1,0 +1,145 @@
+"""Python host mirror of the GPU step: ctypes binding of libkitgpu.so.
+
+The reference advances a step with ``slope!(p4est, ka); flux!(p4est, ka); iterate!(p4est, ka)``
+(src/Solver/Solver.jl:65-67).  ``GpuStep.step`` is that triple on the device; the state
+moves to and from the host only through ``upload_state`` / ``download_state`` (the sync
+points around adaptation, output and restart).  There is no CPU fallback: loading fails
+with an exception when the library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import abi
+from .build import LIB
+
+_lib = None
+
+
+def load_library(path: Optional[str] = None):
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or os.environ.get("KITGPU_LIB", LIB)
+    if not os.path.exists(p):
+        raise RuntimeError(f"libkitgpu.so not built ({p}); run kitgpu/build.py or __graft_entry__.build()")
+    L = C.CDLL(p)
+    vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    L.kg_create.argtypes = [vp, C.c_int, C.POINTER(vp)]
+    L.kg_destroy.argtypes = [vp]
+    L.kg_upload_topology.argtypes = [vp, vp]
+    L.kg_upload_state.argtypes = [vp, vp, vp, vp]
+    L.kg_download_state.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.kg_step.argtypes = [vp, dbl, i64, i32, vp]
+    L.kg_profile_enable.argtypes = [vp, C.c_int]
+    L.kg_profile_read.argtypes = [vp, C.POINTER(C.c_char_p), C.POINTER(dbl), C.POINTER(i64), i32, C.POINTER(i32)]
+    L.kg_memory_footprint.argtypes = [vp, C.POINTER(i64)]
+    L.kg_topology_footprint.argtypes = [vp, vp, C.POINTER(i64)]
+    L.kg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
+    L.kg_use_graph.argtypes = [vp, C.c_int]
+    _lib = L
+    return L
+
+
+EXPORTS = [
+    "kg_create", "kg_destroy", "kg_upload_topology", "kg_upload_state", "kg_download_state",
+    "kg_step", "kg_profile_enable", "kg_profile_read", "kg_memory_footprint",
+    "kg_topology_footprint", "kg_last_error", "kg_use_graph",
+]
+
+
+class KitGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{abi.ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _check(L, h, rc):
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        L.kg_last_error(h, buf, 1024)
+        raise KitGpuError(rc, buf.value.decode(errors="replace"))
+
+
+def topology_footprint(params: abi.KgParams, topo: Dict) -> int:
+    L = load_library()
+    tref = abi.TopologyRef(topo)
+    b = C.c_int64()
+    _check(L, None, L.kg_topology_footprint(C.byref(params), C.cast(tref.ptr, C.c_void_p), C.byref(b)))
+    return b.value
+
+
+class GpuStep:
+    """One libkitgpu handle holding one topology and its state on one device."""
+
+    def __init__(self, params: abi.KgParams, topo: Dict, device: int = 0):
+        self.L = load_library()
+        self.params = params
+        self.topo = topo
+        h = C.c_void_p()
+        _check(self.L, None, self.L.kg_create(C.byref(params), device, C.byref(h)))
+        self.h = h
+        self._tref = abi.TopologyRef(topo)
+        _check(self.L, self.h, self.L.kg_upload_topology(self.h, C.cast(self._tref.ptr, C.c_void_p)))
+        from .mesh import f_offsets
+        self.foff = f_offsets(topo)
+        self.nc = int(topo["n_cells"])
+        self.dim = int(topo["dim"])
+
+    def close(self):
+        if self.h:
+            self.L.kg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload_state(self, f: np.ndarray, w: np.ndarray, prim: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        assert f.size == self.foff[-1] and w.size == self.nc * (self.dim + 2)
+        _check(self.L, self.h, self.L.kg_upload_state(self.h, f.ctypes.data, w.ctypes.data, prim.ctypes.data))
+
+    def step(self, dt: float, step0: int, nsteps: int) -> abi.KgStepReport:
+        rep = abi.KgStepReport()
+        _check(self.L, self.h, self.L.kg_step(self.h, dt, step0, nsteps, C.byref(rep)))
+        return rep
+
+    def download_state(self, sdf: bool = False) -> Dict[str, np.ndarray]:
+        nf = int(self.foff[-1])
+        out = dict(f=np.empty(nf), w=np.empty(self.nc * (self.dim + 2)), prim=np.empty(self.nc * (self.dim + 2)),
+                   qf=np.empty(self.nc * self.dim))
+        if sdf:
+            out["sdf"] = np.empty(nf * self.dim)
+        _check(self.L, self.h, self.L.kg_download_state(
+            self.h, out["f"].ctypes.data, out["w"].ctypes.data, out["prim"].ctypes.data, out["qf"].ctypes.data,
+            out["sdf"].ctypes.data if sdf else None))
+        return out
+
+    def profile(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
+
+    def profile_read(self):
+        cap = 16
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        cnt = (C.c_int64 * cap)()
+        n = C.c_int32()
+        _check(self.L, self.h, self.L.kg_profile_read(self.h, names, ms, cnt, cap, C.byref(n)))
+        return {names[i].decode(): (ms[i], cnt[i]) for i in range(min(n.value, cap))}
+
+    def use_graph(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_use_graph(self.h, int(enable)))
+
+    def memory_footprint(self) -> int:
+        b = C.c_int64()
+        _check(self.L, self.h, self.L.kg_memory_footprint(self.h, C.byref(b)))
+        return b.value

@@ -1,0 +1,93 @@
+"""ctypes front end of the FP64 CPU oracle (oracle/kg_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as the
+checker, and by bench.py for the CPU baseline.  The product path never uses it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+from typing import Dict, Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libkgoracle.so")
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "kitamr.jl_gb300"))
+from kitgpu import abi  # noqa: E402
+
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "kg_oracle.cpp")):
+            build()
+        L = C.CDLL(LIB)
+        L.kgo_sizes.argtypes = [C.c_void_p] + [C.POINTER(C.c_int64)] * 4
+        L.kgo_run.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_int64, C.c_int32] + \
+            [C.POINTER(C.c_double)] * 7 + [C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                           C.POINTER(C.c_int32), C.c_int32]
+        L.kgo_moments.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4
+        L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        _lib = L
+    return _lib
+
+
+class OracleState:
+    """Full state of one problem as the oracle advances it (cells and wall records)."""
+
+    def __init__(self, topo: Dict, state: Dict):
+        self.topo = topo
+        self.tref = abi.TopologyRef(topo)
+        n = [C.c_int64() for _ in range(4)]
+        lib().kgo_sizes(C.cast(self.tref.ptr, C.c_void_p), *[C.byref(x) for x in n])
+        nf, nsdf, nwf, nwsdf = [x.value for x in n]
+        self.f = np.ascontiguousarray(state["f"], dtype=np.float64).copy()
+        assert self.f.size == nf, (self.f.size, nf)
+        self.sdf = np.zeros(max(nsdf, 1))
+        self.w = np.ascontiguousarray(state["w"], dtype=np.float64).copy()
+        self.prim = np.ascontiguousarray(state["prim"], dtype=np.float64).copy()
+        dim = topo["dim"]
+        self.qf = np.zeros(max(topo["n_cells"] * dim, 1))
+        # SolidNeighbor df starts as a copy of the donor's df (Immersed_boundary.jl:290-298)
+        self.wall_f = np.zeros(max(nwf, 1))
+        self.wall_sdf = np.zeros(max(nwsdf, 1))
+        if topo["n_walls"]:
+            from kitgpu.mesh import f_offsets
+            off = f_offsets(topo)
+            pos = 0
+            for wd in topo["wall_donor"]:
+                blk = self.f[off[wd]:off[wd + 1]]
+                self.wall_f[pos:pos + blk.size] = blk
+                pos += blk.size
+        self.sum_res = np.zeros(5)
+        self.sum_avg = np.zeros(5)
+        self.checked = C.c_int32(0)
+
+    def run(self, params, dt: float, step0: int, nsteps: int, nthreads: int = 1):
+        rc = lib().kgo_run(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), dt, step0, nsteps,
+                           abi.dptr(self.f), abi.dptr(self.sdf), abi.dptr(self.w), abi.dptr(self.prim),
+                           abi.dptr(self.qf), abi.dptr(self.wall_f), abi.dptr(self.wall_sdf),
+                           abi.dptr(self.sum_res), abi.dptr(self.sum_avg), C.byref(self.checked), nthreads)
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            lib().kgo_last_error(buf, 512)
+            raise RuntimeError(f"oracle failed: {abi.ERRORS.get(rc, rc)}: {buf.value.decode()}")
+        return self
+
+    def moments(self, params):
+        nc, nw = self.topo["n_cells"], self.topo["dim"] + 2
+        w = np.zeros(nc * nw)
+        q = np.zeros(nc * self.topo["dim"])
+        lib().kgo_moments(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.f),
+                          abi.dptr(self.prim), abi.dptr(w), abi.dptr(q))
+        return w.reshape(nc, nw), q.reshape(nc, self.topo["dim"])

@@ -1,0 +1,59 @@
+"""GPU parity through the C-ABI: libkitgpu.so against the FP64 oracle on the same inputs."""
+import numpy as np
+import pytest
+
+from kitgpu import abi, cases
+from parity import TOL_FP64, TOL_MIXED, f_error, moment_errors, run_pair
+
+pytestmark = pytest.mark.gpu
+
+CASES_FP64 = [
+    ("couette", lambda: cases.couette(n=12, nv=16), 6),
+    ("cavity_levels", lambda: cases.cavity(n=8, nv=16, levels=2), 6),
+    ("sod_levels", lambda: cases.sod(scale=0.125, nv=16), 6),
+    ("cylinder_ib_adapted", lambda: cases.cylinder(scale=0.25, nv=24, vs_levels=2), 4),
+    ("box3d_levels", lambda: cases.box3d(n=(6, 4, 4), nv=8, levels=1), 4),
+]
+
+
+@pytest.mark.parametrize("name,make,nsteps", CASES_FP64, ids=[c[0] for c in CASES_FP64])
+def test_fp64_caidvm_matches_oracle(name, make, nsteps):
+    topo, ref, out, rep = run_pair(make(), nsteps)
+    errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
+    errs["f"] = f_error(topo, ref.f, out["f"])
+    bad = {k: v for k, v in errs.items() if not v <= TOL_FP64}
+    assert not bad, f"{name}: {bad}"
+    assert rep.kernel_launches > 0
+    # residual sums of the last checked step
+    nw = topo["dim"] + 2
+    assert np.allclose(np.array(rep.sum_res[:nw]), ref.sum_res[:nw], rtol=1e-9, atol=1e-300)
+    assert np.allclose(np.array(rep.sum_avg[:nw]), ref.sum_avg[:nw], rtol=1e-12)
+
+
+@pytest.mark.parametrize("flux,march", [(abi.KG_FLUX_CAIDVM, abi.KG_MARCH_EULER), (abi.KG_FLUX_DVM, abi.KG_MARCH_EULER)])
+def test_fp64_euler_and_dvm(flux, march):
+    p = cases.sod(scale=0.125, nv=16)
+    topo, ref, out, rep = run_pair(p, 4, flux=flux, march=march)
+    errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
+    errs["f"] = f_error(topo, ref.f, out["f"])
+    bad = {k: v for k, v in errs.items() if not v <= TOL_FP64}
+    assert not bad, bad
+
+
+def test_fp64_chunked_calls_and_graph_match_single_call():
+    p = cases.cylinder(scale=0.25, nv=16, vs_levels=1)
+    topo, ref, out1, _ = run_pair(p, 6, chunks=1)
+    _, _, out2, _ = run_pair(p, 6, chunks=3)
+    _, _, out3, _ = run_pair(p, 6, chunks=3, graph=True)
+    assert np.array_equal(out1["f"], out2["f"])
+    assert np.array_equal(out1["f"], out3["f"])
+    assert f_error(topo, ref.f, out1["f"]) <= TOL_FP64
+
+
+@pytest.mark.parametrize("name,make,nsteps", CASES_FP64[:4], ids=[c[0] for c in CASES_FP64[:4]])
+def test_mixed_within_1e5_of_fp64(name, make, nsteps):
+    topo, ref, out, rep = run_pair(make(), nsteps, precision=abi.KG_PREC_MIXED)
+    errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
+    keep = {k: v for k, v in errs.items() if k in ("rho", "T") or k.startswith("U") or k.startswith("q")}
+    bad = {k: v for k, v in keep.items() if not v <= TOL_MIXED}
+    assert not bad, f"{name}: {bad}"
