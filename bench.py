@@ -119,7 +119,7 @@ def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     from kitgpu import cases
-    prob = make_problem()
+    prob = make_problem(args.scale)
     topo, state = cases.build(prob)
     P = mesh.phase_cells(topo)
     dt = prob.dt()
@@ -221,6 +221,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (profiling captures)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -280,7 +281,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-f/f64-moments",
         "data": "synthetic (seeded cylinder_buffer_IC state on a generated forest)",
-        "config": {"workload": WORKLOAD, "phase_cells": P, "form": "mixed", "l2": "inputs > L2 (f is 488 MB FP32)",
+        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} at scale {args.scale}",
+                   "phase_cells": P, "form": "mixed", "l2": "inputs > L2 (f is 488 MB FP32)",
                    "parallelism": f"replicas{world}"},
         "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
                   "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
