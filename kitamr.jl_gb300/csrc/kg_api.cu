@@ -295,6 +295,8 @@ int kg_upload_topology(kg_handle* h, const kg_topology* topo) {
     P.PG = (int64_t)F.vw.size();
 #define UP(field, vec) do { int r__ = upload(h, F.vec, &P.field); if (r__) return r__; } while (0)
     UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
+    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(vidx, vidx);
+    P.max_axis = F.max_axis;
     UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds);
     UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
     UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);

@@ -24,6 +24,12 @@ struct Dev {
     const int8_t* vlev;
     const double* vw;
     const double* vu;                  // [dim][PG]
+    const float* vuf;                  // FP32 copies (mixed form)
+    const float* vwf;
+    const int32_t* ax_off;             // axis tables of the factorised Maxwellian
+    const double* ax_val;
+    const uint16_t* vidx;
+    int max_axis;
     // data table
     const int64_t* foff;
     const int32_t* dgrid;

@@ -120,6 +120,34 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
                 if (m[(size_t)d * nv + i] == 0.0) { err = "a velocity midpoint lies on u_d = 0 (v = 0 must be a root corner)"; return KG_ERR_TOPOLOGY; }
     }
 
+    F.vuf.assign(F.vu.begin(), F.vu.end());
+    F.vwf.assign(F.vw.begin(), F.vw.end());
+    // axis tables: exp(-λ|u-U|²) = Π_d exp(-λ(u_d-U_d)²), so a Maxwellian on a grid needs the
+    // 1D factors at the distinct coordinates only
+    F.ax_off.assign((size_t)t.n_grids * MAXD + 1, 0);
+    F.vidx.assign((size_t)D * PG, 0);
+    for (int g = 0; g < t.n_grids; ++g) {
+        int nv = grid_nv(t, g);
+        for (int d = 0; d < MAXD; ++d) {
+            size_t slot = (size_t)g * MAXD + d;
+            F.ax_off[slot] = (int32_t)F.ax_val.size();
+            if (d < D) {
+                std::vector<double> vals(F.vu.begin() + (size_t)d * PG + t.grid_off[g],
+                                         F.vu.begin() + (size_t)d * PG + t.grid_off[g] + nv);
+                std::sort(vals.begin(), vals.end());
+                vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
+                if (vals.size() > 65535) { err = "more than 65535 distinct velocity coordinates on an axis"; return KG_ERR_TOPOLOGY; }
+                F.max_axis = std::max(F.max_axis, (int)vals.size());
+                for (int i = 0; i < nv; ++i) {
+                    double x = F.vu[(size_t)d * PG + t.grid_off[g] + i];
+                    F.vidx[(size_t)d * PG + t.grid_off[g] + i] = (uint16_t)(std::lower_bound(vals.begin(), vals.end(), x) - vals.begin());
+                }
+                F.ax_val.insert(F.ax_val.end(), vals.begin(), vals.end());
+            }
+            F.ax_off[slot + 1] = (int32_t)F.ax_val.size();
+        }
+    }
+
     // ---- data table: cells then walls -------------------------------------------
     F.foff.assign(F.n_data + 1, 0);
     F.dgrid.resize(F.n_data); F.dbe.resize(F.n_data);
@@ -265,6 +293,13 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
                 if (rc) return rc;
                 F.slope_ops.push_back(op);
             }
+            int nlist = 0;
+            for (int dir = 0; dir < D; ++dir) {
+                const SlopeOp& o = F.slope_ops[F.slope_ops.size() - D + dir];
+                if (o.kind == SLOPE_ONE || o.kind == SLOPE_TWO) nlist += o.cntA;
+                if (o.kind == SLOPE_TWO) nlist += o.cntB;
+            }
+            if (nlist > 2 * MAXD * 4) { err = "a cell's slope neighbour lists exceed 24 entries (not 2:1 balanced)"; return KG_ERR_TOPOLOGY; }
         }
         F.pass_off.push_back((int32_t)F.slope_ops.size());
         F.pass_cells_off.push_back((int32_t)F.pass_cells.size());

@@ -79,6 +79,13 @@ struct Flat {
     std::vector<int8_t> vlev;
     std::vector<double> vw;
     std::vector<double> vu;       // [dim][P_g] (dimension-major)
+    std::vector<float> vuf, vwf;  // FP32 copies for the mixed form
+    // factorised Maxwellian: per grid and dimension the distinct midpoint coordinates
+    // ("axis values") and, per velocity cell, the index of its coordinate on each axis
+    std::vector<int32_t> ax_off;  // n_grids * MAXD + 1
+    std::vector<double> ax_val;
+    std::vector<uint16_t> vidx;   // [dim][P_g]
+    int max_axis = 0;
     // data table
     std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)
     std::vector<int32_t> dgrid, dbe;

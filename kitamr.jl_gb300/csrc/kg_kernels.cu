@@ -40,6 +40,18 @@ template <> struct Acc<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
+// velocity metadata in the arithmetic precision (FP32 copies for the mixed form)
+template <typename A> __device__ __forceinline__ const A* vel(const Dev& P);
+template <> __device__ __forceinline__ const double* vel<double>(const Dev& P) { return P.vu; }
+template <> __device__ __forceinline__ const float* vel<float>(const Dev& P) { return P.vuf; }
+template <typename A> __device__ __forceinline__ const A* wts(const Dev& P);
+template <> __device__ __forceinline__ const double* wts<double>(const Dev& P) { return P.vw; }
+template <> __device__ __forceinline__ const float* wts<float>(const Dev& P) { return P.vwf; }
+// 2^-(D*(lj-li)) when the source cell is finer (exact power of two), else 1
+template <int D, typename A> __device__ __forceinline__ A merge_scale(int li, int lj) {
+    return lj > li ? (A)ldexpf(1.0f, -D * (lj - li)) : (A)1;
+}
+
 struct VGridView {
     int64_t goff;
     int nv;
@@ -61,25 +73,32 @@ __device__ __forceinline__ VGridView grid_view(const Dev& P, int data) {
 // =============================================================================
 // slope
 // =============================================================================
+// per-neighbour constants of a slope list, in the arithmetic precision (set up once per CTA)
+template <typename A> struct SlopeNbrA {
+    A dm[MAXD];      // transverse midpoint offsets (0 when the list is not projected)
+    int32_t data, pair, any;
+};
+constexpr int MAX_SLOPE_NBR = 2 * MAXD * 4;   // 2 sides x dim x 2^(dim-1) neighbours
+
 template <int D, int NDF, typename T>
-__device__ __forceinline__ void slope_side(const Dev& P, int cell, int dir, int i, int li, const double* fc,
-                                           int list, int cnt, double inv_ds, bool proj, double* s) {
+__device__ __forceinline__ void slope_side(const Dev& P, int i, int li, const typename Arith<T>::type* fc,
+                                           const SlopeNbrA<typename Arith<T>::type>* nb, int cnt,
+                                           typename Arith<T>::type inv_ds, typename Arith<T>::type inv_cnt,
+                                           typename Arith<T>::type* s) {
     using A = typename Arith<T>::type;
     const T* f = (const T*)P.f_in;
     const T* sdf = (const T*)P.sdf;
     A acc[NDF];
 #pragma unroll
     for (int k = 0; k < NDF; ++k) acc[k] = 0;
-    const double* cm = P.dmid + (int64_t)cell * MAXD;
     for (int n = 0; n < cnt; ++n) {
-        NbrRef r = P.slope_nbr[list + n];
+        const SlopeNbrA<A>& r = nb[n];
         const int64_t fo = P.foff[r.data];
         const int nvn = (int)((P.foff[r.data + 1] - fo) / NDF);
         const T* fn = f + fo;
         const T* sn = sdf + fo * D;
-        A dm[D];
-#pragma unroll
-        for (int t = 0; t < D; ++t) dm[t] = (proj && t != dir) ? (A)(cm[t] - P.dmid[(int64_t)r.data * MAXD + t]) : (A)0;
+        const bool any = r.any;
+        const A* dm = r.dm;
         int j0 = i, jc = 1;
         int64_t gn = 0;
         if (r.pair >= 0) {
@@ -89,20 +108,21 @@ __device__ __forceinline__ void slope_side(const Dev& P, int cell, int dir, int 
             gn = P.g_off[P.dgrid[r.data]];
         }
         for (int j = j0; j < j0 + jc; ++j) {
-            A sc = 1;
-            if (r.pair >= 0) sc = (A)merge_inv_scale<D>(li, P.vlev[gn + j]);
+            const A sc = r.pair >= 0 ? merge_scale<D, A>(li, P.vlev[gn + j]) : (A)1;
 #pragma unroll
             for (int k = 0; k < NDF; ++k) {
                 A p = (A)fn[(int64_t)k * nvn + j];
+                if (any) {
 #pragma unroll
-                for (int t = 0; t < D; ++t)
-                    if (dm[t] != (A)0) p += dm[t] * (A)sn[((int64_t)t * NDF + k) * nvn + j];
-                acc[k] += ((A)fc[k] - p) * sc * (A)inv_ds;
+                    for (int t = 0; t < D; ++t)
+                        if (dm[t] != (A)0) p += dm[t] * (A)sn[((int64_t)t * NDF + k) * nvn + j];
+                }
+                acc[k] += (fc[k] - p) * sc * inv_ds;
             }
         }
     }
 #pragma unroll
-    for (int k = 0; k < NDF; ++k) s[k] = (double)(acc[k] / (A)cnt);
+    for (int k = 0; k < NDF; ++k) s[k] = acc[k] * inv_cnt;
 }
 
 template <int D, int NDF, typename T>
@@ -117,32 +137,63 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
     const T* fcell = (const T*)P.f_in + fo;
     T* scell = (T*)P.sdf + fo * D;
     __shared__ SlopeOp ops[MAXD];
+    __shared__ SlopeNbrA<A> snb[MAX_SLOPE_NBR];
+    __shared__ int sbase[2 * MAXD];
+    __shared__ A sconst[4 * MAXD];   // inv_dsA, inv_dsB, 1/cntA, 1/cntB per direction
     if (threadIdx.x < D) ops[threadIdx.x] = P.slope_ops[op0 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const double* cm = P.dmid + (int64_t)cell * MAXD;
+        int n = 0;
+        for (int dir = 0; dir < D; ++dir) {
+            const SlopeOp& op = ops[dir];
+            for (int side = 0; side < 2; ++side) {
+                const int list = side == 0 ? op.listA : op.listB;
+                const int cnt = (op.kind == SLOPE_ONE || op.kind == SLOPE_TWO) ? (side == 0 ? op.cntA : (op.kind == SLOPE_TWO ? op.cntB : 0)) : 0;
+                const bool proj = side == 0 ? op.projA : op.projB;
+                sbase[2 * dir + side] = n;
+                for (int j = 0; j < cnt && n < MAX_SLOPE_NBR; ++j, ++n) {
+                    NbrRef r = P.slope_nbr[list + j];
+                    SlopeNbrA<A> e;
+                    e.data = r.data; e.pair = r.pair; e.any = 0;
+                    for (int t = 0; t < MAXD; ++t) {
+                        e.dm[t] = (t < D && proj && t != dir) ? (A)(cm[t] - P.dmid[(int64_t)r.data * MAXD + t]) : (A)0;
+                        e.any |= e.dm[t] != (A)0;
+                    }
+                    snb[n] = e;
+                }
+            }
+            sconst[4 * dir + 0] = (A)op.inv_dsA;
+            sconst[4 * dir + 1] = (A)op.inv_dsB;
+            sconst[4 * dir + 2] = op.cntA > 0 ? (A)(1.0 / op.cntA) : (A)0;
+            sconst[4 * dir + 3] = op.cntB > 0 ? (A)(1.0 / op.cntB) : (A)0;
+        }
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
-        double fc[NDF];
+        A fc[NDF];
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) fc[k] = (double)fcell[(int64_t)k * nv + i];
+        for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[(int64_t)k * nv + i];
 #pragma unroll
         for (int dir = 0; dir < D; ++dir) {
             const SlopeOp& op = ops[dir];
             if (op.kind == SLOPE_SKIP) continue;
-            double out[NDF];
+            A out[NDF];
             if (op.kind == SLOPE_ZERO) {
 #pragma unroll
-                for (int k = 0; k < NDF; ++k) out[k] = 0.0;
+                for (int k = 0; k < NDF; ++k) out[k] = 0;
             } else {
-                double sA[NDF];
-                slope_side<D, NDF, T>(P, cell, dir, i, li, fc, op.listA, op.cntA, op.inv_dsA, op.projA, sA);
+                A sA[NDF];
+                slope_side<D, NDF, T>(P, i, li, fc, &snb[sbase[2 * dir]], op.cntA, sconst[4 * dir], sconst[4 * dir + 2], sA);
                 if (op.kind == SLOPE_ONE) {
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) out[k] = sA[k];
                 } else {
-                    double sB[NDF];
-                    slope_side<D, NDF, T>(P, cell, dir, i, li, fc, op.listB, op.cntB, op.inv_dsB, op.projB, sB);
+                    A sB[NDF];
+                    slope_side<D, NDF, T>(P, i, li, fc, &snb[sbase[2 * dir + 1]], op.cntB, sconst[4 * dir + 1], sconst[4 * dir + 3], sB);
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) out[k] = (double)minmod((A)sA[k], (A)sB[k]);
+                    for (int k = 0; k < NDF; ++k) out[k] = minmod(sA[k], sB[k]);
                 }
             }
 #pragma unroll
@@ -431,31 +482,123 @@ __device__ __forceinline__ void psi_add(double* m, double wgt, const double* u, 
     else m[D + 1] += 0.5 * wgt * u2 * v[0];
 }
 
+// Compensated (Kahan) accumulator for the FP32 arithmetic of the mixed form; plain sum in FP64.
+template <typename A> struct KSum {
+    A s = 0, c = 0;
+    __device__ __forceinline__ void add(A x) { A y = x - c; A t = s + y; c = (t - s) - y; s = t; }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <> struct KSum<double> {
+    double s = 0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// own-side reconstruction from registers (positivity / plain / none)
+template <int D, typename A>
+__device__ __forceinline__ A own_recon(int mode, A f, const A* s, const A* dx, const A* ds) {
+    if (mode == 2) return f;
+    A sdx = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) sdx += dx[d] * s[d];
+    if (mode == 1) return f + sdx;
+    // positivity_preserving_reconstruct (Flux/CAIDVM.jl:127-142)
+    A sabs = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) sabs += ds[d] * fabs(s[d]);
+    A th = fabs((f - (A)JL_EPS) / ((A)0.5 * sabs + (A)EPS_REF));
+    th = th < (A)1 ? th : (A)1;
+    return f + th * sdx;
+}
+
+// micro flux of another data item (velocity j of its grid, velocities u) through a face
+template <int D, int NDF, typename T, typename A>
+__device__ __forceinline__ void other_micro(const T* f, const T* sdf, int nvd, int j, const A* u, const A* dxo,
+                                            const A* ds, A adt, int dir, int mode, A* out) {
+    A dx[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) dx[d] = dxo[d] - u[d] * adt;
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) {
+        A s[D];
+        const A fk = (A)f[(int64_t)k * nvd + j];
+        if (mode != 2) {
+#pragma unroll
+            for (int d = 0; d < D; ++d) s[d] = (A)sdf[((int64_t)d * NDF + k) * nvd + j];
+        }
+        out[k] = own_recon<D, A>(mode, fk, s, dx, ds) * u[dir];
+    }
+}
+
+// exp of an FP64 exponent into the arithmetic precision: FP64 for the plain form; for the
+// mixed form the FP64 argument is split a = hi + lo (hi = float(a)) and
+// exp(a) = expf(hi) * (1 + lo), accurate to FP32 rounding with a handful of FP64 operations
+template <typename A> __device__ __forceinline__ A exp_arg(double a);
+template <> __device__ __forceinline__ double exp_arg<double>(double a) { return exp(a); }
+template <> __device__ __forceinline__ float exp_arg<float>(double a) {
+    const float hi = (float)a;
+    const float lo = (float)(a - (double)hi);
+    return expf(hi) * (1.0f + lo);
+}
+
+// per-incidence constants in the arithmetic precision
+template <typename A> struct IncA {
+    A dxm[MAXD];    // face midpoint - my reconstruction centre
+    A dxo[MAXD];    // face midpoint - other side's reconstruction centre
+    A ods[MAXD];    // other side's ds
+    A orient, sarea;
+};
+
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, int64_t step, int check_interval) {
+__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P, double dt, int64_t step, int check_interval) {
     using A = typename Arith<T>::type;
-    extern __shared__ double sh[];
+    extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ Incidence sinc[MAX_INC];
+    __shared__ IncA<A> sia[MAX_INC];
     __shared__ double srho[MAX_INC];
     __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
     __shared__ double sscal[4 * MAXW];
     const int fcx = blockIdx.x;
     const int cell = P.fluid_cells[fcx];
     const int i0 = P.inc_off[fcx], ninc = P.inc_off[fcx + 1] - i0;
-    for (int e = threadIdx.x; e < ninc; e += BLOCK) sinc[e] = P.inc[i0 + e];
+    for (int e = threadIdx.x; e < ninc; e += BLOCK) {
+        const Incidence I = P.inc[i0 + e];
+        sinc[e] = I;
+        IncA<A> ia;
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d) {
+            ia.dxm[d] = (A)(I.fmid[d] - I.my_mid[d]);
+            ia.dxo[d] = (A)(I.fmid[d] - I.ot_mid[d]);
+            ia.ods[d] = (A)I.ot_ds[d];
+        }
+        ia.orient = (A)I.orient;
+        ia.sarea = (A)I.sarea;
+        sia[e] = ia;
+    }
     __syncthreads();
     const VGridView g = grid_view(P, cell);
     const int nv = g.nv;
+    const int gid = P.dgrid[cell];
+    const int64_t PG = P.PG;
+    const A* VU = vel<A>(P);
+    const A* VW = wts<A>(P) + g.goff;
     const int64_t fo = P.foff[cell];
     const T* fcell = (const T*)P.f_in + fo;
+    const T* scl = (const T*)P.sdf + fo * D;
     T* fnew = (T*)P.f_out + fo;
     const double* vw = P.vw + g.goff;
     const double* cds = P.dds + (int64_t)cell * MAXD;
     double V = cds[0];
 #pragma unroll
     for (int d = 1; d < D; ++d) V *= cds[d];
-    const double s_dt = dt / V;
-    double* fst = sh;                       // NDF * nv : convected f (then corrected f)
+    A myds[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) myds[d] = (A)cds[d];
+    const A s_dt = (A)(dt / V);
+    const A adt = (A)dt;
+    A* fst = (A*)sh_raw;                                  // NDF * nv
+    A* Ec = fst + (size_t)NDF * nv;                       // D * max_axis
+    A* En = Ec + (size_t)D * P.max_axis;                  // D * max_axis
     const bool caidvm = P.flux == KG_FLUX_CAIDVM;
 
     // ---- 0. wall density of Maxwellian domain faces (calc_ρw, Theory/Math.jl:251-282) --
@@ -467,15 +610,14 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
         for (int i = threadIdx.x; i < nv; i += BLOCK) {
             const double ud = g.u(i, I.dir);
             if (I.orient * ud <= 0.0) {
-                // SF = Σ w u_n h_reconstructed over the outgoing half
                 A fk = (A)fcell[i];
                 A s[D], dx[D];
 #pragma unroll
                 for (int d = 0; d < D; ++d) {
-                    s[d] = (A)((const T*)P.sdf)[(fo * D) + (int64_t)d * NDF * nv + i];
-                    dx[d] = (A)(I.fmid[d] - g.u(i, d) * dt - I.my_mid[d]);
+                    s[d] = (A)scl[(int64_t)d * NDF * nv + i];
+                    dx[d] = sia[e].dxm[d] - VU[(int64_t)d * PG + g.goff + i] * adt;
                 }
-                red[0] += vw[i] * ud * (double)plain_recon<D, A>(fk, s, dx);
+                red[0] += vw[i] * ud * (double)own_recon<D, A>(1, fk, s, dx, myds);
             } else {
                 double c2 = 0.0;
 #pragma unroll
@@ -493,128 +635,134 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
     }
 
     // ---- 1. fluxes gathered over the incidences; convected f into shared memory ----
-    double wacc[D + 2], wfc[D + 2];
-#pragma unroll
-    for (int e = 0; e < D + 2; ++e) { wacc[e] = 0.0; wfc[e] = 0.0; }
+    KSum<A> wacc[D + 2], wfc[D + 2];
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
-        double u[D];
+        A u[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) u[d] = g.u(i, d);
-        const double wi = vw[i];
-        double acc[NDF];
+        for (int d = 0; d < D; ++d) u[d] = VU[(int64_t)d * PG + g.goff + i];
+        A fr[NDF], sr[NDF][D];
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) acc[k] = 0.0;
+        for (int k = 0; k < NDF; ++k) {
+            fr[k] = (A)fcell[(int64_t)k * nv + i];
+#pragma unroll
+            for (int d = 0; d < D; ++d) sr[k][d] = (A)scl[((int64_t)d * NDF + k) * nv + i];
+        }
+        A acc[NDF], accM[NDF];
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) { acc[k] = 0; accM[k] = 0; }
         for (int e = 0; e < ninc; ++e) {
             const Incidence& I = sinc[e];
-            const double ud = u[I.dir];
-            double mic[NDF];
-            if (I.orient * ud <= 0.0) {
-                // outgoing from this cell: its own reconstruction
-                A m[NDF];
+            const IncA<A>& ia = sia[e];
+            const A ud = u[I.dir];
+            const A sa = ia.sarea;
+            if (ia.orient * ud <= (A)0) {
+                // outgoing from this cell: its own reconstruction at the face
                 int mode;
                 if (I.kind == INC_DOMAIN) mode = (I.bc_kind == KG_BC_OUTFLOW) ? 2 : 1;
                 else mode = (I.kind == INC_SOLID) ? 1 : 0;
-                side_micro<D, NDF, T>(P, cell, fo, nv, g, i, I.fmid, I.my_mid, cds, dt, I.dir, mode, m);
+                A dx[D];
 #pragma unroll
-                for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
-                if (caidvm) {
-                    double t[D + 2];
+                for (int d = 0; d < D; ++d) dx[d] = ia.dxm[d] - u[d] * adt;
 #pragma unroll
-                    for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
-                    psi_add<D, NDF>(t, wi, u, mic);
-#pragma unroll
-                    for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+                for (int k = 0; k < NDF; ++k) {
+                    const A m = own_recon<D, A>(mode, fr[k], sr[k], dx, myds) * ud;
+                    acc[k] += sa * m;
+                    accM[k] += sa * m;
                 }
             } else if (I.kind == INC_DOMAIN) {
                 const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
+                A mic[NDF];
                 if (I.bc_kind == KG_BC_MAXWELL || I.bc_kind == KG_BC_INFLOW) {
                     double pr[MAXW];
 #pragma unroll
                     for (int q = 0; q < D + 2; ++q) pr[q] = bc[q];
                     if (I.bc_kind == KG_BC_MAXWELL) pr[0] = srho[e];
                     const double mh = maxwell_h<D>(g, i, pr);
-                    mic[0] = mh * ud;
-                    if (NDF == 2) mic[NDF - 1] = mh * P.K / (2.0 * pr[D + 1]) * ud;
+                    mic[0] = (A)mh * ud;
+                    if (NDF == 2) mic[NDF - 1] = (A)(mh * P.K / (2.0 * pr[D + 1])) * ud;
                 } else if (I.bc_kind == KG_BC_OUTFLOW) {
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) mic[k] = (double)fcell[(int64_t)k * nv + i] * ud;
-                } else {  // interpolated outflow (CAIDVM.jl:71-94)
-                    const T* sc = (const T*)P.sdf + fo * D;
-                    double tpm[D];
+                    for (int k = 0; k < NDF; ++k) mic[k] = fr[k] * ud;
+                } else {  // interpolated outflow (CAIDVM.jl:71-94): mirror centre 2*face - centre
+                    A tdx[D];
 #pragma unroll
-                    for (int d = 0; d < D; ++d) tpm[d] = 2.0 * I.fmid[d] - I.my_mid[d];
+                    for (int d = 0; d < D; ++d) tdx[d] = -ia.dxm[d] - u[d] * adt;
+                    const A shift = (A)2 * ia.dxm[I.dir];
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) {
-                        double s[D];
-#pragma unroll
-                        for (int d = 0; d < D; ++d) s[d] = (double)sc[((int64_t)d * NDF + k) * nv + i];
-                        double tdf = (double)fcell[(int64_t)k * nv + i] + (tpm[I.dir] - I.my_mid[I.dir]) * s[I.dir];
-                        double sdx = 0.0;
-#pragma unroll
-                        for (int d = 0; d < D; ++d) sdx += (I.fmid[d] - u[d] * dt - tpm[d]) * s[d];
-                        mic[k] = (tdf + sdx) * ud;
+                        A tdf = fr[k] + shift * sr[k][I.dir];
+                        mic[k] = own_recon<D, A>(1, tdf, sr[k], tdx, myds) * ud;
                     }
                 }
-                if (caidvm) {
-                    double t[D + 2];
 #pragma unroll
-                    for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
-                    psi_add<D, NDF>(t, wi, u, mic);
-#pragma unroll
-                    for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
-                }
+                for (int k = 0; k < NDF; ++k) { acc[k] += sa * mic[k]; accM[k] += sa * mic[k]; }
             } else {
                 // incoming: the other side's micro flux mapped onto this grid
                 const int od = I.other;
                 const int64_t ofo = P.foff[od];
                 const int onv = (int)((P.foff[od + 1] - ofo) / NDF);
-                int mode;
-                if (I.kind == INC_SOLID) mode = caidvm ? 2 : 1;
-                else mode = 0;
+                const T* of = (const T*)P.f_in + ofo;
+                const T* os = (const T*)P.sdf + ofo * D;
+                const int mode = (I.kind == INC_SOLID) ? (caidvm ? 2 : 1) : 0;
                 if (I.pair < 0) {
                     A m[NDF];
-                    side_micro<D, NDF, T>(P, od, ofo, onv, g, i, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
+                    other_micro<D, NDF, T, A>(of, os, onv, i, u, ia.dxo, ia.ods, adt, I.dir, mode, m);
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
-                    if (caidvm) {
-                        double t[D + 2];
-#pragma unroll
-                        for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
-                        psi_add<D, NDF>(t, wi, u, mic);
-#pragma unroll
-                        for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
-                    }
+                    for (int k = 0; k < NDF; ++k) { acc[k] += sa * m[k]; accM[k] += sa * m[k]; }
                 } else {
-                    const VGridView go = grid_view(P, od);
+                    const int64_t ogo = P.g_off[P.dgrid[od]];
                     const int64_t po = P.p_off[I.pair] + i;
                     const int j0 = P.p_j0[po], jc = P.p_cnt[po];
+                    A mic[NDF];
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) mic[k] = 0.0;
+                    for (int k = 0; k < NDF; ++k) mic[k] = 0;
                     for (int j = j0; j < j0 + jc; ++j) {
-                        A m[NDF];
-                        side_micro<D, NDF, T>(P, od, ofo, onv, go, j, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
-                        const double sc = merge_inv_scale<D>(li, P.vlev[go.goff + j]);
+                        A uj[D], m[NDF];
 #pragma unroll
-                        for (int k = 0; k < NDF; ++k) mic[k] += (double)m[k] * sc;
+                        for (int d = 0; d < D; ++d) uj[d] = VU[(int64_t)d * PG + ogo + j];
+                        other_micro<D, NDF, T, A>(of, os, onv, j, uj, ia.dxo, ia.ods, adt, I.dir, mode, m);
+                        const A sc = merge_scale<D, A>(li, P.vlev[ogo + j]);
+#pragma unroll
+                        for (int k = 0; k < NDF; ++k) mic[k] += m[k] * sc;
                     }
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) acc[k] += sa * mic[k];
                 }
             }
-#pragma unroll
-            for (int k = 0; k < NDF; ++k) acc[k] += I.sarea * mic[k];
         }
-        double fv[NDF], fs[NDF];
+        const A wi = VW[i];
+        A fs[NDF];
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
-            fv[k] = (double)fcell[(int64_t)k * nv + i];
-            fs[k] = fv[k] + s_dt * acc[k];
+            fs[k] = fr[k] + s_dt * acc[k];
             fst[(int64_t)k * nv + i] = fs[k];
         }
-        // CAIDVM: moments of the convected f; Euler+DVM: moments of f before convection
-        if (P.marching == KG_MARCH_CAIDVM) moments_add<D, NDF>(g, wi, i, fs, wfc);
-        else moments_add<D, NDF>(g, wi, i, fv, wfc);
+        // macro flux of this grid's micro fluxes: Σ_faces area w ψ micro = w ψ Σ_faces area micro
+        A u2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) u2 += u[d] * u[d];
+        if (caidvm) {
+            const A a0 = wi * accM[0];
+            wacc[0].add(a0);
+#pragma unroll
+            for (int d = 0; d < D; ++d) wacc[1 + d].add(u[d] * a0);
+            if (NDF == 2) wacc[D + 1].add((A)0.5 * wi * (u2 * accM[0] + accM[NDF - 1]));
+            else wacc[D + 1].add((A)0.5 * u2 * a0);
+        }
+        // CAIDVM: moments of the convected f; Euler: moments of f before convection
+        const A* mf = (P.marching == KG_MARCH_CAIDVM) ? fs : fr;
+        const A b0 = wi * mf[0];
+        wfc[0].add(b0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) wfc[1 + d].add(u[d] * b0);
+        if (NDF == 2) wfc[D + 1].add((A)0.5 * wi * (u2 * mf[0] + mf[NDF - 1]));
+        else wfc[D + 1].add((A)0.5 * u2 * b0);
     }
-    // macro flux of incoming halves whose grid differs (moments on the other side's grid)
+    double wax[D + 2];
+#pragma unroll
+    for (int q = 0; q < D + 2; ++q) wax[q] = wacc[q].value();
+    // macro flux of incoming halves on a different grid (moments on the other side's grid)
     if (caidvm) {
         for (int e = 0; e < ninc; ++e) {
             const Incidence& I = sinc[e];
@@ -623,12 +771,16 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
             const VGridView go = grid_view(P, od);
             const int64_t ofo = P.foff[od];
             const int onv = go.nv;
+            const T* of = (const T*)P.f_in + ofo;
+            const T* os = (const T*)P.sdf + ofo * D;
             const int mode = I.kind == INC_SOLID ? 2 : 0;
             for (int j = threadIdx.x; j < onv; j += BLOCK) {
-                const double ud = go.u(j, I.dir);
-                if (I.orient * ud <= 0.0) continue;   // not leaving the other side towards us
+                A uj[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) uj[d] = VU[(int64_t)d * PG + go.goff + j];
+                if (sia[e].orient * uj[I.dir] <= (A)0) continue;   // not leaving the other side towards us
                 A m[NDF];
-                side_micro<D, NDF, T>(P, od, ofo, onv, go, j, I.fmid, I.ot_mid, I.ot_ds, dt, I.dir, mode, m);
+                other_micro<D, NDF, T, A>(of, os, onv, j, uj, sia[e].dxo, sia[e].ods, adt, I.dir, mode, m);
                 double mic[NDF], uo[D], t[D + 2];
 #pragma unroll
                 for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
@@ -638,7 +790,7 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
                 for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
                 psi_add<D, NDF>(t, P.vw[go.goff + j], uo, mic);
 #pragma unroll
-                for (int q = 0; q < D + 2; ++q) wacc[q] += I.sarea * t[q];
+                for (int q = 0; q < D + 2; ++q) wax[q] += I.sarea * t[q];
             }
         }
     }
@@ -646,7 +798,7 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
     {
         double red[2 * (D + 2)];
 #pragma unroll
-        for (int q = 0; q < D + 2; ++q) { red[q] = wacc[q]; red[D + 2 + q] = wfc[q]; }
+        for (int q = 0; q < D + 2; ++q) { red[q] = wax[q]; red[D + 2 + q] = wfc[q].value(); }
         block_sum<2 * (D + 2)>(red, sred);
         if (threadIdx.x == 0) {
             double* w = P.w + (int64_t)cell * MAXW;
@@ -673,8 +825,7 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
             }
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) { w[q] = wn[q]; sscal[q] = pc[q]; sscal[MAXW + q] = pn[q]; }
-            const double tau = P.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - P.omega) / pc[0];
-            sscal[2 * MAXW] = tau;
+            sscal[2 * MAXW] = P.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - P.omega) / pc[0];
             int bad = 0;
             for (int q = 0; q < D + 2; ++q) if (!isfinite(pc[q])) bad |= ST_NONFINITE;
             if (!(pc[0] > 0.0) || !(pc[D + 1] > 0.0)) bad |= ST_NEGATIVE;
@@ -686,59 +837,98 @@ __global__ void __launch_bounds__(BLOCK) flux_collide_kernel(Dev P, double dt, i
 #pragma unroll
     for (int q = 0; q < D + 2; ++q) { pc[q] = sscal[q]; pn[q] = sscal[MAXW + q]; }
     const double tau = sscal[2 * MAXW];
-    // ---- 3. conservation correction and heat flux --------------------------------
-    double qv[D];
+    const double lamc = pc[D + 1], lamn = pn[D + 1];
+    // factor tables of the two Maxwellians: exponents in FP64 (discrete_maxwell, 2D2F.jl:1-21)
+    const bool need_n = P.marching == KG_MARCH_CAIDVM;
 #pragma unroll
-    for (int d = 0; d < D; ++d) qv[d] = 0.0;
-    const double lamc = pc[D + 1];
+    for (int d = 0; d < D; ++d) {
+        const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
+        for (int a = threadIdx.x; a < na; a += BLOCK) {
+            const double x = P.ax_val[a0 + a];
+            const double cu = x - pc[1 + d];
+            Ec[d * P.max_axis + a] = exp_arg<A>(-lamc * cu * cu);
+            if (need_n) { const double cn = x - pn[1 + d]; En[d * P.max_axis + a] = exp_arg<A>(-lamn * cn * cn); }
+        }
+    }
+    __syncthreads();
+    const A prec = (A)(pc[0] * (D == 2 ? lamc / PI : pow(lamc / PI, 1.5)));
+    const A pren = (A)(pn[0] * (D == 2 ? lamn / PI : pow(lamn / PI, 1.5)));
+    const A bfc = (A)(P.K / (2.0 * lamc)), bfn = (A)(P.K / (2.0 * lamn));
+    const uint16_t* vx = P.vidx + g.goff;
+    const int MA = P.max_axis;
+    // peculiar velocity c = u - U with U split into two floats (hi + lo), so that c keeps
+    // the precision of c rather than that of U
+    A Uh[D], Ul[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { Uh[d] = (A)pc[1 + d]; Ul[d] = (A)(pc[1 + d] - (double)Uh[d]); }
+    // ---- 3. conservation correction and heat flux --------------------------------
+    KSum<A> qs[D];
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
-        double fv[NDF];
-        if (P.marching == KG_MARCH_CAIDVM) {
-            const double mc = maxwell_h<D>(g, i, pc);
-            const double mn = maxwell_h<D>(g, i, pn);
+        A fv[NDF];
+        A mc = prec, mn = pren;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const int ix = vx[(int64_t)d * PG + i];
+            mc *= Ec[d * MA + ix];
+            if (need_n) mn *= En[d * MA + ix];
+        }
+        if (need_n) {
             fv[0] = fst[i] + (mc - mn);
-            if (NDF == 2) fv[NDF - 1] = fst[nv + i] + (mc * P.K / (2.0 * lamc) - mn * P.K / (2.0 * pn[D + 1]));
+            if (NDF == 2) fv[NDF - 1] = fst[nv + i] + (mc * bfc - mn * bfn);
 #pragma unroll
             for (int k = 0; k < NDF; ++k) fst[(int64_t)k * nv + i] = fv[k];
         } else {
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) fv[k] = (double)fcell[(int64_t)k * nv + i];
+            for (int k = 0; k < NDF; ++k) fv[k] = (A)fcell[(int64_t)k * nv + i];
         }
         // heat_flux_2D2F / 3D1F (lib/KitCore/2D2F.jl:68-88, 3D1F.jl:41-72)
-        double c[D], c2 = 0.0;
+        A c[D], c2 = 0;
 #pragma unroll
-        for (int d = 0; d < D; ++d) { c[d] = g.u(i, d) - pc[1 + d]; c2 += c[d] * c[d]; }
-        const double wi = vw[i];
+        for (int d = 0; d < D; ++d) { c[d] = (VU[(int64_t)d * PG + g.goff + i] - Uh[d]) - Ul[d]; c2 += c[d] * c[d]; }
+        const A wi = VW[i];
+        const A hb = NDF == 2 ? (c2 * fv[0] + fv[NDF - 1]) : c2 * fv[0];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            if (NDF == 2) qv[d] += wi * c[d] * (c2 * fv[0] + fv[NDF - 1]);
-            else qv[d] += wi * c[d] * c2 * fv[0];
-        }
+        for (int d = 0; d < D; ++d) qs[d].add(wi * c[d] * hb);
     }
+    double qv[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) qv[d] = qs[d].value();
     block_sum<D>(qv, sred);
 #pragma unroll
     for (int d = 0; d < D; ++d) qv[d] *= 0.5;
     // ---- 4. Shakhov g+ and implicit relaxation -------------------------------------
-    const double r1 = tau / (tau + dt), r2 = dt / (tau + dt);
-    const double sk = 0.8 * (1.0 - P.Pr) * lamc * lamc / pc[0];
-    for (int i = threadIdx.x; i < nv; i += BLOCK) {
-        const double mc = maxwell_h<D>(g, i, pc);
-        double c[D], c2 = 0.0, cq = 0.0;
+    const A r1 = (A)(tau / (tau + dt)), r2 = (A)(dt / (tau + dt));
+    const A sk = (A)(0.8 * (1.0 - P.Pr) * lamc * lamc / pc[0]);
+    const A lc = (A)lamc, Kk = (A)P.K;
+    A qa[D];
 #pragma unroll
-        for (int d = 0; d < D; ++d) { c[d] = g.u(i, d) - pc[1 + d]; c2 += c[d] * c[d]; cq += c[d] * qv[d]; }
-        double gp[NDF];
+    for (int d = 0; d < D; ++d) qa[d] = (A)qv[d];
+    const bool cai = P.marching == KG_MARCH_CAIDVM;
+    const double tdt = tau / (tau + dt);
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        A mc = prec;
+#pragma unroll
+        for (int d = 0; d < D; ++d) mc *= Ec[d * MA + vx[(int64_t)d * PG + i]];
+        A c2 = 0, cq = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const A cd = (VU[(int64_t)d * PG + g.goff + i] - Uh[d]) - Ul[d];
+            c2 += cd * cd;
+            cq += cd * qa[d];
+        }
+        A gp[NDF];
         if (NDF == 2) {
-            const double mb = mc * P.K / (2.0 * lamc);
-            gp[0] = mc + sk * cq * (2.0 * lamc * c2 + P.K - 5.0) * mc;
-            gp[NDF - 1] = mb + sk * cq * (2.0 * lamc * c2 + P.K - 3.0) * mb;
+            const A mb = mc * bfc;
+            gp[0] = mc + sk * cq * ((A)2 * lc * c2 + Kk - (A)5) * mc;
+            gp[NDF - 1] = mb + sk * cq * ((A)2 * lc * c2 + Kk - (A)3) * mb;
         } else {
-            gp[0] = mc + sk * cq * (2.0 * lamc * c2 - 5.0) * mc;
+            gp[0] = mc + sk * cq * ((A)2 * lc * c2 - (A)5) * mc;
         }
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
-            double v;
-            if (P.marching == KG_MARCH_CAIDVM) v = fst[(int64_t)k * nv + i] * r1 + r2 * gp[k];
-            else v = fst[(int64_t)k * nv + i] * tau / (tau + dt) + r2 * gp[k];
+            A v;
+            if (cai) v = fst[(int64_t)k * nv + i] * r1 + r2 * gp[k];
+            else v = (A)((double)fst[(int64_t)k * nv + i] * tdt) + r2 * gp[k];
             fnew[(int64_t)k * nv + i] = (T)v;
         }
     }
@@ -796,7 +986,8 @@ struct Launch {
         return cudaGetLastError();
     }
     static cudaError_t flux(const Dev& P, int n, int max_nv, double dt, int64_t step, int check, cudaStream_t s) {
-        size_t smem = (size_t)NDF * max_nv * sizeof(double);
+        using A = typename Arith<T>::type;
+        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, dt, step, check);

@@ -34,7 +34,10 @@ def moment_errors(topo, ref_w, ref_prim, ref_qf, w, prim, qf):
     for d in range(dim):
         out[f"m{d}"] = rel_err(gw[:, 1 + d], rw[:, 1 + d], rho * vt)
         out[f"U{d}"] = rel_err(gp[:, 1 + d], rp[:, 1 + d], vt)
-        out[f"q{d}"] = rel_err(gq[:, d], rq[:, d], rho * vt ** 3 * 1e-3)
+        # q: relative to its largest magnitude, floored at 10 % of the free-molecular heat-flux
+        # scale p v_th = ρ v_th^3 / 2 (q of a near-equilibrium or symmetric flow is close to 0,
+        # and FP32 storage of f alone limits q to ~1e-7 ρ v_th^3 absolute)
+        out[f"q{d}"] = rel_err(gq[:, d], rq[:, d], 0.05 * rho * vt ** 3)
     return out
 
 
