@@ -204,6 +204,23 @@ int kg_last_error(const kg_handle *h, char *buf, size_t cap);
  * with the same nsteps and dt.                                               */
 int kg_use_graph(kg_handle *h, int enable);
 
+/* Residual sums without any device allocation (no counterpart in the reference).
+ * Computes Σ_c (prim_new - prim_old)^2 and Σ_c |prim_new| (the two sums of
+ * residual_check!) over n_cells cells of row-major n_cells x (dim+2) device arrays and
+ * writes 2*(dim+2) doubles (the squared differences, then the magnitudes) to the device
+ * array `sums`, asynchronously on `stream` (NULL: the legacy default stream).
+ * For callers that cannot allocate device memory where they need the residual: a host
+ * runtime whose device memory belongs to its own pool allocator, or a serving loop that
+ * must not let an allocation synchronise the device while other problems run.  Its
+ * scratch is a fixed file-scope device array (80 KiB, held by every GPU that loads the
+ * library until exit); n_cells above 4,194,304 is rejected with KG_ERR_ARG.  The first
+ * call on a device resolves that array's device address (make it before any stream
+ * capture).  Calls share the array, so calls that overlap on the GPU race; each call
+ * writes every scratch row it reads, so no state carries over between calls.
+ * Errors: kg_last_error(NULL, ...).                                           */
+int kg_residual_sums_noalloc(const double *prim_new, const double *prim_old, int64_t n_cells,
+                             int32_t dim, double *sums, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,6 +19,11 @@ cudaError_t launch_residual(const double*, int, double*, cudaStream_t);
 
 using namespace kg;
 
+namespace kg {
+// message for kg_last_error(NULL, ...) from entry points that take no handle
+void set_global_error(const std::string& msg);
+}
+
 namespace {
 
 thread_local std::string g_create_err;
@@ -47,6 +52,8 @@ struct DBuf {
 };
 
 }  // namespace
+
+void kg::set_global_error(const std::string& msg) { g_create_err = msg; }
 
 struct kg_handle {
     kg_params prm{};
