@@ -194,6 +194,86 @@ def run_ours(args, rank, world, dist):
     return P, res, launches_total
 
 
+def batch_shapes():
+    """Eight mesh / velocity-grid shapes of the batched workload (Sod tubes and lid-driven
+    cavities, base meshes 32^2..128^2-class, 0-2 levels, velocity grids 16^2..40^2 on [-6,6]^2)."""
+    from kitgpu import cases
+    out = []
+    for n, lev, m in ((32, 0, 16), (48, 1, 24), (64, 1, 32), (40, 2, 20)):
+        p = cases.cavity(n=n, nv=m, levels=lev)
+        out.append(("cavity", p, cases.build(p)))
+    for sc, lev, m in ((0.25, 2, 24), (0.5, 1, 28), (0.75, 2, 40), (0.5, 0, 16)):
+        p = cases.sod(scale=sc, max_level=lev, nv=m)
+        p.case.quadrature = [-6.0, 6.0, -6.0, 6.0]
+        out.append(("sod", p, cases.build(p)))
+    return out
+
+
+def run_batched(args):
+    import math
+    import torch
+    from kitgpu import abi, cases, mesh
+    from kitgpu.solver import GpuBatch
+    rng = np.random.default_rng(20261203 + 4)
+    shapes = batch_shapes()
+    forms = {}
+    for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
+        base = abi.make_params(shapes[0][1], precision=prec, st_check_interval=100)
+        free = torch.cuda.mem_get_info()[0]
+        b = GpuBatch(base, int(free * 0.85))
+        b.use_graph(True)
+        P = 0
+        for k in range(args.problems):
+            name, prob, (topo, state) = shapes[k % len(shapes)]
+            prob.gas.Kn = float(10 ** rng.uniform(-3, 0))
+            prm = abi.make_params(prob, precision=prec, st_check_interval=100)
+            b.admit(prm, topo, state["f"], state["w"], state["prim"], prob.dt(), 0)
+            P += mesh.phase_cells(topo)
+        for _ in range(args.warmup):
+            b.step(1)
+        reps = b.step(args.steps)       # graph capture of `steps` steps
+        reps = b.step(args.steps)       # replay, timed
+        ms = next(iter(reps.values())).device_ms
+        forms[form] = {"value": P * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "phase_cells": P,
+                       "launches_per_call": int(next(iter(reps.values())).kernel_launches)}
+        b.close()
+    m = forms["mixed"]
+    return {"metric": METRIC + " (batched)", "value": m["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-f/f64-moments", "data": "synthetic",
+            "config": {"workload": f"batched_{args.problems}_sod_cavity_8_shapes", "phase_cells": m["phase_cells"],
+                       "graph": True},
+            "forms": forms, "mixed_over_fp64": forms["mixed"]["value"] / forms["fp64"]["value"],
+            "gpu_launches": m["launches_per_call"]}
+
+
+def run_serve(args):
+    import torch
+    from kitgpu import abi, serve
+    rng = np.random.default_rng(20261203 + 5)
+    arrivals = serve.poisson_arrivals(rng, args.rate, args.requests)
+    reqs = [serve.random_request(rng, i, a, small=False) for i, a in enumerate(arrivals)]
+    for r in reqs:   # generate before the clock starts
+        from kitgpu import cases
+        r.topo, r.state = cases.build(r.problem)
+    out = {}
+    for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
+        for r in reqs:
+            r.slot, r.admitted, r.finished, r.steps, r.residual, r.converged = -1, -1.0, -1.0, 0, float("inf"), False
+        free = torch.cuda.mem_get_info()[0]
+        srv = serve.Server(precision=prec, pool_bytes=int(free * 0.8), chunk=50, tol=1e-6, max_steps=args.steps * 50)
+        st = srv.run(reqs)
+        srv.close()
+        out[form] = st.summary()
+        out[form]["converged"] = sum(1 for r in reqs if r.converged)
+    m = out["mixed"]
+    return {"metric": "serve p50/p99 time-to-steady-state", "value": m["p99_ms"], "unit": "ms", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-f/f64-moments", "data": "synthetic",
+            "config": {"workload": f"serve_poisson_{args.rate}_per_s_{args.requests}_requests", "tol": 1e-6},
+            "forms": out}
+
+
 def cpu_baseline(threads, budget_s=12.0):
     import oracle as O
     from kitgpu import abi, cases, mesh
@@ -222,6 +302,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (profiling captures)")
+    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "batched", "serve"])
+    ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
+    ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
+    ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -261,6 +345,16 @@ def main():
         print(json.dumps(line))
         return
 
+    if args.mode == "batched":
+        line = run_batched(args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
+    if args.mode == "serve":
+        line = run_serve(args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
     P, res, launches = run_ours(args, rank, world, dist)
     if rank != 0:
         return

@@ -204,6 +204,24 @@ int kg_last_error(const kg_handle *h, char *buf, size_t cap);
  * with the same nsteps and dt.                                               */
 int kg_use_graph(kg_handle *h, int enable);
 
+/* ---- batches --------------------------------------------------------------
+ * Many independent problems (uneven cell and velocity counts, their own gas constants,
+ * Δt and step counters) advanced together: every sub-step is one launch over all of
+ * them.  A batch handle owns one pool of `pool_bytes` for f / sdf; kg_batch_admit places
+ * a problem in a free slot or returns KG_ERR_BUDGET when its footprint does not fit;
+ * kg_batch_release frees it.  Problems that stay keep their device state across
+ * admissions and releases.  params: dim, ndf, flux, marching, precision are those of
+ * every problem of the batch (the gas fields of kg_batch_create's params are unused).
+ * reports[slot] receives each live problem's report (cap: length of `reports`).     */
+int kg_batch_create(const kg_params *params, int device, int64_t pool_bytes, kg_handle **out);
+int kg_batch_admit(kg_handle *h, const kg_params *params, const kg_topology *topo, const double *f,
+                   const double *w, const double *prim, double dt, int64_t step, int32_t *slot);
+int kg_batch_release(kg_handle *h, int32_t slot);
+int kg_batch_step(kg_handle *h, int32_t nsteps, kg_step_report *reports, int32_t cap);
+int kg_batch_download(kg_handle *h, int32_t slot, double *f, double *w, double *prim, double *qf);
+int kg_batch_info(const kg_handle *h, int32_t *n_live, int64_t *f_free_elems, int64_t *bytes_per_elem);
+int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
+
 /* Residual sums without any device allocation (no counterpart in the reference).
  * Computes Σ_c (prim_new - prim_old)^2 and Σ_c |prim_new| (the two sums of
  * residual_check!) over n_cells cells of row-major n_cells x (dim+2) device arrays and

@@ -3,6 +3,8 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <iterator>
 #include <string>
 #include <vector>
 #include "kg_device.cuh"
@@ -12,9 +14,9 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t slope(const Dev&, int, int, cudaStream_t);
     static cudaError_t solid(const Dev&, int, cudaStream_t);
     static cudaError_t wall(const Dev&, int, int, cudaStream_t);
-    static cudaError_t flux(const Dev&, int, int, double, int64_t, int, cudaStream_t);
+    static cudaError_t flux(const Dev&, int, int, cudaStream_t);
 };
-cudaError_t launch_residual(const double*, int, double*, cudaStream_t);
+cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
 
 using namespace kg;
@@ -37,42 +39,86 @@ template <typename T>
 __global__ void from_storage(const T* __restrict__ src, double* __restrict__ dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) dst[i] = (double)src[i];
 }
-// SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298)
-template <typename T>
-__global__ void init_walls(const WallOp* ops, const int64_t* foff, T* fa, T* fb) {
-    const WallOp op = ops[blockIdx.x];
-    const int64_t src = foff[op.donor], dst = foff[op.data];
-    const int64_t n = foff[op.data + 1] - dst;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) { fa[dst + i] = fa[src + i]; fb[dst + i] = fa[src + i]; }
-}
-
-struct DBuf {
-    void* p = nullptr;
-    size_t n = 0;
-};
-
 }  // namespace
 
 void kg::set_global_error(const std::string& msg) { g_create_err = msg; }
+
+namespace {
+
+// first-fit allocator of contiguous ranges (f elements or data slots) within a pool
+struct RangeAlloc {
+    std::map<int64_t, int64_t> free_;   // start -> length
+    int64_t cap = 0;
+    void reset(int64_t c) { free_.clear(); cap = c; if (c > 0) free_[0] = c; }
+    bool alloc(int64_t n, int64_t* at) {
+        if (n <= 0) { *at = 0; return true; }
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *at = it->first;
+                int64_t rest = it->second - n, ns = it->first + n;
+                free_.erase(it);
+                if (rest > 0) free_[ns] = rest;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(int64_t at, int64_t n) {
+        if (n <= 0) return;
+        auto it = free_.emplace(at, n).first;
+        auto nx = std::next(it);
+        if (nx != free_.end() && it->first + it->second == nx->first) { it->second += nx->second; free_.erase(nx); }
+        if (it != free_.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) { pv->second += it->second; free_.erase(it); }
+        }
+    }
+    int64_t free_total() const { int64_t t = 0; for (auto& kv : free_) t += kv.second; return t; }
+};
+
+struct Problem {
+    bool live = false;
+    Flat F;
+    int64_t fbase = 0, fsize = 0;
+    int64_t dbase = 0, dsize = 0;
+    ProbParams pp{};
+};
+
+}  // namespace
 
 struct kg_handle {
     kg_params prm{};
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
-    Flat F;
-    bool topo = false, state = false;
-    // device buffers
-    std::vector<void*> allocs;
-    Dev dev{};
+    bool is_batch = false;
+    bool have_state = false;       // single-problem API: state uploaded
+    std::vector<Problem> probs;    // slots
+    RangeAlloc fslab, dslab;
+    int64_t fcap = 0, dcap = 0;
+    // pools (persist across membership changes)
+    std::vector<void*> pool_allocs;
     void* fA = nullptr;
     void* fB = nullptr;
-    int parity = 0;             // 0: f_in = fA
-    double* staging = nullptr;  // FP64 staging for the mixed form
-    double* res_out = nullptr;  // [2*MAXW + 1] residual sums of the last checked step (+ step)
-    double* h_res = nullptr;    // pinned copy
+    void* sdf = nullptr;
+    double *w = nullptr, *prim = nullptr, *qf = nullptr, *staging = nullptr;
+    ProbParams* d_probs = nullptr;
+    int64_t* d_step = nullptr;
     int* d_status = nullptr;
-    int64_t bytes = 0;
+    double* res_out = nullptr;     // [MAX_SLOTS][RES_STRIDE]
+    double* h_res = nullptr;       // pinned copy
+    int* h_status = nullptr;       // pinned copy
+    int64_t pool_bytes = 0;
+    // merged topology (rebuilt when membership changes)
+    bool dirty = true;
+    int64_t version = 0;
+    std::vector<void*> topo_allocs;
+    int64_t topo_bytes = 0;
+    Flat M;
+    Dev dev{};
+    std::vector<int32_t> live;
+    int32_t* d_live = nullptr;
+    int parity = 0;                // 0: f_in = fA
     // profiling
     bool prof = false;
     std::vector<std::string> pnames;
@@ -83,8 +129,7 @@ struct kg_handle {
     bool use_graph = false;
     cudaGraphExec_t gexec = nullptr;
     int g_nsteps = -1, g_parity = -1;
-    int64_t g_step_mod = -1;
-    double g_dt = 0.0;
+    int64_t g_version = -1;
     int64_t last_launches = 0;
 };
 
@@ -103,14 +148,16 @@ int cuda_fail(kg_handle* h, cudaError_t e, const char* what) {
         if (e__ != cudaSuccess) return cuda_fail((h), e__, #call);    \
     } while (0)
 
+size_t storage_size(const kg_handle* h) { return h->prm.precision == KG_PREC_FP64 ? sizeof(double) : sizeof(float); }
+
 template <typename V>
-int upload(kg_handle* h, const std::vector<V>& v, const V** out) {
+int upload_vec(kg_handle* h, const std::vector<V>& v, const V** out) {
     size_t n = std::max<size_t>(v.size(), 1) * sizeof(V);
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    h->allocs.push_back(p);
-    h->bytes += (int64_t)n;
+    h->topo_allocs.push_back(p);
+    h->topo_bytes += (int64_t)n;
     if (!v.empty()) {
         e = cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpy topology");
@@ -118,29 +165,64 @@ int upload(kg_handle* h, const std::vector<V>& v, const V** out) {
     *out = (const V*)p;
     return KG_OK;
 }
-int alloc(kg_handle* h, size_t n, void** out) {
+int pool_alloc(kg_handle* h, size_t n, void** out) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 8));
     if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     e = cudaMemset(p, 0, std::max<size_t>(n, 8));
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemset");
-    h->allocs.push_back(p);
-    h->bytes += (int64_t)n;
+    h->pool_allocs.push_back(p);
+    h->pool_bytes += (int64_t)n;
     *out = p;
     return KG_OK;
 }
 
-void free_device(kg_handle* h) {
+void free_topology(kg_handle* h) {
     if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
-    for (void* p : h->allocs) cudaFree(p);
-    h->allocs.clear();
-    h->bytes = 0;
-    h->topo = h->state = false;
-    h->fA = h->fB = nullptr;
     h->g_nsteps = -1;
+    for (void* p : h->topo_allocs) cudaFree(p);
+    h->topo_allocs.clear();
+    h->topo_bytes = 0;
+}
+void free_pools(kg_handle* h) {
+    free_topology(h);
+    for (void* p : h->pool_allocs) cudaFree(p);
+    h->pool_allocs.clear();
+    h->pool_bytes = 0;
+    h->fA = h->fB = h->sdf = nullptr;
+    h->w = h->prim = h->qf = h->staging = nullptr;
+    h->probs.clear();
+    h->live.clear();
+    h->dirty = true;
+    h->have_state = false;
 }
 
-size_t storage_size(const kg_handle* h) { return h->prm.precision == KG_PREC_FP64 ? sizeof(double) : sizeof(float); }
+// Pools for fcap f elements and dcap data slots.
+int make_pools(kg_handle* h, int64_t fcap, int64_t dcap) {
+    free_pools(h);
+    const int D = h->prm.dim;
+    size_t ss = storage_size(h);
+    void* p;
+    int rc;
+    if ((rc = pool_alloc(h, fcap * ss, &h->fA))) return rc;
+    if ((rc = pool_alloc(h, fcap * ss, &h->fB))) return rc;
+    if ((rc = pool_alloc(h, fcap * D * ss, &h->sdf))) return rc;
+    if ((rc = pool_alloc(h, sizeof(double) * dcap * MAXW, &p))) return rc; h->w = (double*)p;
+    if ((rc = pool_alloc(h, sizeof(double) * dcap * MAXW, &p))) return rc; h->prim = (double*)p;
+    if ((rc = pool_alloc(h, sizeof(double) * dcap * MAXD, &p))) return rc; h->qf = (double*)p;
+    if (h->prm.precision != KG_PREC_FP64) { if ((rc = pool_alloc(h, sizeof(double) * fcap, &p))) return rc; h->staging = (double*)p; }
+    if ((rc = pool_alloc(h, sizeof(ProbParams) * MAX_SLOTS, &p))) return rc; h->d_probs = (ProbParams*)p;
+    if ((rc = pool_alloc(h, sizeof(int64_t) * MAX_SLOTS, &p))) return rc; h->d_step = (int64_t*)p;
+    if ((rc = pool_alloc(h, sizeof(int) * MAX_SLOTS, &p))) return rc; h->d_status = (int*)p;
+    if ((rc = pool_alloc(h, sizeof(double) * MAX_SLOTS * RES_STRIDE, &p))) return rc; h->res_out = (double*)p;
+    h->fcap = fcap; h->dcap = dcap;
+    h->fslab.reset(fcap);
+    h->dslab.reset(dcap);
+    h->probs.assign(MAX_SLOTS, Problem());
+    h->parity = 0;
+    h->dirty = true;
+    return KG_OK;
+}
 
 int prof_slot(kg_handle* h, const char* name) {
     for (size_t i = 0; i < h->pnames.size(); ++i)
@@ -162,19 +244,94 @@ cudaError_t dispatch(const kg_handle* h, Fn fn) {
     return fn(Launch<3, 1, float>());
 }
 
-// One step on the handle's stream (graph-capturable: no host synchronisation).
-int enqueue_step(kg_handle* h, double dt, int64_t host_step, bool timed, int64_t* launches) {
-    Flat& F = h->F;
+ProbParams params_of(const kg_params& p, double dt) {
+    ProbParams pp{};
+    pp.gamma = p.gamma; pp.K = p.K; pp.Pr = p.Pr; pp.omega = p.omega; pp.mu_ref = p.mu_ref;
+    pp.dt = dt; pp.check = p.st_check_interval;
+    return pp;
+}
+
+// Rebuilds the merged gather form of the live problems and uploads it.
+int rebuild(kg_handle* h) {
+    if (!h->dirty) return KG_OK;
+    cudaStreamSynchronize(h->stream);
+    free_topology(h);
+    std::vector<Part> parts;
+    h->live.clear();
+    for (int s = 0; s < (int)h->probs.size(); ++s) {
+        Problem& pb = h->probs[s];
+        if (!pb.live) continue;
+        parts.push_back(Part{&pb.F, pb.fbase, (int32_t)pb.dbase, s});
+        h->live.push_back(s);
+    }
+    std::vector<int32_t> ranges;
+    merge(parts, (int32_t)h->dcap, h->M, ranges);
+    Flat& M = h->M;
+    if (!parts.empty()) {
+        if (M.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
+        int dev_smem = 0;
+        cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+        size_t smax = ((size_t)M.ndf * M.max_nv + 2 * (size_t)M.dim * M.max_axis) * sizeof(double) + 16384;
+        if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
+    }
+    Dev& P = h->dev;
+    P = Dev{};
+    P.dim = h->prm.dim; P.ndf = h->prm.ndf; P.n_cells = M.n_cells; P.n_walls = M.n_walls;
+    P.PG = (int64_t)M.vw.size();
+#define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
+    UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
+    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(vidx, vidx);
+    UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dnv, dnv); UP(dprob, dprob);
+    UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
+    UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
+    UP(fluid_cells, fluid_cells); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim);
+    UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
+    UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
+#undef UP
+    P.max_axis = M.max_axis;
+    const int32_t* dl;
+    { int r = upload_vec(h, h->live, &dl); if (r) return r; }
+    h->d_live = const_cast<int32_t*>(dl);
+    void* cr = nullptr;
+    size_t crn = sizeof(double) * std::max<int64_t>(M.n_fluid, 1) * 2 * MAXW;
+    cudaError_t e = cudaMalloc(&cr, crn);
+    if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc residual scratch");
+    h->topo_allocs.push_back(cr);
+    h->topo_bytes += (int64_t)crn;
+    P.cell_res = (double*)cr;
+    // per-slot parameters with the fluid ranges of this layout
+    std::vector<ProbParams> table(MAX_SLOTS);
+    for (size_t q = 0; q < parts.size(); ++q) {
+        Problem& pb = h->probs[parts[q].slot];
+        pb.pp.fluid_begin = ranges[2 * q];
+        pb.pp.fluid_end = ranges[2 * q + 1];
+        pb.pp.slot = parts[q].slot;
+    }
+    for (int s = 0; s < MAX_SLOTS; ++s) table[s] = h->probs[s].pp;
+    KG_CUDA(h, cudaMemcpy(h->d_probs, table.data(), sizeof(ProbParams) * MAX_SLOTS, cudaMemcpyHostToDevice));
+    P.probs = h->d_probs;
+    P.prob_step = h->d_step;
+    P.status = h->d_status;
+    P.w = h->w; P.prim = h->prim; P.qf = h->qf;
+    P.sdf = h->sdf;
+    P.flux = h->prm.flux; P.marching = h->prm.marching;
+    h->dirty = false;
+    h->version += 1;
+    return KG_OK;
+}
+
+// One step of every live problem on the handle's stream (graph-capturable).
+int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
+    Flat& F = h->M;
     Dev P = h->dev;
     P.f_in = h->parity == 0 ? h->fA : h->fB;
     P.f_out = h->parity == 0 ? h->fB : h->fA;
     cudaStream_t s = h->stream;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
-    auto begin = [&]() -> int {
-        if (!timed) return 0;
+    auto begin = [&]() {
+        if (!timed) return;
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         cudaEventRecord(e0, s);
-        return 0;
     };
     auto end = [&](const char* name) {
         if (!timed) return;
@@ -188,7 +345,7 @@ int enqueue_step(kg_handle* h, double dt, int64_t host_step, bool timed, int64_t
         cudaEventDestroy(e0); cudaEventDestroy(e1);
     };
     cudaError_t e;
-    int npass = (int)F.pass_off.size() - 1;
+    int npass = (int)F.pass_cells_off.size() - 1;
     for (int p = 0; p < npass; ++p) {
         int base = F.pass_cells_off[p], n = F.pass_cells_off[p + 1] - base;
         if (n <= 0) continue;
@@ -212,34 +369,204 @@ int enqueue_step(kg_handle* h, double dt, int64_t host_step, bool timed, int64_t
         end("wall_kernel");
         ++*launches;
     }
-    begin();
-    e = dispatch(h, [&](auto L) { return decltype(L)::flux(P, F.n_fluid, F.max_nv, dt, host_step, h->prm.st_check_interval, s); });
-    if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
-    end("flux_collide_kernel");
-    ++*launches;
-    if (host_step % h->prm.st_check_interval == 0) {
-        e = launch_residual(h->dev.cell_res, F.n_fluid, h->res_out, s);
-        if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
+    if (F.n_fluid > 0) {
+        begin();
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux(P, F.n_fluid, F.max_nv, s); });
+        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        end("flux_collide_kernel");
         ++*launches;
     }
+    e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
+    if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
+    ++*launches;
     h->parity ^= 1;
     return KG_OK;
 }
 
-}  // namespace
-
-extern "C" {
-
-int kg_create(const kg_params* params, int device, kg_handle** out) {
-    if (!params || !out) { g_create_err = "null argument"; return KG_ERR_ARG; }
-    if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) {
-        g_create_err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1";
-        return KG_ERR_ARG;
+// Runs nsteps steps of all live problems; fills per-slot residual flags/sums into h_res.
+int run_steps(kg_handle* h, int32_t nsteps, double* device_ms, int64_t* launches_out) {
+    int rc = rebuild(h);
+    if (rc) return rc;
+    // clear the checked flags so the report covers this call only
+    for (int s : h->live)
+        KG_CUDA(h, cudaMemsetAsync(h->res_out + (int64_t)s * RES_STRIDE + 2 * MAXW + 1, 0, sizeof(double), h->stream));
+    cudaEvent_t t0, t1;
+    KG_CUDA(h, cudaEventCreate(&t0));
+    KG_CUDA(h, cudaEventCreate(&t1));
+    KG_CUDA(h, cudaEventRecord(t0, h->stream));
+    int64_t launches = 0;
+    if (h->use_graph && !h->prof && nsteps > 0) {
+        bool reuse = h->gexec && h->g_nsteps == nsteps && h->g_parity == h->parity && h->g_version == h->version;
+        if (!reuse) {
+            if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+            int parity0 = h->parity;
+            cudaGraph_t graph;
+            KG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+            int r = KG_OK;
+            int64_t l = 0;
+            for (int s = 0; s < nsteps && r == KG_OK; ++s) r = enqueue_step(h, false, &l);
+            cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
+            h->parity = parity0;
+            if (r) return r;
+            if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
+            ce = cudaGraphInstantiate(&h->gexec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaGraphInstantiate");
+            h->g_nsteps = nsteps; h->g_parity = parity0; h->g_version = h->version;
+            h->last_launches = l;
+        }
+        KG_CUDA(h, cudaGraphLaunch(h->gexec, h->stream));
+        launches = h->last_launches;
+        if (nsteps % 2) h->parity ^= 1;
+    } else {
+        for (int s = 0; s < nsteps; ++s) {
+            rc = enqueue_step(h, h->prof, &launches);
+            if (rc) return rc;
+        }
     }
-    if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { g_create_err = "bad precision"; return KG_ERR_ARG; }
-    if (params->flux != KG_FLUX_CAIDVM && params->flux != KG_FLUX_DVM) { g_create_err = "bad flux"; return KG_ERR_ARG; }
-    if (params->marching != KG_MARCH_CAIDVM && params->marching != KG_MARCH_EULER) { g_create_err = "bad marching"; return KG_ERR_ARG; }
-    if (params->st_check_interval <= 0) { g_create_err = "st_check_interval must be positive"; return KG_ERR_ARG; }
+    KG_CUDA(h, cudaEventRecord(t1, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->h_res, h->res_out, sizeof(double) * MAX_SLOTS * RES_STRIDE, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->h_status, h->d_status, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    *device_ms = ms;
+    *launches_out = launches;
+    return KG_OK;
+}
+
+void fill_report(const kg_handle* h, int slot, double ms, int64_t launches, kg_step_report* r) {
+    std::memset(r, 0, sizeof(*r));
+    const double* o = h->h_res + (int64_t)slot * RES_STRIDE;
+    r->checked = o[2 * MAXW + 1] != 0.0;
+    r->checked_step = r->checked ? (int64_t)o[2 * MAXW] : -1;
+    for (int e = 0; e < 5; ++e) { r->sum_res[e] = o[e]; r->sum_avg[e] = o[MAXW + e]; }
+    r->device_ms = ms;
+    r->phase_cells = h->probs[slot].F.phase_cells;
+    r->kernel_launches = (int32_t)launches;
+    int st = h->h_status[slot];
+    r->status = st ? ((st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE) : KG_OK;
+}
+
+// Uploads a placed problem's state into its slabs (both f buffers).
+int upload_problem_state(kg_handle* h, int slot, const double* f, const double* w, const double* prim, int64_t step) {
+    Problem& pb = h->probs[slot];
+    const int64_t nf = pb.fsize, nd = pb.dsize, fb = pb.fbase, db = pb.dbase;
+    Flat& L = pb.F;
+    const int D = h->prm.dim, NW = D + 2;
+    const int64_t nfc = L.foff[L.n_cells];
+    size_t ss = storage_size(h);
+    char* fa = (char*)h->fA + fb * ss;
+    char* fbp = (char*)h->fB + fb * ss;
+    // both f buffers carry the state (the step reads one, writes the other)
+    if (h->prm.precision == KG_PREC_FP64) {
+        KG_CUDA(h, cudaMemcpyAsync(fa, f, sizeof(double) * nfc, cudaMemcpyHostToDevice, h->stream));
+    } else {
+        double* st = h->staging + fb;
+        KG_CUDA(h, cudaMemcpyAsync(st, f, sizeof(double) * nfc, cudaMemcpyHostToDevice, h->stream));
+        to_storage<float><<<1024, 256, 0, h->stream>>>(st, (float*)fa, nfc);
+        KG_CUDA(h, cudaGetLastError());
+    }
+    // SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298)
+    for (const WallOp& wo : L.wall_ops) {
+        int64_t src = L.foff[wo.donor], dst = L.foff[wo.data], n = L.foff[wo.data + 1] - dst;
+        KG_CUDA(h, cudaMemcpyAsync(fa + dst * ss, fa + src * ss, n * ss, cudaMemcpyDeviceToDevice, h->stream));
+    }
+    KG_CUDA(h, cudaMemcpyAsync(fbp, fa, nf * ss, cudaMemcpyDeviceToDevice, h->stream));
+    KG_CUDA(h, cudaMemsetAsync((char*)h->sdf + fb * D * ss, 0, nf * D * ss, h->stream));
+    std::vector<double> pw((size_t)nd * MAXW, 0.0), pp((size_t)nd * MAXW, 0.0);
+    for (int c = 0; c < L.n_cells; ++c)
+        for (int e = 0; e < NW; ++e) { pw[(size_t)c * MAXW + e] = w[(size_t)c * NW + e]; pp[(size_t)c * MAXW + e] = prim[(size_t)c * NW + e]; }
+    KG_CUDA(h, cudaMemcpyAsync(h->w + db * MAXW, pw.data(), sizeof(double) * pw.size(), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->prim + db * MAXW, pp.data(), sizeof(double) * pp.size(), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->qf + db * MAXD, 0, sizeof(double) * nd * MAXD, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->d_step + slot, &step, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->d_status + slot, 0, sizeof(int), h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // host temporaries
+    return KG_OK;
+}
+
+// Places a flattened problem into the pools (the merged topology is rebuilt before the
+// next step) and uploads its state.
+int place_problem(kg_handle* h, int slot, Flat&& F, const kg_params& prm, const double* f, const double* w,
+                  const double* prim, double dt, int64_t step) {
+    Problem& pb = h->probs[slot];
+    const int64_t nf = F.foff.back();
+    const int64_t nd = F.n_data;
+    int64_t fb, db;
+    if (!h->fslab.alloc(nf, &fb)) return fail(h, KG_ERR_BUDGET, "f pool exhausted (admission refused by footprint)");
+    if (!h->dslab.alloc(nd, &db)) { h->fslab.release(fb, nf); return fail(h, KG_ERR_BUDGET, "cell pool exhausted"); }
+    pb.F = std::move(F);
+    pb.fbase = fb; pb.fsize = nf; pb.dbase = db; pb.dsize = nd;
+    pb.pp = params_of(prm, dt);
+    pb.live = true;
+    h->dirty = true;
+    return upload_problem_state(h, slot, f, w, prim, step);
+}
+
+int download_problem(kg_handle* h, int slot, double* f, double* w, double* prim, double* qf, double* sdf) {
+    Problem& pb = h->probs[slot];
+    Flat& L = pb.F;
+    const int D = h->prm.dim, NW = D + 2;
+    const int64_t nfc = L.foff[L.n_cells];
+    size_t ss = storage_size(h);
+    void* fin = h->parity == 0 ? h->fA : h->fB;
+    const char* fsrc = (const char*)fin + pb.fbase * ss;
+    if (f) {
+        if (h->prm.precision == KG_PREC_FP64) {
+            KG_CUDA(h, cudaMemcpyAsync(f, fsrc, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
+        } else {
+            double* st = h->staging + pb.fbase;
+            from_storage<float><<<1024, 256, 0, h->stream>>>((const float*)fsrc, st, nfc);
+            KG_CUDA(h, cudaGetLastError());
+            KG_CUDA(h, cudaMemcpyAsync(f, st, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
+        }
+    }
+    if (sdf) {
+        const char* ssrc = (const char*)h->sdf + pb.fbase * D * ss;
+        if (h->prm.precision == KG_PREC_FP64) {
+            KG_CUDA(h, cudaMemcpyAsync(sdf, ssrc, sizeof(double) * nfc * D, cudaMemcpyDeviceToHost, h->stream));
+        } else {
+            double* st = h->staging + pb.fbase;   // the problem's staging slab holds nf >= nfc doubles
+            for (int d = 0; d < D; ++d) {
+                from_storage<float><<<1024, 256, 0, h->stream>>>((const float*)ssrc + (int64_t)d * nfc, st, nfc);
+                KG_CUDA(h, cudaGetLastError());
+                KG_CUDA(h, cudaMemcpyAsync(sdf + (int64_t)d * nfc, st, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
+                KG_CUDA(h, cudaStreamSynchronize(h->stream));
+            }
+        }
+    }
+    const int64_t nd = pb.dsize;
+    std::vector<double> pw((size_t)nd * MAXW), pp((size_t)nd * MAXW), pq((size_t)nd * MAXD);
+    if (w) KG_CUDA(h, cudaMemcpyAsync(pw.data(), h->w + pb.dbase * MAXW, sizeof(double) * pw.size(), cudaMemcpyDeviceToHost, h->stream));
+    if (prim) KG_CUDA(h, cudaMemcpyAsync(pp.data(), h->prim + pb.dbase * MAXW, sizeof(double) * pp.size(), cudaMemcpyDeviceToHost, h->stream));
+    if (qf) KG_CUDA(h, cudaMemcpyAsync(pq.data(), h->qf + pb.dbase * MAXD, sizeof(double) * pq.size(), cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    for (int c = 0; c < L.n_cells; ++c) {
+        for (int e = 0; e < NW; ++e) {
+            if (w) w[(size_t)c * NW + e] = pw[(size_t)c * MAXW + e];
+            if (prim) prim[(size_t)c * NW + e] = pp[(size_t)c * MAXW + e];
+        }
+        if (qf) for (int d = 0; d < D; ++d) qf[(size_t)c * D + d] = pq[(size_t)c * MAXD + d];
+    }
+    return KG_OK;
+}
+
+int check_params(const kg_params* params, std::string& err) {
+    if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) { err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1"; return KG_ERR_ARG; }
+    if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { err = "bad precision"; return KG_ERR_ARG; }
+    if (params->flux != KG_FLUX_CAIDVM && params->flux != KG_FLUX_DVM) { err = "bad flux"; return KG_ERR_ARG; }
+    if (params->marching != KG_MARCH_CAIDVM && params->marching != KG_MARCH_EULER) { err = "bad marching"; return KG_ERR_ARG; }
+    if (params->st_check_interval <= 0) { err = "st_check_interval must be positive"; return KG_ERR_ARG; }
+    return KG_OK;
+}
+
+int create_handle(const kg_params* params, int device, kg_handle** out) {
+    if (!params || !out) { g_create_err = "null argument"; return KG_ERR_ARG; }
+    int rc = check_params(params, g_create_err);
+    if (rc) return rc;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0) {
@@ -255,18 +582,26 @@ int kg_create(const kg_params* params, int device, kg_handle** out) {
     cudaGetDevice(&h->device);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); delete h; return KG_ERR_CUDA; }
-    e = cudaMallocHost(&h->h_res, sizeof(double) * (2 * MAXW + 2));
+    e = cudaMallocHost(&h->h_res, sizeof(double) * MAX_SLOTS * RES_STRIDE);
+    if (e == cudaSuccess) e = cudaMallocHost(&h->h_status, sizeof(int) * MAX_SLOTS);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); cudaStreamDestroy(h->stream); delete h; return KG_ERR_NOMEM; }
     *out = h;
     return KG_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int kg_create(const kg_params* params, int device, kg_handle** out) { return create_handle(params, device, out); }
+
 int kg_destroy(kg_handle* h) {
     if (!h) return KG_ERR_ARG;
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
-    free_device(h);
+    free_pools(h);
     if (h->h_res) cudaFreeHost(h->h_res);
+    if (h->h_status) cudaFreeHost(h->h_status);
     cudaStreamDestroy(h->stream);
     delete h;
     return KG_OK;
@@ -284,207 +619,70 @@ int kg_topology_footprint(const kg_params* params, const kg_topology* topo, int6
 
 int kg_upload_topology(kg_handle* h, const kg_topology* topo) {
     if (!h || !topo) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle admits problems with kg_batch_admit");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
-    free_device(h);
+    Flat F;
     std::string err;
-    int rc = flatten(h->prm, *topo, h->F, err);
-    if (rc) return fail(h, rc, err);
-    Flat& F = h->F;
-    if (F.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported (" + std::to_string(F.max_inc) + ")");
-    size_t smax = (size_t)F.ndf * F.max_nv * sizeof(double);
-    int dev_smem = 0;
-    cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-    if (smax + 16384 > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
-    Dev& P = h->dev;
-    P = Dev{};
-    P.dim = F.dim; P.ndf = F.ndf; P.n_cells = F.n_cells; P.n_walls = F.n_walls;
-    P.PG = (int64_t)F.vw.size();
-#define UP(field, vec) do { int r__ = upload(h, F.vec, &P.field); if (r__) return r__; } while (0)
-    UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
-    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(vidx, vidx);
-    P.max_axis = F.max_axis;
-    UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds);
-    UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
-    UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-    UP(fluid_cells, fluid_cells); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim);
-    UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
-    UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
-#undef UP
-    P.gamma = h->prm.gamma; P.K = h->prm.K; P.Pr = h->prm.Pr; P.omega = h->prm.omega; P.mu_ref = h->prm.mu_ref;
-    P.flux = h->prm.flux; P.marching = h->prm.marching;
-    int64_t nf = F.foff.back();
-    size_t ss = storage_size(h);
-    void* p;
-    if ((rc = alloc(h, nf * ss, &h->fA))) return rc;
-    if ((rc = alloc(h, nf * ss, &h->fB))) return rc;
-    if ((rc = alloc(h, nf * F.dim * ss, &P.sdf))) return rc;
-    if ((rc = alloc(h, sizeof(double) * F.n_data * MAXW, &p))) return rc; P.w = (double*)p;
-    if ((rc = alloc(h, sizeof(double) * F.n_data * MAXW, &p))) return rc; P.prim = (double*)p;
-    if ((rc = alloc(h, sizeof(double) * F.n_data * MAXD, &p))) return rc; P.qf = (double*)p;
-    if ((rc = alloc(h, sizeof(double) * F.n_fluid * 2 * MAXW, &p))) return rc; P.cell_res = (double*)p;
-    if ((rc = alloc(h, sizeof(int), &p))) return rc; P.status = (int*)p; h->d_status = P.status;
-    if ((rc = alloc(h, sizeof(double) * (2 * MAXW + 2), &p))) return rc; h->res_out = (double*)p;
-    if (h->prm.precision != KG_PREC_FP64) { if ((rc = alloc(h, sizeof(double) * nf, &p))) return rc; h->staging = (double*)p; }
-    else h->staging = nullptr;
-    h->parity = 0;
-    h->topo = true;
+    int rc = flatten(h->prm, *topo, F, err);
+    if (rc) { free_pools(h); return fail(h, rc, err); }
+    if (F.max_inc > MAX_INC) { free_pools(h); return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported (" + std::to_string(F.max_inc) + ")"); }
+    if ((rc = make_pools(h, F.foff.back(), F.n_data))) return rc;
+    Problem& pb = h->probs[0];
+    pb.F = std::move(F);
+    pb.fbase = 0; pb.fsize = pb.F.foff.back(); pb.dbase = 0; pb.dsize = pb.F.n_data;
+    h->fslab.alloc(pb.fsize, &pb.fbase);
+    h->dslab.alloc(pb.dsize, &pb.dbase);
+    pb.pp = params_of(h->prm, 0.0);
+    pb.live = false;   // becomes live with its state
+    h->have_state = false;
+    h->dirty = true;
     return KG_OK;
 }
 
 int kg_upload_state(kg_handle* h, const double* f, const double* w, const double* prim) {
     if (!h || !f || !w || !prim) return fail(h, KG_ERR_ARG, "null argument");
-    if (!h->topo) return fail(h, KG_ERR_STATE, "upload a topology first");
+    if (h->is_batch || h->probs.empty() || h->probs[0].F.n_data == 0) return fail(h, KG_ERR_STATE, "upload a topology first");
     cudaSetDevice(h->device);
-    Flat& F = h->F;
-    const int D = F.dim, NW = D + 2;
-    int64_t nfc = F.foff[F.n_cells];   // cells' part of f (walls follow)
-    void* fin = h->parity == 0 ? h->fA : h->fB;
-    void* fout = h->parity == 0 ? h->fB : h->fA;
-    if (h->prm.precision == KG_PREC_FP64) {
-        KG_CUDA(h, cudaMemcpyAsync(fin, f, sizeof(double) * nfc, cudaMemcpyHostToDevice, h->stream));
-        KG_CUDA(h, cudaMemcpyAsync(fout, fin, sizeof(double) * nfc, cudaMemcpyDeviceToDevice, h->stream));
-    } else {
-        KG_CUDA(h, cudaMemcpyAsync(h->staging, f, sizeof(double) * nfc, cudaMemcpyHostToDevice, h->stream));
-        to_storage<float><<<1024, 256, 0, h->stream>>>(h->staging, (float*)fin, nfc);
-        to_storage<float><<<1024, 256, 0, h->stream>>>(h->staging, (float*)fout, nfc);
-        KG_CUDA(h, cudaGetLastError());
+    cudaStreamSynchronize(h->stream);
+    Problem& pb = h->probs[0];
+    if (!pb.live) {
+        // first state for this topology: the slabs were reserved by kg_upload_topology
+        pb.live = true;
+        h->dirty = true;
     }
-    if (!F.wall_ops.empty()) {
-        if (h->prm.precision == KG_PREC_FP64)
-            init_walls<double><<<(int)F.wall_ops.size(), 256, 0, h->stream>>>(h->dev.wall_ops, h->dev.foff, (double*)fin, (double*)fout);
-        else
-            init_walls<float><<<(int)F.wall_ops.size(), 256, 0, h->stream>>>(h->dev.wall_ops, h->dev.foff, (float*)fin, (float*)fout);
-        KG_CUDA(h, cudaGetLastError());
-    }
-    KG_CUDA(h, cudaMemsetAsync(h->dev.sdf, 0, storage_size(h) * F.foff.back() * D, h->stream));
-    std::vector<double> pw((size_t)F.n_data * MAXW, 0.0), pp((size_t)F.n_data * MAXW, 0.0);
-    for (int c = 0; c < F.n_cells; ++c)
-        for (int e = 0; e < NW; ++e) { pw[(size_t)c * MAXW + e] = w[(size_t)c * NW + e]; pp[(size_t)c * MAXW + e] = prim[(size_t)c * NW + e]; }
-    KG_CUDA(h, cudaMemcpyAsync(h->dev.w, pw.data(), sizeof(double) * pw.size(), cudaMemcpyHostToDevice, h->stream));
-    KG_CUDA(h, cudaMemcpyAsync(h->dev.prim, pp.data(), sizeof(double) * pp.size(), cudaMemcpyHostToDevice, h->stream));
-    KG_CUDA(h, cudaMemsetAsync(h->dev.qf, 0, sizeof(double) * F.n_data * MAXD, h->stream));
-    KG_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
-    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // pw / pp are host temporaries
-    h->state = true;
+    int rc = upload_problem_state(h, 0, f, w, prim, 0);
+    if (rc) return rc;
+    h->have_state = true;
     return KG_OK;
 }
 
 int kg_download_state(kg_handle* h, double* f, double* w, double* prim, double* qf, double* sdf) {
     if (!h) return KG_ERR_ARG;
-    if (!h->state) return fail(h, KG_ERR_STATE, "no state on the device");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
     cudaSetDevice(h->device);
-    Flat& F = h->F;
-    const int D = F.dim, NW = D + 2;
-    int64_t nfc = F.foff[F.n_cells];
-    void* fin = h->parity == 0 ? h->fA : h->fB;
-    if (f) {
-        if (h->prm.precision == KG_PREC_FP64) {
-            KG_CUDA(h, cudaMemcpyAsync(f, fin, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
-        } else {
-            from_storage<float><<<1024, 256, 0, h->stream>>>((const float*)fin, h->staging, nfc);
-            KG_CUDA(h, cudaGetLastError());
-            KG_CUDA(h, cudaMemcpyAsync(f, h->staging, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
-        }
-    }
-    if (sdf) {
-        int64_t ns = nfc * D;
-        if (h->prm.precision == KG_PREC_FP64) {
-            KG_CUDA(h, cudaMemcpyAsync(sdf, h->dev.sdf, sizeof(double) * ns, cudaMemcpyDeviceToHost, h->stream));
-        } else {
-            // staging holds nf doubles; convert the sdf in dim chunks of nfc
-            for (int d = 0; d < D; ++d) {
-                from_storage<float><<<1024, 256, 0, h->stream>>>((const float*)h->dev.sdf + (int64_t)d * nfc, h->staging, nfc);
-                KG_CUDA(h, cudaGetLastError());
-                KG_CUDA(h, cudaMemcpyAsync(sdf + (int64_t)d * nfc, h->staging, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->stream));
-                KG_CUDA(h, cudaStreamSynchronize(h->stream));
-            }
-        }
-    }
-    std::vector<double> pw((size_t)F.n_data * MAXW), pp((size_t)F.n_data * MAXW), pq((size_t)F.n_data * MAXD);
-    if (w) KG_CUDA(h, cudaMemcpyAsync(pw.data(), h->dev.w, sizeof(double) * pw.size(), cudaMemcpyDeviceToHost, h->stream));
-    if (prim) KG_CUDA(h, cudaMemcpyAsync(pp.data(), h->dev.prim, sizeof(double) * pp.size(), cudaMemcpyDeviceToHost, h->stream));
-    if (qf) KG_CUDA(h, cudaMemcpyAsync(pq.data(), h->dev.qf, sizeof(double) * pq.size(), cudaMemcpyDeviceToHost, h->stream));
-    KG_CUDA(h, cudaStreamSynchronize(h->stream));
-    for (int c = 0; c < F.n_cells; ++c) {
-        for (int e = 0; e < NW; ++e) {
-            if (w) w[(size_t)c * NW + e] = pw[(size_t)c * MAXW + e];
-            if (prim) prim[(size_t)c * NW + e] = pp[(size_t)c * MAXW + e];
-        }
-        if (qf) for (int d = 0; d < D; ++d) qf[(size_t)c * D + d] = pq[(size_t)c * MAXD + d];
-    }
-    return KG_OK;
+    return download_problem(h, 0, f, w, prim, qf, sdf);
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
     if (!h) return KG_ERR_ARG;
-    if (!h->state) return fail(h, KG_ERR_STATE, "upload topology and state first");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "upload topology and state first");
     if (nsteps < 0 || !(dt > 0.0)) return fail(h, KG_ERR_ARG, "nsteps must be >= 0 and dt > 0");
     cudaSetDevice(h->device);
-    cudaEvent_t t0, t1;
-    KG_CUDA(h, cudaEventCreate(&t0));
-    KG_CUDA(h, cudaEventCreate(&t1));
-    KG_CUDA(h, cudaEventRecord(t0, h->stream));
+    Problem& pb = h->probs[0];
+    if (pb.pp.dt != dt) {
+        pb.pp.dt = dt;
+        if (!h->dirty) KG_CUDA(h, cudaMemcpyAsync(&h->d_probs[0].dt, &pb.pp.dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    }
+    KG_CUDA(h, cudaMemcpyAsync(h->d_step, &step, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    double ms = 0.0;
     int64_t launches = 0;
-    int64_t last_check = -1;
-    const int iv = h->prm.st_check_interval;
-    bool graph_ok = h->use_graph && !h->prof;
-    if (graph_ok) {
-        // a graph covers nsteps steps from a given f parity with the residual cadence baked
-        // in, so it is reused only when step % interval repeats as well
-        bool reuse = h->gexec && h->g_nsteps == nsteps && h->g_dt == dt && h->g_parity == h->parity &&
-                     h->g_step_mod == step % iv;
-        if (!reuse) {
-            if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
-            int parity0 = h->parity;
-            cudaGraph_t graph;
-            KG_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-            int rc = KG_OK;
-            int64_t l = 0;
-            for (int s = 0; s < nsteps && rc == KG_OK; ++s) rc = enqueue_step(h, dt, step + s, false, &l);
-            cudaError_t ce = cudaStreamEndCapture(h->stream, &graph);
-            if (rc) return rc;
-            if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaStreamEndCapture");
-            ce = cudaGraphInstantiate(&h->gexec, graph, 0);
-            cudaGraphDestroy(graph);
-            if (ce != cudaSuccess) return cuda_fail(h, ce, "cudaGraphInstantiate");
-            h->g_nsteps = nsteps; h->g_dt = dt; h->g_parity = parity0; h->g_step_mod = step % iv;
-            h->last_launches = l;
-            h->parity = parity0;
-        }
-        KG_CUDA(h, cudaGraphLaunch(h->gexec, h->stream));
-        launches = h->last_launches;
-        if (nsteps % 2) h->parity ^= 1;
-        for (int s = 0; s < nsteps; ++s) if ((step + s) % iv == 0) last_check = step + s;
-    } else {
-        for (int s = 0; s < nsteps; ++s) {
-            int rc = enqueue_step(h, dt, step + s, h->prof, &launches);
-            if (rc) return rc;
-            if ((step + s) % iv == 0) last_check = step + s;
-        }
-    }
-    KG_CUDA(h, cudaEventRecord(t1, h->stream));
-    KG_CUDA(h, cudaMemcpyAsync(h->h_res, h->res_out, sizeof(double) * 2 * MAXW, cudaMemcpyDeviceToHost, h->stream));
-    int st = 0;
-    KG_CUDA(h, cudaMemcpyAsync(&h->h_res[2 * MAXW], h->d_status, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
-    KG_CUDA(h, cudaStreamSynchronize(h->stream));
-    std::memcpy(&st, &h->h_res[2 * MAXW], sizeof(int));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, t0, t1);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-    if (report) {
-        std::memset(report, 0, sizeof(*report));
-        report->checked = last_check >= 0;
-        report->checked_step = last_check;
-        for (int e = 0; e < 5; ++e) { report->sum_res[e] = h->h_res[e]; report->sum_avg[e] = h->h_res[MAXW + e]; }
-        report->device_ms = ms;
-        report->phase_cells = h->F.phase_cells;
-        report->kernel_launches = (int32_t)launches;
-        report->status = st ? ((st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE) : KG_OK;
-    }
-    if (st) return fail(h, (st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE,
-                        (st & ST_NONFINITE) ? "non-finite primitive variables" : "rho <= 0 or lambda <= 0");
+    int rc = run_steps(h, nsteps, &ms, &launches);
+    if (rc) return rc;
+    kg_step_report r;
+    fill_report(h, 0, ms, launches, &r);
+    if (report) *report = r;
+    if (r.status) return fail(h, r.status, r.status == KG_ERR_NONFINITE ? "non-finite primitive variables" : "rho <= 0 or lambda <= 0");
     return KG_OK;
 }
 
@@ -511,7 +709,7 @@ int kg_profile_read(kg_handle* h, const char** names, double* total_ms, int64_t*
 
 int kg_memory_footprint(const kg_handle* h, int64_t* bytes) {
     if (!h || !bytes) return KG_ERR_ARG;
-    *bytes = h->bytes;
+    *bytes = h->pool_bytes + h->topo_bytes;
     return KG_OK;
 }
 
@@ -524,6 +722,102 @@ int kg_last_error(const kg_handle* h, char* buf, size_t cap) {
 int kg_use_graph(kg_handle* h, int enable) {
     if (!h) return KG_ERR_ARG;
     h->use_graph = enable != 0;
+    return KG_OK;
+}
+
+// ---- batches -------------------------------------------------------------------
+int kg_batch_create(const kg_params* params, int device, int64_t pool_bytes, kg_handle** out) {
+    int rc = create_handle(params, device, out);
+    if (rc) return rc;
+    kg_handle* h = *out;
+    h->is_batch = true;
+    const int D = params->dim;
+    size_t ss = params->precision == KG_PREC_FP64 ? 8 : 4;
+    int64_t per_elem = (int64_t)ss * (2 + D) + (params->precision == KG_PREC_FP64 ? 0 : 8);
+    int64_t fcap = pool_bytes / per_elem;
+    int64_t dcap = std::max<int64_t>(4096, fcap / 64);
+    fcap -= dcap * (int64_t)(sizeof(double) * (2 * MAXW + MAXD)) / per_elem;
+    if (fcap <= 0) { kg_destroy(h); *out = nullptr; g_create_err = "pool too small"; return KG_ERR_BUDGET; }
+    rc = make_pools(h, fcap, dcap);
+    if (rc) { std::string m = h->err; kg_destroy(h); *out = nullptr; g_create_err = m; return rc; }
+    return KG_OK;
+}
+
+int kg_batch_admit(kg_handle* h, const kg_params* params, const kg_topology* topo, const double* f, const double* w,
+                   const double* prim, double dt, int64_t step, int32_t* slot) {
+    if (!h || !params || !topo || !f || !w || !prim || !slot) return fail(h, KG_ERR_ARG, "null argument");
+    if (!h->is_batch) return fail(h, KG_ERR_STATE, "not a batch handle");
+    if (params->dim != h->prm.dim || params->ndf != h->prm.ndf || params->precision != h->prm.precision ||
+        params->flux != h->prm.flux || params->marching != h->prm.marching)
+        return fail(h, KG_ERR_ARG, "a batch holds problems of one dim / precision / flux / marching");
+    if (!(dt > 0.0)) return fail(h, KG_ERR_ARG, "dt must be > 0");
+    cudaSetDevice(h->device);
+    Flat F;
+    std::string err;
+    int rc = flatten(*params, *topo, F, err);
+    if (rc) return fail(h, rc, err);
+    if (F.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
+    int s = -1;
+    for (int i = 0; i < MAX_SLOTS; ++i) if (!h->probs[i].live) { s = i; break; }
+    if (s < 0) return fail(h, KG_ERR_BUDGET, "all problem slots are in use");
+    cudaStreamSynchronize(h->stream);
+    rc = place_problem(h, s, std::move(F), *params, f, w, prim, dt, step);
+    if (rc) return rc;
+    *slot = s;
+    return KG_OK;
+}
+
+int kg_batch_release(kg_handle* h, int32_t slot) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    Problem& pb = h->probs[slot];
+    h->fslab.release(pb.fbase, pb.fsize);
+    h->dslab.release(pb.dbase, pb.dsize);
+    pb = Problem();
+    h->dirty = true;
+    return KG_OK;
+}
+
+int kg_batch_step(kg_handle* h, int32_t nsteps, kg_step_report* reports, int32_t cap) {
+    if (!h || !h->is_batch || nsteps < 0) return fail(h, KG_ERR_ARG, "bad argument");
+    cudaSetDevice(h->device);
+    double ms = 0.0;
+    int64_t launches = 0;
+    int rc = run_steps(h, nsteps, &ms, &launches);
+    if (rc) return rc;
+    int bad = 0;
+    for (int s : h->live) {
+        kg_step_report r;
+        fill_report(h, s, ms, launches, &r);
+        if (reports && s < cap) reports[s] = r;
+        if (r.status) bad = r.status;
+    }
+    if (bad) return fail(h, bad, "a problem of the batch produced invalid primitive variables (see its report)");
+    return KG_OK;
+}
+
+int kg_batch_download(kg_handle* h, int32_t slot, double* f, double* w, double* prim, double* qf) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    cudaSetDevice(h->device);
+    return download_problem(h, slot, f, w, prim, qf, nullptr);
+}
+
+int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {
+    if (!h || !h->is_batch) return KG_ERR_ARG;
+    int n = 0;
+    for (auto& p : h->probs) n += p.live ? 1 : 0;
+    if (n_live) *n_live = n;
+    if (f_free_elems) *f_free_elems = h->fslab.free_total();
+    if (bytes_per_elem) *bytes_per_elem = (int64_t)storage_size(h) * (2 + h->prm.dim) + (h->prm.precision == KG_PREC_FP64 ? 0 : 8);
+    return KG_OK;
+}
+
+int kg_batch_set_dt(kg_handle* h, int32_t slot, double dt) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !(dt > 0.0)) return fail(h, KG_ERR_ARG, "bad argument");
+    h->probs[slot].pp.dt = dt;
+    if (!h->dirty) KG_CUDA(h, cudaMemcpyAsync(&h->d_probs[slot].dt, &h->probs[slot].pp.dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
     return KG_OK;
 }
 

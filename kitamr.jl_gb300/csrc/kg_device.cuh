@@ -15,6 +15,8 @@ constexpr double PI = 3.141592653589793;
 // status word bits written by the kernels (mapped to KG_ERR_* on the host)
 constexpr int ST_NONFINITE = 1;
 constexpr int ST_NEGATIVE = 2;
+constexpr int RES_STRIDE = 2 * MAXW + 2;   // per slot: sums, checked step, checked flag
+constexpr int MAX_SLOTS = 4096;            // problems a handle can hold
 
 struct Dev {
     int dim, ndf, n_cells, n_walls;
@@ -59,8 +61,11 @@ struct Dev {
     const double* cut_gw;
     const double* cut_sw;
     const double* cvcw;
-    // gas
-    double gamma, K, Pr, omega, mu_ref;
+    // problems: per data item its slot; per slot the parameters and the step counter
+    const int32_t* dnv;
+    const int32_t* dprob;
+    const ProbParams* probs;
+    int64_t* prob_step;
     int flux, marching;
     // state
     void* f_in;                        // T*
@@ -70,13 +75,17 @@ struct Dev {
     double* prim;
     double* qf;                        // [n_cells][MAXD]
     double* cell_res;                  // [n_fluid][2*MAXW] residual scratch
-    int* status;
+    int* status;                       // per slot
 };
 
 // ---- reductions --------------------------------------------------------------
+// Block sums with a fixed combination order (deterministic run to run): a butterfly
+// within each warp, then warp 0 combines the warp partials and broadcasts the result
+// through shared memory, so every thread sees the same bits.
 template <int N>
 __device__ __forceinline__ void block_sum(double (&v)[N], double* sred) {
     // sred: shared scratch of N * (BLOCK/32) doubles
+    constexpr int NWARP = BLOCK / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int e = 0; e < N; ++e) {
@@ -88,16 +97,64 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double* sred) {
     __syncthreads();
     if (lane == 0) {
 #pragma unroll
-        for (int e = 0; e < N; ++e) sred[e * (BLOCK / 32) + wid] = v[e];
+        for (int e = 0; e < N; ++e) sred[e * NWARP + wid] = v[e];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int e = 0; e < N; ++e) {
+            double x = lane < NWARP ? sred[e * NWARP + lane] : 0.0;
+#pragma unroll
+            for (int o = NWARP / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) sred[e * NWARP] = x;
+        }
     }
     __syncthreads();
 #pragma unroll
+    for (int e = 0; e < N; ++e) v[e] = sred[e * NWARP];
+    __syncthreads();
+}
+
+// Block sum of FP32 compensated partials (value = hi + lo per thread): the warp butterfly
+// combines float-float pairs with TwoSum in FP32; only the warp partials meet FP64.
+template <int N>
+__device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], double (&out)[N], double* sred) {
+    constexpr int NWARP = BLOCK / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
     for (int e = 0; e < N; ++e) {
-        double x = 0.0;
-        // fixed order over warps: deterministic
-        for (int k = 0; k < BLOCK / 32; ++k) x += sred[e * (BLOCK / 32) + k];
-        v[e] = x;
+        float h = hi[e], l = lo[e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h2 = __shfl_xor_sync(0xffffffffu, h, o);
+            const float l2 = __shfl_xor_sync(0xffffffffu, l, o);
+            const float sum = h + h2;
+            const float bp = sum - h;
+            const float err = (h - (sum - bp)) + (h2 - bp);
+            l = l + l2 + err;
+            h = sum;
+        }
+        hi[e] = h;
+        lo[e] = l;
     }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int e = 0; e < N; ++e) sred[e * NWARP + wid] = (double)hi[e] + (double)lo[e];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int e = 0; e < N; ++e) {
+            double x = lane < NWARP ? sred[e * NWARP + lane] : 0.0;
+#pragma unroll
+            for (int o = NWARP / 2; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            if (lane == 0) sred[e * NWARP] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < N; ++e) out[e] = sred[e * NWARP];
     __syncthreads();
 }
 

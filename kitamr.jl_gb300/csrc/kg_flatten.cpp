@@ -168,6 +168,9 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         for (int d = 0; d < D; ++d) { F.dmid[(size_t)i * MAXD + d] = t.cell_midpoint[(size_t)sc * D + d]; F.dds[(size_t)i * MAXD + d] = t.cell_ds[(size_t)sc * D + d]; }
     }
     for (int i = 0; i < F.n_data; ++i) F.foff[i + 1] = F.foff[i] + (int64_t)grid_nv(t, F.dgrid[i]) * NDF;
+    F.dnv.resize(F.n_data);
+    F.dprob.assign(F.n_data, 0);
+    for (int i = 0; i < F.n_data; ++i) F.dnv[i] = grid_nv(t, F.dgrid[i]);
 
     // ---- neighbour access helpers ---------------------------------------------------
     const int NF = 2 * D;
@@ -436,6 +439,137 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
     }
     if (F.p_j0.empty()) { F.p_j0.push_back(0); F.p_cnt.push_back(0); }
     return KG_OK;
+}
+
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges) {
+    M = Flat();
+    if (parts.empty()) return;
+    const int D = parts[0].F->dim;
+    M.dim = D; M.ndf = parts[0].F->ndf;
+    M.n_data = dcap;
+    int64_t PGtot = 0;
+    for (auto& p : parts) PGtot += (int64_t)p.F->vw.size();
+    M.vu.assign((size_t)D * PGtot, 0.0);
+    M.vuf.assign((size_t)D * PGtot, 0.0f);
+    M.vidx.assign((size_t)D * PGtot, 0);
+    M.g_off.push_back(0);
+    M.p_off.push_back(0);
+    M.foff.assign((size_t)dcap + 1, 0);
+    M.dgrid.assign(dcap, 0); M.dbe.assign(dcap, 0); M.dnv.assign(dcap, 0); M.dprob.assign(dcap, -1);
+    M.dmid.assign((size_t)dcap * MAXD, 0.0); M.dds.assign((size_t)dcap * MAXD, 0.0);
+    M.inc_off.push_back(0);
+    size_t npass = 0;
+    for (auto& p : parts) npass = std::max(npass, p.F->pass_cells_off.size() - 1);
+    int64_t PGacc = 0;
+    int32_t Gacc = 0;
+    ranges.clear();
+    for (auto& p : parts) {
+        const Flat& F = *p.F;
+        const int64_t PG = (int64_t)F.vw.size();
+        const int32_t G = (int32_t)F.g_off.size() - 1;
+        const int32_t pairacc = (int32_t)M.p_off.size() - 1;
+        const int64_t ptab = (int64_t)M.p_j0.size();
+        const int32_t snb = (int32_t)M.slope_nbr.size();
+        const int32_t sops = (int32_t)M.slope_ops.size();
+        const int32_t incacc = (int32_t)M.inc.size();
+        const int32_t bcacc = (int32_t)(M.bc_prim.size() / MAXW);
+        const int32_t ibacc = (int32_t)M.ib_nbr.size();
+        const int32_t cutacc = (int32_t)M.cut_idx.size();
+        const int64_t cvacc = (int64_t)M.cvcw.size();
+        const int32_t axacc = (int32_t)M.ax_val.size();
+        // velocity grids
+        for (int g = 0; g < G; ++g) M.g_off.push_back(PGacc + F.g_off[g + 1]);
+        M.vlev.insert(M.vlev.end(), F.vlev.begin(), F.vlev.end());
+        M.vw.insert(M.vw.end(), F.vw.begin(), F.vw.end());
+        M.vwf.insert(M.vwf.end(), F.vwf.begin(), F.vwf.end());
+        for (int d = 0; d < D; ++d)
+            for (int64_t i = 0; i < PG; ++i) {
+                M.vu[(size_t)d * PGtot + PGacc + i] = F.vu[(size_t)d * PG + i];
+                M.vuf[(size_t)d * PGtot + PGacc + i] = F.vuf[(size_t)d * PG + i];
+                M.vidx[(size_t)d * PGtot + PGacc + i] = F.vidx[(size_t)d * PG + i];
+            }
+        for (int g = 0; g < G; ++g)
+            for (int d = 0; d < MAXD; ++d) M.ax_off.push_back(axacc + F.ax_off[(size_t)g * MAXD + d]);
+        M.ax_val.insert(M.ax_val.end(), F.ax_val.begin(), F.ax_val.end());
+        M.max_axis = std::max(M.max_axis, F.max_axis);
+        M.max_nv = std::max(M.max_nv, F.max_nv);
+        M.max_inc = std::max(M.max_inc, F.max_inc);
+        M.phase_cells += F.phase_cells;
+        M.n_cells += F.n_cells;
+        M.n_walls += F.n_walls;
+        // data table at pool positions
+        for (int j = 0; j < F.n_data; ++j) {
+            const int32_t m = p.dbase + j;
+            M.foff[m] = p.fbase + F.foff[j];
+            M.dgrid[m] = Gacc + F.dgrid[j];
+            M.dbe[m] = F.dbe[j];
+            M.dnv[m] = F.dnv[j];
+            M.dprob[m] = p.slot;
+            for (int d = 0; d < MAXD; ++d) { M.dmid[(size_t)m * MAXD + d] = F.dmid[(size_t)j * MAXD + d]; M.dds[(size_t)m * MAXD + d] = F.dds[(size_t)j * MAXD + d]; }
+        }
+        // pairings
+        for (size_t q = 1; q < F.p_off.size(); ++q) M.p_off.push_back(ptab + F.p_off[q]);
+        if (F.p_off.size() > 1) {
+            M.p_j0.insert(M.p_j0.end(), F.p_j0.begin(), F.p_j0.begin() + F.p_off.back());
+            M.p_cnt.insert(M.p_cnt.end(), F.p_cnt.begin(), F.p_cnt.begin() + F.p_off.back());
+        }
+        auto rp = [&](int32_t pr) { return pr >= 0 ? pr + pairacc : pr; };
+        // slope ops and neighbour lists
+        for (SlopeOp op : F.slope_ops) { op.cell += p.dbase; op.listA += snb; op.listB += snb; M.slope_ops.push_back(op); }
+        for (NbrRef r : F.slope_nbr) { r.data += p.dbase; r.pair = rp(r.pair); M.slope_nbr.push_back(r); }
+        // flux incidences
+        int32_t fb = (int32_t)M.fluid_cells.size();
+        for (int c : F.fluid_cells) M.fluid_cells.push_back(c + p.dbase);
+        for (size_t q = 1; q < F.inc_off.size(); ++q) M.inc_off.push_back(incacc + F.inc_off[q]);
+        for (Incidence a : F.inc) {
+            if (a.other >= 0) a.other += p.dbase;
+            a.pair = rp(a.pair);
+            a.bc += bcacc;
+            M.inc.push_back(a);
+        }
+        M.bc_prim.insert(M.bc_prim.end(), F.bc_prim.begin(), F.bc_prim.end());
+        ranges.push_back(fb);
+        ranges.push_back((int32_t)M.fluid_cells.size());
+        M.n_fluid += F.n_fluid;
+        // immersed boundary
+        for (SolidOp so : F.solid_ops) { so.cell += p.dbase; so.list += ibacc; M.solid_ops.push_back(so); }
+        for (WallOp wo : F.wall_ops) {
+            wo.donor += p.dbase; wo.solid += p.dbase; wo.data += p.dbase; wo.list += ibacc;
+            wo.spair = rp(wo.spair); wo.cut_off += cutacc; wo.cvcw_off += cvacc;
+            M.wall_ops.push_back(wo);
+        }
+        for (NbrRef r : F.ib_nbr) { r.data += p.dbase; r.pair = rp(r.pair); M.ib_nbr.push_back(r); }
+        M.ib_dx.insert(M.ib_dx.end(), F.ib_dx.begin(), F.ib_dx.end());
+        M.cut_idx.insert(M.cut_idx.end(), F.cut_idx.begin(), F.cut_idx.end());
+        M.cut_gw.insert(M.cut_gw.end(), F.cut_gw.begin(), F.cut_gw.end());
+        M.cut_sw.insert(M.cut_sw.end(), F.cut_sw.begin(), F.cut_sw.end());
+        M.cvcw.insert(M.cvcw.end(), F.cvcw.begin(), F.cvcw.end());
+        PGacc += PG;
+        Gacc += G;
+        (void)sops;
+    }
+    M.ax_off.push_back((int32_t)M.ax_val.size());
+    // slope passes merged by their index relative to each problem's coarsest level
+    M.pass_off.push_back(0);
+    M.pass_cells_off.push_back(0);
+    std::vector<int32_t> sops_base;
+    {
+        int32_t acc = 0;
+        for (auto& p : parts) { sops_base.push_back(acc); acc += (int32_t)p.F->slope_ops.size(); }
+    }
+    for (size_t ps = 0; ps < npass; ++ps) {
+        for (size_t q = 0; q < parts.size(); ++q) {
+            const Flat& F = *parts[q].F;
+            if (ps + 1 >= F.pass_cells_off.size()) continue;
+            for (int32_t k = F.pass_cells_off[ps]; k < F.pass_cells_off[ps + 1]; ++k) {
+                M.pass_cells.push_back(F.pass_cells[k] + parts[q].dbase);
+                M.cell_slope_op.push_back(F.cell_slope_op[k] + sops_base[q]);
+            }
+        }
+        M.pass_off.push_back((int32_t)M.slope_ops.size());
+        M.pass_cells_off.push_back((int32_t)M.pass_cells.size());
+    }
+    if (M.p_j0.empty()) { M.p_j0.push_back(0); M.p_cnt.push_back(0); }
 }
 
 int64_t device_bytes(const Flat& F, int precision) {

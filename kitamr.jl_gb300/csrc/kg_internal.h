@@ -67,6 +67,14 @@ struct WallOp {             // update_solid_neighbor! for one SolidNeighbor
     int64_t cvcw_off;       // dense cut-cell weight vector (weight with cut cells zeroed)
 };
 
+// ---- per-problem parameters (a handle advances one or many independent problems) --
+struct ProbParams {
+    double gamma, K, Pr, omega, mu_ref, dt;
+    int32_t check;                 // st_check_interval
+    int32_t fluid_begin, fluid_end; // range of the problem in the merged fluid-cell list
+    int32_t slot;
+};
+
 // ---- flattened topology (host copy, then mirrored to device) ------------------
 struct Flat {
     int dim = 2, ndf = 2;
@@ -89,6 +97,8 @@ struct Flat {
     // data table
     std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)
     std::vector<int32_t> dgrid, dbe;
+    std::vector<int32_t> dnv;      // velocity cells per data item
+    std::vector<int32_t> dprob;    // problem slot per data item
     std::vector<double> dmid, dds; // n_data * MAXD
     // pairing tables
     std::vector<int64_t> p_off;    // n_pairs + 1 (offsets into p_j0 / p_cnt)
@@ -118,6 +128,18 @@ struct Flat {
 
 // Builds the gather form; returns KG_OK or an error code with a message.
 int flatten(const kg_params& prm, const kg_topology& t, Flat& out, std::string& err);
+
+// One problem of a batch: its own flattened topology placed at data slots
+// [dbase, dbase + n_data) and f elements [fbase, fbase + foff.back()) of the pools.
+struct Part {
+    const Flat* F;
+    int64_t fbase;
+    int32_t dbase;
+    int32_t slot;
+};
+// Concatenates the parts into one gather form whose data indices are pool positions
+// (dcap slots); fills the fluid range of every part into `ranges` (begin, end pairs).
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& out, std::vector<int32_t>& ranges);
 int64_t device_bytes(const Flat& f, int precision);
 
 }  // namespace kg

@@ -94,7 +94,7 @@ __device__ __forceinline__ void slope_side(const Dev& P, int i, int li, const ty
     for (int n = 0; n < cnt; ++n) {
         const SlopeNbrA<A>& r = nb[n];
         const int64_t fo = P.foff[r.data];
-        const int nvn = (int)((P.foff[r.data + 1] - fo) / NDF);
+        const int nvn = P.dnv[r.data];
         const T* fn = f + fo;
         const T* sn = sdf + fo * D;
         const bool any = r.any;
@@ -239,7 +239,7 @@ __device__ __forceinline__ void extrapolate(const Dev& P, const VGridView& g, in
         NbrRef r = P.ib_nbr[list + n];
         const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
         const int64_t fo = P.foff[r.data];
-        const int nvn = (int)((P.foff[r.data + 1] - fo) / NDF);
+        const int nvn = P.dnv[r.data];
         const T* fn = f + fo;
         const T* sn = sdf + fo * D;
         int j0 = i, jc = 1;
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(BLOCK) solid_kernel(Dev P) {
         double* pr = P.prim + (int64_t)op.cell * MAXW;
 #pragma unroll
         for (int e = 0; e < D + 2; ++e) w[e] = m[e];
-        get_prim<D>(m, P.gamma, pr);
+        get_prim<D>(m, P.probs[P.dprob[op.cell]].gamma, pr);
     }
 }
 
@@ -391,6 +391,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     T* wa = (T*)P.f_in + wo;
     T* wb = (T*)P.f_out + wo;
     const double lam = prim1[D + 1];
+    const double Kw = P.probs[P.dprob[op.donor]].K;
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         double vn = 0.0;
 #pragma unroll
@@ -399,7 +400,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
             const double mh = maxwell_h<D>(g, i, prim1);
             double mv[NDF];
             mv[0] = mh;
-            if (NDF == 2) mv[NDF - 1] = mh * P.K / (2.0 * lam);
+            if (NDF == 2) mv[NDF - 1] = mh * Kw / (2.0 * lam);
 #pragma unroll
             for (int k = 0; k < NDF; ++k) { T v = (T)(mv[k] * rho_w); wa[(int64_t)k * nv + i] = v; wb[(int64_t)k * nv + i] = v; }
         } else {
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
         const double mh = maxwell_h<D>(g, idx, prim1);
         double mv[NDF];
         mv[0] = mh;
-        if (NDF == 2) mv[NDF - 1] = mh * P.K / (2.0 * lam);
+        if (NDF == 2) mv[NDF - 1] = mh * Kw / (2.0 * lam);
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
             T v = (T)((gw * aux[(int64_t)k * nv + idx] + sw * (mv[k] * rho_w)) / (gw + sw));
@@ -494,6 +495,26 @@ template <> struct KSum<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
+// Block sum of compensated per-thread accumulators into FP64 results.
+template <int N>
+__device__ __forceinline__ void block_sum_ks(const KSum<double> (&v)[N], double (&out)[N], double* sred) {
+#pragma unroll
+    for (int e = 0; e < N; ++e) out[e] = v[e].s;
+    block_sum<N>(out, sred);
+}
+template <int N>
+__device__ __forceinline__ void block_sum_ks(const KSum<float> (&v)[N], double (&out)[N], double* sred) {
+    float hi[N], lo[N];
+#pragma unroll
+    for (int e = 0; e < N; ++e) { hi[e] = v[e].s; lo[e] = -v[e].c; }
+    block_sum_ff<N>(hi, lo, out, sred);
+}
+
+// limiter ratio: exact division in FP64; the fast FP32 division (2 ulp) in the mixed form,
+// where it only scales the slope term through min(|ratio|, 1)
+__device__ __forceinline__ double lim_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float lim_div(float a, float b) { return __fdividef(a, b); }
+
 // own-side reconstruction from registers (positivity / plain / none)
 template <int D, typename A>
 __device__ __forceinline__ A own_recon(int mode, A f, const A* s, const A* dx, const A* ds) {
@@ -506,7 +527,7 @@ __device__ __forceinline__ A own_recon(int mode, A f, const A* s, const A* dx, c
     A sabs = 0;
 #pragma unroll
     for (int d = 0; d < D; ++d) sabs += ds[d] * fabs(s[d]);
-    A th = fabs((f - (A)JL_EPS) / ((A)0.5 * sabs + (A)EPS_REF));
+    A th = fabs(lim_div(f - (A)JL_EPS, (A)0.5 * sabs + (A)EPS_REF));
     th = th < (A)1 ? th : (A)1;
     return f + th * sdx;
 }
@@ -518,15 +539,16 @@ __device__ __forceinline__ void other_micro(const T* f, const T* sdf, int nvd, i
     A dx[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) dx[d] = dxo[d] - u[d] * adt;
+    const A ud = D == 2 ? (dir == 0 ? u[0] : u[D - 1]) : (dir == 0 ? u[0] : (dir == 1 ? u[1] : u[D - 1]));
 #pragma unroll
     for (int k = 0; k < NDF; ++k) {
         A s[D];
-        const A fk = (A)f[(int64_t)k * nvd + j];
+        const A fk = (A)f[k * nvd + j];
         if (mode != 2) {
 #pragma unroll
-            for (int d = 0; d < D; ++d) s[d] = (A)sdf[((int64_t)d * NDF + k) * nvd + j];
+            for (int d = 0; d < D; ++d) s[d] = (A)sdf[(d * NDF + k) * nvd + j];
         }
-        out[k] = own_recon<D, A>(mode, fk, s, dx, ds) * u[dir];
+        out[k] = own_recon<D, A>(mode, fk, s, dx, ds) * ud;
     }
 }
 
@@ -542,29 +564,43 @@ template <> __device__ __forceinline__ float exp_arg<float>(double a) {
 }
 
 // per-incidence constants in the arithmetic precision
-template <typename A> struct IncA {
+template <typename A, typename T> struct IncA {
     A dxm[MAXD];    // face midpoint - my reconstruction centre
     A dxo[MAXD];    // face midpoint - other side's reconstruction centre
     A ods[MAXD];    // other side's ds
     A orient, sarea;
+    const T* of;    // other side's f and sdf blocks (inner / solid faces)
+    const T* os;
+    int32_t onv, pair, ogo;
+    int8_t kind, dir, bc_kind, mode_out, mode_in;
 };
 
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P, double dt, int64_t step, int check_interval) {
+__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ Incidence sinc[MAX_INC];
-    __shared__ IncA<A> sia[MAX_INC];
+    __shared__ IncA<A, T> sia[MAX_INC];
     __shared__ double srho[MAX_INC];
     __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
     __shared__ double sscal[4 * MAXW];
+    // per-CTA scalars in the arithmetic precision, computed once by thread 0
+    enum { C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
+           C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
+    __shared__ A sc[C_N];
     const int fcx = blockIdx.x;
     const int cell = P.fluid_cells[fcx];
+    const int slot = P.dprob[cell];
+    const ProbParams& PP = P.probs[slot];
+    const double dt = PP.dt;
+    const double Kgas = PP.K;
+    const int64_t step = P.prob_step[slot];
+    const int check_interval = PP.check;
     const int i0 = P.inc_off[fcx], ninc = P.inc_off[fcx + 1] - i0;
     for (int e = threadIdx.x; e < ninc; e += BLOCK) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
-        IncA<A> ia;
+        IncA<A, T> ia;
 #pragma unroll
         for (int d = 0; d < MAXD; ++d) {
             ia.dxm[d] = (A)(I.fmid[d] - I.my_mid[d]);
@@ -573,7 +609,28 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         }
         ia.orient = (A)I.orient;
         ia.sarea = (A)I.sarea;
+        ia.kind = I.kind; ia.dir = I.dir; ia.bc_kind = I.bc_kind; ia.pair = I.pair;
+        if (I.kind == INC_DOMAIN) ia.mode_out = (I.bc_kind == KG_BC_OUTFLOW) ? 2 : 1;
+        else ia.mode_out = (I.kind == INC_SOLID) ? 1 : 0;
+        ia.mode_in = (I.kind == INC_SOLID) ? (P.flux == KG_FLUX_CAIDVM ? 2 : 1) : 0;
+        if (I.other >= 0) {
+            const int64_t ofo = P.foff[I.other];
+            ia.of = (const T*)P.f_in + ofo;
+            ia.os = (const T*)P.sdf + ofo * D;
+            ia.onv = P.dnv[I.other];
+            ia.ogo = (int32_t)P.g_off[P.dgrid[I.other]];
+        } else {
+            ia.of = nullptr; ia.os = nullptr; ia.onv = 0; ia.ogo = 0;
+        }
         sia[e] = ia;
+    }
+    if (threadIdx.x == 0) {
+        const double* cd = P.dds + (int64_t)cell * MAXD;
+        double Vc = cd[0];
+        for (int d = 1; d < D; ++d) Vc *= cd[d];
+        sc[C_SDT] = (A)(dt / Vc);
+        sc[C_ADT] = (A)dt;
+        for (int d = 0; d < D; ++d) sc[C_DS0 + d] = (A)cd[d];
     }
     __syncthreads();
     const VGridView g = grid_view(P, cell);
@@ -581,7 +638,8 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
     const int gid = P.dgrid[cell];
     const int64_t PG = P.PG;
     const A* VU = vel<A>(P);
-    const A* VW = wts<A>(P) + g.goff;
+    const A* VW0 = wts<A>(P);
+    const A* VW = VW0 + g.goff;
     const int64_t fo = P.foff[cell];
     const T* fcell = (const T*)P.f_in + fo;
     const T* scl = (const T*)P.sdf + fo * D;
@@ -593,9 +651,9 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
     for (int d = 1; d < D; ++d) V *= cds[d];
     A myds[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) myds[d] = (A)cds[d];
-    const A s_dt = (A)(dt / V);
-    const A adt = (A)dt;
+    for (int d = 0; d < D; ++d) myds[d] = sc[C_DS0 + d];
+    const A s_dt = sc[C_SDT];
+    const A adt = sc[C_ADT];
     A* fst = (A*)sh_raw;                                  // NDF * nv
     A* Ec = fst + (size_t)NDF * nv;                       // D * max_axis
     A* En = Ec + (size_t)D * P.max_axis;                  // D * max_axis
@@ -644,33 +702,38 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         A fr[NDF], sr[NDF][D];
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
-            fr[k] = (A)fcell[(int64_t)k * nv + i];
+            fr[k] = (A)fcell[k * nv + i];
 #pragma unroll
-            for (int d = 0; d < D; ++d) sr[k][d] = (A)scl[((int64_t)d * NDF + k) * nv + i];
+            for (int d = 0; d < D; ++d) sr[k][d] = (A)scl[(d * NDF + k) * nv + i];
         }
         A acc[NDF], accM[NDF];
 #pragma unroll
         for (int k = 0; k < NDF; ++k) { acc[k] = 0; accM[k] = 0; }
         for (int e = 0; e < ninc; ++e) {
-            const Incidence& I = sinc[e];
-            const IncA<A>& ia = sia[e];
-            const A ud = u[I.dir];
+            const IncA<A, T>& ia = sia[e];
+            const int dir = ia.dir;
+            const A ud = D == 2 ? (dir == 0 ? u[0] : u[D - 1]) : (dir == 0 ? u[0] : (dir == 1 ? u[1] : u[D - 1]));
             const A sa = ia.sarea;
             if (ia.orient * ud <= (A)0) {
                 // outgoing from this cell: its own reconstruction at the face
-                int mode;
-                if (I.kind == INC_DOMAIN) mode = (I.bc_kind == KG_BC_OUTFLOW) ? 2 : 1;
-                else mode = (I.kind == INC_SOLID) ? 1 : 0;
                 A dx[D];
 #pragma unroll
                 for (int d = 0; d < D; ++d) dx[d] = ia.dxm[d] - u[d] * adt;
+                const int mode = ia.mode_out;
 #pragma unroll
                 for (int k = 0; k < NDF; ++k) {
                     const A m = own_recon<D, A>(mode, fr[k], sr[k], dx, myds) * ud;
                     acc[k] += sa * m;
                     accM[k] += sa * m;
                 }
-            } else if (I.kind == INC_DOMAIN) {
+            } else if (ia.kind != INC_DOMAIN && ia.pair < 0) {
+                // incoming through a face to a cell on the same grid (the common case)
+                A m[NDF];
+                other_micro<D, NDF, T, A>(ia.of, ia.os, ia.onv, i, u, ia.dxo, ia.ods, adt, dir, ia.mode_in, m);
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) { acc[k] += sa * m[k]; accM[k] += sa * m[k]; }
+            } else if (ia.kind == INC_DOMAIN) {
+                const Incidence& I = sinc[e];
                 const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
                 A mic[NDF];
                 if (I.bc_kind == KG_BC_MAXWELL || I.bc_kind == KG_BC_INFLOW) {
@@ -680,7 +743,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
                     if (I.bc_kind == KG_BC_MAXWELL) pr[0] = srho[e];
                     const double mh = maxwell_h<D>(g, i, pr);
                     mic[0] = (A)mh * ud;
-                    if (NDF == 2) mic[NDF - 1] = (A)(mh * P.K / (2.0 * pr[D + 1])) * ud;
+                    if (NDF == 2) mic[NDF - 1] = (A)(mh * Kgas / (2.0 * pr[D + 1])) * ud;
                 } else if (I.bc_kind == KG_BC_OUTFLOW) {
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) mic[k] = fr[k] * ud;
@@ -688,47 +751,35 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
                     A tdx[D];
 #pragma unroll
                     for (int d = 0; d < D; ++d) tdx[d] = -ia.dxm[d] - u[d] * adt;
-                    const A shift = (A)2 * ia.dxm[I.dir];
+                    const A shift = (A)2 * ia.dxm[dir];
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) {
-                        A tdf = fr[k] + shift * sr[k][I.dir];
+                        const A sdir = D == 2 ? (dir == 0 ? sr[k][0] : sr[k][D - 1])
+                                              : (dir == 0 ? sr[k][0] : (dir == 1 ? sr[k][1] : sr[k][D - 1]));
+                        A tdf = fr[k] + shift * sdir;
                         mic[k] = own_recon<D, A>(1, tdf, sr[k], tdx, myds) * ud;
                     }
                 }
 #pragma unroll
                 for (int k = 0; k < NDF; ++k) { acc[k] += sa * mic[k]; accM[k] += sa * mic[k]; }
             } else {
-                // incoming: the other side's micro flux mapped onto this grid
-                const int od = I.other;
-                const int64_t ofo = P.foff[od];
-                const int onv = (int)((P.foff[od + 1] - ofo) / NDF);
-                const T* of = (const T*)P.f_in + ofo;
-                const T* os = (const T*)P.sdf + ofo * D;
-                const int mode = (I.kind == INC_SOLID) ? (caidvm ? 2 : 1) : 0;
-                if (I.pair < 0) {
-                    A m[NDF];
-                    other_micro<D, NDF, T, A>(of, os, onv, i, u, ia.dxo, ia.ods, adt, I.dir, mode, m);
+                // incoming from a cell on a different velocity grid: mapped through the pairing
+                const int64_t po = P.p_off[ia.pair] + i;
+                const int j0 = P.p_j0[po], jc = P.p_cnt[po];
+                A mic[NDF];
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) { acc[k] += sa * m[k]; accM[k] += sa * m[k]; }
-                } else {
-                    const int64_t ogo = P.g_off[P.dgrid[od]];
-                    const int64_t po = P.p_off[I.pair] + i;
-                    const int j0 = P.p_j0[po], jc = P.p_cnt[po];
-                    A mic[NDF];
+                for (int k = 0; k < NDF; ++k) mic[k] = 0;
+                for (int j = j0; j < j0 + jc; ++j) {
+                    A uj[D], m[NDF];
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) mic[k] = 0;
-                    for (int j = j0; j < j0 + jc; ++j) {
-                        A uj[D], m[NDF];
+                    for (int d = 0; d < D; ++d) uj[d] = VU[(int64_t)d * PG + ia.ogo + j];
+                    other_micro<D, NDF, T, A>(ia.of, ia.os, ia.onv, j, uj, ia.dxo, ia.ods, adt, dir, ia.mode_in, m);
+                    const A sc = merge_scale<D, A>(li, P.vlev[ia.ogo + j]);
 #pragma unroll
-                        for (int d = 0; d < D; ++d) uj[d] = VU[(int64_t)d * PG + ogo + j];
-                        other_micro<D, NDF, T, A>(of, os, onv, j, uj, ia.dxo, ia.ods, adt, I.dir, mode, m);
-                        const A sc = merge_scale<D, A>(li, P.vlev[ogo + j]);
-#pragma unroll
-                        for (int k = 0; k < NDF; ++k) mic[k] += m[k] * sc;
-                    }
-#pragma unroll
-                    for (int k = 0; k < NDF; ++k) acc[k] += sa * mic[k];
+                    for (int k = 0; k < NDF; ++k) mic[k] += m[k] * sc;
                 }
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) acc[k] += sa * mic[k];
             }
         }
         const A wi = VW[i];
@@ -759,9 +810,6 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         if (NDF == 2) wfc[D + 1].add((A)0.5 * wi * (u2 * mf[0] + mf[NDF - 1]));
         else wfc[D + 1].add((A)0.5 * u2 * b0);
     }
-    double wax[D + 2];
-#pragma unroll
-    for (int q = 0; q < D + 2; ++q) wax[q] = wacc[q].value();
     // macro flux of incoming halves on a different grid (moments on the other side's grid)
     if (caidvm) {
         for (int e = 0; e < ninc; ++e) {
@@ -769,11 +817,10 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
             if (I.kind == INC_DOMAIN || I.pair < 0) continue;
             const int od = I.other;
             const VGridView go = grid_view(P, od);
-            const int64_t ofo = P.foff[od];
             const int onv = go.nv;
-            const T* of = (const T*)P.f_in + ofo;
-            const T* os = (const T*)P.sdf + ofo * D;
-            const int mode = I.kind == INC_SOLID ? 2 : 0;
+            const T* of = sia[e].of;
+            const T* os = sia[e].os;
+            const int mode = sia[e].mode_in;
             for (int j = threadIdx.x; j < onv; j += BLOCK) {
                 A uj[D];
 #pragma unroll
@@ -781,36 +828,39 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
                 if (sia[e].orient * uj[I.dir] <= (A)0) continue;   // not leaving the other side towards us
                 A m[NDF];
                 other_micro<D, NDF, T, A>(of, os, onv, j, uj, sia[e].dxo, sia[e].ods, adt, I.dir, mode, m);
-                double mic[NDF], uo[D], t[D + 2];
+                const A wj = VW0[go.goff + j] * sia[e].sarea;
+                A u2 = 0;
 #pragma unroll
-                for (int k = 0; k < NDF; ++k) mic[k] = (double)m[k];
+                for (int d = 0; d < D; ++d) u2 += uj[d] * uj[d];
+                const A a0 = wj * m[0];
+                wacc[0].add(a0);
 #pragma unroll
-                for (int d = 0; d < D; ++d) uo[d] = go.u(j, d);
-#pragma unroll
-                for (int q = 0; q < D + 2; ++q) t[q] = 0.0;
-                psi_add<D, NDF>(t, P.vw[go.goff + j], uo, mic);
-#pragma unroll
-                for (int q = 0; q < D + 2; ++q) wax[q] += I.sarea * t[q];
+                for (int d = 0; d < D; ++d) wacc[1 + d].add(uj[d] * a0);
+                if (NDF == 2) wacc[D + 1].add((A)0.5 * wj * (u2 * m[0] + m[NDF - 1]));
+                else wacc[D + 1].add((A)0.5 * u2 * a0);
             }
         }
     }
     // ---- 2. cell scalars ---------------------------------------------------------
     {
         double red[2 * (D + 2)];
+        {
+            KSum<A> both[2 * (D + 2)];
 #pragma unroll
-        for (int q = 0; q < D + 2; ++q) { red[q] = wax[q]; red[D + 2 + q] = wfc[q].value(); }
-        block_sum<2 * (D + 2)>(red, sred);
+            for (int q = 0; q < D + 2; ++q) { both[q] = wacc[q]; both[D + 2 + q] = wfc[q]; }
+            block_sum_ks<2 * (D + 2)>(both, red, sred);
+        }
         if (threadIdx.x == 0) {
             double* w = P.w + (int64_t)cell * MAXW;
             double wn[MAXW], pc[MAXW], pn[MAXW];
             if (P.marching == KG_MARCH_CAIDVM) {
 #pragma unroll
                 for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
-                get_prim<D>(wn, P.gamma, pc);
+                get_prim<D>(wn, PP.gamma, pc);
                 double wf[MAXW];
 #pragma unroll
                 for (int q = 0; q < D + 2; ++q) wf[q] = red[D + 2 + q];
-                get_prim<D>(wf, P.gamma, pn);
+                get_prim<D>(wf, PP.gamma, pn);
             } else {
                 if (P.flux == KG_FLUX_DVM) {
 #pragma unroll
@@ -819,17 +869,32 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
 #pragma unroll
                     for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
                 }
-                get_prim<D>(wn, P.gamma, pc);
+                get_prim<D>(wn, PP.gamma, pc);
 #pragma unroll
                 for (int q = 0; q < D + 2; ++q) pn[q] = pc[q];
             }
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) { w[q] = wn[q]; sscal[q] = pc[q]; sscal[MAXW + q] = pn[q]; }
-            sscal[2 * MAXW] = P.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - P.omega) / pc[0];
+            const double tau = PP.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - PP.omega) / pc[0];
+            sscal[2 * MAXW] = tau;
+            const double lc = pc[D + 1], ln = pn[D + 1];
+            sc[C_PREC] = (A)(pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5)));
+            sc[C_PREN] = (A)(pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5)));
+            sc[C_BFC] = (A)(Kgas / (2.0 * lc));
+            sc[C_BFN] = (A)(Kgas / (2.0 * ln));
+            sc[C_R1] = (A)(tau / (tau + dt));
+            sc[C_R2] = (A)(dt / (tau + dt));
+            sc[C_SK] = (A)(0.8 * (1.0 - PP.Pr) * lc * lc / pc[0]);
+            sc[C_LC] = (A)lc;
+            for (int d = 0; d < D; ++d) {
+                const A uh = (A)pc[1 + d];
+                sc[C_UH + d] = uh;
+                sc[C_UL + d] = (A)(pc[1 + d] - (double)uh);
+            }
             int bad = 0;
             for (int q = 0; q < D + 2; ++q) if (!isfinite(pc[q])) bad |= ST_NONFINITE;
             if (!(pc[0] > 0.0) || !(pc[D + 1] > 0.0)) bad |= ST_NEGATIVE;
-            if (bad) atomicOr(P.status, bad);
+            if (bad) atomicOr(&P.status[slot], bad);
         }
         __syncthreads();
     }
@@ -851,16 +916,15 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         }
     }
     __syncthreads();
-    const A prec = (A)(pc[0] * (D == 2 ? lamc / PI : pow(lamc / PI, 1.5)));
-    const A pren = (A)(pn[0] * (D == 2 ? lamn / PI : pow(lamn / PI, 1.5)));
-    const A bfc = (A)(P.K / (2.0 * lamc)), bfn = (A)(P.K / (2.0 * lamn));
+    const A prec = sc[C_PREC], pren = sc[C_PREN];
+    const A bfc = sc[C_BFC], bfn = sc[C_BFN];
     const uint16_t* vx = P.vidx + g.goff;
     const int MA = P.max_axis;
     // peculiar velocity c = u - U with U split into two floats (hi + lo), so that c keeps
     // the precision of c rather than that of U
     A Uh[D], Ul[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) { Uh[d] = (A)pc[1 + d]; Ul[d] = (A)(pc[1 + d] - (double)Uh[d]); }
+    for (int d = 0; d < D; ++d) { Uh[d] = sc[C_UH + d]; Ul[d] = sc[C_UL + d]; }
     // ---- 3. conservation correction and heat flux --------------------------------
     KSum<A> qs[D];
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
@@ -891,18 +955,19 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         for (int d = 0; d < D; ++d) qs[d].add(wi * c[d] * hb);
     }
     double qv[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) qv[d] = qs[d].value();
-    block_sum<D>(qv, sred);
+    block_sum_ks<D>(qs, qv, sred);
 #pragma unroll
     for (int d = 0; d < D; ++d) qv[d] *= 0.5;
+    if (threadIdx.x == 0)
+        for (int d = 0; d < D; ++d) sc[C_QA + d] = (A)qv[d];
+    __syncthreads();
     // ---- 4. Shakhov g+ and implicit relaxation -------------------------------------
-    const A r1 = (A)(tau / (tau + dt)), r2 = (A)(dt / (tau + dt));
-    const A sk = (A)(0.8 * (1.0 - P.Pr) * lamc * lamc / pc[0]);
-    const A lc = (A)lamc, Kk = (A)P.K;
+    const A r1 = sc[C_R1], r2 = sc[C_R2];
+    const A sk = sc[C_SK];
+    const A lc = sc[C_LC], Kk = (A)Kgas;
     A qa[D];
 #pragma unroll
-    for (int d = 0; d < D; ++d) qa[d] = (A)qv[d];
+    for (int d = 0; d < D; ++d) qa[d] = sc[C_QA + d];
     const bool cai = P.marching == KG_MARCH_CAIDVM;
     const double tdt = tau / (tau + dt);
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
@@ -938,30 +1003,49 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         double* res = P.cell_res + (int64_t)fcx * 2 * MAXW;
         const bool chk = (step % check_interval) == 0;
 #pragma unroll
-        for (int q = 0; q < D + 2; ++q) {
-            const double dl = pc[q] - pr[q];
-            res[q] = chk ? dl * dl : 0.0;
-            res[MAXW + q] = chk ? fabs(pc[q]) : 0.0;
-            pr[q] = pc[q];
+        for (int q = 0; q < MAXW; ++q) {
+            if (q < D + 2) {
+                const double dl = pc[q] - pr[q];
+                res[q] = chk ? dl * dl : 0.0;
+                res[MAXW + q] = chk ? fabs(pc[q]) : 0.0;
+                pr[q] = pc[q];
+            } else {
+                res[q] = 0.0;
+                res[MAXW + q] = 0.0;
+            }
         }
 #pragma unroll
         for (int d = 0; d < D; ++d) P.qf[(int64_t)cell * MAXD + d] = qv[d];
     }
 }
 
-// Deterministic Σ of the per-cell residual terms (one CTA).
-__global__ void __launch_bounds__(BLOCK) residual_kernel(const double* cell_res, int n, double* out) {
+// Per problem (one CTA each): Σ of the per-cell residual terms when the step is a check
+// step (residual_check!, Solver/Finalize.jl:5-11), then the problem's step counter
+// advances (iterate!, Theory/Iterate.jl:10).  Fixed summation order: deterministic.
+__global__ void __launch_bounds__(BLOCK) residual_kernel(Dev P, const int32_t* live, double* out) {
     __shared__ double sred[2 * MAXW * (BLOCK / 32)];
-    double v[2 * MAXW];
+    const int slot = live[blockIdx.x];
+    const ProbParams& PP = P.probs[slot];
+    const int64_t step = P.prob_step[slot];
+    const bool chk = (step % PP.check) == 0;
+    if (chk) {
+        double v[2 * MAXW];
 #pragma unroll
-    for (int q = 0; q < 2 * MAXW; ++q) v[q] = 0.0;
-    for (int c = threadIdx.x; c < n; c += BLOCK)
+        for (int q = 0; q < 2 * MAXW; ++q) v[q] = 0.0;
+        for (int c = PP.fluid_begin + threadIdx.x; c < PP.fluid_end; c += BLOCK)
 #pragma unroll
-        for (int q = 0; q < 2 * MAXW; ++q) v[q] += cell_res[(int64_t)c * 2 * MAXW + q];
-    block_sum<2 * MAXW>(v, sred);
-    if (threadIdx.x == 0)
+            for (int q = 0; q < 2 * MAXW; ++q) v[q] += P.cell_res[(int64_t)c * 2 * MAXW + q];
+        block_sum<2 * MAXW>(v, sred);
+        if (threadIdx.x == 0) {
+            double* o = out + (int64_t)slot * RES_STRIDE;
 #pragma unroll
-        for (int q = 0; q < 2 * MAXW; ++q) out[q] = v[q];
+            for (int q = 0; q < 2 * MAXW; ++q) o[q] = v[q];
+            o[2 * MAXW] = (double)step;
+            o[2 * MAXW + 1] = 1.0;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) P.prob_step[slot] = step + 1;
 }
 
 // ---- launchers ------------------------------------------------------------------
@@ -985,18 +1069,19 @@ struct Launch {
         wall_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
         return cudaGetLastError();
     }
-    static cudaError_t flux(const Dev& P, int n, int max_nv, double dt, int64_t step, int check, cudaStream_t s) {
+    static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
         size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, dt, step, check);
+        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
         return cudaGetLastError();
     }
 };
 
-cudaError_t launch_residual(const double* cell_res, int n, double* out, cudaStream_t s) {
-    residual_kernel<<<1, BLOCK, 0, s>>>(cell_res, n, out);
+cudaError_t launch_residual(const Dev& P, const int32_t* live, int n_live, double* out, cudaStream_t s) {
+    if (n_live <= 0) return cudaSuccess;
+    residual_kernel<<<n_live, BLOCK, 0, s>>>(P, live, out);
     return cudaGetLastError();
 }
 

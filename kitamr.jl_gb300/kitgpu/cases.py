@@ -167,3 +167,30 @@ def box3d(n=(6, 4, 4), nv: int = 8, levels: int = 1, Kn: float = 0.05) -> Proble
                    (M.BC_PERIOD, None), (M.BC_PERIOD, None)],
         ic=ic, refine=refine if levels > 0 else None, K=0.0)
     return Problem("box3d", case, Gas(Kn=Kn, K=0.0, omega=0.81, omega_r=0.81), cfl=0.8)
+
+
+def sphere(scale: float = 1.0, max_level: int = 2, nv: int = 24, Ma: float = 3.0, Kn: float = 0.05) -> Problem:
+    """3D Ma 3 / Kn 0.05 flow past a diffuse isothermal sphere of radius 1 on [-6,6]^3,
+    32^3 trees (scaled), 2 levels near the wall, uniform 24^3 velocity grid on [-10,10]^3."""
+    n = max(6, int(round(32 * scale)))
+    Uinf = Ma * math.sqrt(5.0 / 6.0)
+    R = 1.0
+
+    def ic(x):
+        r = math.sqrt(x[0] ** 2 + x[1] ** 2 + x[2] ** 2)
+        if r > R + 1.0:
+            return [1.0, Uinf, 0.0, 0.0, 1.0]
+        return [1.0, (r - R) * Uinf, 0.0, 0.0, 1.0]
+
+    def refine(mid, ds, lev):
+        r = math.sqrt(mid[0] ** 2 + mid[1] ** 2 + mid[2] ** 2)
+        reach = [1.8, 1.0][min(lev, 1)]
+        return abs(r - R) < reach + 0.5 * math.sqrt(ds[0] ** 2 + ds[1] ** 2 + ds[2] ** 2)
+
+    case = M.Case(
+        dim=3, geometry=[-6.0, 6.0, -6.0, 6.0, -6.0, 6.0], trees_num=[n, n, n], max_level=max_level,
+        quadrature=[-10.0, 10.0, -10.0, 10.0, -10.0, 10.0], vs_trees_num=[nv, nv, nv],
+        domain_bc=[(M.BC_INFLOW, [1.0, Uinf, 0.0, 0.0, 1.0]), (M.BC_OUTFLOW, None),
+                   (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None)],
+        ic=ic, refine=refine, circle=([0.0, 0.0, 0.0], R, [1.0, 0.0, 0.0, 0.0, 1.0]), K=0.0)
+    return Problem("sphere", case, Gas(Kn=Kn, K=0.0, omega=0.81, omega_r=0.81), cfl=0.8)

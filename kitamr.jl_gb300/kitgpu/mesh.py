@@ -225,6 +225,83 @@ def cut_cells_2d(normal, g: VGrid, root_ds):
     return index, gas_w, solid_w
 
 
+def _box_below_plane(n, lo, hi) -> float:
+    """Volume of {x in [lo, hi] : n.x <= 0} (exact inclusion-exclusion over the box corners)."""
+    dim = len(n)
+    a, b = [], 0.0
+    for d in range(dim):
+        s = hi[d] - lo[d]
+        ad = n[d] * s
+        b -= n[d] * lo[d]
+        if ad < 0:          # t -> 1 - t makes every coefficient non-negative
+            b -= ad
+            ad = -ad
+        a.append(ad)
+    amax = max(a) if a else 0.0
+    act = [x for x in a if x > 1e-12 * max(amax, 1e-300)]
+    vol = 1.0
+    for d in range(dim):
+        vol *= hi[d] - lo[d]
+    k = len(act)
+    if k == 0:
+        return vol if b >= 0 else 0.0
+    tot = 0.0
+    for mask in range(1 << k):
+        sa, bits = 0.0, 0
+        for i in range(k):
+            if (mask >> i) & 1:
+                sa += act[i]
+                bits += 1
+        r = b - sa
+        if r > 0:
+            tot += (-1) ** bits * r ** k
+    frac = tot / (math.factorial(k) * float(np.prod(act)))
+    return vol * min(max(frac, 0.0), 1.0)
+
+
+def cut_cells_3d(normal, g: VGrid, root_ds):
+    """3D counterpart of the cut-cell split (Immersed_boundary.jl:250-277): for each velocity
+    cell crossed by u.n = 0, its gas (u.n < 0) and solid (u.n > 0) volumes.  The split is
+    host geometry; the volumes come from an exact box / half-space formula."""
+    if sum(1 for x in normal if abs(x) < 1e-6) > 1:
+        return [], [], []
+    index, gas_w, solid_w = [], [], []
+    for i in range(g.nv):
+        ddu = [root_ds[d] / 2 ** int(g.level[i]) for d in range(3)]
+        mid = g.midpoint[i]
+        if abs(sum(mid[d] * normal[d] for d in range(3))) > 0.5 * math.sqrt(sum(x * x for x in ddu)):
+            continue
+        lo = [mid[d] - 0.5 * ddu[d] for d in range(3)]
+        hi = [mid[d] + 0.5 * ddu[d] for d in range(3)]
+        tot = ddu[0] * ddu[1] * ddu[2]
+        gas = _box_below_plane(normal, lo, hi)
+        if 1e-12 * tot < gas < tot * (1 - 1e-12):
+            index.append(i); gas_w.append(gas); solid_w.append(tot - gas)
+    return index, gas_w, solid_w
+
+
+def calc_intersect_sphere(f_mid, s_mid, center, radius, solid=True):
+    """calc_intersect(::Sphere) of Boundary/Circle.jl:52-62 (as written: the normal keeps the
+    donor's coordinates in the two tangential directions; the generated cases use center 0)."""
+    r = radius
+    dirs = [d for d in range(3) if abs(f_mid[d] - s_mid[d]) > 1e-12]
+    dr = dirs[0]
+    rm = [f_mid[d] - center[d] for d in range(3)]
+    x = rm[(dr + 1) % 3]
+    y = rm[(dr + 2) % 3]
+    rz = math.sqrt(r * r - x * x - y * y)
+    if abs((rz - rm[dr]) / (s_mid[dr] - f_mid[dr])) < 1:
+        dz = rz - rm[dr]
+    else:
+        dz = -rz - rm[dr]
+    ap = list(f_mid)
+    nv = list(f_mid)
+    ap[dr] = dz + f_mid[dr]
+    nv[dr] = dz + rm[dr]
+    den = r if solid else -r
+    return ap, [v / den for v in nv]
+
+
 def calc_intersect_circle(f_mid, s_mid, center, radius, solid=True):
     """calc_intersect(::Circle) of Boundary/Circle.jl:33-51 (the reference leaves the
     intersect point relative to the origin; the generated cases use center [0,0])."""
@@ -484,12 +561,13 @@ def build_topology(case: Case, dtype_check: bool = True) -> Dict[str, np.ndarray
                     continue
                 s = r0
                 bound_enc[c] = -bound_enc[s]
-                ap, nrm = calc_intersect_circle(mids[cells[c]], mids[cells[s]], c0, R, True)
                 g = grids[cell_grid[c]]
                 if dim == 2:
+                    ap, nrm = calc_intersect_circle(mids[cells[c]], mids[cells[s]], c0, R, True)
                     cidx, cgw, csw = cut_cells_2d(nrm, g, root_ds)
                 else:
-                    raise NotImplementedError("3D cut cells")
+                    ap, nrm = calc_intersect_sphere(mids[cells[c]], mids[cells[s]], c0, R, True)
+                    cidx, cgw, csw = cut_cells_3d(nrm, g, root_ds)
                 walls.append(dict(donor=c, solid=s, faceid=k, aux=ap, normal=nrm, bc=list(wbc),
                                   cut=cidx, gw=cgw, sw=csw))
                 cnbr[c][k][0] = wall(len(walls) - 1)

@@ -41,6 +41,13 @@ def load_library(path: Optional[str] = None):
     L.kg_topology_footprint.argtypes = [vp, vp, C.POINTER(i64)]
     L.kg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.kg_use_graph.argtypes = [vp, C.c_int]
+    L.kg_batch_create.argtypes = [vp, C.c_int, i64, C.POINTER(vp)]
+    L.kg_batch_admit.argtypes = [vp, vp, vp, vp, vp, vp, dbl, i64, C.POINTER(i32)]
+    L.kg_batch_release.argtypes = [vp, i32]
+    L.kg_batch_step.argtypes = [vp, i32, vp, i32]
+    L.kg_batch_download.argtypes = [vp, i32, vp, vp, vp, vp]
+    L.kg_batch_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
+    L.kg_batch_set_dt.argtypes = [vp, i32, dbl]
     _lib = L
     return L
 
@@ -49,6 +56,8 @@ EXPORTS = [
     "kg_create", "kg_destroy", "kg_upload_topology", "kg_upload_state", "kg_download_state",
     "kg_step", "kg_profile_enable", "kg_profile_read", "kg_memory_footprint",
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
+    "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
+    "kg_batch_info", "kg_batch_set_dt",
 ]
 
 
@@ -143,3 +152,75 @@ class GpuStep:
         b = C.c_int64()
         _check(self.L, self.h, self.L.kg_memory_footprint(self.h, C.byref(b)))
         return b.value
+
+
+MAX_SLOTS = 4096
+
+
+class GpuBatch:
+    """A batch handle: independent problems advanced together on one device."""
+
+    def __init__(self, params: abi.KgParams, pool_bytes: int, device: int = 0):
+        self.L = load_library()
+        self.params = params
+        h = C.c_void_p()
+        _check(self.L, None, self.L.kg_batch_create(C.byref(params), device, int(pool_bytes), C.byref(h)))
+        self.h = h
+        self.meta = {}            # slot -> (topo, foff)
+        self._reports = (abi.KgStepReport * MAX_SLOTS)()
+
+    def close(self):
+        if self.h:
+            self.L.kg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def admit(self, params: abi.KgParams, topo: Dict, f, w, prim, dt: float, step: int = 0) -> int:
+        """Admit a problem; raises KitGpuError with code KG_ERR_BUDGET (8) when it does not fit."""
+        tref = abi.TopologyRef(topo)
+        f = np.ascontiguousarray(f, dtype=np.float64)
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        prim = np.ascontiguousarray(prim, dtype=np.float64)
+        slot = C.c_int32()
+        _check(self.L, self.h, self.L.kg_batch_admit(self.h, C.byref(params), C.cast(tref.ptr, C.c_void_p),
+                                                       f.ctypes.data, w.ctypes.data, prim.ctypes.data, dt, step,
+                                                       C.byref(slot)))
+        from .mesh import f_offsets
+        self.meta[slot.value] = (topo, f_offsets(topo))
+        return slot.value
+
+    def release(self, slot: int):
+        _check(self.L, self.h, self.L.kg_batch_release(self.h, slot))
+        self.meta.pop(slot, None)
+
+    def step(self, nsteps: int = 1) -> Dict[int, abi.KgStepReport]:
+        _check(self.L, self.h, self.L.kg_batch_step(self.h, nsteps, self._reports, MAX_SLOTS))
+        return {s: self._reports[s] for s in self.meta}
+
+    def download(self, slot: int) -> Dict[str, np.ndarray]:
+        topo, foff = self.meta[slot]
+        nc, dim = int(topo["n_cells"]), int(topo["dim"])
+        out = dict(f=np.empty(int(foff[-1])), w=np.empty(nc * (dim + 2)), prim=np.empty(nc * (dim + 2)),
+                   qf=np.empty(nc * dim))
+        _check(self.L, self.h, self.L.kg_batch_download(self.h, slot, out["f"].ctypes.data, out["w"].ctypes.data,
+                                                          out["prim"].ctypes.data, out["qf"].ctypes.data))
+        return out
+
+    def info(self):
+        n, fr, bpe = C.c_int32(), C.c_int64(), C.c_int64()
+        _check(self.L, self.h, self.L.kg_batch_info(self.h, C.byref(n), C.byref(fr), C.byref(bpe)))
+        return n.value, fr.value * bpe.value
+
+    def set_dt(self, slot: int, dt: float):
+        _check(self.L, self.h, self.L.kg_batch_set_dt(self.h, slot, dt))
+
+    def use_graph(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_use_graph(self.h, int(enable)))
+
+    def profile(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))

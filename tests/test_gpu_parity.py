@@ -13,6 +13,7 @@ CASES_FP64 = [
     ("sod_levels", lambda: cases.sod(scale=0.125, nv=16), 6),
     ("cylinder_ib_adapted", lambda: cases.cylinder(scale=0.25, nv=24, vs_levels=2), 4),
     ("box3d_levels", lambda: cases.box3d(n=(6, 4, 4), nv=8, levels=1), 4),
+    ("sphere3d_ib", lambda: cases.sphere(scale=0.25, nv=8), 3),
 ]
 
 
@@ -52,7 +53,10 @@ def test_fp64_chunked_calls_and_graph_match_single_call():
     assert f_error(topo, ref.f, out1["f"]) <= TOL_FP64
 
 
-@pytest.mark.parametrize("name,make,nsteps", CASES_FP64[:4], ids=[c[0] for c in CASES_FP64[:4]])
+MIXED = CASES_FP64[:4] + CASES_FP64[5:]
+
+
+@pytest.mark.parametrize("name,make,nsteps", MIXED, ids=[c[0] for c in MIXED])
 def test_mixed_within_1e5_of_fp64(name, make, nsteps):
     topo, ref, out, rep = run_pair(make(), nsteps, precision=abi.KG_PREC_MIXED)
     errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
