@@ -107,6 +107,22 @@ def ncu_traffic_per_launch():
     return float(m.group(1)) if m else None
 
 
+def aggregate(units_local: int, ms_local: float, steps: int, dist=None):
+    """Whole-job rate of independent replicas: the units all ranks processed divided by the
+    slowest rank's time (max over ranks)."""
+    import torch
+    ms = float(ms_local)
+    units = float(units_local)
+    if dist is not None:
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        u = torch.tensor([units], dtype=torch.float64)
+        dist.all_reduce(u, op=dist.ReduceOp.SUM)
+        units = float(u.item())
+    return units * steps / (ms / 1e3), ms
+
+
 def pinned_empty(n, torch):
     return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
 
@@ -148,13 +164,8 @@ def run_ours(args, rank, world, dist):
         barrier()
         clocks = sampler.stop() if sampler else None
         step += args.steps
-        ms = rep.device_ms
-        if dist is not None:
-            t = torch.tensor([ms], dtype=torch.float64)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        res[form] = dict(ms_per_step=ms / args.steps, value=P * world * args.steps / (ms / 1e3),
-                         launches=rep.kernel_launches)
+        value, ms = aggregate(P, rep.device_ms, args.steps, dist)
+        res[form] = dict(ms_per_step=ms / args.steps, value=value, launches=rep.kernel_launches)
         if form == "mixed":
             launches_total = rep.kernel_launches
             res[form]["clocks"] = clocks

@@ -204,6 +204,15 @@ int kg_last_error(const kg_handle *h, char *buf, size_t cap);
  * with the same nsteps and dt.                                               */
 int kg_use_graph(kg_handle *h, int enable);
 
+/* Autotuner of the flux+collision schedule (one CTA per cell, or a persistent grid of
+ * resident CTAs taking cells from a work queue in cell order or largest-grid-first, at
+ * the occupancy limit or one CTA/SM below).  When enabled, the first step after each
+ * topology or membership change times the candidates on the live layout and keeps the
+ * fastest.  All candidates compute every cell identically, so results do not depend on
+ * the choice.  kg_autotune_result: chosen schedule (0/1/2), CTAs/SM, per-candidate ms. */
+int kg_autotune(kg_handle *h, int enable);
+int kg_autotune_result(const kg_handle *h, int32_t *schedule, int32_t *ctas_per_sm, double *trial_ms, int32_t cap);
+
 /* ---- batches --------------------------------------------------------------
  * Many independent problems (uneven cell and velocity counts, their own gas constants,
  * Δt and step counters) advanced together: every sub-step is one launch over all of

@@ -15,6 +15,8 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t solid(const Dev&, int, cudaStream_t);
     static cudaError_t wall(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
+    static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
+    static int flux_occupancy(const Dev&, int);
 };
 cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
@@ -125,6 +127,15 @@ struct kg_handle {
     std::vector<double> pms;
     std::vector<int64_t> pcount;
     std::vector<const char*> pname_ptrs;
+    // flux schedule (autotuned): 0 one CTA per cell, 1 persistent in cell order,
+    // 2 persistent with the largest velocity grids first
+    int sched = 0;
+    int sched_ctas = 0;           // resident CTAs per SM of the persistent grid
+    bool autotune = false;
+    int64_t tuned_version = -1;
+    double tune_ms[8] = {0};
+    int* d_counter = nullptr;
+    const int32_t* d_order = nullptr;
     // graph
     bool use_graph = false;
     cudaGraphExec_t gexec = nullptr;
@@ -159,8 +170,9 @@ int upload_vec(kg_handle* h, const std::vector<V>& v, const V** out) {
     h->topo_allocs.push_back(p);
     h->topo_bytes += (int64_t)n;
     if (!v.empty()) {
-        e = cudaMemcpy(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpy topology");
+        // on the handle's stream: a non-blocking stream is not ordered after the legacy one
+        e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync topology");
     }
     *out = (const V*)p;
     return KG_OK;
@@ -169,8 +181,8 @@ int pool_alloc(kg_handle* h, size_t n, void** out) {
     void* p = nullptr;
     cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 8));
     if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    e = cudaMemset(p, 0, std::max<size_t>(n, 8));
-    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemset");
+    e = cudaMemsetAsync(p, 0, std::max<size_t>(n, 8), h->stream);
+    if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
     h->pool_allocs.push_back(p);
     h->pool_bytes += (int64_t)n;
     *out = p;
@@ -215,12 +227,16 @@ int make_pools(kg_handle* h, int64_t fcap, int64_t dcap) {
     if ((rc = pool_alloc(h, sizeof(int64_t) * MAX_SLOTS, &p))) return rc; h->d_step = (int64_t*)p;
     if ((rc = pool_alloc(h, sizeof(int) * MAX_SLOTS, &p))) return rc; h->d_status = (int*)p;
     if ((rc = pool_alloc(h, sizeof(double) * MAX_SLOTS * RES_STRIDE, &p))) return rc; h->res_out = (double*)p;
+    if ((rc = pool_alloc(h, sizeof(int) * 4, &p))) return rc; h->d_counter = (int*)p;
     h->fcap = fcap; h->dcap = dcap;
     h->fslab.reset(fcap);
     h->dslab.reset(dcap);
     h->probs.assign(MAX_SLOTS, Problem());
     h->parity = 0;
     h->dirty = true;
+    // the zero fill of a pool of hundreds of GB runs for tens of ms; finish it before any
+    // state upload lands in the pools
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
     return KG_OK;
 }
 
@@ -271,7 +287,11 @@ int rebuild(kg_handle* h) {
         if (M.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
         int dev_smem = 0;
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
-        size_t smax = ((size_t)M.ndf * M.max_nv + 2 * (size_t)M.dim * M.max_axis) * sizeof(double) + 16384;
+        // dynamic shared memory of the flux and wall kernels plus a reserve for their static arrays
+        const size_t sa = storage_size(h);
+        const size_t sflux = ((size_t)M.ndf * M.max_nv + 2 * (size_t)M.dim * M.max_axis) * sa + 16384;
+        const size_t swall = ((size_t)(M.ndf + 1) * M.max_nv + (size_t)M.dim * M.max_axis) * sa + M.max_nv + 4096;
+        const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
     }
     Dev& P = h->dev;
@@ -289,6 +309,15 @@ int rebuild(kg_handle* h) {
     UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
     P.max_axis = M.max_axis;
+    {
+        std::vector<int32_t> order(M.fluid_cells.size());
+        for (size_t q = 0; q < order.size(); ++q) order[q] = (int32_t)q;
+        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+            return M.dnv[M.fluid_cells[a]] > M.dnv[M.fluid_cells[b]];
+        });
+        int r = upload_vec(h, order, &h->d_order);
+        if (r) return r;
+    }
     const int32_t* dl;
     { int r = upload_vec(h, h->live, &dl); if (r) return r; }
     h->d_live = const_cast<int32_t*>(dl);
@@ -308,7 +337,8 @@ int rebuild(kg_handle* h) {
         pb.pp.slot = parts[q].slot;
     }
     for (int s = 0; s < MAX_SLOTS; ++s) table[s] = h->probs[s].pp;
-    KG_CUDA(h, cudaMemcpy(h->d_probs, table.data(), sizeof(ProbParams) * MAX_SLOTS, cudaMemcpyHostToDevice));
+    KG_CUDA(h, cudaMemcpyAsync(h->d_probs, table.data(), sizeof(ProbParams) * MAX_SLOTS, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // host vectors of this layout stay alive until here
     P.probs = h->d_probs;
     P.prob_step = h->d_step;
     P.status = h->d_status;
@@ -317,6 +347,66 @@ int rebuild(kg_handle* h) {
     P.flux = h->prm.flux; P.marching = h->prm.marching;
     h->dirty = false;
     h->version += 1;
+    return KG_OK;
+}
+
+cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
+    const Flat& F = h->M;
+    if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux(P, F.n_fluid, F.max_nv, s); });
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+    int grid = std::max(1, std::min(F.n_fluid, nsm * std::max(ctas, 1)));
+    const int32_t* order = sched == 2 ? h->d_order : nullptr;
+    return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, F.n_fluid, F.max_nv, grid, h->d_counter, order, s); });
+}
+
+// Autotuner: times the flux schedules on the current layout and keeps the fastest.  Every
+// candidate does the same per-cell arithmetic, so the choice never changes results; the
+// per-cell state the trial launches touch (w, prim, qf, status) is restored afterwards.
+int autotune_flux(kg_handle* h) {
+    const Flat& F = h->M;
+    if (F.n_fluid == 0) return KG_OK;
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fA : h->fB;
+    P.f_out = h->parity == 0 ? h->fB : h->fA;
+    int occ = dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, F.max_nv); });
+    struct Cand { int sched, ctas; };
+    std::vector<Cand> cands = {{0, 0}, {1, std::max(occ, 1)}, {2, std::max(occ, 1)}};
+    if (occ > 1) cands.push_back({2, occ - 1});
+    const size_t nw = sizeof(double) * h->dcap * MAXW, nq = sizeof(double) * h->dcap * MAXD;
+    std::vector<char> bw(nw), bp(nw), bq(nq);
+    std::vector<int> bs(MAX_SLOTS);
+    KG_CUDA(h, cudaMemcpyAsync(bw.data(), h->w, nw, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(bp.data(), h->prim, nw, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(bq.data(), h->qf, nq, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(bs.data(), h->d_status, sizeof(int) * MAX_SLOTS, cudaMemcpyDeviceToHost, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0); cudaEventCreate(&e1);
+    double best = 1e300;
+    int bi = 0;
+    for (size_t c = 0; c < cands.size(); ++c) {
+        cudaError_t e = launch_flux(h, P, cands[c].sched, cands[c].ctas, h->stream);   // warm-up
+        if (e != cudaSuccess) return cuda_fail(h, e, "autotune");
+        cudaEventRecord(e0, h->stream);
+        for (int r = 0; r < 3; ++r) launch_flux(h, P, cands[c].sched, cands[c].ctas, h->stream);
+        cudaEventRecord(e1, h->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (c < 8) h->tune_ms[c] = ms / 3.0;
+        if (ms < best) { best = ms; bi = (int)c; }
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    KG_CUDA(h, cudaMemcpyAsync(h->w, bw.data(), nw, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->prim, bp.data(), nw, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->qf, bq.data(), nq, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->d_status, bs.data(), sizeof(int) * MAX_SLOTS, cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->sched = cands[bi].sched;
+    h->sched_ctas = cands[bi].ctas;
+    h->tuned_version = h->version;
+    if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; h->g_nsteps = -1; }
     return KG_OK;
 }
 
@@ -371,7 +461,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
     }
     if (F.n_fluid > 0) {
         begin();
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux(P, F.n_fluid, F.max_nv, s); });
+        e = launch_flux(h, P, h->sched, h->sched_ctas, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         end("flux_collide_kernel");
         ++*launches;
@@ -387,6 +477,10 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
 int run_steps(kg_handle* h, int32_t nsteps, double* device_ms, int64_t* launches_out) {
     int rc = rebuild(h);
     if (rc) return rc;
+    if (h->autotune && h->tuned_version != h->version) {
+        rc = autotune_flux(h);
+        if (rc) return rc;
+    }
     // clear the checked flags so the report covers this call only
     for (int s : h->live)
         KG_CUDA(h, cudaMemsetAsync(h->res_out + (int64_t)s * RES_STRIDE + 2 * MAXW + 1, 0, sizeof(double), h->stream));
@@ -722,6 +816,22 @@ int kg_last_error(const kg_handle* h, char* buf, size_t cap) {
 int kg_use_graph(kg_handle* h, int enable) {
     if (!h) return KG_ERR_ARG;
     h->use_graph = enable != 0;
+    return KG_OK;
+}
+
+int kg_autotune(kg_handle* h, int enable) {
+    if (!h) return KG_ERR_ARG;
+    h->autotune = enable != 0;
+    h->tuned_version = -1;
+    if (!h->autotune) { h->sched = 0; h->sched_ctas = 0; }
+    return KG_OK;
+}
+
+int kg_autotune_result(const kg_handle* h, int32_t* schedule, int32_t* ctas_per_sm, double* trial_ms, int32_t cap) {
+    if (!h) return KG_ERR_ARG;
+    if (schedule) *schedule = h->sched;
+    if (ctas_per_sm) *ctas_per_sm = h->sched_ctas;
+    if (trial_ms) for (int i = 0; i < std::min(cap, 8); ++i) trial_ms[i] = h->tune_ms[i];
     return KG_OK;
 }
 

@@ -52,6 +52,17 @@ template <int D, typename A> __device__ __forceinline__ A merge_scale(int li, in
     return lj > li ? (A)ldexpf(1.0f, -D * (lj - li)) : (A)1;
 }
 
+// exp of an FP64 exponent into the arithmetic precision: FP64 for the plain form; for the
+// mixed form the FP64 argument is split a = hi + lo (hi = float(a)) and
+// exp(a) = expf(hi) * (1 + lo), accurate to FP32 rounding with a handful of FP64 operations
+template <typename A> __device__ __forceinline__ A exp_arg(double a);
+template <> __device__ __forceinline__ double exp_arg<double>(double a) { return exp(a); }
+template <> __device__ __forceinline__ float exp_arg<float>(double a) {
+    const float hi = (float)a;
+    const float lo = (float)(a - (double)hi);
+    return expf(hi) * (1.0f + lo);
+}
+
 struct VGridView {
     int64_t goff;
     int nv;
@@ -202,63 +213,120 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
     }
 }
 
+// Compensated (Kahan) accumulator for the FP32 arithmetic of the mixed form; plain sum in FP64.
+template <typename A> struct KSum {
+    A s = 0, c = 0;
+    __device__ __forceinline__ void add(A x) { A y = x - c; A t = s + y; c = (t - s) - y; s = t; }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+template <> struct KSum<double> {
+    double s = 0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+
+// Block sum of compensated per-thread accumulators into FP64 results.
+template <int N>
+__device__ __forceinline__ void block_sum_ks(const KSum<double> (&v)[N], double (&out)[N], double* sred) {
+#pragma unroll
+    for (int e = 0; e < N; ++e) out[e] = v[e].s;
+    block_sum<N>(out, sred);
+}
+template <int N>
+__device__ __forceinline__ void block_sum_ks(const KSum<float> (&v)[N], double (&out)[N], double* sred) {
+    float hi[N], lo[N];
+#pragma unroll
+    for (int e = 0; e < N; ++e) { hi[e] = v[e].s; lo[e] = -v[e].c; }
+    block_sum_ff<N>(hi, lo, out, sred);
+}
+
+// limiter ratio: exact division in FP64; the fast FP32 division (2 ulp) in the mixed form,
+// where it only scales the slope term through min(|ratio|, 1)
+__device__ __forceinline__ double lim_div(double a, double b) { return a / b; }
+__device__ __forceinline__ float lim_div(float a, float b) { return __fdividef(a, b); }
+
 // =============================================================================
 // immersed boundary
 // =============================================================================
+// Per-CTA constants of one image_df / update_solid_cell! source list, in the arithmetic
+// precision: the unit direction l/|l| and the offset l of each source, and where its f lives.
+template <typename A> struct IbNbrA {
+    A lhat[MAXD];
+    A dx[MAXD];
+    int64_t fo, gn;
+    int32_t nvn, pair;
+};
+constexpr int MAX_IB_NBR = 2 * MAXD + 1;   // face neighbours + the donor (checked by construction)
+
+// filled by the first `cnt` threads; the caller synchronises before use
+template <int D, typename A>
+__device__ __forceinline__ void ib_setup(const Dev& P, int list, int cnt, IbNbrA<A>* nb) {
+    const int n = threadIdx.x;
+    if (n >= cnt || n >= MAX_IB_NBR) return;
+    const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
+    const NbrRef r = P.ib_nbr[list + n];
+    A l[D], nl = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) { l[d] = (A)dx[d]; nl += l[d] * l[d]; }
+    nl = sqrt(nl);
+    IbNbrA<A> c;
+#pragma unroll
+    for (int d = 0; d < MAXD; ++d) { c.lhat[d] = d < D ? l[d] / nl : (A)0; c.dx[d] = d < D ? l[d] : (A)0; }
+    c.fo = P.foff[r.data];
+    c.nvn = P.dnv[r.data];
+    c.pair = r.pair;
+    c.gn = r.pair >= 0 ? P.g_off[P.dgrid[r.data]] : 0;
+    nb[n] = c;
+}
+
 // Σ_n weight_n(u) * merge_n(f_n + sdf_n . dx_n) over a source list, for target velocity i
 // (vs_extrapolate! with the directional weights of update_solid_cell! / image_df).
 template <int D, int NDF, typename T>
-__device__ __forceinline__ void extrapolate(const Dev& P, const VGridView& g, int i, int li, int list, int cnt,
-                                            double* out) {
+__device__ __forceinline__ void extrapolate(const Dev& P, const VGridView& g, int i, int li,
+                                            const IbNbrA<typename Arith<T>::type>* nb, int cnt,
+                                            typename Arith<T>::type* out) {
     using A = typename Arith<T>::type;
     const T* f = (const T*)P.f_in;
     const T* sdf = (const T*)P.sdf;
-    double u[D], un = 0.0;
+    const A* VU = vel<A>(P);
+    A u[D], un = 0;
 #pragma unroll
-    for (int d = 0; d < D; ++d) { u[d] = g.u(i, d); un += u[d] * u[d]; }
+    for (int d = 0; d < D; ++d) { u[d] = VU[(int64_t)d * P.PG + g.goff + i]; un += u[d] * u[d]; }
     un = sqrt(un);
-    double W[2 * MAXD + 1];
-    double wsum = 0.0;
+    A W[MAX_IB_NBR];
+    A wsum = 0;
     for (int n = 0; n < cnt; ++n) {
-        const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
-        double nl = 0.0;
+        A ul = 0;
 #pragma unroll
-        for (int d = 0; d < D; ++d) nl += dx[d] * dx[d];
-        nl = sqrt(nl);
-        double ul = 0.0;
-#pragma unroll
-        for (int d = 0; d < D; ++d) ul += u[d] * (dx[d] / nl);
-        double v = fmax(0.0, ul / un);
+        for (int d = 0; d < D; ++d) ul += u[d] * nb[n].lhat[d];
+        A v = ul / un;
+        v = v > (A)0 ? v : (A)0;
         W[n] = v * v;
         wsum += W[n];
     }
 #pragma unroll
-    for (int k = 0; k < NDF; ++k) out[k] = 0.0;
+    for (int k = 0; k < NDF; ++k) out[k] = 0;
     for (int n = 0; n < cnt; ++n) {
-        const double wi = wsum == 0.0 ? 1.0 / cnt : W[n] / wsum;
-        NbrRef r = P.ib_nbr[list + n];
-        const double* dx = P.ib_dx + (int64_t)(list + n) * MAXD;
-        const int64_t fo = P.foff[r.data];
-        const int nvn = P.dnv[r.data];
-        const T* fn = f + fo;
-        const T* sn = sdf + fo * D;
+        const A wi = wsum == (A)0 ? (A)1 / (A)cnt : W[n] / wsum;
+        const IbNbrA<A>& r = nb[n];
+        const int nvn = r.nvn;
+        const T* fn = f + r.fo;
+        const T* sn = sdf + r.fo * D;
         int j0 = i, jc = 1;
-        int64_t gn = 0;
         if (r.pair >= 0) {
-            int64_t po = P.p_off[r.pair] + i;
+            const int64_t po = P.p_off[r.pair] + i;
             j0 = P.p_j0[po];
             jc = P.p_cnt[po];
-            gn = P.g_off[P.dgrid[r.data]];
         }
         for (int j = j0; j < j0 + jc; ++j) {
-            double sc = r.pair >= 0 ? merge_inv_scale<D>(li, P.vlev[gn + j]) : 1.0;
+            const A sc = r.pair >= 0 ? merge_scale<D, A>(li, P.vlev[r.gn + j]) : (A)1;
 #pragma unroll
             for (int k = 0; k < NDF; ++k) {
-                A v = (A)fn[(int64_t)k * nvn + j];
-                A s = 0;
+                A v = (A)fn[k * nvn + j];
+                A sv = 0;
 #pragma unroll
-                for (int d = 0; d < D; ++d) s += (A)sn[((int64_t)d * NDF + k) * nvn + j] * (A)dx[d];
-                out[k] += (double)(v + s) * sc * wi;
+                for (int d = 0; d < D; ++d) sv += (A)sn[(d * NDF + k) * nvn + j] * r.dx[d];
+                out[k] += (v + sv) * sc * wi;
             }
         }
     }
@@ -275,34 +343,54 @@ __device__ __forceinline__ void moments_add(const VGridView& g, const double wgt
     else m[D + 1] += 0.5 * wgt * u2 * fv[0];
 }
 
+// moments of one velocity cell into compensated accumulators in the arithmetic precision
+template <int D, int NDF, typename A>
+__device__ __forceinline__ void moments_add_a(const A* u, const A wgt, const A* fv, KSum<A>* m) {
+    A u2 = 0;
+    m[0].add(wgt * fv[0]);
+#pragma unroll
+    for (int d = 0; d < D; ++d) { m[1 + d].add(wgt * u[d] * fv[0]); u2 += u[d] * u[d]; }
+    if (NDF == 2) m[D + 1].add((A)0.5 * wgt * (u2 * fv[0] + fv[NDF - 1]));
+    else m[D + 1].add((A)0.5 * wgt * u2 * fv[0]);
+}
+
+// update_solid_cell! (Immersed_boundary.jl:98-146): a solid ghost cell's f is extrapolated
+// from its fluid neighbours; its w and prim are the moments of that f.
 template <int D, int NDF, typename T>
 __global__ void __launch_bounds__(BLOCK) solid_kernel(Dev P) {
+    using A = typename Arith<T>::type;
     __shared__ double sred[(D + 2) * (BLOCK / 32)];
+    __shared__ IbNbrA<A> snb[MAX_IB_NBR];
     const SolidOp op = P.solid_ops[blockIdx.x];
+    ib_setup<D, A>(P, op.list, op.cnt, snb);
+    __syncthreads();
     const VGridView g = grid_view(P, op.cell);
     const int nv = g.nv;
     const int64_t fo = P.foff[op.cell];
     T* fa = (T*)P.f_in + fo;
     T* fb = (T*)P.f_out + fo;
-    const double* vw = P.vw + g.goff;
-    double m[D + 2];
-#pragma unroll
-    for (int e = 0; e < D + 2; ++e) m[e] = 0.0;
+    const A* VU = vel<A>(P);
+    const A* VW = wts<A>(P) + g.goff;
+    KSum<A> m[D + 2];
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
-        double v[NDF];
-        extrapolate<D, NDF, T>(P, g, i, li, op.list, op.cnt, v);
+        A va[NDF];
+        extrapolate<D, NDF, T>(P, g, i, li, snb, op.cnt, va);
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) { fa[(int64_t)k * nv + i] = (T)v[k]; fb[(int64_t)k * nv + i] = (T)v[k]; }
-        moments_add<D, NDF>(g, vw[i], i, v, m);
+        for (int k = 0; k < NDF; ++k) { fa[(int64_t)k * nv + i] = (T)va[k]; fb[(int64_t)k * nv + i] = (T)va[k]; }
+        A u[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) u[d] = VU[(int64_t)d * P.PG + g.goff + i];
+        moments_add_a<D, NDF, A>(u, VW[i], va, m);
     }
-    block_sum<D + 2>(m, sred);
+    double mw[D + 2];
+    block_sum_ks<D + 2>(m, mw, sred);
     if (threadIdx.x == 0) {
         double* w = P.w + (int64_t)op.cell * MAXW;
         double* pr = P.prim + (int64_t)op.cell * MAXW;
 #pragma unroll
-        for (int e = 0; e < D + 2; ++e) w[e] = m[e];
-        get_prim<D>(m, P.probs[P.dprob[op.cell]].gamma, pr);
+        for (int e = 0; e < D + 2; ++e) w[e] = mw[e];
+        get_prim<D>(mw, P.probs[P.dprob[op.cell]].gamma, pr);
     }
 }
 
@@ -317,108 +405,154 @@ __device__ __forceinline__ double maxwell_h(const VGridView& g, int i, const dou
     return prim[0] * pre * exp(-lam * c2);
 }
 
+// shared memory of wall_kernel for a donor grid of nv velocity cells
+template <int D, int NDF, typename A>
+__host__ __device__ __forceinline__ size_t wall_smem(int nv, int max_axis) {
+    return ((size_t)(NDF + 1) * nv + (size_t)D * max_axis) * sizeof(A) + (size_t)nv;
+}
+
+// update_solid_neighbor! (Immersed_boundary.jl:367-483): the SolidNeighbor's f is the
+// diffuse-wall Maxwellian (density from the zero-mass-flux condition) for velocities leaving
+// the wall and the slope-limited image extrapolation for velocities entering it, blended on
+// the cut velocity cells; the wall-direction slope is kept for the flux of the donor.
 template <int D, int NDF, typename T>
 __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
-    extern __shared__ double sh[];
-    double* aux = sh;                          // NDF * nv
+    using A = typename Arith<T>::type;
+    extern __shared__ __align__(16) unsigned char wsh[];
     __shared__ double sred[2 * (BLOCK / 32)];
+    __shared__ IbNbrA<A> snb[MAX_IB_NBR];
+    // per-CTA constants in the arithmetic precision, set by thread 0
+    enum { W_N = 0, W_IDXS = W_N + MAXD, W_IDXF, W_DXL, W_PRE, W_BK, W_COUNT };
+    __shared__ A wc[W_COUNT];
     const WallOp op = P.wall_ops[blockIdx.x];
     const VGridView g = grid_view(P, op.donor);
     const VGridView gs = grid_view(P, op.solid);
     const int nv = g.nv, nvs = gs.nv;
+    const int gid = P.dgrid[op.donor];
+    const int MA = P.max_axis;
+    A* aux = (A*)wsh;                                // NDF * nv: image extrapolation
+    A* mhs = aux + (size_t)NDF * nv;                 // nv: wall Maxwellian with rho = 1
+    A* Ew = mhs + nv;                                // D * max_axis: its 1D factors
+    unsigned char* out_dir = (unsigned char*)(Ew + (size_t)D * MA);   // nv: u.n >= 0
+    ib_setup<D, A>(P, op.list, op.cnt, snb);
+    const double lam = op.bc[D + 1];
+    const double Kw = P.probs[P.dprob[op.donor]].K;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int d = 0; d < MAXD; ++d) wc[W_N + d] = (A)op.normal[d];
+        wc[W_IDXS] = (A)(1.0 / op.dxs);
+        wc[W_IDXF] = (A)(1.0 / op.dxf);
+        wc[W_DXL] = (A)op.dxL;
+        wc[W_PRE] = (A)(D == 2 ? lam / PI : pow(lam / PI, 1.5));
+        wc[W_BK] = (A)(Kw / (2.0 * lam));
+    }
+    // 1D factors exp(-lam (x - U_d)^2) of the wall Maxwellian at the grid's axis coordinates
+    // (FP64 exponents; discrete_maxwell_2D2F / 3D1F)
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
+        for (int a = threadIdx.x; a < na; a += BLOCK) {
+            const double cu = P.ax_val[a0 + a] - op.bc[1 + d];
+            Ew[d * MA + a] = exp_arg<A>(-lam * cu * cu);
+        }
+    }
+    __syncthreads();
     const T* fc = (const T*)P.f_in + P.foff[op.donor];
     const T* fsol = (const T*)P.f_in + P.foff[op.solid];
     const int64_t wo = P.foff[op.data];
     T* wsdf = (T*)P.sdf + wo * D;
     const double* cvcw = P.cvcw + op.cvcw_off;
     const int dir = op.dir;
-    double prim1[MAXW];
-#pragma unroll
-    for (int e = 0; e < D + 2; ++e) prim1[e] = op.bc[e];
-    prim1[0] = 1.0;
-    double red[2] = {0.0, 0.0};  // MuR, SF
+    const A* VU = vel<A>(P);
+    const uint16_t* vx = P.vidx + g.goff;
+    const A idxs = wc[W_IDXS], idxf = wc[W_IDXF], dxL = wc[W_DXL], pre = wc[W_PRE];
+    KSum<A> red[2];   // MuR, SF
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
-        double vn = 0.0;
+        // the sign of u.n picks the branch: FP64, as in the reference
+        double vnd = 0.0;
 #pragma unroll
-        for (int d = 0; d < D; ++d) vn += g.u(i, d) * op.normal[d];
-        const double theta = vn >= 0.0 ? 1.0 : 0.0;
-        double ib[NDF];
-        extrapolate<D, NDF, T>(P, g, i, li, op.list, op.cnt, ib);
+        for (int d = 0; d < D; ++d) vnd += g.u(i, d) * op.normal[d];
+        const bool leaving = vnd >= 0.0;
+        out_dir[i] = leaving;
+        const A vn = (A)vnd;
+        A ib[NDF];
+        extrapolate<D, NDF, T>(P, g, i, li, snb, op.cnt, ib);
         // boundary_slope! (Immersed_boundary.jl:396-435)
-        double sL[NDF];
+        A sL[NDF];
         int j0 = i, jc = 1;
         if (op.spair >= 0) {
-            int64_t po = P.p_off[op.spair] + i;
+            const int64_t po = P.p_off[op.spair] + i;
             j0 = P.p_j0[po];
             jc = P.p_cnt[po];
         }
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) sL[k] = 0.0;
+        for (int k = 0; k < NDF; ++k) sL[k] = 0;
         for (int j = j0; j < j0 + jc; ++j) {
-            double sc = op.spair >= 0 ? merge_inv_scale<D>(li, P.vlev[gs.goff + j]) : 1.0;
+            const A sc = op.spair >= 0 ? merge_scale<D, A>(li, P.vlev[gs.goff + j]) : (A)1;
 #pragma unroll
             for (int k = 0; k < NDF; ++k)
-                sL[k] += ((double)fc[(int64_t)k * nv + i] - (double)fsol[(int64_t)k * nvs + j]) * sc / op.dxs;
+                sL[k] += ((A)fc[(int64_t)k * nv + i] - (A)fsol[(int64_t)k * nvs + j]) * sc * idxs;
         }
-        double a0 = 0.0;
+        A a0 = 0;
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
-            double fck = (double)fc[(int64_t)k * nv + i];
-            double ss = minmod(sL[k], (ib[k] - fck) / op.dxf);
-            ss = fmin(fabs((ib[k] - JL_EPS) / (ss * op.dxL + JL_EPS)), 1.0) * ss;
+            const A fck = (A)fc[(int64_t)k * nv + i];
+            A ss = minmod(sL[k], (ib[k] - fck) * idxf);
+            const A r = fabs(lim_div(ib[k] - (A)JL_EPS, ss * dxL + (A)JL_EPS));
+            ss = (r < (A)1 ? r : (A)1) * ss;
             wsdf[((int64_t)dir * NDF + k) * nv + i] = (T)ss;
-            double a = ib[k] + ss * op.dxL;
+            const A a = ib[k] + ss * dxL;
             aux[(int64_t)k * nv + i] = a;
             if (k == 0) a0 = a;
         }
-        const double mh = maxwell_h<D>(g, i, prim1);
-        red[0] += cvcw[i] * vn * mh * theta;
-        red[1] += cvcw[i] * vn * a0 * (1.0 - theta);
+        A mh = pre;
+#pragma unroll
+        for (int d = 0; d < D; ++d) mh *= Ew[d * MA + vx[(int64_t)d * P.PG + i]];
+        mhs[i] = mh;
+        const A cw = (A)cvcw[i];
+        if (leaving) red[0].add(cw * vn * mh);
+        else red[1].add(cw * vn * a0);
     }
     __syncthreads();
     for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
         const int idx = P.cut_idx[op.cut_off + a];
-        double vn = 0.0;
+        A vn = 0;
 #pragma unroll
-        for (int d = 0; d < D; ++d) vn += g.u(idx, d) * op.normal[d];
-        const double mh = maxwell_h<D>(g, idx, prim1);
-        red[0] += P.cut_sw[op.cut_off + a] * vn * mh;
-        red[1] += P.cut_gw[op.cut_off + a] * vn * aux[idx];
+        for (int d = 0; d < D; ++d) vn += VU[(int64_t)d * P.PG + g.goff + idx] * wc[W_N + d];
+        red[0].add((A)P.cut_sw[op.cut_off + a] * vn * mhs[idx]);
+        red[1].add((A)P.cut_gw[op.cut_off + a] * vn * aux[idx]);
     }
-    block_sum<2>(red, sred);
-    const double rho_w = -red[1] / red[0];
+    double rs[2];
+    block_sum_ks<2>(red, rs, sred);
+    const double rho_w = -rs[1] / rs[0];
+    const A rw = (A)rho_w, bk = wc[W_BK];
     T* wa = (T*)P.f_in + wo;
     T* wb = (T*)P.f_out + wo;
-    const double lam = prim1[D + 1];
-    const double Kw = P.probs[P.dprob[op.donor]].K;
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
-        double vn = 0.0;
-#pragma unroll
-        for (int d = 0; d < D; ++d) vn += g.u(i, d) * op.normal[d];
-        if (vn >= 0.0) {
-            const double mh = maxwell_h<D>(g, i, prim1);
-            double mv[NDF];
-            mv[0] = mh;
-            if (NDF == 2) mv[NDF - 1] = mh * Kw / (2.0 * lam);
-#pragma unroll
-            for (int k = 0; k < NDF; ++k) { T v = (T)(mv[k] * rho_w); wa[(int64_t)k * nv + i] = v; wb[(int64_t)k * nv + i] = v; }
+        A v[NDF];
+        if (out_dir[i]) {
+            const A mh = mhs[i];
+            v[0] = mh * rw;
+            if (NDF == 2) v[NDF - 1] = mh * bk * rw;
         } else {
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) { T v = (T)aux[(int64_t)k * nv + i]; wa[(int64_t)k * nv + i] = v; wb[(int64_t)k * nv + i] = v; }
+            for (int k = 0; k < NDF; ++k) v[k] = aux[(int64_t)k * nv + i];
         }
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) { wa[(int64_t)k * nv + i] = (T)v[k]; wb[(int64_t)k * nv + i] = (T)v[k]; }
     }
     __syncthreads();
     for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
         const int idx = P.cut_idx[op.cut_off + a];
-        const double gw = P.cut_gw[op.cut_off + a], sw = P.cut_sw[op.cut_off + a];
-        const double mh = maxwell_h<D>(g, idx, prim1);
-        double mv[NDF];
-        mv[0] = mh;
-        if (NDF == 2) mv[NDF - 1] = mh * Kw / (2.0 * lam);
+        const A gw = (A)P.cut_gw[op.cut_off + a], sw = (A)P.cut_sw[op.cut_off + a];
+        const A mh = mhs[idx];
+        A mv[NDF];
+        mv[0] = mh * rw;
+        if (NDF == 2) mv[NDF - 1] = mh * bk * rw;
 #pragma unroll
         for (int k = 0; k < NDF; ++k) {
-            T v = (T)((gw * aux[(int64_t)k * nv + idx] + sw * (mv[k] * rho_w)) / (gw + sw));
+            const T v = (T)((gw * aux[(int64_t)k * nv + idx] + sw * mv[k]) / (gw + sw));
             wa[(int64_t)k * nv + idx] = v;
             wb[(int64_t)k * nv + idx] = v;
         }
@@ -483,38 +617,6 @@ __device__ __forceinline__ void psi_add(double* m, double wgt, const double* u, 
     else m[D + 1] += 0.5 * wgt * u2 * v[0];
 }
 
-// Compensated (Kahan) accumulator for the FP32 arithmetic of the mixed form; plain sum in FP64.
-template <typename A> struct KSum {
-    A s = 0, c = 0;
-    __device__ __forceinline__ void add(A x) { A y = x - c; A t = s + y; c = (t - s) - y; s = t; }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-template <> struct KSum<double> {
-    double s = 0;
-    __device__ __forceinline__ void add(double x) { s += x; }
-    __device__ __forceinline__ double value() const { return s; }
-};
-
-// Block sum of compensated per-thread accumulators into FP64 results.
-template <int N>
-__device__ __forceinline__ void block_sum_ks(const KSum<double> (&v)[N], double (&out)[N], double* sred) {
-#pragma unroll
-    for (int e = 0; e < N; ++e) out[e] = v[e].s;
-    block_sum<N>(out, sred);
-}
-template <int N>
-__device__ __forceinline__ void block_sum_ks(const KSum<float> (&v)[N], double (&out)[N], double* sred) {
-    float hi[N], lo[N];
-#pragma unroll
-    for (int e = 0; e < N; ++e) { hi[e] = v[e].s; lo[e] = -v[e].c; }
-    block_sum_ff<N>(hi, lo, out, sred);
-}
-
-// limiter ratio: exact division in FP64; the fast FP32 division (2 ulp) in the mixed form,
-// where it only scales the slope term through min(|ratio|, 1)
-__device__ __forceinline__ double lim_div(double a, double b) { return a / b; }
-__device__ __forceinline__ float lim_div(float a, float b) { return __fdividef(a, b); }
-
 // own-side reconstruction from registers (positivity / plain / none)
 template <int D, typename A>
 __device__ __forceinline__ A own_recon(int mode, A f, const A* s, const A* dx, const A* ds) {
@@ -552,17 +654,6 @@ __device__ __forceinline__ void other_micro(const T* f, const T* sdf, int nvd, i
     }
 }
 
-// exp of an FP64 exponent into the arithmetic precision: FP64 for the plain form; for the
-// mixed form the FP64 argument is split a = hi + lo (hi = float(a)) and
-// exp(a) = expf(hi) * (1 + lo), accurate to FP32 rounding with a handful of FP64 operations
-template <typename A> __device__ __forceinline__ A exp_arg(double a);
-template <> __device__ __forceinline__ double exp_arg<double>(double a) { return exp(a); }
-template <> __device__ __forceinline__ float exp_arg<float>(double a) {
-    const float hi = (float)a;
-    const float lo = (float)(a - (double)hi);
-    return expf(hi) * (1.0f + lo);
-}
-
 // per-incidence constants in the arithmetic precision
 template <typename A, typename T> struct IncA {
     A dxm[MAXD];    // face midpoint - my reconstruction centre
@@ -575,8 +666,9 @@ template <typename A, typename T> struct IncA {
     int8_t kind, dir, bc_kind, mode_out, mode_in;
 };
 
+// flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part)
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P) {
+__device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ Incidence sinc[MAX_INC];
@@ -588,7 +680,6 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
     enum { C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
            C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
     __shared__ A sc[C_N];
-    const int fcx = blockIdx.x;
     const int cell = P.fluid_cells[fcx];
     const int slot = P.dprob[cell];
     const ProbParams& PP = P.probs[slot];
@@ -927,25 +1018,8 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
     for (int d = 0; d < D; ++d) { Uh[d] = sc[C_UH + d]; Ul[d] = sc[C_UL + d]; }
     // ---- 3. conservation correction and heat flux --------------------------------
     KSum<A> qs[D];
-    for (int i = threadIdx.x; i < nv; i += BLOCK) {
-        A fv[NDF];
-        A mc = prec, mn = pren;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const int ix = vx[(int64_t)d * PG + i];
-            mc *= Ec[d * MA + ix];
-            if (need_n) mn *= En[d * MA + ix];
-        }
-        if (need_n) {
-            fv[0] = fst[i] + (mc - mn);
-            if (NDF == 2) fv[NDF - 1] = fst[nv + i] + (mc * bfc - mn * bfn);
-#pragma unroll
-            for (int k = 0; k < NDF; ++k) fst[(int64_t)k * nv + i] = fv[k];
-        } else {
-#pragma unroll
-            for (int k = 0; k < NDF; ++k) fv[k] = (A)fcell[(int64_t)k * nv + i];
-        }
-        // heat_flux_2D2F / 3D1F (lib/KitCore/2D2F.jl:68-88, 3D1F.jl:41-72)
+    // heat_flux_2D2F / 3D1F (lib/KitCore/2D2F.jl:68-88, 3D1F.jl:41-72) of f at velocity i
+    auto qadd = [&](int i, const A* fv) {
         A c[D], c2 = 0;
 #pragma unroll
         for (int d = 0; d < D; ++d) { c[d] = (VU[(int64_t)d * PG + g.goff + i] - Uh[d]) - Ul[d]; c2 += c[d] * c[d]; }
@@ -953,6 +1027,32 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         const A hb = NDF == 2 ? (c2 * fv[0] + fv[NDF - 1]) : c2 * fv[0];
 #pragma unroll
         for (int d = 0; d < D; ++d) qs[d].add(wi * c[d] * hb);
+    };
+    if (need_n) {
+        // conservation correction f += M(prim_c) - M(prim)  (Theory/Iterate.jl:117), then q
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A mc = prec, mn = pren;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const int ix = vx[(int64_t)d * PG + i];
+                mc *= Ec[d * MA + ix];
+                mn *= En[d * MA + ix];
+            }
+            A fv[NDF];
+            fv[0] = fst[i] + (mc - mn);
+            if (NDF == 2) fv[NDF - 1] = fst[nv + i] + (mc * bfc - mn * bfn);
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fst[k * nv + i] = fv[k];
+            qadd(i, fv);
+        }
+    } else {
+        // Euler: q of f before convection (Theory/Iterate.jl:153)
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A fv[NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fv[k] = (A)fcell[k * nv + i];
+            qadd(i, fv);
+        }
     }
     double qv[D];
     block_sum_ks<D>(qs, qv, sred);
@@ -968,9 +1068,8 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
     A qa[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) qa[d] = sc[C_QA + d];
-    const bool cai = P.marching == KG_MARCH_CAIDVM;
-    const double tdt = tau / (tau + dt);
-    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+    // g+ = M_c (1 + Shakhov(q)) at velocity i (shakhov_part_2D2F / 3D1F)
+    auto gplus = [&](int i, A* gp) {
         A mc = prec;
 #pragma unroll
         for (int d = 0; d < D; ++d) mc *= Ec[d * MA + vx[(int64_t)d * PG + i]];
@@ -981,7 +1080,6 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
             c2 += cd * cd;
             cq += cd * qa[d];
         }
-        A gp[NDF];
         if (NDF == 2) {
             const A mb = mc * bfc;
             gp[0] = mc + sk * cq * ((A)2 * lc * c2 + Kk - (A)5) * mc;
@@ -989,12 +1087,23 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         } else {
             gp[0] = mc + sk * cq * ((A)2 * lc * c2 - (A)5) * mc;
         }
+    };
+    if (P.marching == KG_MARCH_CAIDVM) {
+        // f = f tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:121-122)
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A gp[NDF];
+            gplus(i, gp);
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) {
-            A v;
-            if (cai) v = fst[(int64_t)k * nv + i] * r1 + r2 * gp[k];
-            else v = (A)((double)fst[(int64_t)k * nv + i] * tdt) + r2 * gp[k];
-            fnew[(int64_t)k * nv + i] = (T)v;
+            for (int k = 0; k < NDF; ++k) fnew[k * nv + i] = (T)(fst[k * nv + i] * r1 + r2 * gp[k]);
+        }
+    } else {
+        // f = (f + dt/V flux) tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:156)
+        const double tdt = tau / (tau + dt);
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A gp[NDF];
+            gplus(i, gp);
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fnew[k * nv + i] = (T)((A)((double)fst[k * nv + i] * tdt) + r2 * gp[k]);
         }
     }
     // ---- 5. per-cell outputs and residual terms ------------------------------------
@@ -1016,6 +1125,31 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         }
 #pragma unroll
         for (int d = 0; d < D; ++d) P.qf[(int64_t)cell * MAXD + d] = qv[d];
+    }
+}
+
+// Flux + collision of the fluid cells.  Two schedules share this one function, so the
+// arithmetic of a cell compiles once and gives the same bits under either:
+//  * counter == nullptr: one CTA per fluid cell (cell = blockIdx.x);
+//  * persistent: `gridDim.x` resident CTAs take cells from the work counter (in `order`,
+//    when given), so a batch of uneven problems keeps every SM busy to the end of the
+//    sub-step.  The counter must be zero at launch.
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P, int* counter,
+                                                                                  const int32_t* order, int n) {
+    __shared__ int item;
+    int it = blockIdx.x;
+    for (;;) {
+        if (counter) {
+            if (threadIdx.x == 0) item = atomicAdd(counter, 1);
+            __syncthreads();
+            it = item;
+            __syncthreads();
+        }
+        if (it >= n) break;
+        flux_collide_cell<D, NDF, T>(P, order ? order[it] : it);
+        if (!counter) break;
+        __syncthreads();
     }
 }
 
@@ -1063,7 +1197,7 @@ struct Launch {
     }
     static cudaError_t wall(const Dev& P, int n, int max_nv, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        size_t smem = (size_t)NDF * max_nv * sizeof(double);
+        size_t smem = wall_smem<D, NDF, typename Arith<T>::type>(max_nv, P.max_axis);
         cudaError_t e = cudaFuncSetAttribute(wall_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         wall_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
@@ -1074,8 +1208,29 @@ struct Launch {
         size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
+        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
         return cudaGetLastError();
+    }
+    // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
+    static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,
+                                       cudaStream_t s) {
+        using A = typename Arith<T>::type;
+        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
+        cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+        if (e != cudaSuccess) return e;
+        flux_collide_kernel<D, NDF, T><<<grid, BLOCK, smem, s>>>(P, counter, order, n);
+        return cudaGetLastError();
+    }
+    // resident CTAs per SM the flux kernel reaches (for the persistent grid size)
+    static int flux_occupancy(const Dev& P, int max_nv) {
+        using A = typename Arith<T>::type;
+        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
+        cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, flux_collide_kernel<D, NDF, T>, BLOCK, smem);
+        return nb;
     }
 };
 

@@ -57,12 +57,17 @@ def random_request(rng: np.random.Generator, rid: int, arrival: float, small: bo
     else:
         n = int(rng.integers(32, 97))
         m = int(rng.integers(8, 25)) * 2
+    Ma = float(rng.uniform(0.1, 5.0))
+    U = Ma * math.sqrt(5.0 / 6.0)
+    # velocity domain [-L, L]^2 covering the bulk speed plus five thermal speeds; with an
+    # even m, v = 0 stays on a root corner (check_vs_setting)
+    L = float(math.ceil(U + 5.0))
     if kind == "cavity":
-        lid = float(rng.uniform(0.1, 5.0)) * math.sqrt(5.0 / 6.0) * 0.1
-        p = cases.cavity(n=n, nv=m, levels=0, Kn=Kn, lid=lid)
+        p = cases.cavity(n=n, nv=m, levels=0, Kn=Kn, lid=U)
+        p.case.quadrature = [-L, L, -L, L]
     else:
-        Ma = float(rng.uniform(0.1, 5.0))
         p = cases.cylinder(scale=n / 64.0, max_level=1 if small else 2, nv=m, vs_levels=0, Ma=Ma, Kn=Kn)
+        p.case.quadrature = [-L, L, -L, L]
     return Request(rid, p, arrival)
 
 

@@ -48,6 +48,8 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_download.argtypes = [vp, i32, vp, vp, vp, vp]
     L.kg_batch_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
     L.kg_batch_set_dt.argtypes = [vp, i32, dbl]
+    L.kg_autotune.argtypes = [vp, C.c_int]
+    L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     _lib = L
     return L
 
@@ -57,8 +59,15 @@ EXPORTS = [
     "kg_step", "kg_profile_enable", "kg_profile_read", "kg_memory_footprint",
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
-    "kg_batch_info", "kg_batch_set_dt",
+    "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
 ]
+
+
+def _autotune_result(L, h):
+    sch, ctas = C.c_int32(), C.c_int32()
+    ms = (C.c_double * 8)()
+    _check(L, h, L.kg_autotune_result(h, C.byref(sch), C.byref(ctas), ms, 8))
+    return {"schedule": sch.value, "ctas_per_sm": ctas.value, "trial_ms": [ms[i] for i in range(8) if ms[i] > 0]}
 
 
 class KitGpuError(RuntimeError):
@@ -135,6 +144,12 @@ class GpuStep:
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
+
+    def autotune(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
+
+    def autotune_result(self):
+        return _autotune_result(self.L, self.h)
 
     def profile_read(self):
         cap = 16
@@ -224,3 +239,9 @@ class GpuBatch:
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
+
+    def autotune(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
+
+    def autotune_result(self):
+        return _autotune_result(self.L, self.h)

@@ -67,3 +67,47 @@ def test_batch_refuses_over_budget():
             b.admit(abi.make_params(p), t, s["f"], s["w"], s["prim"], p.dt())
     assert e.value.code == 8   # KG_ERR_BUDGET
     b.close()
+
+
+@pytest.mark.parametrize("prec", [abi.KG_PREC_FP64, abi.KG_PREC_MIXED])
+def test_autotuned_persistent_schedule_gives_same_results(prec):
+    probs = _problems()
+    built = [cases.build(p) for p in probs]
+    outs = []
+    for tune in (False, True):
+        b = GpuBatch(abi.make_params(probs[0], precision=prec), 512 << 20)
+        b.autotune(tune)
+        slots = [b.admit(abi.make_params(p, precision=prec, st_check_interval=2), t, s["f"], s["w"], s["prim"], p.dt())
+                 for p, (t, s) in zip(probs, built)]
+        b.step(3)
+        res = b.autotune_result()
+        if tune:
+            assert len(res["trial_ms"]) >= 3
+        outs.append([b.download(sl) for sl in slots])
+        b.close()
+    for a, c in zip(outs[0], outs[1]):
+        for key in ("f", "w", "prim", "qf"):
+            assert np.array_equal(a[key], c[key])
+
+
+@pytest.mark.parametrize("prec", [abi.KG_PREC_FP64, abi.KG_PREC_MIXED])
+def test_large_pool_admission_keeps_state(prec):
+    """A pool of about half the device: its zero fill takes tens of ms, and an admission
+    right after creating the batch must still find its state intact (the fill and the
+    upload run in order on the handle's stream) and step like the problem alone."""
+    import torch
+    free = torch.cuda.mem_get_info()[0]
+    p = cases.cavity(n=8, nv=12, levels=0, Kn=0.3)
+    t, s = cases.build(p)
+    b = GpuBatch(abi.make_params(p, precision=prec), int(min(free * 0.5, 160 << 30)))
+    slot = b.admit(abi.make_params(p, precision=prec, st_check_interval=2), t, s["f"], s["w"], s["prim"], p.dt())
+    got = b.download(slot)
+    assert np.array_equal(got["w"], s["w"]) and np.array_equal(got["prim"], s["prim"])
+    if prec == abi.KG_PREC_FP64:
+        assert np.array_equal(got["f"], s["f"])
+    else:
+        assert np.array_equal(got["f"], s["f"].astype(np.float32).astype(np.float64))
+    b.step(2)
+    ref, _ = _alone(p, t, s, prec, 2)
+    assert np.array_equal(b.download(slot)["f"], ref["f"])
+    b.close()
