@@ -181,6 +181,14 @@ int kg_upload_topology(kg_handle *h, const kg_topology *topo);
 int kg_upload_state(kg_handle *h, const double *f, const double *w, const double *prim);
 int kg_download_state(kg_handle *h, double *f, double *w, double *prim, double *qf, double *sdf);
 
+/* Macroscopic slopes sw of update_macro_slope! (Flux/Slope.jl:1022-1036, the last call of
+ * slope!, Slope.jl:1064): for every cell with bound_enc >= 0 and each direction dir,
+ * sw[:, dir] = calc_w0 of sdf[:, :, dir].  Computed on demand from the slopes on the device,
+ * which are those the last kg_step used, so AMR criteria and output at a sync point read the
+ * values PsData.sw holds.  sw: n_cells blocks of (dim+2) x dim doubles, column-major (the
+ * PsData.sw memory); solid cells (bound_enc < 0) get zeros.                    */
+int kg_download_sw(kg_handle *h, double *sw);
+
 /* Advance `nsteps` steps with time step dt; `step` is status.step before the
  * first of them (drives the residual cadence).  One call = nsteps x
  * (slope -> flux -> iterate).                                               */
@@ -228,6 +236,7 @@ int kg_batch_admit(kg_handle *h, const kg_params *params, const kg_topology *top
 int kg_batch_release(kg_handle *h, int32_t slot);
 int kg_batch_step(kg_handle *h, int32_t nsteps, kg_step_report *reports, int32_t cap);
 int kg_batch_download(kg_handle *h, int32_t slot, double *f, double *w, double *prim, double *qf);
+int kg_batch_download_sw(kg_handle *h, int32_t slot, double *sw);   /* kg_download_sw of one problem */
 int kg_batch_info(const kg_handle *h, int32_t *n_live, int64_t *f_free_elems, int64_t *bytes_per_elem);
 int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
 

@@ -17,6 +17,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
+    static cudaError_t macro_slope(const Dev&, int, int, double*, cudaStream_t);
 };
 cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
@@ -289,7 +290,7 @@ int rebuild(kg_handle* h) {
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
         // dynamic shared memory of the flux and wall kernels plus a reserve for their static arrays
         const size_t sa = storage_size(h);
-        const size_t sflux = ((size_t)M.ndf * M.max_nv + 2 * (size_t)M.dim * M.max_axis) * sa + 16384;
+        const size_t sflux = ((size_t)M.ndf * M.max_nv + (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis) * sa + 16384;
         const size_t swall = ((size_t)(M.ndf + 1) * M.max_nv + (size_t)M.dim * M.max_axis) * sa + M.max_nv + 4096;
         const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
@@ -300,15 +301,16 @@ int rebuild(kg_handle* h) {
     P.PG = (int64_t)M.vw.size();
 #define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
     UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
-    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(vidx, vidx);
+    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
     UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dnv, dnv); UP(dprob, dprob);
     UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
     UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-    UP(fluid_cells, fluid_cells); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim);
+    UP(fluid_cells, fluid_cells); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
     UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
     UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
     P.max_axis = M.max_axis;
+    P.max_bcm = M.max_bcm;
     {
         std::vector<int32_t> order(M.fluid_cells.size());
         for (size_t q = 0; q < order.size(); ++q) order[q] = (int32_t)q;
@@ -648,6 +650,34 @@ int download_problem(kg_handle* h, int slot, double* f, double* w, double* prim,
     return KG_OK;
 }
 
+// sw of the problem in `slot` (update_macro_slope!) from the slopes on the device, scattered
+// into n_cells blocks of (dim+2) x dim doubles; cells without a fluid-list entry get zeros.
+int download_sw(kg_handle* h, int slot, double* sw) {
+    int rc = rebuild(h);
+    if (rc) return rc;
+    Problem& pb = h->probs[slot];
+    const int D = h->prm.dim, N = D * (D + 2);
+    const int fb = pb.pp.fluid_begin, n = pb.pp.fluid_end - pb.pp.fluid_begin;
+    std::vector<double> host((size_t)std::max(n, 1) * N);
+    if (n > 0) {
+        double* d = nullptr;
+        cudaError_t e = cudaMalloc(&d, sizeof(double) * (size_t)n * N);
+        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc sw");
+        const Dev P = h->dev;
+        e = dispatch(h, [&](auto L) { return decltype(L)::macro_slope(P, fb, n, d, h->stream); });
+        if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), d, sizeof(double) * (size_t)n * N, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        cudaFree(d);
+        if (e != cudaSuccess) return cuda_fail(h, e, "macro_slope_kernel");
+    }
+    std::fill(sw, sw + (size_t)pb.F.n_cells * N, 0.0);
+    for (int q = 0; q < n; ++q) {
+        const int64_t cell = h->M.fluid_cells[fb + q] - pb.dbase;
+        std::copy(host.begin() + (size_t)q * N, host.begin() + (size_t)(q + 1) * N, sw + cell * N);
+    }
+    return KG_OK;
+}
+
 int check_params(const kg_params* params, std::string& err) {
     if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) { err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1"; return KG_ERR_ARG; }
     if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { err = "bad precision"; return KG_ERR_ARG; }
@@ -756,6 +786,15 @@ int kg_download_state(kg_handle* h, double* f, double* w, double* prim, double* 
     if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
     cudaSetDevice(h->device);
     return download_problem(h, 0, f, w, prim, qf, sdf);
+}
+
+int kg_download_sw(kg_handle* h, double* sw) {
+    if (!h) return KG_ERR_ARG;
+    if (!sw) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_download_sw");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return download_sw(h, 0, sw);
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
@@ -911,6 +950,12 @@ int kg_batch_download(kg_handle* h, int32_t slot, double* f, double* w, double* 
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
     return download_problem(h, slot, f, w, prim, qf, nullptr);
+}
+
+int kg_batch_download_sw(kg_handle* h, int32_t slot, double* sw) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !sw) return fail(h, KG_ERR_ARG, "bad slot");
+    cudaSetDevice(h->device);
+    return download_sw(h, slot, sw);
 }
 
 int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {

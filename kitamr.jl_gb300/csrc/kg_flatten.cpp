@@ -143,6 +143,11 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
                     F.vidx[(size_t)d * PG + t.grid_off[g] + i] = (uint16_t)(std::lower_bound(vals.begin(), vals.end(), x) - vals.begin());
                 }
                 F.ax_val.insert(F.ax_val.end(), vals.begin(), vals.end());
+                for (double x : vals) {
+                    const float hi = (float)x;
+                    F.ax_hi.push_back(hi);
+                    F.ax_lo.push_back((float)(x - (double)hi));
+                }
             }
             F.ax_off[slot + 1] = (int32_t)F.ax_val.size();
         }
@@ -328,6 +333,11 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
             a.orient = rot; a.sarea = area;
             a.bc = (int32_t)(F.bc_prim.size() / MAXW);
             for (int e = 0; e < MAXW; ++e) F.bc_prim.push_back(e < D + 2 ? t.face_bc[(size_t)fi * (D + 2) + e] : 0.0);
+            {
+                const double* b = &F.bc_prim[F.bc_prim.size() - MAXW];
+                for (int e = 0; e < MAXW; ++e) F.bc_hl.push_back((float)b[e]);
+                for (int e = 0; e < MAXW; ++e) F.bc_hl.push_back((float)(b[e] - (double)(float)b[e]));
+            }
             per[here].push_back(a);
             continue;
         }
@@ -361,8 +371,13 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
     for (int i = 0; i < NC; ++i) {
         if (t.cell_bound_enc[i] < 0) continue;
         F.fluid_cells.push_back(i);
-        for (auto& a : per[i]) F.inc.push_back(a);
+        int nbcm = 0;
+        for (auto& a : per[i]) {
+            F.inc.push_back(a);
+            if (a.kind == INC_DOMAIN && (a.bc_kind == KG_BC_MAXWELL || a.bc_kind == KG_BC_INFLOW)) ++nbcm;
+        }
         F.max_inc = std::max(F.max_inc, (int)per[i].size());
+        F.max_bcm = std::max(F.max_bcm, nbcm);
         F.inc_off.push_back((int32_t)F.inc.size());
     }
 
@@ -491,9 +506,12 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         for (int g = 0; g < G; ++g)
             for (int d = 0; d < MAXD; ++d) M.ax_off.push_back(axacc + F.ax_off[(size_t)g * MAXD + d]);
         M.ax_val.insert(M.ax_val.end(), F.ax_val.begin(), F.ax_val.end());
+        M.ax_hi.insert(M.ax_hi.end(), F.ax_hi.begin(), F.ax_hi.end());
+        M.ax_lo.insert(M.ax_lo.end(), F.ax_lo.begin(), F.ax_lo.end());
         M.max_axis = std::max(M.max_axis, F.max_axis);
         M.max_nv = std::max(M.max_nv, F.max_nv);
         M.max_inc = std::max(M.max_inc, F.max_inc);
+        M.max_bcm = std::max(M.max_bcm, F.max_bcm);
         M.phase_cells += F.phase_cells;
         M.n_cells += F.n_cells;
         M.n_walls += F.n_walls;
@@ -528,6 +546,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             M.inc.push_back(a);
         }
         M.bc_prim.insert(M.bc_prim.end(), F.bc_prim.begin(), F.bc_prim.end());
+        M.bc_hl.insert(M.bc_hl.end(), F.bc_hl.begin(), F.bc_hl.end());
         ranges.push_back(fb);
         ranges.push_back((int32_t)M.fluid_cells.size());
         M.n_fluid += F.n_fluid;

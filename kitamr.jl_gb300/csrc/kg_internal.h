@@ -92,6 +92,7 @@ struct Flat {
     // ("axis values") and, per velocity cell, the index of its coordinate on each axis
     std::vector<int32_t> ax_off;  // n_grids * MAXD + 1
     std::vector<double> ax_val;
+    std::vector<float> ax_hi, ax_lo;   // ax_val = hi + lo in FP32 pairs (mixed form exponents)
     std::vector<uint16_t> vidx;   // [dim][P_g]
     int max_axis = 0;
     // data table
@@ -115,6 +116,7 @@ struct Flat {
     std::vector<int32_t> inc_off;         // n_fluid + 1
     std::vector<Incidence> inc;
     std::vector<double> bc_prim;          // domain-face bc prim, MAXW per entry
+    std::vector<float> bc_hl;             // the same as FP32 hi (MAXW) then lo (MAXW) per entry
     // immersed boundary
     std::vector<SolidOp> solid_ops;
     std::vector<WallOp> wall_ops;
@@ -124,6 +126,7 @@ struct Flat {
     std::vector<double> cut_gw, cut_sw;
     std::vector<double> cvcw;
     int max_inc = 0;
+    int max_bcm = 0;                      // most Maxwellian-state domain faces (wall, inflow) of a cell
 };
 
 // Builds the gather form; returns KG_OK or an error code with a message.

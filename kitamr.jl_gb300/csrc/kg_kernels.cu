@@ -666,6 +666,52 @@ template <typename A, typename T> struct IncA {
     int8_t kind, dir, bc_kind, mode_out, mode_in;
 };
 
+// Factor tables E[d][a] = exp(-lam (x_a - U_d)^2) of a Maxwellian at the distinct axis
+// coordinates x_a of grid gid (exp(-lam|u-U|^2) = Π_d E[d][axis index of u_d]); every thread
+// of the block takes entries.  FP64 form: FP64 exponents.
+template <int D>
+__device__ __forceinline__ void gauss_table(const Dev& P, int gid, const double* U, double lam, double* E) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
+        for (int a = threadIdx.x; a < na; a += BLOCK) {
+            const double cu = P.ax_val[a0 + a] - U[d];
+            E[d * P.max_axis + a] = exp(-lam * cu * cu);
+        }
+    }
+}
+// Mixed form: FP32 tables whose exponents are formed in float-float arithmetic from the
+// FP32 hi + lo pairs of x, U and lam, so no FP64 instruction runs per entry.
+template <int D>
+__device__ __forceinline__ void gauss_table(const Dev& P, int gid, const float* Uh, const float* Ul, float lh,
+                                            float ll, float* E) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
+        for (int a = threadIdx.x; a < na; a += BLOCK)
+            E[d * P.max_axis + a] = exp_gauss_ff(P.ax_hi[a0 + a], P.ax_lo[a0 + a], Uh[d], Ul[d], lh, ll);
+    }
+}
+
+// get_prim_2D / 3D (lib/KitCore/2D.jl:9-16, 3D.jl:12-20) with one reciprocal of ρ and one
+// division for λ (the FP64 divisions of the scalar section are its slowest instructions)
+template <int D>
+__device__ __forceinline__ void get_prim_r(const double* w, double gamma, double* prim) {
+    const double inv = 1.0 / w[0];
+    prim[0] = w[0];
+    double m2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) { prim[1 + d] = w[1 + d] * inv; m2 += w[1 + d] * w[1 + d]; }
+    prim[D + 1] = 0.5 * w[0] / ((gamma - 1.0) * (w[D + 1] - 0.5 * m2 * inv));
+}
+
+// dynamic shared memory of the flux kernel: convected f, then the factor tables (two
+// collision Maxwellians, or one per Maxwellian-state domain face earlier in the step)
+template <int D, int NDF, typename A>
+__host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, int max_bcm) {
+    return ((size_t)NDF * max_nv + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
+}
+
 // flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part)
 template <int D, int NDF, typename T>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
@@ -673,12 +719,14 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ Incidence sinc[MAX_INC];
     __shared__ IncA<A, T> sia[MAX_INC];
-    __shared__ double srho[MAX_INC];
+    __shared__ int8_t sbt[MAX_INC];             // incidence -> its Maxwellian factor table, -1 none
+    __shared__ A sbpre[MAX_INC], sbk[MAX_INC];  // ρ (λ/π)^{D/2} and K/(2λ) of that Maxwellian
     __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
     __shared__ double sscal[4 * MAXW];
     // per-CTA scalars in the arithmetic precision, computed once by thread 0
     enum { C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
-           C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
+           C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_UNH = C_QA + MAXD, C_UNL = C_UNH + MAXD,
+           C_LCH = C_UNL + MAXD, C_LCL, C_LNH, C_LNL, C_N };
     __shared__ A sc[C_N];
     const int cell = P.fluid_cells[fcx];
     const int slot = P.dprob[cell];
@@ -735,7 +783,6 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const T* fcell = (const T*)P.f_in + fo;
     const T* scl = (const T*)P.sdf + fo * D;
     T* fnew = (T*)P.f_out + fo;
-    const double* vw = P.vw + g.goff;
     const double* cds = P.dds + (int64_t)cell * MAXD;
     double V = cds[0];
 #pragma unroll
@@ -746,39 +793,75 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const A s_dt = sc[C_SDT];
     const A adt = sc[C_ADT];
     A* fst = (A*)sh_raw;                                  // NDF * nv
-    A* Ec = fst + (size_t)NDF * nv;                       // D * max_axis
-    A* En = Ec + (size_t)D * P.max_axis;                  // D * max_axis
+    A* Ec = fst + (size_t)NDF * nv;                       // factor tables (flux_smem)
     const bool caidvm = P.flux == KG_FLUX_CAIDVM;
 
-    // ---- 0. wall density of Maxwellian domain faces (calc_ρw, Theory/Math.jl:251-282) --
+    const int MA = P.max_axis;
+    const uint16_t* vx = P.vidx + g.goff;
+
+    // ---- 0. Maxwellians of the domain faces with a Maxwellian state (wall, inflow) ---------
+    // Per such face: factor tables of exp(-λ|u-U|²) at the grid's axis coordinates (in the
+    // region of the collision tables, which are built after the flux), the prefactor
+    // ρ (λ/π)^{D/2} and K/(2λ).  A wall face's density is calc_ρw (Theory/Math.jl:251-282):
+    // ρ_w = -Σ_out w u_n f̂ / ((λ/π)^{D/2} Σ_in w u_n e^{-λ|u-U|²}).
+    int nbt = 0;
     for (int e = 0; e < ninc; ++e) {
         const Incidence& I = sinc[e];
-        if (!(I.kind == INC_DOMAIN && I.bc_kind == KG_BC_MAXWELL)) continue;
-        const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
-        double red[2] = {0.0, 0.0};
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
-            const double ud = g.u(i, I.dir);
-            if (I.orient * ud <= 0.0) {
-                A fk = (A)fcell[i];
-                A s[D], dx[D];
-#pragma unroll
-                for (int d = 0; d < D; ++d) {
-                    s[d] = (A)scl[(int64_t)d * NDF * nv + i];
-                    dx[d] = sia[e].dxm[d] - VU[(int64_t)d * PG + g.goff + i] * adt;
-                }
-                red[0] += vw[i] * ud * (double)own_recon<D, A>(1, fk, s, dx, myds);
-            } else {
-                double c2 = 0.0;
-#pragma unroll
-                for (int d = 0; d < D; ++d) { double cu = g.u(i, d) - bc[1 + d]; c2 += cu * cu; }
-                red[1] += vw[i] * ud * exp(-bc[D + 1] * c2);
-            }
+        const bool tab = I.kind == INC_DOMAIN && (I.bc_kind == KG_BC_MAXWELL || I.bc_kind == KG_BC_INFLOW);
+        if (threadIdx.x == 0) sbt[e] = tab ? (int8_t)nbt : (int8_t)-1;
+        if (!tab) continue;
+        A* Eb = Ec + (size_t)nbt * D * MA;
+        if constexpr (sizeof(A) == 8) {
+            const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
+            gauss_table<D>(P, gid, bc + 1, bc[D + 1], (double*)Eb);
+        } else {
+            const float* hl = P.bc_hl + (int64_t)I.bc * 2 * MAXW;
+            gauss_table<D>(P, gid, hl + 1, hl + MAXW + 1, hl[D + 1], hl[MAXW + D + 1], (float*)Eb);
         }
-        block_sum<2>(red, sred);
-        if (threadIdx.x == 0) {
-            const double lam = bc[D + 1];
-            const double SG = (D == 2 ? lam / PI : pow(lam / PI, 1.5)) * red[1];
-            srho[e] = -red[0] / SG;
+        ++nbt;
+    }
+    if (nbt > 0) {
+        __syncthreads();
+        for (int e = 0; e < ninc; ++e) {
+            const Incidence& I = sinc[e];
+            const int b = sbt[e];
+            if (b < 0) continue;
+            const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
+            if (I.bc_kind == KG_BC_MAXWELL) {
+                const A* Eb = Ec + (size_t)b * D * MA;
+                KSum<A> red[2];
+                for (int i = threadIdx.x; i < nv; i += BLOCK) {
+                    const A ud = VU[(int64_t)I.dir * PG + g.goff + i];
+                    if (sia[e].orient * ud <= (A)0) {
+                        const A fk = (A)fcell[i];
+                        A sl[D], dx[D];
+#pragma unroll
+                        for (int d = 0; d < D; ++d) {
+                            sl[d] = (A)scl[(int64_t)d * NDF * nv + i];
+                            dx[d] = sia[e].dxm[d] - VU[(int64_t)d * PG + g.goff + i] * adt;
+                        }
+                        red[0].add(VW[i] * ud * own_recon<D, A>(1, fk, sl, dx, myds));
+                    } else {
+                        A shape = (A)1;
+#pragma unroll
+                        for (int d = 0; d < D; ++d) shape *= Eb[d * MA + vx[(int64_t)d * PG + i]];
+                        red[1].add(VW[i] * ud * shape);
+                    }
+                }
+                double rs[2];
+                block_sum_ks<2>(red, rs, sred);
+                if (threadIdx.x == 0) {
+                    const double lam = bc[D + 1];
+                    const double pre = D == 2 ? lam / PI : pow(lam / PI, 1.5);
+                    const double rho = -rs[0] / (pre * rs[1]);
+                    sbpre[e] = (A)(rho * pre);
+                    sbk[e] = (A)(Kgas / (2.0 * lam));
+                }
+            } else if (threadIdx.x == 0) {
+                const double lam = bc[D + 1];
+                sbpre[e] = (A)(bc[0] * (D == 2 ? lam / PI : pow(lam / PI, 1.5)));
+                sbk[e] = (A)(Kgas / (2.0 * lam));
+            }
         }
         __syncthreads();
     }
@@ -825,16 +908,14 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
                 for (int k = 0; k < NDF; ++k) { acc[k] += sa * m[k]; accM[k] += sa * m[k]; }
             } else if (ia.kind == INC_DOMAIN) {
                 const Incidence& I = sinc[e];
-                const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
                 A mic[NDF];
                 if (I.bc_kind == KG_BC_MAXWELL || I.bc_kind == KG_BC_INFLOW) {
-                    double pr[MAXW];
+                    const A* Eb = Ec + (size_t)sbt[e] * D * MA;
+                    A mh = sbpre[e];
 #pragma unroll
-                    for (int q = 0; q < D + 2; ++q) pr[q] = bc[q];
-                    if (I.bc_kind == KG_BC_MAXWELL) pr[0] = srho[e];
-                    const double mh = maxwell_h<D>(g, i, pr);
-                    mic[0] = (A)mh * ud;
-                    if (NDF == 2) mic[NDF - 1] = (A)(mh * Kgas / (2.0 * pr[D + 1])) * ud;
+                    for (int d = 0; d < D; ++d) mh *= Eb[d * MA + vx[(int64_t)d * PG + i]];
+                    mic[0] = mh * ud;
+                    if (NDF == 2) mic[NDF - 1] = mh * sbk[e] * ud;
                 } else if (I.bc_kind == KG_BC_OUTFLOW) {
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) mic[k] = fr[k] * ud;
@@ -944,39 +1025,66 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         if (threadIdx.x == 0) {
             double* w = P.w + (int64_t)cell * MAXW;
             double wn[MAXW], pc[MAXW], pn[MAXW];
+            const double dtV = dt / V;
             if (P.marching == KG_MARCH_CAIDVM) {
 #pragma unroll
-                for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
-                get_prim<D>(wn, PP.gamma, pc);
+                for (int q = 0; q < D + 2; ++q) wn[q] = fma(red[q], dtV, w[q]);
+                get_prim_r<D>(wn, PP.gamma, pc);
                 double wf[MAXW];
 #pragma unroll
                 for (int q = 0; q < D + 2; ++q) wf[q] = red[D + 2 + q];
-                get_prim<D>(wf, PP.gamma, pn);
+                get_prim_r<D>(wf, PP.gamma, pn);
             } else {
                 if (P.flux == KG_FLUX_DVM) {
 #pragma unroll
                     for (int q = 0; q < D + 2; ++q) wn[q] = red[D + 2 + q];
                 } else {
 #pragma unroll
-                    for (int q = 0; q < D + 2; ++q) wn[q] = w[q] + red[q] * dt / V;
+                    for (int q = 0; q < D + 2; ++q) wn[q] = fma(red[q], dtV, w[q]);
                 }
-                get_prim<D>(wn, PP.gamma, pc);
+                get_prim_r<D>(wn, PP.gamma, pc);
 #pragma unroll
                 for (int q = 0; q < D + 2; ++q) pn[q] = pc[q];
             }
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) { w[q] = wn[q]; sscal[q] = pc[q]; sscal[MAXW + q] = pn[q]; }
-            const double tau = PP.mu_ref * 2.0 * pow(pc[D + 1], 1.0 - PP.omega) / pc[0];
-            sscal[2 * MAXW] = tau;
             const double lc = pc[D + 1], ln = pn[D + 1];
-            sc[C_PREC] = (A)(pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5)));
-            sc[C_PREN] = (A)(pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5)));
-            sc[C_BFC] = (A)(Kgas / (2.0 * lc));
-            sc[C_BFN] = (A)(Kgas / (2.0 * ln));
-            sc[C_R1] = (A)(tau / (tau + dt));
-            sc[C_R2] = (A)(dt / (tau + dt));
-            sc[C_SK] = (A)(0.8 * (1.0 - PP.Pr) * lc * lc / pc[0]);
-            sc[C_LC] = (A)lc;
+            if constexpr (sizeof(A) == 8) {
+                // get_τ (Gas/Model.jl:14) and the constants of discrete_maxwell / shakhov_part
+                const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
+                sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
+                sc[C_PREN] = pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5));
+                sc[C_BFC] = Kgas / (2.0 * lc);
+                sc[C_BFN] = Kgas / (2.0 * ln);
+                sc[C_R1] = tau / (tau + dt);
+                sc[C_R2] = dt / (tau + dt);
+                sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
+                sc[C_LC] = lc;
+            } else {
+                // mixed form: the same constants in FP32 from the FP64 primitives (they scale
+                // FP32 per-velocity values), plus hi/lo pairs of U and λ for the tables
+                const float rc = (float)pc[0], rn = (float)pn[0], lcf = (float)lc, lnf = (float)ln;
+                const float dtf = (float)dt;
+                const float tau = (float)(2.0 * PP.mu_ref) * powf(lcf, (float)(1.0 - PP.omega)) / rc;
+                constexpr float IPI = (float)(1.0 / PI);
+                sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
+                sc[C_PREN] = rn * (D == 2 ? lnf * IPI : powf(lnf * IPI, 1.5f));
+                sc[C_BFC] = (float)Kgas / (2.f * lcf);
+                sc[C_BFN] = (float)Kgas / (2.f * lnf);
+                sc[C_R1] = tau / (tau + dtf);
+                sc[C_R2] = dtf / (tau + dtf);
+                sc[C_SK] = (float)(0.8 * (1.0 - PP.Pr)) * lcf * lcf / rc;
+                sc[C_LC] = lcf;
+                sc[C_LCH] = lcf;
+                sc[C_LCL] = (float)(lc - (double)lcf);
+                sc[C_LNH] = lnf;
+                sc[C_LNL] = (float)(ln - (double)lnf);
+                for (int d = 0; d < D; ++d) {
+                    const float uh = (float)pn[1 + d];
+                    sc[C_UNH + d] = uh;
+                    sc[C_UNL + d] = (float)(pn[1 + d] - (double)uh);
+                }
+            }
             for (int d = 0; d < D; ++d) {
                 const A uh = (A)pc[1 + d];
                 sc[C_UH + d] = uh;
@@ -989,28 +1097,20 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
         __syncthreads();
     }
-    double pc[MAXW], pn[MAXW];
-#pragma unroll
-    for (int q = 0; q < D + 2; ++q) { pc[q] = sscal[q]; pn[q] = sscal[MAXW + q]; }
-    const double tau = sscal[2 * MAXW];
-    const double lamc = pc[D + 1], lamn = pn[D + 1];
-    // factor tables of the two Maxwellians: exponents in FP64 (discrete_maxwell, 2D2F.jl:1-21)
+    // factor tables of the two Maxwellians (discrete_maxwell, 2D2F.jl:1-21 / 3D1F.jl:1-23)
     const bool need_n = P.marching == KG_MARCH_CAIDVM;
-#pragma unroll
-    for (int d = 0; d < D; ++d) {
-        const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
-        for (int a = threadIdx.x; a < na; a += BLOCK) {
-            const double x = P.ax_val[a0 + a];
-            const double cu = x - pc[1 + d];
-            Ec[d * P.max_axis + a] = exp_arg<A>(-lamc * cu * cu);
-            if (need_n) { const double cn = x - pn[1 + d]; En[d * P.max_axis + a] = exp_arg<A>(-lamn * cn * cn); }
-        }
+    A* En = Ec + (size_t)D * MA;
+    if constexpr (sizeof(A) == 8) {
+        gauss_table<D>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
+        if (need_n) gauss_table<D>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
+    } else {
+        gauss_table<D>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
+        if (need_n)
+            gauss_table<D>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
     }
     __syncthreads();
     const A prec = sc[C_PREC], pren = sc[C_PREN];
     const A bfc = sc[C_BFC], bfn = sc[C_BFN];
-    const uint16_t* vx = P.vidx + g.goff;
-    const int MA = P.max_axis;
     // peculiar velocity c = u - U with U split into two floats (hi + lo), so that c keeps
     // the precision of c rather than that of U
     A Uh[D], Ul[D];
@@ -1056,10 +1156,8 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     }
     double qv[D];
     block_sum_ks<D>(qs, qv, sred);
-#pragma unroll
-    for (int d = 0; d < D; ++d) qv[d] *= 0.5;
     if (threadIdx.x == 0)
-        for (int d = 0; d < D; ++d) sc[C_QA + d] = (A)qv[d];
+        for (int d = 0; d < D; ++d) sc[C_QA + d] = (A)(0.5 * qv[d]);
     __syncthreads();
     // ---- 4. Shakhov g+ and implicit relaxation -------------------------------------
     const A r1 = sc[C_R1], r2 = sc[C_R2];
@@ -1098,33 +1196,33 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
     } else {
         // f = (f + dt/V flux) tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:156)
-        const double tdt = tau / (tau + dt);
         for (int i = threadIdx.x; i < nv; i += BLOCK) {
             A gp[NDF];
             gplus(i, gp);
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) fnew[k * nv + i] = (T)((A)((double)fst[k * nv + i] * tdt) + r2 * gp[k]);
+            for (int k = 0; k < NDF; ++k) fnew[k * nv + i] = (T)(fst[k * nv + i] * r1 + r2 * gp[k]);
         }
     }
     // ---- 5. per-cell outputs and residual terms ------------------------------------
-    if (threadIdx.x == 0) {
+    // one lane per component
+    if (threadIdx.x < MAXW) {
+        const int q = threadIdx.x;
         double* pr = P.prim + (int64_t)cell * MAXW;
         double* res = P.cell_res + (int64_t)fcx * 2 * MAXW;
         const bool chk = (step % check_interval) == 0;
-#pragma unroll
-        for (int q = 0; q < MAXW; ++q) {
-            if (q < D + 2) {
-                const double dl = pc[q] - pr[q];
-                res[q] = chk ? dl * dl : 0.0;
-                res[MAXW + q] = chk ? fabs(pc[q]) : 0.0;
-                pr[q] = pc[q];
-            } else {
-                res[q] = 0.0;
-                res[MAXW + q] = 0.0;
-            }
+        if (q < D + 2) {
+            const double pcq = sscal[q];
+            const double dl = pcq - pr[q];
+            res[q] = chk ? dl * dl : 0.0;
+            res[MAXW + q] = chk ? fabs(pcq) : 0.0;
+            pr[q] = pcq;
+        } else {
+            res[q] = 0.0;
+            res[MAXW + q] = 0.0;
         }
 #pragma unroll
-        for (int d = 0; d < D; ++d) P.qf[(int64_t)cell * MAXD + d] = qv[d];
+        for (int d = 0; d < D; ++d)
+            if (q == d) P.qf[(int64_t)cell * MAXD + d] = 0.5 * qv[d];
     }
 }
 
@@ -1151,6 +1249,48 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_ke
         if (!counter) break;
         __syncthreads();
     }
+}
+
+// update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
+// weight) for the fluid-list cells [fbegin, fbegin + gridDim.x), one CTA each; out holds
+// dim x (dim+2) doubles per listed cell (the column-major memory of PsData.sw).  Not part of
+// a step: it reads the slopes the last step left, at a host sync point.
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) macro_slope_kernel(Dev P, int fbegin, double* out) {
+    using A = typename Arith<T>::type;
+    constexpr int N = D * (D + 2);
+    __shared__ double sred[N * (BLOCK / 32)];
+    const int cell = P.fluid_cells[fbegin + blockIdx.x];
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const T* s = (const T*)P.sdf + P.foff[cell] * D;
+    const A* VU = vel<A>(P);
+    const A* VW = wts<A>(P) + g.goff;
+    KSum<A> m[N];
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        A u[D], u2 = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { u[d] = VU[(int64_t)d * P.PG + g.goff + i]; u2 += u[d] * u[d]; }
+        const A wi = VW[i];
+#pragma unroll
+        for (int dir = 0; dir < D; ++dir) {
+            const A s0 = (A)s[((int64_t)dir * NDF) * nv + i];
+            m[dir * (D + 2)].add(wi * s0);
+#pragma unroll
+            for (int d = 0; d < D; ++d) m[dir * (D + 2) + 1 + d].add(wi * u[d] * s0);
+            if (NDF == 2) {
+                const A s1 = (A)s[((int64_t)dir * NDF + NDF - 1) * nv + i];
+                m[dir * (D + 2) + D + 1].add((A)0.5 * wi * (u2 * s0 + s1));
+            } else {
+                m[dir * (D + 2) + D + 1].add((A)0.5 * wi * u2 * s0);
+            }
+        }
+    }
+    double r[N];
+    block_sum_ks<N>(m, r, sred);
+#pragma unroll
+    for (int e = 0; e < N; ++e)
+        if (threadIdx.x == e) out[(int64_t)blockIdx.x * N + e] = r[e];
 }
 
 // Per problem (one CTA each): Σ of the per-cell residual terms when the step is a check
@@ -1205,7 +1345,7 @@ struct Launch {
     }
     static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
-        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
@@ -1215,7 +1355,7 @@ struct Launch {
     static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,
                                        cudaStream_t s) {
         using A = typename Arith<T>::type;
-        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(counter, 0, sizeof(int), s);
@@ -1223,10 +1363,15 @@ struct Launch {
         flux_collide_kernel<D, NDF, T><<<grid, BLOCK, smem, s>>>(P, counter, order, n);
         return cudaGetLastError();
     }
+    static cudaError_t macro_slope(const Dev& P, int fbegin, int n, double* out, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        macro_slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, fbegin, out);
+        return cudaGetLastError();
+    }
     // resident CTAs per SM the flux kernel reaches (for the persistent grid size)
     static int flux_occupancy(const Dev& P, int max_nv) {
         using A = typename Arith<T>::type;
-        size_t smem = ((size_t)NDF * max_nv + 2 * (size_t)D * P.max_axis) * sizeof(A);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
         cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, flux_collide_kernel<D, NDF, T>, BLOCK, smem);

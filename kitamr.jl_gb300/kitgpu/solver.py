@@ -49,6 +49,8 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
     L.kg_batch_set_dt.argtypes = [vp, i32, dbl]
     L.kg_autotune.argtypes = [vp, C.c_int]
+    L.kg_download_sw.argtypes = [vp, vp]
+    L.kg_batch_download_sw.argtypes = [vp, i32, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     _lib = L
     return L
@@ -60,6 +62,7 @@ EXPORTS = [
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
+    "kg_download_sw", "kg_batch_download_sw",
 ]
 
 
@@ -141,6 +144,12 @@ class GpuStep:
             self.h, out["f"].ctypes.data, out["w"].ctypes.data, out["prim"].ctypes.data, out["qf"].ctypes.data,
             out["sdf"].ctypes.data if sdf else None))
         return out
+
+    def download_sw(self) -> np.ndarray:
+        """sw of every cell (update_macro_slope!), shape (n_cells, dim, dim + 2)."""
+        sw = np.empty(self.nc * self.dim * (self.dim + 2))
+        _check(self.L, self.h, self.L.kg_download_sw(self.h, sw.ctypes.data))
+        return sw.reshape(self.nc, self.dim, self.dim + 2)
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
@@ -225,6 +234,13 @@ class GpuBatch:
         _check(self.L, self.h, self.L.kg_batch_download(self.h, slot, out["f"].ctypes.data, out["w"].ctypes.data,
                                                           out["prim"].ctypes.data, out["qf"].ctypes.data))
         return out
+
+    def download_sw(self, slot: int) -> np.ndarray:
+        topo, _ = self.meta[slot]
+        nc, dim = int(topo["n_cells"]), int(topo["dim"])
+        sw = np.empty(nc * dim * (dim + 2))
+        _check(self.L, self.h, self.L.kg_batch_download_sw(self.h, slot, sw.ctypes.data))
+        return sw.reshape(nc, dim, dim + 2)
 
     def info(self):
         n, fr, bpe = C.c_int32(), C.c_int64(), C.c_int64()

@@ -1139,6 +1139,25 @@ int kgo_moments(const kg_params* prm, const kg_topology* t, const double* f, con
     return KG_OK;
 }
 
+// update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0 of sdf[:, :, dir] for
+// every cell with bound_enc >= 0; sw_out holds (dim+2) x dim doubles per cell (column-major,
+// as PsData.sw); solid cells are left at zero.
+int kgo_macro_slope(const kg_params* prm, const kg_topology* t, const double* sdf, double* sw_out) {
+    Model m;
+    int rc = setup(m, prm, t);
+    if (rc) return rc;
+    const int nw = m.nw(), D = m.dim;
+    for (int c = 0; c < t->n_cells; ++c) {
+        double* o = sw_out + (size_t)c * nw * D;
+        for (int e = 0; e < nw * D; ++e) o[e] = 0.0;
+        if (t->cell_bound_enc[c] < 0) continue;
+        const Grid& g = m.grids[t->cell_grid[c]];
+        for (int dir = 0; dir < D; ++dir)
+            calc_w0(m, g, sdf + m.soff[c] + (size_t)g.nv * t->ndf * dir, o + (size_t)dir * nw);
+    }
+    return KG_OK;
+}
+
 int kgo_last_error(char* buf, size_t cap) {
     std::snprintf(buf, cap, "%s", g_err.c_str());
     return 0;

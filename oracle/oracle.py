@@ -37,6 +37,7 @@ def lib():
             [C.POINTER(C.c_double)] * 7 + [C.POINTER(C.c_double), C.POINTER(C.c_double),
                                            C.POINTER(C.c_int32), C.c_int32]
         L.kgo_moments.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4
+        L.kgo_macro_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 2
         L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
         _lib = L
     return _lib
@@ -83,6 +84,15 @@ class OracleState:
             lib().kgo_last_error(buf, 512)
             raise RuntimeError(f"oracle failed: {abi.ERRORS.get(rc, rc)}: {buf.value.decode()}")
         return self
+
+    def macro_slope(self, params):
+        """sw of every cell (update_macro_slope!), shape (n_cells, dim, dim + 2)."""
+        nc, dim = self.topo["n_cells"], self.topo["dim"]
+        sw = np.zeros(nc * dim * (dim + 2))
+        rc = lib().kgo_macro_slope(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.sdf), abi.dptr(sw))
+        if rc != 0:
+            raise RuntimeError(f"oracle macro_slope failed: {rc}")
+        return sw.reshape(nc, dim, dim + 2)
 
     def moments(self, params):
         nc, nw = self.topo["n_cells"], self.topo["dim"] + 2

@@ -71,5 +71,6 @@ def run_pair(problem, nsteps, precision=abi.KG_PREC_FP64, flux=abi.KG_FLUX_CAIDV
         rep = g.step(dt, done, n)
         done += n
     out = g.download_state()
+    out["sw"] = g.download_sw()
     g.close()
     return topo, ref, out, rep

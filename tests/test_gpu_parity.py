@@ -63,3 +63,27 @@ def test_mixed_within_1e5_of_fp64(name, make, nsteps):
     keep = {k: v for k, v in errs.items() if k in ("rho", "T") or k.startswith("U") or k.startswith("q")}
     bad = {k: v for k, v in keep.items() if not v <= TOL_MIXED}
     assert not bad, f"{name}: {bad}"
+
+
+SW_CASES = [CASES_FP64[1], CASES_FP64[3], CASES_FP64[4]]
+
+
+@pytest.mark.parametrize("prec", [abi.KG_PREC_FP64, abi.KG_PREC_MIXED])
+@pytest.mark.parametrize("name,make,nsteps", SW_CASES, ids=[c[0] for c in SW_CASES])
+def test_macro_slopes_match_oracle(name, make, nsteps, prec):
+    """sw of update_macro_slope! (moments of each direction's slopes) from the slopes the last
+    step left: 1e-10 of each component's scale in FP64; 1e-4 in the mixed form, whose slopes are
+    stored in FP32.  Solid cells get zeros."""
+    p = make()
+    topo, ref, out, _ = run_pair(p, nsteps, precision=prec)
+    ref_sw = ref.macro_slope(abi.make_params(p))
+    got = out["sw"]
+    be = np.asarray(topo["cell_bound_enc"])
+    assert np.all(got[be < 0] == 0.0)
+    tol = 1e-10 if prec == abi.KG_PREC_FP64 else 1e-4
+    floor = 1e-3 * float(np.max(np.abs(ref_sw)))
+    for j in range(topo["dim"] + 2):
+        r, g = ref_sw[be >= 0, :, j], got[be >= 0, :, j]
+        scale = max(float(np.max(np.abs(r))), floor)
+        err = float(np.max(np.abs(g - r))) / scale
+        assert err <= tol, (name, j, err)
