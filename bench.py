@@ -31,10 +31,19 @@ import numpy as np  # noqa: E402
 WORKLOAD = "cylinder_ma5_kn0.1_64x64_L3_v48x48_vsL2"
 METRIC = "phase-cell updates/s"
 UNIT = "updates/s"
+# single-problem workloads: name, default scale, generator note
+SINGLE = {
+    "cylinder": (WORKLOAD, 1.0, "seeded cylinder_buffer_IC state on a generated forest"),
+    # the 3D sphere (Ma 3, Kn 0.05, 32^3 trees, 2 levels, 24^3 velocity grid) at half the base
+    # mesh by default: 13,536 cells, 183 M phase cells (the full mesh needs a 22 GB host state)
+    "sphere": ("sphere_ma3_kn0.05_32x32x32_L2_v24x24x24", 0.5, "seeded sphere buffer state on a generated octree"),
+}
 
 
-def make_problem(scale=1.0):
+def make_problem(scale=1.0, mode="cylinder"):
     from kitgpu import cases
+    if mode == "sphere":
+        return cases.sphere(scale=scale)
     return cases.cylinder(scale=scale, nv=48, vs_levels=2)
 
 
@@ -135,11 +144,11 @@ def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     from kitgpu import cases
-    prob = make_problem(args.scale)
+    prob = make_problem(args.scale, args.mode)
     topo, state = cases.build(prob)
     P = mesh.phase_cells(topo)
     dt = prob.dt()
-    res = {}
+    res = {"ndf": int(topo["ndf"])}
     launches_total = 0
 
     def barrier():
@@ -285,10 +294,10 @@ def run_serve(args):
             "forms": out}
 
 
-def cpu_baseline(threads, budget_s=12.0):
+def cpu_baseline(threads, budget_s=12.0, mode="cylinder"):
     import oracle as O
     from kitgpu import abi, cases, mesh
-    prob = make_problem(scale=0.25)
+    prob = make_problem(scale=0.25, mode=mode)
     topo, state = cases.build(prob)
     P = mesh.phase_cells(topo)
     st = O.OracleState(topo, state)
@@ -302,7 +311,7 @@ def cpu_baseline(threads, budget_s=12.0):
         if el > budget_s or n >= 40:
             break
     return {"value": P * n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"cylinder at scale 0.25 (16x16 trees, same velocity grids), {P} phase cells, {n} steps, FP64"}
+            "sample": f"{mode} at scale 0.25 (same velocity grids), {P} phase cells, {n} steps, FP64"}
 
 
 def main():
@@ -312,13 +321,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--scale", type=float, default=1.0, help="shrink the workload (profiling captures)")
-    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "batched", "serve"])
+    ap.add_argument("--scale", type=float, default=None,
+                    help="scale of the base mesh (default: the workload's own; smaller for profiling captures)")
+    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "batched", "serve"])
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.scale is None:
+        args.scale = SINGLE[args.mode][1] if args.mode in SINGLE else 1.0
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
@@ -369,6 +381,8 @@ def main():
     P, res, launches = run_ours(args, rank, world, dist)
     if rank != 0:
         return
+    wname, wscale, wdata = SINGLE[args.mode]
+    ndf = res["ndf"]
     peak, peak_kind = measured_peaks()
     mixed = res["mixed"]
     kern = mixed.get("kernels", {})
@@ -376,18 +390,20 @@ def main():
     if "flux_collide_kernel" in kern:
         ms, cnt = kern["flux_collide_kernel"]
         avg_s = ms / cnt / 1e3
-        b_alg = 2 * 2 * 4 * P          # 2 * NDF * sizeof(float) per phase cell (one read, one write of f)
+        b_alg = 2 * ndf * 4 * P        # 2 * NDF * sizeof(float) per phase cell (one read, one write of f)
         ach = b_alg / avg_s / 1e9
+        traffic = ncu_traffic_per_launch() if (args.mode == "cylinder" and args.scale == 1.0) else None
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": ncu_traffic_per_launch(), "kernel": "flux_collide_kernel",
+                "traffic": traffic, "kernel": "flux_collide_kernel",
                 "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg}
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32-f/f64-moments",
-        "data": "synthetic (seeded cylinder_buffer_IC state on a generated forest)",
-        "config": {"workload": WORKLOAD if args.scale == 1.0 else f"{WORKLOAD} at scale {args.scale}",
-                   "phase_cells": P, "form": "mixed", "l2": "inputs > L2 (f is 488 MB FP32)",
+        "data": f"synthetic ({wdata})",
+        "config": {"workload": wname if args.scale == wscale else f"{wname} at scale {args.scale}",
+                   "phase_cells": P, "form": "mixed",
+                   "l2": f"inputs > L2 (f is {P * ndf * 4 / 1e6:.0f} MB FP32, sdf {P * ndf * 4 * (2 if ndf == 2 else 3) / 1e6:.0f} MB)",
                    "parallelism": f"replicas{world}"},
         "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
                   "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
@@ -398,7 +414,7 @@ def main():
         "clocks": mixed.get("clocks"),
     }
     if not args.no_cpu and world == 1:
-        line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, mode=args.mode)
     print(json.dumps(line))
 
 

@@ -51,6 +51,7 @@ struct Dev {
     const NbrRef* slope_nbr;
     // flux
     const int32_t* fluid_cells;
+    const uint8_t* fluid_reg;          // per fluid cell: regular (fast path of the flux kernel)
     const int32_t* inc_off;
     const Incidence* inc;
     const double* bc_prim;

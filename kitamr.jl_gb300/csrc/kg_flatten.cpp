@@ -378,6 +378,27 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         }
         F.max_inc = std::max(F.max_inc, (int)per[i].size());
         F.max_bcm = std::max(F.max_bcm, nbcm);
+        // regular cell: per direction one face at -ds/2 and one at +ds/2, each an inner face to
+        // a same-sized fluid neighbour on this cell's velocity grid, oriented so that a velocity
+        // leaves through the face it points at (the flux kernel's fast path relies on all of it)
+        bool reg = (int)per[i].size() == 2 * D;
+        int seen[2 * MAXD] = {0};
+        for (auto& a : per[i]) {
+            if (!reg) break;
+            const int d = a.dir;
+            const double h = 0.5 * t.cell_ds[(size_t)i * D + d];
+            const double dm = a.fmid[d] - a.my_mid[d], dox = a.fmid[d] - a.ot_mid[d];
+            reg = a.kind == INC_INNER && a.pair < 0 && a.other >= 0 && a.other < NC &&
+                  std::fabs(std::fabs(dm) - h) <= 1e-12 * h && std::fabs(dox + dm) <= 1e-12 * h &&
+                  a.orient * dm < 0.0;
+            for (int e = 0; reg && e < D; ++e) {
+                if (e != d && (std::fabs(a.fmid[e] - a.my_mid[e]) > 1e-12 * h || std::fabs(a.fmid[e] - a.ot_mid[e]) > 1e-12 * h)) reg = false;
+                if (a.ot_ds[e] != t.cell_ds[(size_t)i * D + e]) reg = false;
+            }
+            if (reg) ++seen[2 * d + (dm > 0.0 ? 1 : 0)];
+        }
+        for (int e = 0; reg && e < 2 * D; ++e) reg = seen[e] == 1;
+        F.fluid_reg.push_back(reg ? 1 : 0);
         F.inc_off.push_back((int32_t)F.inc.size());
     }
 
@@ -538,6 +559,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         // flux incidences
         int32_t fb = (int32_t)M.fluid_cells.size();
         for (int c : F.fluid_cells) M.fluid_cells.push_back(c + p.dbase);
+        M.fluid_reg.insert(M.fluid_reg.end(), F.fluid_reg.begin(), F.fluid_reg.end());
         for (size_t q = 1; q < F.inc_off.size(); ++q) M.inc_off.push_back(incacc + F.inc_off[q]);
         for (Incidence a : F.inc) {
             if (a.other >= 0) a.other += p.dbase;

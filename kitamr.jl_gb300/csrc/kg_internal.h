@@ -113,6 +113,8 @@ struct Flat {
     std::vector<NbrRef> slope_nbr;
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
+    std::vector<uint8_t> fluid_reg;       // per fluid cell: 1 when its faces are 2*dim full inner faces
+                                          // to same-sized neighbours on the same velocity grid
     std::vector<int32_t> inc_off;         // n_fluid + 1
     std::vector<Incidence> inc;
     std::vector<double> bc_prim;          // domain-face bc prim, MAXW per entry

@@ -84,49 +84,46 @@ __device__ __forceinline__ VGridView grid_view(const Dev& P, int data) {
 // =============================================================================
 // slope
 // =============================================================================
-// per-neighbour constants of a slope list, in the arithmetic precision (set up once per CTA)
-template <typename A> struct SlopeNbrA {
-    A dm[MAXD];      // transverse midpoint offsets (0 when the list is not projected)
-    int32_t data, pair, any;
+// per-neighbour constants of a slope list (set up once per CTA, one thread per entry): where
+// the neighbour's f and sdf live, its velocity count, its pairing rows and velocity levels,
+// and the transverse midpoint offsets in the arithmetic precision (0 when not projected)
+template <typename A, typename T> struct SlopeNbrA {
+    const T* fn;
+    const T* sn;
+    const int32_t* pj0;    // pairing rows (my grid <- neighbour's grid), when pair >= 0
+    const int32_t* pcnt;
+    const int8_t* vl;      // the neighbour grid's velocity levels
+    A dm[MAXD];
+    int32_t nvn, pair, any;
 };
 constexpr int MAX_SLOPE_NBR = 2 * MAXD * 4;   // 2 sides x dim x 2^(dim-1) neighbours
 
 template <int D, int NDF, typename T>
-__device__ __forceinline__ void slope_side(const Dev& P, int i, int li, const typename Arith<T>::type* fc,
-                                           const SlopeNbrA<typename Arith<T>::type>* nb, int cnt,
+__device__ __forceinline__ void slope_side(int i, int li, const typename Arith<T>::type* fc,
+                                           const SlopeNbrA<typename Arith<T>::type, T>* nb, int cnt,
                                            typename Arith<T>::type inv_ds, typename Arith<T>::type inv_cnt,
                                            typename Arith<T>::type* s) {
     using A = typename Arith<T>::type;
-    const T* f = (const T*)P.f_in;
-    const T* sdf = (const T*)P.sdf;
     A acc[NDF];
 #pragma unroll
     for (int k = 0; k < NDF; ++k) acc[k] = 0;
     for (int n = 0; n < cnt; ++n) {
-        const SlopeNbrA<A>& r = nb[n];
-        const int64_t fo = P.foff[r.data];
-        const int nvn = P.dnv[r.data];
-        const T* fn = f + fo;
-        const T* sn = sdf + fo * D;
-        const bool any = r.any;
-        const A* dm = r.dm;
+        const SlopeNbrA<A, T>& r = nb[n];
+        const T* fn = r.fn;
+        const T* sn = r.sn;
+        const int nvn = r.nvn;
+        const bool paired = r.pair >= 0;
         int j0 = i, jc = 1;
-        int64_t gn = 0;
-        if (r.pair >= 0) {
-            int64_t po = P.p_off[r.pair] + i;
-            j0 = P.p_j0[po];
-            jc = P.p_cnt[po];
-            gn = P.g_off[P.dgrid[r.data]];
-        }
+        if (paired) { j0 = r.pj0[i]; jc = r.pcnt[i]; }
         for (int j = j0; j < j0 + jc; ++j) {
-            const A sc = r.pair >= 0 ? merge_scale<D, A>(li, P.vlev[gn + j]) : (A)1;
+            const A sc = paired ? merge_scale<D, A>(li, r.vl[j]) : (A)1;
 #pragma unroll
             for (int k = 0; k < NDF; ++k) {
-                A p = (A)fn[(int64_t)k * nvn + j];
-                if (any) {
+                A p = (A)fn[k * nvn + j];
+                if (r.any) {
 #pragma unroll
                     for (int t = 0; t < D; ++t)
-                        if (dm[t] != (A)0) p += dm[t] * (A)sn[((int64_t)t * NDF + k) * nvn + j];
+                        if (r.dm[t] != (A)0) p += r.dm[t] * (A)sn[(t * NDF + k) * nvn + j];
                 }
                 acc[k] += (fc[k] - p) * sc * inv_ds;
             }
@@ -148,44 +145,103 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
     const T* fcell = (const T*)P.f_in + fo;
     T* scell = (T*)P.sdf + fo * D;
     __shared__ SlopeOp ops[MAXD];
-    __shared__ SlopeNbrA<A> snb[MAX_SLOPE_NBR];
-    __shared__ int sbase[2 * MAXD];
+    __shared__ SlopeNbrA<A, T> snb[MAX_SLOPE_NBR];
+    __shared__ int sbase[2 * MAXD + 1];
     __shared__ A sconst[4 * MAXD];   // inv_dsA, inv_dsB, 1/cntA, 1/cntB per direction
     if (threadIdx.x < D) ops[threadIdx.x] = P.slope_ops[op0 + threadIdx.x];
     __syncthreads();
     if (threadIdx.x == 0) {
-        const double* cm = P.dmid + (int64_t)cell * MAXD;
         int n = 0;
         for (int dir = 0; dir < D; ++dir) {
             const SlopeOp& op = ops[dir];
             for (int side = 0; side < 2; ++side) {
-                const int list = side == 0 ? op.listA : op.listB;
                 const int cnt = (op.kind == SLOPE_ONE || op.kind == SLOPE_TWO) ? (side == 0 ? op.cntA : (op.kind == SLOPE_TWO ? op.cntB : 0)) : 0;
-                const bool proj = side == 0 ? op.projA : op.projB;
                 sbase[2 * dir + side] = n;
-                for (int j = 0; j < cnt && n < MAX_SLOPE_NBR; ++j, ++n) {
-                    NbrRef r = P.slope_nbr[list + j];
-                    SlopeNbrA<A> e;
-                    e.data = r.data; e.pair = r.pair; e.any = 0;
-                    for (int t = 0; t < MAXD; ++t) {
-                        e.dm[t] = (t < D && proj && t != dir) ? (A)(cm[t] - P.dmid[(int64_t)r.data * MAXD + t]) : (A)0;
-                        e.any |= e.dm[t] != (A)0;
-                    }
-                    snb[n] = e;
-                }
+                n += cnt;
             }
             sconst[4 * dir + 0] = (A)op.inv_dsA;
             sconst[4 * dir + 1] = (A)op.inv_dsB;
-            sconst[4 * dir + 2] = op.cntA > 0 ? (A)(1.0 / op.cntA) : (A)0;
-            sconst[4 * dir + 3] = op.cntB > 0 ? (A)(1.0 / op.cntB) : (A)0;
+            sconst[4 * dir + 2] = op.cntA > 0 ? (A)1 / (A)op.cntA : (A)0;
+            sconst[4 * dir + 3] = op.cntB > 0 ? (A)1 / (A)op.cntB : (A)0;
         }
+        sbase[2 * D] = n < MAX_SLOPE_NBR ? n : MAX_SLOPE_NBR;
     }
     __syncthreads();
+    // one thread per neighbour entry (at most 2 * dim * 2^(dim-1), checked on the host)
+    if (threadIdx.x < sbase[2 * D]) {
+        const int e = threadIdx.x;
+        int ds = 0;
+        while (ds + 1 < 2 * D && sbase[ds + 1] <= e) ++ds;
+        const int dir = ds >> 1, side = ds & 1;
+        const SlopeOp& op = ops[dir];
+        const NbrRef r = P.slope_nbr[(side == 0 ? op.listA : op.listB) + (e - sbase[ds])];
+        const bool proj = side == 0 ? op.projA : op.projB;
+        const double* cm = P.dmid + (int64_t)cell * MAXD;
+        const double* nm = P.dmid + (int64_t)r.data * MAXD;
+        SlopeNbrA<A, T> c;
+        const int64_t nfo = P.foff[r.data];
+        c.fn = (const T*)P.f_in + nfo;
+        c.sn = (const T*)P.sdf + nfo * D;
+        c.nvn = P.dnv[r.data];
+        c.pair = r.pair;
+        const int64_t gn = P.g_off[P.dgrid[r.data]];
+        c.vl = P.vlev + gn;
+        if (r.pair >= 0) {
+            const int64_t po = P.p_off[r.pair];
+            c.pj0 = P.p_j0 + po;
+            c.pcnt = P.p_cnt + po;
+        } else {
+            c.pj0 = nullptr;
+            c.pcnt = nullptr;
+        }
+        c.any = 0;
+#pragma unroll
+        for (int t = 0; t < MAXD; ++t) {
+            c.dm[t] = (t < D && proj && t != dir) ? (A)(cm[t] - nm[t]) : (A)0;
+            c.any |= c.dm[t] != (A)0;
+        }
+        snb[e] = c;
+    }
+    __syncthreads();
+    // regular cell: in every direction a two-sided slope from one neighbour per side, on
+    // this cell's velocity grid and without transverse projection -- slope_side below with
+    // its loops and branches resolved
+    bool reg = true;
+#pragma unroll
+    for (int dir = 0; dir < D; ++dir) {
+        const SlopeOp& op = ops[dir];
+        reg = reg && op.kind == SLOPE_TWO && op.cntA == 1 && op.cntB == 1;
+        if (reg) {
+            const SlopeNbrA<A, T>& a = snb[sbase[2 * dir]];
+            const SlopeNbrA<A, T>& b = snb[sbase[2 * dir + 1]];
+            reg = a.pair < 0 && b.pair < 0 && !a.any && !b.any && a.nvn == nv && b.nvn == nv;
+        }
+    }
+    if (reg) {
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A fc[NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[k * nv + i];
+#pragma unroll
+            for (int dir = 0; dir < D; ++dir) {
+                const T* fa = snb[sbase[2 * dir]].fn;
+                const T* fb = snb[sbase[2 * dir + 1]].fn;
+                const A ia = sconst[4 * dir], ib = sconst[4 * dir + 1];
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    const A sA = (fc[k] - (A)fa[k * nv + i]) * ia;
+                    const A sB = (fc[k] - (A)fb[k * nv + i]) * ib;
+                    scell[(dir * NDF + k) * nv + i] = (T)minmod(sA, sB);
+                }
+            }
+        }
+        return;
+    }
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[(int64_t)k * nv + i];
+        for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[k * nv + i];
 #pragma unroll
         for (int dir = 0; dir < D; ++dir) {
             const SlopeOp& op = ops[dir];
@@ -196,19 +252,19 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
                 for (int k = 0; k < NDF; ++k) out[k] = 0;
             } else {
                 A sA[NDF];
-                slope_side<D, NDF, T>(P, i, li, fc, &snb[sbase[2 * dir]], op.cntA, sconst[4 * dir], sconst[4 * dir + 2], sA);
+                slope_side<D, NDF, T>(i, li, fc, &snb[sbase[2 * dir]], op.cntA, sconst[4 * dir], sconst[4 * dir + 2], sA);
                 if (op.kind == SLOPE_ONE) {
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) out[k] = sA[k];
                 } else {
                     A sB[NDF];
-                    slope_side<D, NDF, T>(P, i, li, fc, &snb[sbase[2 * dir + 1]], op.cntB, sconst[4 * dir + 1], sconst[4 * dir + 3], sB);
+                    slope_side<D, NDF, T>(i, li, fc, &snb[sbase[2 * dir + 1]], op.cntB, sconst[4 * dir + 1], sconst[4 * dir + 3], sB);
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) out[k] = minmod(sA[k], sB[k]);
                 }
             }
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) scell[((int64_t)dir * NDF + k) * nv + i] = (T)out[k];
+            for (int k = 0; k < NDF; ++k) scell[(dir * NDF + k) * nv + i] = (T)out[k];
         }
     }
 }
@@ -712,6 +768,14 @@ __host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, i
     return ((size_t)NDF * max_nv + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
 }
 
+// the faces of a regular cell (fluid_reg), by direction and side (2*dir + (face at +ds/2))
+template <typename A, typename T> struct RegFace {
+    const T* of;    // the neighbour's f and sdf blocks
+    const T* os;
+    A dxm;          // face midpoint - my centre along dir (= -(face midpoint - neighbour's centre))
+    A sarea;
+};
+
 // flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part)
 template <int D, int NDF, typename T>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
@@ -719,6 +783,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ Incidence sinc[MAX_INC];
     __shared__ IncA<A, T> sia[MAX_INC];
+    __shared__ RegFace<A, T> srf[2 * MAXD];
     __shared__ int8_t sbt[MAX_INC];             // incidence -> its Maxwellian factor table, -1 none
     __shared__ A sbpre[MAX_INC], sbk[MAX_INC];  // ρ (λ/π)^{D/2} and K/(2λ) of that Maxwellian
     __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
@@ -736,6 +801,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const int64_t step = P.prob_step[slot];
     const int check_interval = PP.check;
     const int i0 = P.inc_off[fcx], ninc = P.inc_off[fcx + 1] - i0;
+    const bool reg = P.fluid_reg[fcx] != 0;
     for (int e = threadIdx.x; e < ninc; e += BLOCK) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
@@ -762,6 +828,14 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             ia.of = nullptr; ia.os = nullptr; ia.onv = 0; ia.ogo = 0;
         }
         sia[e] = ia;
+        if (reg) {
+            // (selects rather than a runtime index keep ia and I in registers)
+            const int d = I.dir;
+            const A dm = d == 0 ? ia.dxm[0] : (d == 1 ? ia.dxm[1] : ia.dxm[MAXD - 1]);
+            RegFace<A, T> rf;
+            rf.of = ia.of; rf.os = ia.os; rf.dxm = dm; rf.sarea = ia.sarea;
+            srf[2 * d + (dm > (A)0 ? 1 : 0)] = rf;
+        }
     }
     if (threadIdx.x == 0) {
         const double* cd = P.dds + (int64_t)cell * MAXD;
@@ -883,6 +957,34 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         A acc[NDF], accM[NDF];
 #pragma unroll
         for (int k = 0; k < NDF; ++k) { acc[k] = 0; accM[k] = 0; }
+        if (reg) {
+            // regular cell: per direction the velocity leaves through the face it points at
+            // (own reconstruction there) and enters through the opposite face (the upwind
+            // neighbour's reconstruction) -- the generic loop below with its branches resolved
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const A ud = u[d];
+                const int so = 2 * d + (ud > (A)0 ? 1 : 0);
+                const RegFace<A, T>& fo_ = srf[so];
+                const RegFace<A, T>& fi_ = srf[so ^ 1];
+                A dx[D], dxo[D];
+#pragma unroll
+                for (int d2 = 0; d2 < D; ++d2) {
+                    dx[d2] = (d2 == d ? fo_.dxm : (A)0) - u[d2] * adt;
+                    dxo[d2] = d2 == d ? -fi_.dxm : (A)0;
+                }
+                A mi[NDF];
+                other_micro<D, NDF, T, A>(fi_.of, fi_.os, nv, i, u, dxo, myds, adt, d, 0, mi);
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    const A mo = own_recon<D, A>(0, fr[k], sr[k], dx, myds) * ud;
+                    acc[k] += fo_.sarea * mo;
+                    acc[k] += fi_.sarea * mi[k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) accM[k] = acc[k];
+        } else
         for (int e = 0; e < ninc; ++e) {
             const IncA<A, T>& ia = sia[e];
             const int dir = ia.dir;
@@ -1233,7 +1335,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 //    when given), so a batch of uneven problems keeps every SM busy to the end of the
 //    sub-step.  The counter must be zero at launch.
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 3 : 2) flux_collide_kernel(Dev P, int* counter,
+__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_kernel(Dev P, int* counter,
                                                                                   const int32_t* order, int n) {
     __shared__ int item;
     int it = blockIdx.x;
