@@ -265,7 +265,19 @@ ProbParams params_of(const kg_params& p, double dt) {
     ProbParams pp{};
     pp.gamma = p.gamma; pp.K = p.K; pp.Pr = p.Pr; pp.omega = p.omega; pp.mu_ref = p.mu_ref;
     pp.dt = dt; pp.check = p.st_check_interval;
+    pp.dtf = (float)dt; pp.Kf = (float)p.K; pp.mu2f = (float)(2.0 * p.mu_ref);
+    pp.omf = (float)(1.0 - p.omega); pp.shkf = (float)(0.8 * (1.0 - p.Pr));
     return pp;
+}
+
+// new dt of a problem, on the device too when the merged table is current
+int set_prob_dt(kg_handle* h, int slot, double dt) {
+    ProbParams& pp = h->probs[slot].pp;
+    pp.dt = dt;
+    pp.dtf = (float)dt;
+    if (!h->dirty) KG_CUDA(h, cudaMemcpyAsync(&h->d_probs[slot], &pp, sizeof(ProbParams), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // pp is host memory the copy reads
+    return KG_OK;
 }
 
 // Rebuilds the merged gather form of the live problems and uploads it.
@@ -291,7 +303,7 @@ int rebuild(kg_handle* h) {
         // dynamic shared memory of the flux and wall kernels plus a reserve for their static arrays
         const size_t sa = storage_size(h);
         const size_t sflux = ((size_t)M.ndf * M.max_nv + (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis) * sa + 16384;
-        const size_t swall = ((size_t)(M.ndf + 1) * M.max_nv + (size_t)M.dim * M.max_axis) * sa + M.max_nv + 4096;
+        const size_t swall = ((size_t)M.ndf * M.max_nv + (size_t)M.dim * M.max_axis) * sa + M.max_nv + 4096;
         const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
     }
@@ -302,7 +314,7 @@ int rebuild(kg_handle* h) {
 #define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
     UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
     UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
-    UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dnv, dnv); UP(dprob, dprob);
+    UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
     UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
     UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
     UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
@@ -804,8 +816,8 @@ int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_repor
     cudaSetDevice(h->device);
     Problem& pb = h->probs[0];
     if (pb.pp.dt != dt) {
-        pb.pp.dt = dt;
-        if (!h->dirty) KG_CUDA(h, cudaMemcpyAsync(&h->d_probs[0].dt, &pb.pp.dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+        int rc = set_prob_dt(h, 0, dt);
+        if (rc) return rc;
     }
     KG_CUDA(h, cudaMemcpyAsync(h->d_step, &step, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
     double ms = 0.0;
@@ -970,10 +982,7 @@ int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, in
 
 int kg_batch_set_dt(kg_handle* h, int32_t slot, double dt) {
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !(dt > 0.0)) return fail(h, KG_ERR_ARG, "bad argument");
-    h->probs[slot].pp.dt = dt;
-    if (!h->dirty) KG_CUDA(h, cudaMemcpyAsync(&h->d_probs[slot].dt, &h->probs[slot].pp.dt, sizeof(double), cudaMemcpyHostToDevice, h->stream));
-    KG_CUDA(h, cudaStreamSynchronize(h->stream));
-    return KG_OK;
+    return set_prob_dt(h, slot, dt);
 }
 
 }  // extern "C"

@@ -40,6 +40,7 @@ struct Dev {
     const int32_t* dbe;
     const double* dmid;                // [n_data][MAXD]
     const double* dds;
+    const double* dinvv;               // 1 / cell volume
     // pairings
     const int64_t* p_off;
     const int32_t* p_j0;

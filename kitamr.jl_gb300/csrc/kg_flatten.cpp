@@ -173,6 +173,12 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         for (int d = 0; d < D; ++d) { F.dmid[(size_t)i * MAXD + d] = t.cell_midpoint[(size_t)sc * D + d]; F.dds[(size_t)i * MAXD + d] = t.cell_ds[(size_t)sc * D + d]; }
     }
     for (int i = 0; i < F.n_data; ++i) F.foff[i + 1] = F.foff[i] + (int64_t)grid_nv(t, F.dgrid[i]) * NDF;
+    F.dinvv.resize(F.n_data);
+    for (int i = 0; i < F.n_data; ++i) {
+        double v = F.dds[(size_t)i * MAXD];
+        for (int d = 1; d < D; ++d) v *= F.dds[(size_t)i * MAXD + d];
+        F.dinvv[i] = 1.0 / v;
+    }
     F.dnv.resize(F.n_data);
     F.dprob.assign(F.n_data, 0);
     for (int i = 0; i < F.n_data; ++i) F.dnv[i] = grid_nv(t, F.dgrid[i]);
@@ -492,6 +498,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
     M.p_off.push_back(0);
     M.foff.assign((size_t)dcap + 1, 0);
     M.dgrid.assign(dcap, 0); M.dbe.assign(dcap, 0); M.dnv.assign(dcap, 0); M.dprob.assign(dcap, -1);
+    M.dinvv.assign(dcap, 0.0);
     M.dmid.assign((size_t)dcap * MAXD, 0.0); M.dds.assign((size_t)dcap * MAXD, 0.0);
     M.inc_off.push_back(0);
     size_t npass = 0;
@@ -544,6 +551,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             M.dbe[m] = F.dbe[j];
             M.dnv[m] = F.dnv[j];
             M.dprob[m] = p.slot;
+            M.dinvv[m] = F.dinvv[j];
             for (int d = 0; d < MAXD; ++d) { M.dmid[(size_t)m * MAXD + d] = F.dmid[(size_t)j * MAXD + d]; M.dds[(size_t)m * MAXD + d] = F.dds[(size_t)j * MAXD + d]; }
         }
         // pairings

@@ -73,6 +73,8 @@ struct ProbParams {
     int32_t check;                 // st_check_interval
     int32_t fluid_begin, fluid_end; // range of the problem in the merged fluid-cell list
     int32_t slot;
+    // FP32 copies for the mixed form's per-cell constants: dt, K, 2 mu_ref, 1 - omega, 0.8 (1 - Pr)
+    float dtf, Kf, mu2f, omf, shkf;
 };
 
 // ---- flattened topology (host copy, then mirrored to device) ------------------
@@ -98,6 +100,7 @@ struct Flat {
     // data table
     std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)
     std::vector<int32_t> dgrid, dbe;
+    std::vector<double> dinvv;    // n_data: 1 / cell volume (Π ds)
     std::vector<int32_t> dnv;      // velocity cells per data item
     std::vector<int32_t> dprob;    // problem slot per data item
     std::vector<double> dmid, dds; // n_data * MAXD

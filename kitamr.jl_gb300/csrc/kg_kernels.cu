@@ -218,20 +218,44 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
         }
     }
     if (reg) {
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
-            A fc[NDF];
+        // two velocity cells per thread and pass: all their loads are issued before any
+        // store, so each thread keeps twice the loads in flight (the kernel waits on memory)
+        const T* fa[D];
+        const T* fb[D];
+        A ia[D], ib[D];
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[k * nv + i];
+        for (int dir = 0; dir < D; ++dir) {
+            fa[dir] = snb[sbase[2 * dir]].fn;
+            fb[dir] = snb[sbase[2 * dir + 1]].fn;
+            ia[dir] = sconst[4 * dir];
+            ib[dir] = sconst[4 * dir + 1];
+        }
+        for (int i0 = threadIdx.x; i0 < nv; i0 += 2 * BLOCK) {
+            const int i1 = i0 + BLOCK;
+            const bool two = i1 < nv;
+            const int j1 = two ? i1 : i0;    // a valid index for the second set of loads
+            A fc0[NDF], fc1[NDF], a0[D][NDF], a1[D][NDF], b0[D][NDF], b1[D][NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) { fc0[k] = (A)fcell[k * nv + i0]; fc1[k] = (A)fcell[k * nv + j1]; }
 #pragma unroll
             for (int dir = 0; dir < D; ++dir) {
-                const T* fa = snb[sbase[2 * dir]].fn;
-                const T* fb = snb[sbase[2 * dir + 1]].fn;
-                const A ia = sconst[4 * dir], ib = sconst[4 * dir + 1];
 #pragma unroll
                 for (int k = 0; k < NDF; ++k) {
-                    const A sA = (fc[k] - (A)fa[k * nv + i]) * ia;
-                    const A sB = (fc[k] - (A)fb[k * nv + i]) * ib;
-                    scell[(dir * NDF + k) * nv + i] = (T)minmod(sA, sB);
+                    a0[dir][k] = (A)fa[dir][k * nv + i0];
+                    b0[dir][k] = (A)fb[dir][k * nv + i0];
+                    a1[dir][k] = (A)fa[dir][k * nv + j1];
+                    b1[dir][k] = (A)fb[dir][k * nv + j1];
+                }
+            }
+#pragma unroll
+            for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    scell[(dir * NDF + k) * nv + i0] =
+                        (T)minmod((fc0[k] - a0[dir][k]) * ia[dir], (fc0[k] - b0[dir][k]) * ib[dir]);
+                    if (two)
+                        scell[(dir * NDF + k) * nv + i1] =
+                            (T)minmod((fc1[k] - a1[dir][k]) * ia[dir], (fc1[k] - b1[dir][k]) * ib[dir]);
                 }
             }
         }
@@ -464,7 +488,7 @@ __device__ __forceinline__ double maxwell_h(const VGridView& g, int i, const dou
 // shared memory of wall_kernel for a donor grid of nv velocity cells
 template <int D, int NDF, typename A>
 __host__ __device__ __forceinline__ size_t wall_smem(int nv, int max_axis) {
-    return ((size_t)(NDF + 1) * nv + (size_t)D * max_axis) * sizeof(A) + (size_t)nv;
+    return ((size_t)NDF * nv + (size_t)D * max_axis) * sizeof(A) + (size_t)nv;
 }
 
 // update_solid_neighbor! (Immersed_boundary.jl:367-483): the SolidNeighbor's f is the
@@ -487,8 +511,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     const int gid = P.dgrid[op.donor];
     const int MA = P.max_axis;
     A* aux = (A*)wsh;                                // NDF * nv: image extrapolation
-    A* mhs = aux + (size_t)NDF * nv;                 // nv: wall Maxwellian with rho = 1
-    A* Ew = mhs + nv;                                // D * max_axis: its 1D factors
+    A* Ew = aux + (size_t)NDF * nv;                  // D * max_axis: 1D factors of the wall Maxwellian
     unsigned char* out_dir = (unsigned char*)(Ew + (size_t)D * MA);   // nv: u.n >= 0
     ib_setup<D, A>(P, op.list, op.cnt, snb);
     const double lam = op.bc[D + 1];
@@ -522,6 +545,13 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     const A* VU = vel<A>(P);
     const uint16_t* vx = P.vidx + g.goff;
     const A idxs = wc[W_IDXS], idxf = wc[W_IDXF], dxL = wc[W_DXL], pre = wc[W_PRE];
+    // the wall Maxwellian with rho = 1 at velocity i, from its factor tables
+    auto mh_of = [&](int i) {
+        A m = pre;
+#pragma unroll
+        for (int d = 0; d < D; ++d) m *= Ew[d * MA + vx[(int64_t)d * P.PG + i]];
+        return m;
+    };
     KSum<A> red[2];   // MuR, SF
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
@@ -562,10 +592,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
             aux[(int64_t)k * nv + i] = a;
             if (k == 0) a0 = a;
         }
-        A mh = pre;
-#pragma unroll
-        for (int d = 0; d < D; ++d) mh *= Ew[d * MA + vx[(int64_t)d * P.PG + i]];
-        mhs[i] = mh;
+        const A mh = mh_of(i);
         const A cw = (A)cvcw[i];
         if (leaving) red[0].add(cw * vn * mh);
         else red[1].add(cw * vn * a0);
@@ -576,7 +603,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
         A vn = 0;
 #pragma unroll
         for (int d = 0; d < D; ++d) vn += VU[(int64_t)d * P.PG + g.goff + idx] * wc[W_N + d];
-        red[0].add((A)P.cut_sw[op.cut_off + a] * vn * mhs[idx]);
+        red[0].add((A)P.cut_sw[op.cut_off + a] * vn * mh_of(idx));
         red[1].add((A)P.cut_gw[op.cut_off + a] * vn * aux[idx]);
     }
     double rs[2];
@@ -588,7 +615,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         A v[NDF];
         if (out_dir[i]) {
-            const A mh = mhs[i];
+            const A mh = mh_of(i);
             v[0] = mh * rw;
             if (NDF == 2) v[NDF - 1] = mh * bk * rw;
         } else {
@@ -602,7 +629,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
         const int idx = P.cut_idx[op.cut_off + a];
         const A gw = (A)P.cut_gw[op.cut_off + a], sw = (A)P.cut_sw[op.cut_off + a];
-        const A mh = mhs[idx];
+        const A mh = mh_of(idx);
         A mv[NDF];
         mv[0] = mh * rw;
         if (NDF == 2) mv[NDF - 1] = mh * bk * rw;
@@ -837,11 +864,10 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             srf[2 * d + (dm > (A)0 ? 1 : 0)] = rf;
         }
     }
+    const double invV = P.dinvv[cell];
     if (threadIdx.x == 0) {
         const double* cd = P.dds + (int64_t)cell * MAXD;
-        double Vc = cd[0];
-        for (int d = 1; d < D; ++d) Vc *= cd[d];
-        sc[C_SDT] = (A)(dt / Vc);
+        sc[C_SDT] = (A)(dt * invV);
         sc[C_ADT] = (A)dt;
         for (int d = 0; d < D; ++d) sc[C_DS0 + d] = (A)cd[d];
     }
@@ -857,10 +883,6 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const T* fcell = (const T*)P.f_in + fo;
     const T* scl = (const T*)P.sdf + fo * D;
     T* fnew = (T*)P.f_out + fo;
-    const double* cds = P.dds + (int64_t)cell * MAXD;
-    double V = cds[0];
-#pragma unroll
-    for (int d = 1; d < D; ++d) V *= cds[d];
     A myds[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) myds[d] = sc[C_DS0 + d];
@@ -1124,78 +1146,83 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             for (int q = 0; q < D + 2; ++q) { both[q] = wacc[q]; both[D + 2 + q] = wfc[q]; }
             block_sum_ks<2 * (D + 2)>(both, red, sred);
         }
-        if (threadIdx.x == 0) {
+        // Two lanes recover the two sets of primitives in one FP64 instruction stream (on
+        // GB300 an FP64 warp instruction costs the same for one lane or 32): lane 0 the
+        // conserved update w + dt/V·flux and prim_c, lane 1 the primitives of the convected f
+        // (Euler: both lanes the same, so prim_n = prim_c)
+        if (threadIdx.x < 2) {
+            const int ln = threadIdx.x;
             double* w = P.w + (int64_t)cell * MAXW;
-            double wn[MAXW], pc[MAXW], pn[MAXW];
-            const double dtV = dt / V;
-            if (P.marching == KG_MARCH_CAIDVM) {
+            const double dtV = dt * invV;
+            const bool lane_mom = P.marching == KG_MARCH_CAIDVM ? ln == 1 : P.flux == KG_FLUX_DVM;
+            double wv[MAXW], pv[MAXW];
 #pragma unroll
-                for (int q = 0; q < D + 2; ++q) wn[q] = fma(red[q], dtV, w[q]);
-                get_prim_r<D>(wn, PP.gamma, pc);
-                double wf[MAXW];
+            for (int q = 0; q < D + 2; ++q) wv[q] = lane_mom ? red[D + 2 + q] : fma(red[q], dtV, w[q]);
+            get_prim_r<D>(wv, PP.gamma, pv);
 #pragma unroll
-                for (int q = 0; q < D + 2; ++q) wf[q] = red[D + 2 + q];
-                get_prim_r<D>(wf, PP.gamma, pn);
-            } else {
-                if (P.flux == KG_FLUX_DVM) {
+            for (int q = 0; q < D + 2; ++q) sscal[ln * MAXW + q] = pv[q];
+            if (ln == 0) {
 #pragma unroll
-                    for (int q = 0; q < D + 2; ++q) wn[q] = red[D + 2 + q];
-                } else {
-#pragma unroll
-                    for (int q = 0; q < D + 2; ++q) wn[q] = fma(red[q], dtV, w[q]);
-                }
-                get_prim_r<D>(wn, PP.gamma, pc);
-#pragma unroll
-                for (int q = 0; q < D + 2; ++q) pn[q] = pc[q];
+                for (int q = 0; q < D + 2; ++q) w[q] = wv[q];
             }
-#pragma unroll
-            for (int q = 0; q < D + 2; ++q) { w[q] = wn[q]; sscal[q] = pc[q]; sscal[MAXW + q] = pn[q]; }
-            const double lc = pc[D + 1], ln = pn[D + 1];
-            if constexpr (sizeof(A) == 8) {
-                // get_τ (Gas/Model.jl:14) and the constants of discrete_maxwell / shakhov_part
-                const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
-                sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
-                sc[C_PREN] = pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5));
-                sc[C_BFC] = Kgas / (2.0 * lc);
-                sc[C_BFN] = Kgas / (2.0 * ln);
-                sc[C_R1] = tau / (tau + dt);
-                sc[C_R2] = dt / (tau + dt);
-                sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
-                sc[C_LC] = lc;
-            } else {
-                // mixed form: the same constants in FP32 from the FP64 primitives (they scale
-                // FP32 per-velocity values), plus hi/lo pairs of U and λ for the tables
-                const float rc = (float)pc[0], rn = (float)pn[0], lcf = (float)lc, lnf = (float)ln;
-                const float dtf = (float)dt;
-                const float tau = (float)(2.0 * PP.mu_ref) * powf(lcf, (float)(1.0 - PP.omega)) / rc;
-                constexpr float IPI = (float)(1.0 / PI);
-                sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
-                sc[C_PREN] = rn * (D == 2 ? lnf * IPI : powf(lnf * IPI, 1.5f));
-                sc[C_BFC] = (float)Kgas / (2.f * lcf);
-                sc[C_BFN] = (float)Kgas / (2.f * lnf);
-                sc[C_R1] = tau / (tau + dtf);
-                sc[C_R2] = dtf / (tau + dtf);
-                sc[C_SK] = (float)(0.8 * (1.0 - PP.Pr)) * lcf * lcf / rc;
-                sc[C_LC] = lcf;
-                sc[C_LCH] = lcf;
-                sc[C_LCL] = (float)(lc - (double)lcf);
-                sc[C_LNH] = lnf;
-                sc[C_LNL] = (float)(ln - (double)lnf);
-                for (int d = 0; d < D; ++d) {
-                    const float uh = (float)pn[1 + d];
-                    sc[C_UNH + d] = uh;
-                    sc[C_UNL + d] = (float)(pn[1 + d] - (double)uh);
-                }
+        }
+        if (threadIdx.x < 32) {
+            __syncwarp();
+            const int lane = threadIdx.x;
+            // hi/lo pairs (one lane each, one instruction stream): U_c (lanes 0..D-1),
+            // U_n (8..), lambda_c (16), lambda_n (17)
+            int src = -1, dh = 0, dl = 0;
+            if (lane < D) { src = 1 + lane; dh = C_UH + lane; dl = C_UL + lane; }
+            else if (lane >= 8 && lane < 8 + D) { src = MAXW + 1 + lane - 8; dh = C_UNH + lane - 8; dl = C_UNL + lane - 8; }
+            else if (lane == 16) { src = D + 1; dh = C_LCH; dl = C_LCL; }
+            else if (lane == 17) { src = MAXW + D + 1; dh = C_LNH; dl = C_LNL; }
+            if (src >= 0) {
+                const double x = sscal[src];
+                const A h = (A)x;
+                sc[dh] = h;
+                sc[dl] = (A)(x - (double)h);
             }
-            for (int d = 0; d < D; ++d) {
-                const A uh = (A)pc[1 + d];
-                sc[C_UH + d] = uh;
-                sc[C_UL + d] = (A)(pc[1 + d] - (double)uh);
-            }
+            // status of prim_c: one lane per component
             int bad = 0;
-            for (int q = 0; q < D + 2; ++q) if (!isfinite(pc[q])) bad |= ST_NONFINITE;
-            if (!(pc[0] > 0.0) || !(pc[D + 1] > 0.0)) bad |= ST_NEGATIVE;
-            if (bad) atomicOr(&P.status[slot], bad);
+            if (lane < D + 2) {
+                const double x = sscal[lane];
+                if (!isfinite(x)) bad |= ST_NONFINITE;
+                if ((lane == 0 || lane == D + 1) && !(x > 0.0)) bad |= ST_NEGATIVE;
+            }
+            bad = __reduce_or_sync(0xffffffffu, bad);
+            if (lane == 0) {
+                if (bad) atomicOr(&P.status[slot], bad);
+                const double* pc = sscal;
+                const double* pn = sscal + MAXW;
+                const double lc = pc[D + 1], ln = pn[D + 1];
+                if constexpr (sizeof(A) == 8) {
+                    // get_τ (Gas/Model.jl:14) and the constants of discrete_maxwell / shakhov_part
+                    const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
+                    sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
+                    sc[C_PREN] = pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5));
+                    sc[C_BFC] = Kgas / (2.0 * lc);
+                    sc[C_BFN] = Kgas / (2.0 * ln);
+                    sc[C_R1] = tau / (tau + dt);
+                    sc[C_R2] = dt / (tau + dt);
+                    sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
+                    sc[C_LC] = lc;
+                } else {
+                    // mixed form: the same constants in FP32 (they scale FP32 per-velocity values)
+                    const float rc = (float)pc[0], rn = (float)pn[0];
+                    const float lcf = (float)sc[C_LCH], lnf = (float)sc[C_LNH];
+                    const float dtf = PP.dtf;
+                    const float tau = PP.mu2f * powf(lcf, PP.omf) / rc;
+                    constexpr float IPI = (float)(1.0 / PI);
+                    sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
+                    sc[C_PREN] = rn * (D == 2 ? lnf * IPI : powf(lnf * IPI, 1.5f));
+                    sc[C_BFC] = PP.Kf / (2.f * lcf);
+                    sc[C_BFN] = PP.Kf / (2.f * lnf);
+                    sc[C_R1] = tau / (tau + dtf);
+                    sc[C_R2] = dtf / (tau + dtf);
+                    sc[C_SK] = PP.shkf * lcf * lcf / rc;
+                    sc[C_LC] = lcf;
+                }
+            }
         }
         __syncthreads();
     }
