@@ -570,10 +570,37 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         M.fluid_reg.insert(M.fluid_reg.end(), F.fluid_reg.begin(), F.fluid_reg.end());
         for (size_t q = 1; q < F.inc_off.size(); ++q) M.inc_off.push_back(incacc + F.inc_off[q]);
         for (Incidence a : F.inc) {
-            if (a.other >= 0) a.other += p.dbase;
+            if (a.other >= 0) {
+                a.other += p.dbase;
+                a.ofoff = M.foff[a.other];
+                a.onv = M.dnv[a.other];
+                a.ogo = (int32_t)M.g_off[M.dgrid[a.other]];
+            } else {
+                a.ofoff = -1; a.onv = 0; a.ogo = 0;
+            }
+            for (int d = 0; d < MAXD; ++d) {
+                a.dxm_f[d] = (float)(a.fmid[d] - a.my_mid[d]);
+                a.dxo_f[d] = (float)(a.fmid[d] - a.ot_mid[d]);
+                a.ods_f[d] = (float)a.ot_ds[d];
+            }
+            a.orient_f = (float)a.orient;
+            a.sarea_f = (float)a.sarea;
             a.pair = rp(a.pair);
             a.bc += bcacc;
             M.inc.push_back(a);
+        }
+        for (size_t k = 0; k < F.fluid_cells.size(); ++k) {
+            const int32_t m = F.fluid_cells[k] + p.dbase;
+            FluxCell fc{};
+            fc.foff = M.foff[m];
+            fc.goff = M.g_off[M.dgrid[m]];
+            fc.invV = M.dinvv[m];
+            for (int d = 0; d < MAXD; ++d) fc.ds[d] = M.dds[(size_t)m * MAXD + d];
+            fc.cell = m; fc.slot = p.slot;
+            fc.inc0 = incacc + F.inc_off[k];
+            fc.ninc = F.inc_off[k + 1] - F.inc_off[k];
+            fc.nv = M.dnv[m]; fc.gid = M.dgrid[m]; fc.reg = F.fluid_reg[k];
+            M.fcrec.push_back(fc);
         }
         M.bc_prim.insert(M.bc_prim.end(), F.bc_prim.begin(), F.bc_prim.end());
         M.bc_hl.insert(M.bc_hl.end(), F.bc_hl.begin(), F.bc_hl.end());
@@ -631,7 +658,7 @@ int64_t device_bytes(const Flat& F, int precision) {
     b += (int64_t)F.vu.size() * 8 + (int64_t)F.vw.size() * 8 + (int64_t)F.vlev.size();
     b += (int64_t)(F.p_j0.size() + F.p_cnt.size()) * 4;
     b += (int64_t)F.slope_ops.size() * sizeof(SlopeOp) + (int64_t)F.slope_nbr.size() * sizeof(NbrRef);
-    b += (int64_t)F.inc.size() * sizeof(Incidence);
+    b += (int64_t)F.inc.size() * sizeof(Incidence) + (int64_t)F.fluid_cells.size() * sizeof(FluxCell);
     b += (int64_t)F.wall_ops.size() * sizeof(WallOp) + (int64_t)F.cvcw.size() * 8;
     b += (int64_t)F.n_data * 64;
     return b;

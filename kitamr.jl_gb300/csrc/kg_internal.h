@@ -40,7 +40,7 @@ enum IncKind : int8_t { INC_INNER = 0, INC_DOMAIN = 1, INC_SOLID = 2 };
 // solid PsData); the reference reconstructs the here side without the positivity
 // limiter and (CAIDVM) takes the there side unreconstructed.
 
-struct Incidence {          // 128 bytes
+struct Incidence {          // 192 bytes
     double fmid[MAXD];      // face (sub-face) midpoint
     double my_mid[MAXD];    // centre used for this cell's reconstruction
     double ot_mid[MAXD];    // centre used for the other side's reconstruction
@@ -51,6 +51,21 @@ struct Incidence {          // 128 bytes
     int32_t pair;           // pairing (my grid <- other's grid), -1 identity
     int8_t kind, dir, bc_kind, here_side;
     int32_t bc;             // index into bc_prim (domain faces)
+    // resolved when the problems are merged, so the flux kernel needs no further lookups:
+    int64_t ofoff;          // f offset of the other side (-1 for a domain face)
+    int32_t onv, ogo;       // its velocity count and grid offset
+    float dxm_f[MAXD], dxo_f[MAXD], ods_f[MAXD], orient_f, sarea_f;   // FP32 roundings
+};
+
+// What the flux kernel needs of a fluid cell before its first barrier, in one record
+// (built when the problems are merged).
+struct FluxCell {
+    int64_t foff;           // f offset of the cell
+    int64_t goff;           // first velocity cell of its grid
+    double invV;            // 1 / cell volume
+    double ds[MAXD];
+    int32_t cell, slot, inc0, ninc;
+    int32_t nv, gid, reg, pad;
 };
 
 // ---- immersed boundary ----------------------------------------------------
@@ -116,6 +131,7 @@ struct Flat {
     std::vector<NbrRef> slope_nbr;
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
+    std::vector<FluxCell> fcrec;          // merged layout only: per fluid cell
     std::vector<uint8_t> fluid_reg;       // per fluid cell: 1 when its faces are 2*dim full inner faces
                                           // to same-sized neighbours on the same velocity grid
     std::vector<int32_t> inc_off;         // n_fluid + 1

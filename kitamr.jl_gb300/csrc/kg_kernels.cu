@@ -820,37 +820,45 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
            C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_UNH = C_QA + MAXD, C_UNL = C_UNH + MAXD,
            C_LCH = C_UNL + MAXD, C_LCL, C_LNH, C_LNL, C_N };
     __shared__ A sc[C_N];
-    const int cell = P.fluid_cells[fcx];
-    const int slot = P.dprob[cell];
+    // one record of the cell, then its incidences: two dependent loads before the barrier
+    const FluxCell FC = P.fcrec[fcx];
+    const int cell = FC.cell;
+    const int slot = FC.slot;
     const ProbParams& PP = P.probs[slot];
     const double dt = PP.dt;
     const double Kgas = PP.K;
     const int64_t step = P.prob_step[slot];
     const int check_interval = PP.check;
-    const int i0 = P.inc_off[fcx], ninc = P.inc_off[fcx + 1] - i0;
-    const bool reg = P.fluid_reg[fcx] != 0;
+    const int i0 = FC.inc0, ninc = FC.ninc;
+    const bool reg = FC.reg != 0;
     for (int e = threadIdx.x; e < ninc; e += BLOCK) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
         IncA<A, T> ia;
+        if constexpr (sizeof(A) == 4) {
 #pragma unroll
-        for (int d = 0; d < MAXD; ++d) {
-            ia.dxm[d] = (A)(I.fmid[d] - I.my_mid[d]);
-            ia.dxo[d] = (A)(I.fmid[d] - I.ot_mid[d]);
-            ia.ods[d] = (A)I.ot_ds[d];
+            for (int d = 0; d < MAXD; ++d) { ia.dxm[d] = I.dxm_f[d]; ia.dxo[d] = I.dxo_f[d]; ia.ods[d] = I.ods_f[d]; }
+            ia.orient = I.orient_f;
+            ia.sarea = I.sarea_f;
+        } else {
+#pragma unroll
+            for (int d = 0; d < MAXD; ++d) {
+                ia.dxm[d] = (A)(I.fmid[d] - I.my_mid[d]);
+                ia.dxo[d] = (A)(I.fmid[d] - I.ot_mid[d]);
+                ia.ods[d] = (A)I.ot_ds[d];
+            }
+            ia.orient = (A)I.orient;
+            ia.sarea = (A)I.sarea;
         }
-        ia.orient = (A)I.orient;
-        ia.sarea = (A)I.sarea;
         ia.kind = I.kind; ia.dir = I.dir; ia.bc_kind = I.bc_kind; ia.pair = I.pair;
         if (I.kind == INC_DOMAIN) ia.mode_out = (I.bc_kind == KG_BC_OUTFLOW) ? 2 : 1;
         else ia.mode_out = (I.kind == INC_SOLID) ? 1 : 0;
         ia.mode_in = (I.kind == INC_SOLID) ? (P.flux == KG_FLUX_CAIDVM ? 2 : 1) : 0;
         if (I.other >= 0) {
-            const int64_t ofo = P.foff[I.other];
-            ia.of = (const T*)P.f_in + ofo;
-            ia.os = (const T*)P.sdf + ofo * D;
-            ia.onv = P.dnv[I.other];
-            ia.ogo = (int32_t)P.g_off[P.dgrid[I.other]];
+            ia.of = (const T*)P.f_in + I.ofoff;
+            ia.os = (const T*)P.sdf + I.ofoff * D;
+            ia.onv = I.onv;
+            ia.ogo = I.ogo;
         } else {
             ia.of = nullptr; ia.os = nullptr; ia.onv = 0; ia.ogo = 0;
         }
@@ -864,22 +872,25 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             srf[2 * d + (dm > (A)0 ? 1 : 0)] = rf;
         }
     }
-    const double invV = P.dinvv[cell];
+    const double invV = FC.invV;
     if (threadIdx.x == 0) {
-        const double* cd = P.dds + (int64_t)cell * MAXD;
         sc[C_SDT] = (A)(dt * invV);
         sc[C_ADT] = (A)dt;
-        for (int d = 0; d < D; ++d) sc[C_DS0 + d] = (A)cd[d];
+        for (int d = 0; d < D; ++d) sc[C_DS0 + d] = (A)FC.ds[d];
     }
     __syncthreads();
-    const VGridView g = grid_view(P, cell);
+    VGridView g;
+    g.goff = FC.goff;
+    g.nv = FC.nv;
+    g.vu = P.vu;
+    g.PG = P.PG;
     const int nv = g.nv;
-    const int gid = P.dgrid[cell];
+    const int gid = FC.gid;
     const int64_t PG = P.PG;
     const A* VU = vel<A>(P);
     const A* VW0 = wts<A>(P);
     const A* VW = VW0 + g.goff;
-    const int64_t fo = P.foff[cell];
+    const int64_t fo = FC.foff;
     const T* fcell = (const T*)P.f_in + fo;
     const T* scl = (const T*)P.sdf + fo * D;
     T* fnew = (T*)P.f_out + fo;
