@@ -42,6 +42,14 @@ template <typename T>
 __global__ void from_storage(const T* __restrict__ src, double* __restrict__ dst, int64_t n) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) dst[i] = (double)src[i];
 }
+// Block copies within one array, one CTA per (src, dst, length) triple (in elements); the
+// destination blocks never overlap a source block (SolidNeighbor f <- its donor's f).
+template <typename T>
+__global__ void copy_blocks(T* f, const int64_t* tri) {
+    const int64_t* t = tri + 3 * (int64_t)blockIdx.x;
+    const int64_t src = t[0], dst = t[1], len = t[2];
+    for (int64_t i = threadIdx.x; i < len; i += blockDim.x) f[dst + i] = f[src + i];
+}
 }  // namespace
 
 void kg::set_global_error(const std::string& msg) { g_create_err = msg; }
@@ -137,6 +145,8 @@ struct kg_handle {
     double tune_ms[8] = {0};
     int* d_counter = nullptr;
     const int32_t* d_order = nullptr;
+    int64_t* d_tri = nullptr;      // wall-initialisation copies of an upload (grown on demand)
+    int64_t tri_cap = 0;
     // graph
     bool use_graph = false;
     cudaGraphExec_t gexec = nullptr;
@@ -566,9 +576,9 @@ int upload_problem_state(kg_handle* h, int slot, const double* f, const double* 
     const int D = h->prm.dim, NW = D + 2;
     const int64_t nfc = L.foff[L.n_cells];
     size_t ss = storage_size(h);
-    char* fa = (char*)h->fA + fb * ss;
-    char* fbp = (char*)h->fB + fb * ss;
-    // both f buffers carry the state (the step reads one, writes the other)
+    // into the buffer the next step reads; a step writes every data item's other buffer
+    // (flux: fluid cells; solid and wall kernels: both buffers of theirs)
+    char* fa = (char*)(h->parity == 0 ? h->fA : h->fB) + fb * ss;
     if (h->prm.precision == KG_PREC_FP64) {
         KG_CUDA(h, cudaMemcpyAsync(fa, f, sizeof(double) * nfc, cudaMemcpyHostToDevice, h->stream));
     } else {
@@ -577,12 +587,32 @@ int upload_problem_state(kg_handle* h, int slot, const double* f, const double* 
         to_storage<float><<<1024, 256, 0, h->stream>>>(st, (float*)fa, nfc);
         KG_CUDA(h, cudaGetLastError());
     }
-    // SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298)
-    for (const WallOp& wo : L.wall_ops) {
-        int64_t src = L.foff[wo.donor], dst = L.foff[wo.data], n = L.foff[wo.data + 1] - dst;
-        KG_CUDA(h, cudaMemcpyAsync(fa + dst * ss, fa + src * ss, n * ss, cudaMemcpyDeviceToDevice, h->stream));
+    // SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298): one
+    // launch for all walls of the problem
+    const int nwall = (int)L.wall_ops.size();
+    std::vector<int64_t> tri((size_t)nwall * 3);
+    for (int k = 0; k < nwall; ++k) {
+        const WallOp& wo = L.wall_ops[k];
+        tri[3 * k] = L.foff[wo.donor];
+        tri[3 * k + 1] = L.foff[wo.data];
+        tri[3 * k + 2] = L.foff[wo.data + 1] - L.foff[wo.data];
     }
-    KG_CUDA(h, cudaMemcpyAsync(fbp, fa, nf * ss, cudaMemcpyDeviceToDevice, h->stream));
+    if (nwall > 0) {
+        if (h->tri_cap < (int64_t)tri.size()) {
+            if (h->d_tri) cudaFree(h->d_tri);
+            h->d_tri = nullptr;
+            h->tri_cap = 0;
+            void* p = nullptr;
+            cudaError_t e = cudaMalloc(&p, sizeof(int64_t) * tri.size());
+            if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc wall copies");
+            h->d_tri = (int64_t*)p;
+            h->tri_cap = (int64_t)tri.size();
+        }
+        KG_CUDA(h, cudaMemcpyAsync(h->d_tri, tri.data(), sizeof(int64_t) * tri.size(), cudaMemcpyHostToDevice, h->stream));
+        if (h->prm.precision == KG_PREC_FP64) copy_blocks<double><<<nwall, 256, 0, h->stream>>>((double*)fa, h->d_tri);
+        else copy_blocks<float><<<nwall, 256, 0, h->stream>>>((float*)fa, h->d_tri);
+        KG_CUDA(h, cudaGetLastError());
+    }
     KG_CUDA(h, cudaMemsetAsync((char*)h->sdf + fb * D * ss, 0, nf * D * ss, h->stream));
     std::vector<double> pw((size_t)nd * MAXW, 0.0), pp((size_t)nd * MAXW, 0.0);
     for (int c = 0; c < L.n_cells; ++c)
@@ -736,6 +766,7 @@ int kg_destroy(kg_handle* h) {
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
     free_pools(h);
+    if (h->d_tri) cudaFree(h->d_tri);
     if (h->h_res) cudaFreeHost(h->h_res);
     if (h->h_status) cudaFreeHost(h->h_status);
     cudaStreamDestroy(h->stream);
