@@ -54,6 +54,7 @@ struct Dev {
     const int32_t* fluid_cells;
     const uint8_t* fluid_reg;          // per fluid cell: regular (fast path of the flux kernel)
     const FluxCell* fcrec;             // per fluid cell: its record
+    const SlopeCell* screc;            // per pass-cell entry: its record
     const int32_t* inc_off;
     const Incidence* inc;
     const double* bc_prim;

@@ -645,6 +645,29 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         M.pass_off.push_back((int32_t)M.slope_ops.size());
         M.pass_cells_off.push_back((int32_t)M.pass_cells.size());
     }
+    M.screc.resize(M.pass_cells.size());
+    for (size_t k = 0; k < M.pass_cells.size(); ++k) {
+        const int32_t m = M.pass_cells[k];
+        SlopeCell c{};
+        c.foff = M.foff[m];
+        c.nv = M.dnv[m];
+        bool reg = true;
+        for (int d = 0; d < D && reg; ++d) {
+            const SlopeOp& op = M.slope_ops[M.cell_slope_op[k] + d];
+            reg = op.kind == SLOPE_TWO && op.cntA == 1 && op.cntB == 1 && !op.projA && !op.projB;
+            if (!reg) break;
+            const NbrRef a = M.slope_nbr[op.listA], b = M.slope_nbr[op.listB];
+            reg = a.pair < 0 && b.pair < 0 && M.dnv[a.data] == c.nv && M.dnv[b.data] == c.nv;
+            c.nfoff[2 * d] = M.foff[a.data];
+            c.nfoff[2 * d + 1] = M.foff[b.data];
+            c.inv_d[2 * d] = op.inv_dsA;
+            c.inv_d[2 * d + 1] = op.inv_dsB;
+            c.inv_f[2 * d] = (float)op.inv_dsA;
+            c.inv_f[2 * d + 1] = (float)op.inv_dsB;
+        }
+        c.regular = reg ? 1 : 0;
+        M.screc[k] = c;
+    }
     if (M.p_j0.empty()) { M.p_j0.push_back(0); M.p_cnt.push_back(0); }
 }
 

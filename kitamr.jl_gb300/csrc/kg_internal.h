@@ -29,6 +29,18 @@ struct SlopeOp {            // 48 bytes
     int32_t cell;
 };
 
+// A pass-cell entry of the slope sweep in one record (built when the problems are merged).
+// Regular: every direction takes a two-sided slope from one neighbour per side, on the
+// cell's own velocity grid and without transverse projection; the kernel then needs
+// nothing else (the generic path reads the SlopeOps and their neighbour lists).
+struct SlopeCell {
+    int64_t foff;                 // f offset of the cell
+    int64_t nfoff[2 * MAXD];      // f offsets of the neighbours: per direction side A, side B
+    double inv_d[2 * MAXD];       // 1/ds of those sides
+    float inv_f[2 * MAXD];
+    int32_t nv, regular;
+};
+
 struct NbrRef {             // neighbour in a slope / extrapolation list
     int32_t data;           // data index (cell, or n_cells + wall)
     int32_t pair;           // velocity pairing id (my grid <- its grid), -1 = identity
@@ -132,6 +144,7 @@ struct Flat {
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
     std::vector<FluxCell> fcrec;          // merged layout only: per fluid cell
+    std::vector<SlopeCell> screc;         // merged layout only: per pass-cell entry
     std::vector<uint8_t> fluid_reg;       // per fluid cell: 1 when its faces are 2*dim full inner faces
                                           // to same-sized neighbours on the same velocity grid
     std::vector<int32_t> inc_off;         // n_fluid + 1

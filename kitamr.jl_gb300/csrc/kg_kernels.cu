@@ -137,6 +137,56 @@ template <int D, int NDF, typename T>
 __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
     using A = typename Arith<T>::type;
     const int pc = pc_base + blockIdx.x;
+    const SlopeCell& SC = P.screc[pc];
+    if (SC.regular) {
+        // regular cell (one record, no shared-memory setup): in every direction
+        // minmod((f - f_A)/ds_A, (f - f_B)/ds_B) -- slope_side with its loops and unit factors
+        // resolved.  Two velocity cells per thread and pass: all their loads are issued
+        // before any store, so each thread keeps twice the loads in flight.
+        const int nv = SC.nv;
+        const T* fcell = (const T*)P.f_in + SC.foff;
+        T* scell = (T*)P.sdf + SC.foff * D;
+        const T* fa[D];
+        const T* fb[D];
+        A ia[D], ib[D];
+#pragma unroll
+        for (int dir = 0; dir < D; ++dir) {
+            fa[dir] = (const T*)P.f_in + SC.nfoff[2 * dir];
+            fb[dir] = (const T*)P.f_in + SC.nfoff[2 * dir + 1];
+            if constexpr (sizeof(A) == 4) { ia[dir] = SC.inv_f[2 * dir]; ib[dir] = SC.inv_f[2 * dir + 1]; }
+            else { ia[dir] = SC.inv_d[2 * dir]; ib[dir] = SC.inv_d[2 * dir + 1]; }
+        }
+        for (int i0 = threadIdx.x; i0 < nv; i0 += 2 * BLOCK) {
+            const int i1 = i0 + BLOCK;
+            const bool two = i1 < nv;
+            const int j1 = two ? i1 : i0;    // a valid index for the second set of loads
+            A fc0[NDF], fc1[NDF], a0[D][NDF], a1[D][NDF], b0[D][NDF], b1[D][NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) { fc0[k] = (A)fcell[k * nv + i0]; fc1[k] = (A)fcell[k * nv + j1]; }
+#pragma unroll
+            for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    a0[dir][k] = (A)fa[dir][k * nv + i0];
+                    b0[dir][k] = (A)fb[dir][k * nv + i0];
+                    a1[dir][k] = (A)fa[dir][k * nv + j1];
+                    b1[dir][k] = (A)fb[dir][k * nv + j1];
+                }
+            }
+#pragma unroll
+            for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    scell[(dir * NDF + k) * nv + i0] =
+                        (T)minmod((fc0[k] - a0[dir][k]) * ia[dir], (fc0[k] - b0[dir][k]) * ib[dir]);
+                    if (two)
+                        scell[(dir * NDF + k) * nv + i1] =
+                            (T)minmod((fc1[k] - a1[dir][k]) * ia[dir], (fc1[k] - b1[dir][k]) * ib[dir]);
+                }
+            }
+        }
+        return;
+    }
     const int cell = P.pass_cells[pc];
     const int op0 = P.cell_slope_op[pc];
     const VGridView g = grid_view(P, cell);
@@ -203,64 +253,6 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
         snb[e] = c;
     }
     __syncthreads();
-    // regular cell: in every direction a two-sided slope from one neighbour per side, on
-    // this cell's velocity grid and without transverse projection -- slope_side below with
-    // its loops and branches resolved
-    bool reg = true;
-#pragma unroll
-    for (int dir = 0; dir < D; ++dir) {
-        const SlopeOp& op = ops[dir];
-        reg = reg && op.kind == SLOPE_TWO && op.cntA == 1 && op.cntB == 1;
-        if (reg) {
-            const SlopeNbrA<A, T>& a = snb[sbase[2 * dir]];
-            const SlopeNbrA<A, T>& b = snb[sbase[2 * dir + 1]];
-            reg = a.pair < 0 && b.pair < 0 && !a.any && !b.any && a.nvn == nv && b.nvn == nv;
-        }
-    }
-    if (reg) {
-        // two velocity cells per thread and pass: all their loads are issued before any
-        // store, so each thread keeps twice the loads in flight (the kernel waits on memory)
-        const T* fa[D];
-        const T* fb[D];
-        A ia[D], ib[D];
-#pragma unroll
-        for (int dir = 0; dir < D; ++dir) {
-            fa[dir] = snb[sbase[2 * dir]].fn;
-            fb[dir] = snb[sbase[2 * dir + 1]].fn;
-            ia[dir] = sconst[4 * dir];
-            ib[dir] = sconst[4 * dir + 1];
-        }
-        for (int i0 = threadIdx.x; i0 < nv; i0 += 2 * BLOCK) {
-            const int i1 = i0 + BLOCK;
-            const bool two = i1 < nv;
-            const int j1 = two ? i1 : i0;    // a valid index for the second set of loads
-            A fc0[NDF], fc1[NDF], a0[D][NDF], a1[D][NDF], b0[D][NDF], b1[D][NDF];
-#pragma unroll
-            for (int k = 0; k < NDF; ++k) { fc0[k] = (A)fcell[k * nv + i0]; fc1[k] = (A)fcell[k * nv + j1]; }
-#pragma unroll
-            for (int dir = 0; dir < D; ++dir) {
-#pragma unroll
-                for (int k = 0; k < NDF; ++k) {
-                    a0[dir][k] = (A)fa[dir][k * nv + i0];
-                    b0[dir][k] = (A)fb[dir][k * nv + i0];
-                    a1[dir][k] = (A)fa[dir][k * nv + j1];
-                    b1[dir][k] = (A)fb[dir][k * nv + j1];
-                }
-            }
-#pragma unroll
-            for (int dir = 0; dir < D; ++dir) {
-#pragma unroll
-                for (int k = 0; k < NDF; ++k) {
-                    scell[(dir * NDF + k) * nv + i0] =
-                        (T)minmod((fc0[k] - a0[dir][k]) * ia[dir], (fc0[k] - b0[dir][k]) * ib[dir]);
-                    if (two)
-                        scell[(dir * NDF + k) * nv + i1] =
-                            (T)minmod((fc1[k] - a1[dir][k]) * ia[dir], (fc1[k] - b1[dir][k]) * ib[dir]);
-                }
-            }
-        }
-        return;
-    }
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
