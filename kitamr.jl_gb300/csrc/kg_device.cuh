@@ -125,8 +125,8 @@ __device__ __forceinline__ void block_sum(double (&v)[N], double* sred) {
 
 // Block sum of FP32 compensated partials (value = hi + lo per thread), all in float-float
 // arithmetic: a TwoSum butterfly within each warp, then warp 0 combines the warp partials the
-// same way, eight lanes per element, and one lane per element converts the total to FP64
-// (three FP64 instructions per group of four elements instead of three per element and warp).
+// same way, one lane per warp and element, and one lane per element converts the total to FP64
+// (three FP64 instructions per round of elements instead of three per element and warp).
 // Fixed combination order: deterministic run to run, and every thread sees the same bits.
 __device__ __forceinline__ void two_sum_acc(float& h, float& l, float h2, float l2) {
     const float sum = h + h2;
@@ -139,7 +139,8 @@ template <int N>
 __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], double (&out)[N], double* sred) {
     // sred: shared scratch of at least N * (BLOCK/32) doubles
     constexpr int NWARP = BLOCK / 32;
-    static_assert(NWARP == 8, "the warp-0 stage maps eight lanes per element");
+    static_assert(NWARP == 4 || NWARP == 8, "the warp-0 stage maps NWARP lanes per element");
+    constexpr int GROUPS = 32 / NWARP;            // elements per round of warp 0
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int e = 0; e < N; ++e) {
@@ -158,12 +159,12 @@ __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], dou
     }
     __syncthreads();
     if (wid == 0) {
-        const int grp = lane >> 3, w = lane & 7;
-        constexpr int ROUNDS = (N + 3) / 4;
+        const int grp = lane / NWARP, w = lane % NWARP;
+        constexpr int ROUNDS = (N + GROUPS - 1) / GROUPS;
         float2 v[ROUNDS];
 #pragma unroll
         for (int r = 0; r < ROUNDS; ++r) {
-            const int e = r * 4 + grp;
+            const int e = r * GROUPS + grp;
             v[r] = e < N ? sf[e * NWARP + w] : make_float2(0.f, 0.f);
         }
         __syncwarp();
@@ -171,9 +172,9 @@ __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], dou
         for (int r = 0; r < ROUNDS; ++r) {
             float h = v[r].x, l = v[r].y;
 #pragma unroll
-            for (int o = 4; o > 0; o >>= 1)
+            for (int o = NWARP / 2; o > 0; o >>= 1)
                 two_sum_acc(h, l, __shfl_xor_sync(0xffffffffu, h, o), __shfl_xor_sync(0xffffffffu, l, o));
-            const int e = r * 4 + grp;
+            const int e = r * GROUPS + grp;
             if (w == 0 && e < N) sred[e] = (double)h + (double)l;
         }
     }

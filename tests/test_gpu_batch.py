@@ -111,3 +111,21 @@ def test_large_pool_admission_keeps_state(prec):
     ref, _ = _alone(p, t, s, prec, 2)
     assert np.array_equal(b.download(slot)["f"], ref["f"])
     b.close()
+
+
+def test_batch_sw_equals_single_handle():
+    """kg_batch_download_sw of a problem in a batch is bitwise kg_download_sw of it alone."""
+    probs = _problems()[:2]
+    built = [cases.build(p) for p in probs]
+    prec = abi.KG_PREC_MIXED
+    b = GpuBatch(abi.make_params(probs[0], precision=prec), 512 << 20)
+    slots = [b.admit(abi.make_params(p, precision=prec, st_check_interval=2), t, s["f"], s["w"], s["prim"], p.dt())
+             for p, (t, s) in zip(probs, built)]
+    b.step(3)
+    for k, (p, (t, s)) in enumerate(zip(probs, built)):
+        g = GpuStep(abi.make_params(p, precision=prec, st_check_interval=2), t)
+        g.upload_state(s["f"], s["w"], s["prim"])
+        g.step(p.dt(), 0, 3)
+        assert np.array_equal(b.download_sw(slots[k]), g.download_sw())
+        g.close()
+    b.close()

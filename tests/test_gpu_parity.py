@@ -99,3 +99,29 @@ def test_macro_slopes_match_oracle(name, make, nsteps, prec):
             tol, scale = 1e-5, mag / ds_min
         err = float(np.max(np.abs(g - r))) / scale
         assert err <= tol, (name, j, err)
+
+
+@pytest.mark.parametrize("name,make,nsteps", [CASES_FP64[1], CASES_FP64[3]], ids=["cavity_levels", "cylinder_ib_adapted"])
+def test_downloaded_slopes_match_oracle(name, make, nsteps):
+    """sdf after the last step (kg_download_state's sdf): the slopes that step's flux used,
+    FP64 within 1e-12 of the largest slope."""
+    import oracle as O
+    from kitgpu.solver import GpuStep
+    p = make()
+    topo, state = cases.build(p)
+    prm = abi.make_params(p, st_check_interval=1)
+    ref = O.OracleState(topo, state).run(prm, p.dt(), 0, nsteps, nthreads=4)
+    g = GpuStep(prm, topo)
+    g.upload_state(state["f"], state["w"], state["prim"])
+    g.step(p.dt(), 0, nsteps)
+    out = g.download_state(sdf=True)
+    g.close()
+    be = np.asarray(topo["cell_bound_enc"])
+    from kitgpu import mesh
+    off = mesh.f_offsets(topo)
+    dim = topo["dim"]
+    mask = np.zeros(ref.sdf.size, bool)
+    for c in np.nonzero(be >= 0)[0]:
+        mask[off[c] * dim:off[c + 1] * dim] = True
+    scale = float(np.max(np.abs(ref.sdf[mask])))
+    assert float(np.max(np.abs(out["sdf"][mask] - ref.sdf[mask]))) <= 1e-12 * scale

@@ -74,3 +74,39 @@ def test_create_fails_loudly_without_device(lib):
     prm = abi.make_params(cases.couette(n=4, nv=8))
     rc = lib.kg_create(C.byref(prm), 0, C.byref(h))
     assert rc == 3  # KG_ERR_CUDA: no CPU fallback
+
+
+def test_create_rejects_bad_parameters_before_touching_a_device(lib):
+    prm = abi.make_params(cases.couette(n=4, nv=8))
+    h = C.c_void_p()
+    for field, value in (("dim", 4), ("precision", 7), ("flux", 9), ("st_check_interval", 0)):
+        bad = abi.KgParams.from_buffer_copy(prm)
+        setattr(bad, field, value)
+        assert lib.kg_create(C.byref(bad), 0, C.byref(h)) == 1, field   # KG_ERR_ARG
+        buf = C.create_string_buffer(256)
+        lib.kg_last_error(None, buf, 256)
+        assert buf.value, field
+
+
+@pytest.mark.parametrize("make", [lambda: cases.box3d(n=(4, 3, 3), nv=6, levels=1),
+                                  lambda: cases.sphere(scale=0.2, nv=6)], ids=["box3d", "sphere"])
+def test_flattens_3d_topologies(lib, make):
+    p = make()
+    topo, _ = cases.build(p)
+    for prec in (abi.KG_PREC_FP64, abi.KG_PREC_MIXED):
+        assert S.topology_footprint(abi.make_params(p, precision=prec), topo) > 0
+
+
+def test_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference: the reference's CPU path (the oracle port) on the bench's
+    workload, one JSON line with the keys the driver reads."""
+    import json
+    import subprocess
+    import sys
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "3"], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["metric"] == "phase-cell updates/s" and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
