@@ -5,11 +5,16 @@ Workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x6
 synthetic initial state; 61 M phase cells, so f is far larger than L2 between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+  python bench.py --mode sphere | batched | serve   (the other workloads, one line each)
 
 Metric: phase-cell updates/s of the mixed-precision form (FP32 f, compensated moments,
 FP64 conserved update), with the plain FP64 form, the roofline of the dominant kernel, the
 oracle CPU baseline and the end-to-end rate through the C-ABI with host buffers beside it.
 N > 1: independent replicas, one per GPU (the path has no exchange on one device).
+Other modes:
+* sphere: the 3D Ma 3 sphere at half its base mesh (183 M phase cells).
+* batched: 256 Sod / cavity problems in one batch handle.
+* serve: Poisson arrivals solved to residual < 1e-6.
 """
 from __future__ import annotations
 
