@@ -190,9 +190,11 @@ int upload_vec(kg_handle* h, const std::vector<V>& v, const V** out) {
 }
 int pool_alloc(kg_handle* h, size_t n, void** out) {
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, std::max<size_t>(n, 8));
+    // 256 bytes past the end: the kernels' L2 prefetches round a block's end up to 16 bytes
+    const size_t bytes = n + 256;
+    cudaError_t e = cudaMalloc(&p, bytes);
     if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    e = cudaMemsetAsync(p, 0, std::max<size_t>(n, 8), h->stream);
+    e = cudaMemsetAsync(p, 0, bytes, h->stream);
     if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemsetAsync");
     h->pool_allocs.push_back(p);
     h->pool_bytes += (int64_t)n;
@@ -313,7 +315,7 @@ int rebuild(kg_handle* h) {
         // dynamic shared memory of the flux and wall kernels plus a reserve for their static arrays
         const size_t sa = storage_size(h);
         const size_t sflux = ((size_t)M.ndf * M.max_nv + (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis) * sa + 16384;
-        const size_t swall = ((size_t)M.ndf * M.max_nv + (size_t)M.dim * M.max_axis) * sa + M.max_nv + 4096;
+        const size_t swall = (size_t)M.dim * M.max_axis * sa + M.max_nv + 4096;
         const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
     }

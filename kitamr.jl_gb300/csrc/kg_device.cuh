@@ -202,6 +202,17 @@ __device__ __forceinline__ float exp_gauss_ff(float xh, float xl, float Uh, floa
     return expf(-q) * (1.f - qe);
 }
 
+// Asks the bulk-copy engine to bring a global byte range into L2 (cp.async.bulk.prefetch,
+// sm_90+; a hint, nothing is written).  The start is rounded down and the end up to 16 bytes;
+// the pools carry 256 bytes past their end, so the rounded range stays inside the allocation.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+    const size_t g = __cvta_generic_to_global(p);
+    const size_t a = g & ~(size_t)15;
+    const size_t n = (g + bytes - a + 15) & ~(size_t)15;
+    if (n == 0 || n > 0xFFFFFFF0u) return;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" :: "l"(a), "r"((unsigned)n) : "memory");
+}
+
 __device__ __forceinline__ double sgn(double x) { return x > 0.0 ? 1.0 : (x < 0.0 ? -1.0 : 0.0); }
 __device__ __forceinline__ double minmod(double a, double b) {
     return 0.5 * (sgn(a) + sgn(b)) * fmin(fabs(a), fabs(b));

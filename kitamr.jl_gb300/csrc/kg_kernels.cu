@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
         const int nv = SC.nv;
         const T* fcell = (const T*)P.f_in + SC.foff;
         T* scell = (T*)P.sdf + SC.foff * D;
+        if (threadIdx.x == 0) prefetch_l2(fcell, sizeof(T) * (size_t)NDF * nv);
         const T* fa[D];
         const T* fb[D];
         A ia[D], ib[D];
@@ -477,10 +478,12 @@ __device__ __forceinline__ double maxwell_h(const VGridView& g, int i, const dou
     return prim[0] * pre * exp(-lam * c2);
 }
 
-// shared memory of wall_kernel for a donor grid of nv velocity cells
+// shared memory of wall_kernel for a donor grid of nv velocity cells: the wall Maxwellian's
+// factor tables and the direction flag per velocity (the image extrapolation waits in the
+// wall record's output f block, so a 24^3 grid still leaves room for 4 CTAs per SM)
 template <int D, int NDF, typename A>
 __host__ __device__ __forceinline__ size_t wall_smem(int nv, int max_axis) {
-    return ((size_t)NDF * nv + (size_t)D * max_axis) * sizeof(A) + (size_t)nv;
+    return (size_t)D * max_axis * sizeof(A) + (size_t)nv;
 }
 
 // update_solid_neighbor! (Immersed_boundary.jl:367-483): the SolidNeighbor's f is the
@@ -502,9 +505,12 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
     const int nv = g.nv, nvs = gs.nv;
     const int gid = P.dgrid[op.donor];
     const int MA = P.max_axis;
-    A* aux = (A*)wsh;                                // NDF * nv: image extrapolation
-    A* Ew = aux + (size_t)NDF * nv;                  // D * max_axis: 1D factors of the wall Maxwellian
+    A* Ew = (A*)wsh;                                 // D * max_axis: 1D factors of the wall Maxwellian
     unsigned char* out_dir = (unsigned char*)(Ew + (size_t)D * MA);   // nv: u.n >= 0
+    // the record's two f blocks: wa ends with the new f; wb holds the image extrapolation
+    // (aux) until the last pass copies wa over it
+    T* wa = (T*)P.f_in + P.foff[op.data];
+    T* wb = (T*)P.f_out + P.foff[op.data];
     ib_setup<D, A>(P, op.list, op.cnt, snb);
     const double lam = op.bc[D + 1];
     const double Kw = P.probs[P.dprob[op.donor]].K;
@@ -581,7 +587,7 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
             ss = (r < (A)1 ? r : (A)1) * ss;
             wsdf[((int64_t)dir * NDF + k) * nv + i] = (T)ss;
             const A a = ib[k] + ss * dxL;
-            aux[(int64_t)k * nv + i] = a;
+            wb[(int64_t)k * nv + i] = (T)a;
             if (k == 0) a0 = a;
         }
         const A mh = mh_of(i);
@@ -596,14 +602,12 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
 #pragma unroll
         for (int d = 0; d < D; ++d) vn += VU[(int64_t)d * P.PG + g.goff + idx] * wc[W_N + d];
         red[0].add((A)P.cut_sw[op.cut_off + a] * vn * mh_of(idx));
-        red[1].add((A)P.cut_gw[op.cut_off + a] * vn * aux[idx]);
+        red[1].add((A)P.cut_gw[op.cut_off + a] * vn * (A)wb[idx]);
     }
     double rs[2];
     block_sum_ks<2>(red, rs, sred);
     const double rho_w = -rs[1] / rs[0];
     const A rw = (A)rho_w, bk = wc[W_BK];
-    T* wa = (T*)P.f_in + wo;
-    T* wb = (T*)P.f_out + wo;
     for (int i = threadIdx.x; i < nv; i += BLOCK) {
         A v[NDF];
         if (out_dir[i]) {
@@ -612,10 +616,10 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
             if (NDF == 2) v[NDF - 1] = mh * bk * rw;
         } else {
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) v[k] = aux[(int64_t)k * nv + i];
+            for (int k = 0; k < NDF; ++k) v[k] = (A)wb[(int64_t)k * nv + i];
         }
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) { wa[(int64_t)k * nv + i] = (T)v[k]; wb[(int64_t)k * nv + i] = (T)v[k]; }
+        for (int k = 0; k < NDF; ++k) wa[(int64_t)k * nv + i] = (T)v[k];
     }
     __syncthreads();
     for (int a = threadIdx.x; a < op.cut_cnt; a += BLOCK) {
@@ -626,12 +630,12 @@ __global__ void __launch_bounds__(BLOCK) wall_kernel(Dev P) {
         mv[0] = mh * rw;
         if (NDF == 2) mv[NDF - 1] = mh * bk * rw;
 #pragma unroll
-        for (int k = 0; k < NDF; ++k) {
-            const T v = (T)((gw * aux[(int64_t)k * nv + idx] + sw * mv[k]) / (gw + sw));
-            wa[(int64_t)k * nv + idx] = v;
-            wb[(int64_t)k * nv + idx] = v;
-        }
+        for (int k = 0; k < NDF; ++k)
+            wa[(int64_t)k * nv + idx] = (T)((gw * (A)wb[(int64_t)k * nv + idx] + sw * mv[k]) / (gw + sw));
     }
+    __syncthreads();
+    // both buffers carry the record's f (the next step reads the other one)
+    for (int64_t e = threadIdx.x; e < (int64_t)NDF * nv; e += BLOCK) wb[e] = wa[e];
 }
 
 // =============================================================================
@@ -814,6 +818,11 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     __shared__ A sc[C_N];
     // one record of the cell, then its incidences: two dependent loads before the barrier
     const FluxCell FC = P.fcrec[fcx];
+    if (threadIdx.x == 32) {
+        // the cell's own f and sdf blocks into L2 while the block sets up (warp 0 is busy)
+        prefetch_l2((const T*)P.f_in + FC.foff, sizeof(T) * (size_t)NDF * FC.nv);
+        prefetch_l2((const T*)P.sdf + FC.foff * D, sizeof(T) * (size_t)D * NDF * FC.nv);
+    }
     const int cell = FC.cell;
     const int slot = FC.slot;
     const ProbParams& PP = P.probs[slot];
