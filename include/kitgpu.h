@@ -189,6 +189,18 @@ int kg_download_state(kg_handle *h, double *f, double *w, double *prim, double *
  * PsData.sw memory); solid cells (bound_enc < 0) get zeros.                    */
 int kg_download_sw(kg_handle *h, double *sw);
 
+/* Physical-space refinement sensor of the adaptation step: PsData.lohner as
+ * update_criterion! leaves it (Physical_space/AMR.jl:256-284; update_Lohner_inner_ps!,
+ * Physical_space/Criteria.jl:95-158), including apply_amr_buffer!'s one-cell buffer layer
+ * (AMR.jl:286-330) with threshold adapt_coeffi_ps (solver.ADAPT_COEFFI_PS).  Computed on
+ * demand from the device state (w, prim and the sw of the last step's slopes) in FP64; the
+ * host applies ps_refine_flag / ps_coarsen_flag (user-defined functions) to it, so only
+ * (dim+2) x dim doubles per cell cross the link at an adaptation instead of f.
+ * lohner: n_cells blocks of (dim+2) x dim doubles, column-major (PsData.lohner memory);
+ * solid cells get zeros.  A direction whose two sides are both coarser uses 1.5 ds on
+ * both sides (the reference has no applicable method for that case).          */
+int kg_criterion(kg_handle *h, double adapt_coeffi_ps, double *lohner);
+
 /* Advance `nsteps` steps with time step dt; `step` is status.step before the
  * first of them (drives the residual cadence).  One call = nsteps x
  * (slope -> flux -> iterate).                                               */
@@ -207,9 +219,9 @@ int kg_topology_footprint(const kg_params *params, const kg_topology *topo, int6
 /* Last error message of the handle (or of the last failed kg_create if h is NULL). */
 int kg_last_error(const kg_handle *h, char *buf, size_t cap);
 
-/* Capture the kg_step sequence of `nsteps` steps as a CUDA graph (step
- * counter handling stays on the host); kg_step then replays it when called
- * with the same nsteps and dt.                                               */
+/* Capture the kg_step sequence of `nsteps` steps as a CUDA graph; kg_step then
+ * replays it when called again with the same nsteps on the same layout (dt and
+ * the step counter live on the device, so a replay uses their current values). */
 int kg_use_graph(kg_handle *h, int enable);
 
 /* Autotuner of the flux+collision schedule (one CTA per cell, or a persistent grid of
@@ -237,6 +249,7 @@ int kg_batch_release(kg_handle *h, int32_t slot);
 int kg_batch_step(kg_handle *h, int32_t nsteps, kg_step_report *reports, int32_t cap);
 int kg_batch_download(kg_handle *h, int32_t slot, double *f, double *w, double *prim, double *qf);
 int kg_batch_download_sw(kg_handle *h, int32_t slot, double *sw);   /* kg_download_sw of one problem */
+int kg_batch_criterion(kg_handle *h, int32_t slot, double adapt_coeffi_ps, double *lohner);   /* kg_criterion of one problem */
 int kg_batch_info(const kg_handle *h, int32_t *n_live, int64_t *f_free_elems, int64_t *bytes_per_elem);
 int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
 

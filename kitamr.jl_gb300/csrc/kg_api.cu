@@ -17,7 +17,8 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
-    static cudaError_t macro_slope(const Dev&, int, int, double*, cudaStream_t);
+    static cudaError_t macro_slope(const Dev&, int, int, int, double*, cudaStream_t);
+    static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
 };
 cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
@@ -329,7 +330,7 @@ int rebuild(kg_handle* h) {
     UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
     UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
     UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-    UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+    UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
     UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
     UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
@@ -694,31 +695,38 @@ int download_problem(kg_handle* h, int slot, double* f, double* w, double* prim,
     return KG_OK;
 }
 
-// sw of the problem in `slot` (update_macro_slope!) from the slopes on the device, scattered
-// into n_cells blocks of (dim+2) x dim doubles; cells without a fluid-list entry get zeros.
-int download_sw(kg_handle* h, int slot, double* sw) {
+// sw of the problem in `slot` (update_macro_slope!) from the slopes on the device, into a
+// device array of (dim+2) x dim doubles per data item of the problem (zero rows for items
+// without a fluid-list entry); optionally followed by the physical-space criterion with the
+// buffer layer (update_criterion! + apply_amr_buffer!) into a second such array.  The host
+// receives the rows of the problem's cells.
+int sync_point_rows(kg_handle* h, int slot, double* sw_host, double thr, double* loh_host) {
     int rc = rebuild(h);
     if (rc) return rc;
     Problem& pb = h->probs[slot];
     const int D = h->prm.dim, N = D * (D + 2);
     const int fb = pb.pp.fluid_begin, n = pb.pp.fluid_end - pb.pp.fluid_begin;
-    std::vector<double> host((size_t)std::max(n, 1) * N);
-    if (n > 0) {
-        double* d = nullptr;
-        cudaError_t e = cudaMalloc(&d, sizeof(double) * (size_t)n * N);
-        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc sw");
-        const Dev P = h->dev;
-        e = dispatch(h, [&](auto L) { return decltype(L)::macro_slope(P, fb, n, d, h->stream); });
-        if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), d, sizeof(double) * (size_t)n * N, cudaMemcpyDeviceToHost, h->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-        cudaFree(d);
-        if (e != cudaSuccess) return cuda_fail(h, e, "macro_slope_kernel");
-    }
-    std::fill(sw, sw + (size_t)pb.F.n_cells * N, 0.0);
-    for (int q = 0; q < n; ++q) {
-        const int64_t cell = h->M.fluid_cells[fb + q] - pb.dbase;
-        std::copy(host.begin() + (size_t)q * N, host.begin() + (size_t)(q + 1) * N, sw + cell * N);
-    }
+    const int64_t nd = pb.dsize, nc = pb.F.n_cells;
+    const size_t bytes = sizeof(double) * (size_t)std::max<int64_t>(nd, 1) * N;
+    double* d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 3 * bytes);
+    if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc sync-point rows");
+    double* dsw = d;
+    double* dloh = d + bytes / sizeof(double);
+    double* dout = dloh + bytes / sizeof(double);
+    const Dev P = h->dev;
+    e = cudaMemsetAsync(d, 0, 3 * bytes, h->stream);
+    if (e == cudaSuccess)
+        e = dispatch(h, [&](auto L) { return decltype(L)::macro_slope(P, fb, n, (int)pb.dbase, dsw, h->stream); });
+    if (e == cudaSuccess && loh_host)
+        e = dispatch(h, [&](auto L) { return decltype(L)::criterion(P, fb, n, (int)pb.dbase, dsw, thr, dloh, dout, h->stream); });
+    if (e == cudaSuccess && sw_host)
+        e = cudaMemcpyAsync(sw_host, dsw, sizeof(double) * (size_t)nc * N, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && loh_host)
+        e = cudaMemcpyAsync(loh_host, dout, sizeof(double) * (size_t)nc * N, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return cuda_fail(h, e, "sync-point rows");
     return KG_OK;
 }
 
@@ -839,7 +847,16 @@ int kg_download_sw(kg_handle* h, double* sw) {
     if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_download_sw");
     if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
     cudaSetDevice(h->device);
-    return download_sw(h, 0, sw);
+    return sync_point_rows(h, 0, sw, 0.0, nullptr);
+}
+
+int kg_criterion(kg_handle* h, double adapt_coeffi_ps, double* lohner) {
+    if (!h) return KG_ERR_ARG;
+    if (!lohner) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_criterion");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return sync_point_rows(h, 0, nullptr, adapt_coeffi_ps, lohner);
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
@@ -1000,7 +1017,13 @@ int kg_batch_download(kg_handle* h, int32_t slot, double* f, double* w, double* 
 int kg_batch_download_sw(kg_handle* h, int32_t slot, double* sw) {
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !sw) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
-    return download_sw(h, slot, sw);
+    return sync_point_rows(h, slot, sw, 0.0, nullptr);
+}
+
+int kg_batch_criterion(kg_handle* h, int32_t slot, double adapt_coeffi_ps, double* lohner) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !lohner) return fail(h, KG_ERR_ARG, "bad slot");
+    cudaSetDevice(h->device);
+    return sync_point_rows(h, slot, nullptr, adapt_coeffi_ps, lohner);
 }
 
 int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {

@@ -55,6 +55,8 @@ struct Dev {
     const uint8_t* fluid_reg;          // per fluid cell: regular (fast path of the flux kernel)
     const FluxCell* fcrec;             // per fluid cell: its record
     const SlopeCell* screc;            // per pass-cell entry: its record
+    const CritOp* crit_ops;            // per fluid cell and direction (physical-space criterion)
+    const int32_t* crit_nbr;
     const int32_t* inc_off;
     const Incidence* inc;
     const double* bc_prim;
@@ -230,12 +232,6 @@ __device__ __forceinline__ void get_prim(const double* w, double gamma, double* 
 #pragma unroll
     for (int d = 0; d < D; ++d) { prim[1 + d] = w[1 + d] / w[0]; m2 += w[1 + d] * w[1 + d]; }
     prim[D + 1] = 0.5 * w[0] / (gamma - 1.0) / (w[D + 1] - 0.5 * m2 / w[0]);
-}
-
-// scale factor 2^(D*(lj-li)) of the merge walk when the source is finer, else 1
-template <int D>
-__device__ __forceinline__ double merge_inv_scale(int li, int lj) {
-    return lj > li ? ldexp(1.0, -D * (lj - li)) : 1.0;
 }
 
 }  // namespace kg

@@ -319,6 +319,35 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         F.pass_cells_off.push_back((int32_t)F.pass_cells.size());
     }
 
+    // ---- physical-space criterion (update_criterion!, Physical_space/AMR.jl:1-284) --------
+    for (int i = 0; i < NC; ++i) {
+        if (t.cell_bound_enc[i] < 0) continue;
+        for (int dir = 0; dir < D; ++dir) {
+            CritOp op{};
+            const int sA = st(i, 2 * dir), sB = st(i, 2 * dir + 1);
+            const double ds = t.cell_ds[(size_t)i * D + dir];
+            auto factor = [&](int s) { return s == 1 ? 1.0 : (s == -1 ? 1.5 : 0.75); };
+            auto add = [&](int k, int32_t* lst0, int32_t* n) {
+                *lst0 = (int32_t)F.crit_nbr.size();
+                *n = cnt(i, k);
+                for (int j = 0; j < *n; ++j) {
+                    const int32_t r = lst(i, k)[j];
+                    F.crit_nbr.push_back(r >= 0 ? r : -1);   // -1: a SolidNeighbor (w = sw = 0)
+                }
+            };
+            // the lists of every non-boundary side (the buffer layer of apply_amr_buffer! reads
+            // them even when the other side is a boundary)
+            if (sA != 0) add(2 * dir, &op.listA, &op.cntA);
+            if (sB != 0) add(2 * dir + 1, &op.listB, &op.cntB);
+            op.dsA = factor(sA) * ds;
+            op.dsB = factor(sB) * ds;
+            op.coarseA = sA == -1;
+            op.coarseB = sB == -1;
+            op.kind = (sA != 0 && sB != 0) ? 1 : 0;
+            F.crit_ops.push_back(op);
+        }
+    }
+
     // ---- flux incidences (flux!, Flux/Flux.jl:19-111,458-503) -----------------------------
     std::vector<std::vector<Incidence>> per(NC);
     for (int fi = 0; fi < t.n_faces; ++fi) {
@@ -601,6 +630,11 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             fc.ninc = F.inc_off[k + 1] - F.inc_off[k];
             fc.nv = M.dnv[m]; fc.gid = M.dgrid[m]; fc.reg = F.fluid_reg[k];
             M.fcrec.push_back(fc);
+        }
+        {
+            const int32_t cacc = (int32_t)M.crit_nbr.size();
+            for (CritOp op : F.crit_ops) { op.listA += cacc; op.listB += cacc; M.crit_ops.push_back(op); }
+            for (int32_t r : F.crit_nbr) M.crit_nbr.push_back(r >= 0 ? r + p.dbase : -1);
         }
         M.bc_prim.insert(M.bc_prim.end(), F.bc_prim.begin(), F.bc_prim.end());
         M.bc_hl.insert(M.bc_hl.end(), F.bc_hl.begin(), F.bc_hl.end());

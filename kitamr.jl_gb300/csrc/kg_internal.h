@@ -29,6 +29,18 @@ struct SlopeOp {            // 48 bytes
     int32_t cell;
 };
 
+// update_criterion! of one fluid cell and direction (Physical_space/AMR.jl:1-253): the
+// neighbour lists of both sides (-1: a SolidNeighbor, whose w and sw are zeros), their
+// distances (ds, 0.75 ds for finer, 1.5 ds for a coarser side) and whether a side is coarser
+// (transverse correction from its first neighbour).  kind 0: a domain-boundary side, the
+// row is zero.
+struct CritOp {
+    double dsA, dsB;
+    int32_t listA, cntA, listB, cntB;   // into crit_nbr (data indices)
+    int8_t kind, coarseA, coarseB, pad;
+    int32_t pad2;
+};
+
 // A pass-cell entry of the slope sweep in one record (built when the problems are merged).
 // Regular: every direction takes a two-sided slope from one neighbour per side, on the
 // cell's own velocity grid and without transverse projection; the kernel then needs
@@ -145,6 +157,8 @@ struct Flat {
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
     std::vector<FluxCell> fcrec;          // merged layout only: per fluid cell
     std::vector<SlopeCell> screc;         // merged layout only: per pass-cell entry
+    std::vector<CritOp> crit_ops;         // per fluid cell and direction (fluid-list order)
+    std::vector<int32_t> crit_nbr;        // their neighbour lists (data indices)
     std::vector<uint8_t> fluid_reg;       // per fluid cell: 1 when its faces are 2*dim full inner faces
                                           // to same-sized neighbours on the same velocity grid
     std::vector<int32_t> inc_off;         // n_fluid + 1

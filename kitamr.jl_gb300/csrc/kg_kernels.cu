@@ -405,17 +405,6 @@ __device__ __forceinline__ void extrapolate(const Dev& P, const VGridView& g, in
     }
 }
 
-template <int D, int NDF>
-__device__ __forceinline__ void moments_add(const VGridView& g, const double wgt, int i, const double* fv, double* m) {
-    // micro_to_macro_2D2F / 3D1F terms of one velocity cell
-    double u2 = 0.0;
-    m[0] += wgt * fv[0];
-#pragma unroll
-    for (int d = 0; d < D; ++d) { double u = g.u(i, d); m[1 + d] += wgt * u * fv[0]; u2 += u * u; }
-    if (NDF == 2) m[D + 1] += 0.5 * wgt * (u2 * fv[0] + fv[NDF - 1]);
-    else m[D + 1] += 0.5 * wgt * u2 * fv[0];
-}
-
 // moments of one velocity cell into compensated accumulators in the arithmetic precision
 template <int D, int NDF, typename A>
 __device__ __forceinline__ void moments_add_a(const A* u, const A wgt, const A* fv, KSum<A>* m) {
@@ -465,17 +454,6 @@ __global__ void __launch_bounds__(BLOCK) solid_kernel(Dev P) {
         for (int e = 0; e < D + 2; ++e) w[e] = mw[e];
         get_prim<D>(mw, P.probs[P.dprob[op.cell]].gamma, pr);
     }
-}
-
-template <int D>
-__device__ __forceinline__ double maxwell_h(const VGridView& g, int i, const double* prim) {
-    // h of discrete_maxwell_2D2F / M of discrete_maxwell_3D1F (FP64 exponent)
-    double c2 = 0.0;
-#pragma unroll
-    for (int d = 0; d < D; ++d) { double cu = g.u(i, d) - prim[1 + d]; c2 += cu * cu; }
-    const double lam = prim[D + 1];
-    const double pre = D == 2 ? lam / PI : pow(lam / PI, 1.5);
-    return prim[0] * pre * exp(-lam * c2);
 }
 
 // shared memory of wall_kernel for a donor grid of nv velocity cells: the wall Maxwellian's
@@ -1394,10 +1372,10 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_ke
 
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
 // weight) for the fluid-list cells [fbegin, fbegin + gridDim.x), one CTA each; out holds
-// dim x (dim+2) doubles per listed cell (the column-major memory of PsData.sw).  Not part of
-// a step: it reads the slopes the last step left, at a host sync point.
+// dim x (dim+2) doubles per data item from dbase on (the column-major memory of PsData.sw).
+// Not part of a step: it reads the slopes the last step left, at a host sync point.
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK) macro_slope_kernel(Dev P, int fbegin, double* out) {
+__global__ void __launch_bounds__(BLOCK) macro_slope_kernel(Dev P, int fbegin, int dbase, double* out) {
     using A = typename Arith<T>::type;
     constexpr int N = D * (D + 2);
     __shared__ double sred[N * (BLOCK / 32)];
@@ -1431,7 +1409,164 @@ __global__ void __launch_bounds__(BLOCK) macro_slope_kernel(Dev P, int fbegin, d
     block_sum_ks<N>(m, r, sred);
 #pragma unroll
     for (int e = 0; e < N; ++e)
-        if (threadIdx.x == e) out[(int64_t)blockIdx.x * N + e] = r[e];
+        if (threadIdx.x == e) out[(int64_t)(cell - dbase) * N + e] = r[e];
+}
+
+// ---- physical-space criterion (update_criterion!, Physical_space/AMR.jl:256-284) --------
+// Julia's max of floats propagates NaN (fmax does not)
+__device__ __forceinline__ double jl_max(double a, double b) { return (a != a || b != b) ? a + b : (a > b ? a : b); }
+
+// lohner_value (Physical_space/Criteria.jl:24-30)
+__device__ __forceinline__ double lohner_value(double l, double c, double r, double dsL, double dsR, double eps) {
+    const double scale = dsR * fabs(l) + (dsL + dsR) * fabs(c) + dsL * fabs(r);
+    if (scale < 1e-4 * (dsL < dsR ? dsL : dsR)) return 0.0;            // PS_LOHNER_ABS_FLOOR
+    const double denom = dsR * fabs(l - c) + dsL * fabs(r - c) + eps * scale;
+    if (denom <= 0.0) return 0.0;
+    return fabs(dsR * l - (dsL + dsR) * c + dsL * r) / denom;
+}
+// primitive_amplitude_ok (Criteria.jl:32-36)
+__device__ __forceinline__ bool primitive_amplitude_ok(double l, double c, double r) {
+    const double jump = jl_max(fabs(l - c), fabs(r - c));
+    const double scale = jl_max(fabs(c), 1e-4);
+    return jump >= 1e-3 * scale;                                        // PS_PRIMITIVE_REL_JUMP_FLOOR
+}
+// velocity_slope and vorticity (Criteria.jl:38-52): sw is [dir][component] (PsData.sw memory)
+template <int D>
+__device__ __forceinline__ double velocity_slope(const double* sw, const double* prim, int c, int dir) {
+    return (sw[dir * (D + 2) + c] - prim[c] * sw[dir * (D + 2)]) / prim[0];
+}
+template <int D>
+__device__ __forceinline__ double vorticity(const double* sw, const double* prim) {
+    if (D == 2) return velocity_slope<D>(sw, prim, 1, 1) - velocity_slope<D>(sw, prim, 2, 0);
+    const double c1 = velocity_slope<D>(sw, prim, 2, 2) - velocity_slope<D>(sw, prim, 3, 1);
+    const double c2 = velocity_slope<D>(sw, prim, 3, 0) - velocity_slope<D>(sw, prim, 1, 2);
+    const double c3 = velocity_slope<D>(sw, prim, 1, 1) - velocity_slope<D>(sw, prim, 2, 0);
+    return sqrt(c1 * c1 + c2 * c2 + c3 * c3);
+}
+// velocity_scale, vorticity_amplitude_ok (Criteria.jl:54-66)
+template <int D>
+__device__ __forceinline__ bool vorticity_amplitude_ok(double l, double c, double r, const double* prim, double h) {
+    double speed2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) speed2 += prim[1 + d] * prim[1 + d];
+    const double lambda = jl_max(fabs(prim[D + 1]), JL_EPS);
+    const double vscale = jl_max(sqrt(speed2), 1.0 / sqrt(lambda));
+    const double omega = jl_max(fabs(l), jl_max(fabs(c), fabs(r)));
+    return omega * h >= 2e-2 * vscale;                                  // PS_VORTICITY_JUMP_FLOOR
+}
+
+// update_Lohner_inner_ps! (Criteria.jl:95-158) of the fluid cells [fbegin, fbegin + n), one
+// thread each, in FP64; sw and loh are indexed by data index - dbase, (dim+2) x dim doubles
+// per item (the column-major memory of PsData.sw / PsData.lohner).
+template <int D>
+__global__ void criterion_kernel(Dev P, int fbegin, int n, int dbase, const double* sw, double* loh) {
+    constexpr int NW = D + 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int fcx = fbegin + q;
+    const int cell = P.fluid_cells[fcx];
+    const double* swc = sw + (int64_t)(cell - dbase) * NW * D;
+    double* lo = loh + (int64_t)(cell - dbase) * NW * D;
+    const double* pc = P.prim + (int64_t)cell * MAXW;
+    const double* mc = P.dmid + (int64_t)cell * MAXD;
+    const double gamma = P.probs[P.dprob[cell]].gamma;
+    const double omega_c = vorticity<D>(swc, pc);
+    for (int dir = 0; dir < D; ++dir) {
+        const CritOp op = P.crit_ops[(int64_t)fcx * D + dir];
+        double* row = lo + dir * NW;
+        if (op.kind == 0) {
+#pragma unroll
+            for (int j = 0; j < NW; ++j) row[j] = 0.0;
+            continue;
+        }
+        // each side: the mean of its neighbours' w and sw, a coarser side's w corrected along
+        // the transverse directions with its sw; then its primitives and vorticity
+        double pside[2][NW], omega[2];
+        for (int side = 0; side < 2; ++side) {
+            const int list = side == 0 ? op.listA : op.listB, nl = side == 0 ? op.cntA : op.cntB;
+            double ws[NW], sws[NW * D];
+#pragma unroll
+            for (int j = 0; j < NW; ++j) ws[j] = 0.0;
+            for (int e = 0; e < NW * D; ++e) sws[e] = 0.0;
+            for (int k = 0; k < nl; ++k) {
+                const int nb = P.crit_nbr[list + k];
+                // a SolidNeighbor keeps w = sw = 0 (Immersed_boundary.jl:300-302, 481-482): its
+                // side's density is 0 and its velocities and lambda NaN, so only the density
+                // row of that direction can be nonzero
+                if (nb < 0) continue;
+                const double* wn = P.w + (int64_t)nb * MAXW;
+                const double* swn = sw + (int64_t)(nb - dbase) * NW * D;
+#pragma unroll
+                for (int j = 0; j < NW; ++j) ws[j] += wn[j];
+                for (int e = 0; e < NW * D; ++e) sws[e] += swn[e];
+            }
+            if ((side == 0 ? op.coarseA : op.coarseB) && P.crit_nbr[list] >= 0) {
+                const int nb = P.crit_nbr[list];
+                const double* nm = P.dmid + (int64_t)nb * MAXD;
+                const double* swn = sw + (int64_t)(nb - dbase) * NW * D;
+                for (int t = 0; t < D; ++t) {
+                    if (t == dir) continue;                    // FAT: the transverse directions
+                    const double dx = mc[t] - nm[t];
+#pragma unroll
+                    for (int j = 0; j < NW; ++j) ws[j] += dx * swn[t * NW + j];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NW; ++j) ws[j] /= nl;
+            for (int e = 0; e < NW * D; ++e) sws[e] /= nl;
+            get_prim<D>(ws, gamma, pside[side]);
+            omega[side] = vorticity<D>(sws, pside[side]);
+        }
+        const double dsL = op.dsA, dsR = op.dsB;
+        const bool use_vort = vorticity_amplitude_ok<D>(omega[0], omega_c, omega[1], pc, dsL > dsR ? dsL : dsR);
+        const double eps_l = 0.2 * P.dds[(int64_t)cell * MAXD + dir];
+#pragma unroll
+        for (int j = 0; j < NW; ++j) {
+            if (j == 1)
+                row[j] = use_vort ? lohner_value(omega[0], omega_c, omega[1], dsL, dsR, eps_l) : 0.0;
+            else
+                row[j] = primitive_amplitude_ok(pside[0][j], pc[j], pside[1][j])
+                             ? lohner_value(pside[0][j], pc[j], pside[1][j], dsL, dsR, eps_l) : 0.0;
+        }
+    }
+}
+
+// ps_sensor (Criteria.jl:14-21): max over directions of the density and last rows
+template <int D>
+__device__ __forceinline__ double ps_sensor(const double* lo) {
+    double v = 0.0;
+    for (int dir = 0; dir < D; ++dir) v = jl_max(v, jl_max(lo[dir * (D + 2)], lo[dir * (D + 2) + D + 1]));
+    return v;
+}
+
+// apply_amr_buffer! (Physical_space/AMR.jl:286-330): a cell at or below the threshold whose
+// neighbour (any non-boundary side, fluid cells only) is above it gets lohner = 2 threshold;
+// decide on loh, write out.
+template <int D>
+__global__ void criterion_buffer_kernel(Dev P, int fbegin, int n, int dbase, double thr, const double* loh,
+                                        double* out) {
+    constexpr int NW = D + 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int fcx = fbegin + q;
+    const int cell = P.fluid_cells[fcx];
+    const double* lo = loh + (int64_t)(cell - dbase) * NW * D;
+    bool flagged = false;
+    if (!(ps_sensor<D>(lo) > thr)) {
+        for (int dir = 0; dir < D && !flagged; ++dir) {
+            const CritOp op = P.crit_ops[(int64_t)fcx * D + dir];
+            for (int side = 0; side < 2 && !flagged; ++side) {
+                const int list = side == 0 ? op.listA : op.listB, nl = side == 0 ? op.cntA : op.cntB;
+                for (int k = 0; k < nl; ++k) {
+                    const int nb = P.crit_nbr[list + k];
+                    if (nb < 0 || P.dbe[nb] < 0) continue;
+                    if (ps_sensor<D>(loh + (int64_t)(nb - dbase) * NW * D) > thr) { flagged = true; break; }
+                }
+            }
+        }
+    }
+    double* o = out + (int64_t)(cell - dbase) * NW * D;
+    for (int e = 0; e < NW * D; ++e) o[e] = flagged ? 2.0 * thr : lo[e];
 }
 
 // Per problem (one CTA each): Σ of the per-cell residual terms when the step is a check
@@ -1504,9 +1639,19 @@ struct Launch {
         flux_collide_kernel<D, NDF, T><<<grid, BLOCK, smem, s>>>(P, counter, order, n);
         return cudaGetLastError();
     }
-    static cudaError_t macro_slope(const Dev& P, int fbegin, int n, double* out, cudaStream_t s) {
+    static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        macro_slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, fbegin, out);
+        macro_slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, fbegin, dbase, out);
+        return cudaGetLastError();
+    }
+    // physical-space criterion of the fluid cells [fbegin, fbegin + n): loh from sw, then
+    // the buffer layer into out (both per data item from dbase on)
+    static cudaError_t criterion(const Dev& P, int fbegin, int n, int dbase, const double* sw, double thr,
+                                 double* loh, double* out, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        const int nb = (n + 127) / 128;
+        criterion_kernel<D><<<nb, 128, 0, s>>>(P, fbegin, n, dbase, sw, loh);
+        criterion_buffer_kernel<D><<<nb, 128, 0, s>>>(P, fbegin, n, dbase, thr, loh, out);
         return cudaGetLastError();
     }
     // resident CTAs per SM the flux kernel reaches (for the persistent grid size)

@@ -51,6 +51,8 @@ def load_library(path: Optional[str] = None):
     L.kg_autotune.argtypes = [vp, C.c_int]
     L.kg_download_sw.argtypes = [vp, vp]
     L.kg_batch_download_sw.argtypes = [vp, i32, vp]
+    L.kg_criterion.argtypes = [vp, dbl, vp]
+    L.kg_batch_criterion.argtypes = [vp, i32, dbl, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     _lib = L
     return L
@@ -62,7 +64,7 @@ EXPORTS = [
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
-    "kg_download_sw", "kg_batch_download_sw",
+    "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
 ]
 
 
@@ -150,6 +152,12 @@ class GpuStep:
         sw = np.empty(self.nc * self.dim * (self.dim + 2))
         _check(self.L, self.h, self.L.kg_download_sw(self.h, sw.ctypes.data))
         return sw.reshape(self.nc, self.dim, self.dim + 2)
+
+    def criterion(self, adapt_coeffi_ps: float) -> np.ndarray:
+        """PsData.lohner of every cell (update_criterion! + buffer layer), shape (n_cells, dim, dim + 2)."""
+        lo = np.empty(self.nc * self.dim * (self.dim + 2))
+        _check(self.L, self.h, self.L.kg_criterion(self.h, float(adapt_coeffi_ps), lo.ctypes.data))
+        return lo.reshape(self.nc, self.dim, self.dim + 2)
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
@@ -241,6 +249,13 @@ class GpuBatch:
         sw = np.empty(nc * dim * (dim + 2))
         _check(self.L, self.h, self.L.kg_batch_download_sw(self.h, slot, sw.ctypes.data))
         return sw.reshape(nc, dim, dim + 2)
+
+    def criterion(self, slot: int, adapt_coeffi_ps: float) -> np.ndarray:
+        topo, _ = self.meta[slot]
+        nc, dim = int(topo["n_cells"]), int(topo["dim"])
+        lo = np.empty(nc * dim * (dim + 2))
+        _check(self.L, self.h, self.L.kg_batch_criterion(self.h, slot, float(adapt_coeffi_ps), lo.ctypes.data))
+        return lo.reshape(nc, dim, dim + 2)
 
     def info(self):
         n, fr, bpe = C.c_int32(), C.c_int64(), C.c_int64()

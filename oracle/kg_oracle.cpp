@@ -1139,6 +1139,120 @@ int kgo_moments(const kg_params* prm, const kg_topology* t, const double* f, con
     return KG_OK;
 }
 
+// ---- physical-space criterion: update_criterion! (Physical_space/AMR.jl:1-284), the
+// Löhner sensor of update_Lohner_inner_ps! (Physical_space/Criteria.jl:24-158) and the
+// buffer layer of apply_amr_buffer! (AMR.jl:286-330), restated from the topology arrays.
+static double jl_max(double a, double b) { return (std::isnan(a) || std::isnan(b)) ? NAN : (a > b ? a : b); }
+static double o_lohner_value(double l, double c, double r, double dsL, double dsR, double eps) {
+    const double scale = dsR * std::fabs(l) + (dsL + dsR) * std::fabs(c) + dsL * std::fabs(r);
+    if (scale < 1e-4 * std::min(dsL, dsR)) return 0.0;
+    const double denom = dsR * std::fabs(l - c) + dsL * std::fabs(r - c) + eps * scale;
+    if (denom <= 0.0) return 0.0;
+    return std::fabs(dsR * l - (dsL + dsR) * c + dsL * r) / denom;
+}
+static bool o_primitive_ok(double l, double c, double r) {
+    const double jump = jl_max(std::fabs(l - c), std::fabs(r - c));
+    return jump >= 1e-3 * jl_max(std::fabs(c), 1e-4);
+}
+// sw: (dim+2) x dim column-major; comp and dir 1-based as in the reference
+static double o_velocity_slope(const double* sw, const double* prim, int nw, int comp, int dir) {
+    const double* col = sw + (size_t)nw * (dir - 1);
+    return (col[comp] - prim[comp] * col[0]) / prim[0];
+}
+static double o_vorticity(const double* sw, const double* prim, int D) {
+    const int nw = D + 2;
+    if (D == 2) return o_velocity_slope(sw, prim, nw, 1, 2) - o_velocity_slope(sw, prim, nw, 2, 1);
+    const double c1 = o_velocity_slope(sw, prim, nw, 2, 3) - o_velocity_slope(sw, prim, nw, 3, 2);
+    const double c2 = o_velocity_slope(sw, prim, nw, 3, 1) - o_velocity_slope(sw, prim, nw, 1, 3);
+    const double c3 = o_velocity_slope(sw, prim, nw, 1, 2) - o_velocity_slope(sw, prim, nw, 2, 1);
+    return std::sqrt(c1 * c1 + c2 * c2 + c3 * c3);
+}
+static bool o_vorticity_ok(double l, double c, double r, const double* prim, int D, double h) {
+    double speed2 = 0.0;
+    for (int i = 1; i <= D; ++i) speed2 += prim[i] * prim[i];
+    const double lambda = jl_max(std::fabs(prim[D + 1]), 2.220446049250313e-16);
+    const double vscale = jl_max(std::sqrt(speed2), 1.0 / std::sqrt(lambda));
+    const double omega = jl_max(std::fabs(l), jl_max(std::fabs(c), std::fabs(r)));
+    return omega * h >= 2e-2 * vscale;
+}
+static double o_sensor(const double* lo, int D) {
+    double v = 0.0;
+    for (int dir = 0; dir < D; ++dir) v = jl_max(v, jl_max(lo[(size_t)dir * (D + 2)], lo[(size_t)dir * (D + 2) + D + 1]));
+    return v;
+}
+
+extern "C" int kgo_criterion(const kg_params* prm, const kg_topology* t, const double* w, const double* prim,
+                             const double* sw, double thr, double* loh_out) {
+    Model m;
+    int rc = setup(m, prm, t);
+    if (rc) return rc;
+    const int D = t->dim, NW = D + 2, NF = 2 * D, N = NW * D;
+    const int NC = t->n_cells;
+    std::vector<double> lo((size_t)NC * N, 0.0);
+    for (int c = 0; c < NC; ++c) {
+        if (t->cell_bound_enc[c] < 0) continue;
+        const double* pc = prim + (size_t)c * NW;
+        const double* swc = sw + (size_t)c * N;
+        const double omega_c = o_vorticity(swc, pc, D);
+        for (int dir = 0; dir < D; ++dir) {
+            double* row = lo.data() + (size_t)c * N + (size_t)dir * NW;
+            const int s[2] = {t->nbr_state[c * NF + 2 * dir], t->nbr_state[c * NF + 2 * dir + 1]};
+            if (s[0] == 0 || s[1] == 0) continue;                 // the Val{0} methods: zero row
+            const double ds = t->cell_ds[(size_t)c * D + dir];
+            double dss[2], pside[2][5], om[2];
+            for (int side = 0; side < 2; ++side) {
+                dss[side] = (s[side] == 1 ? 1.0 : (s[side] == -1 ? 1.5 : 0.75)) * ds;
+                const int k = 2 * dir + side;
+                const int32_t* lst = t->nbr_ref + t->nbr_off[c * NF + k];
+                const int n = t->nbr_off[c * NF + k + 1] - t->nbr_off[c * NF + k];
+                double ws[5] = {0, 0, 0, 0, 0};
+                std::vector<double> sws(N, 0.0);
+                // a SolidNeighbor's w and sw stay zero (Immersed_boundary.jl:300-302, 481-482)
+                for (int j = 0; j < n; ++j) {
+                    if (lst[j] < 0) continue;
+                    for (int q = 0; q < NW; ++q) ws[q] += w[(size_t)lst[j] * NW + q];
+                    for (int e = 0; e < N; ++e) sws[e] += sw[(size_t)lst[j] * N + e];
+                }
+                if (dss[side] > ds && lst[0] >= 0) {                // a coarser side
+                    const int nb = lst[0];
+                    for (int tr = 0; tr < D; ++tr) {
+                        if (tr == dir) continue;
+                        const double dx = t->cell_midpoint[(size_t)c * D + tr] - t->cell_midpoint[(size_t)nb * D + tr];
+                        for (int q = 0; q < NW; ++q) ws[q] += dx * sw[(size_t)nb * N + (size_t)tr * NW + q];
+                    }
+                }
+                for (int q = 0; q < NW; ++q) ws[q] /= n;
+                for (int e = 0; e < N; ++e) sws[e] /= n;
+                get_prim(m, ws, pside[side]);
+                om[side] = o_vorticity(sws.data(), pside[side], D);
+            }
+            const bool use_vort = o_vorticity_ok(om[0], omega_c, om[1], pc, D, std::max(dss[0], dss[1]));
+            const double eps_l = 0.2 * ds;
+            for (int q = 0; q < NW; ++q) {
+                if (q == 1) row[q] = use_vort ? o_lohner_value(om[0], omega_c, om[1], dss[0], dss[1], eps_l) : 0.0;
+                else row[q] = o_primitive_ok(pside[0][q], pc[q], pside[1][q])
+                                  ? o_lohner_value(pside[0][q], pc[q], pside[1][q], dss[0], dss[1], eps_l) : 0.0;
+            }
+        }
+    }
+    for (int c = 0; c < NC; ++c) {
+        double* o = loh_out + (size_t)c * N;
+        for (int e = 0; e < N; ++e) o[e] = lo[(size_t)c * N + e];
+        if (t->cell_bound_enc[c] < 0 || o_sensor(lo.data() + (size_t)c * N, D) > thr) continue;
+        bool flagged = false;
+        for (int k = 0; k < NF && !flagged; ++k) {
+            if (t->nbr_state[c * NF + k] == 0) continue;
+            for (int j = t->nbr_off[c * NF + k]; j < t->nbr_off[c * NF + k + 1]; ++j) {
+                const int32_t r = t->nbr_ref[j];
+                if (r < 0 || t->cell_bound_enc[r] < 0) continue;
+                if (o_sensor(lo.data() + (size_t)r * N, D) > thr) { flagged = true; break; }
+            }
+        }
+        if (flagged) for (int e = 0; e < N; ++e) o[e] = 2.0 * thr;
+    }
+    return KG_OK;
+}
+
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0 of sdf[:, :, dir] for
 // every cell with bound_enc >= 0; sw_out holds (dim+2) x dim doubles per cell (column-major,
 // as PsData.sw); solid cells are left at zero.

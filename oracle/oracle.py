@@ -38,6 +38,8 @@ def lib():
                                            C.POINTER(C.c_int32), C.c_int32]
         L.kgo_moments.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4
         L.kgo_macro_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 2
+        L.kgo_criterion.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + \
+            [C.c_double, C.POINTER(C.c_double)]
         L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
         _lib = L
     return _lib
@@ -93,6 +95,20 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle macro_slope failed: {rc}")
         return sw.reshape(nc, dim, dim + 2)
+
+    def criterion(self, params, adapt_coeffi_ps, sw=None):
+        """PsData.lohner of every cell (update_criterion! + buffer layer) from this state's
+        w, prim and sw (default: macro_slope of its sdf), shape (n_cells, dim, dim + 2)."""
+        nc, dim = self.topo["n_cells"], self.topo["dim"]
+        if sw is None:
+            sw = self.macro_slope(params)
+        sw = np.ascontiguousarray(sw, dtype=np.float64).reshape(-1)
+        lo = np.zeros(nc * dim * (dim + 2))
+        rc = lib().kgo_criterion(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.w),
+                                 abi.dptr(self.prim), abi.dptr(sw), float(adapt_coeffi_ps), abi.dptr(lo))
+        if rc != 0:
+            raise RuntimeError(f"oracle criterion failed: {rc}")
+        return lo.reshape(nc, dim, dim + 2)
 
     def moments(self, params):
         nc, nw = self.topo["n_cells"], self.topo["dim"] + 2

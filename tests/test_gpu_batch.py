@@ -129,3 +129,20 @@ def test_batch_sw_equals_single_handle():
         assert np.array_equal(b.download_sw(slots[k]), g.download_sw())
         g.close()
     b.close()
+
+
+def test_batch_criterion_equals_single_handle():
+    probs = _problems()[:3]
+    built = [cases.build(p) for p in probs]
+    prec = abi.KG_PREC_MIXED
+    b = GpuBatch(abi.make_params(probs[0], precision=prec), 512 << 20)
+    slots = [b.admit(abi.make_params(p, precision=prec, st_check_interval=2), t, s["f"], s["w"], s["prim"], p.dt())
+             for p, (t, s) in zip(probs, built)]
+    b.step(2)
+    for k, (p, (t, s)) in enumerate(zip(probs, built)):
+        g = GpuStep(abi.make_params(p, precision=prec, st_check_interval=2), t)
+        g.upload_state(s["f"], s["w"], s["prim"])
+        g.step(p.dt(), 0, 2)
+        assert np.array_equal(b.criterion(slots[k], 0.05), g.criterion(0.05))
+        g.close()
+    b.close()

@@ -125,3 +125,26 @@ def test_downloaded_slopes_match_oracle(name, make, nsteps):
         mask[off[c] * dim:off[c + 1] * dim] = True
     scale = float(np.max(np.abs(ref.sdf[mask])))
     assert float(np.max(np.abs(out["sdf"][mask] - ref.sdf[mask]))) <= 1e-12 * scale
+
+
+@pytest.mark.parametrize("name,make,nsteps", [CASES_FP64[1], CASES_FP64[3], CASES_FP64[4]],
+                         ids=["cavity_levels", "cylinder_ib_adapted", "box3d_levels"])
+def test_criterion_matches_oracle(name, make, nsteps):
+    """PsData.lohner after the last step (update_criterion! + buffer layer) through
+    kg_criterion, against the oracle's restatement on its own state: FP64 within 1e-9."""
+    import oracle as O
+    from kitgpu.solver import GpuStep
+    p = make()
+    topo, state = cases.build(p)
+    prm = abi.make_params(p, st_check_interval=1)
+    ref = O.OracleState(topo, state).run(prm, p.dt(), 0, nsteps, nthreads=4)
+    g = GpuStep(prm, topo)
+    g.upload_state(state["f"], state["w"], state["prim"])
+    g.step(p.dt(), 0, nsteps)
+    thr = 0.05
+    got = g.criterion(thr)
+    g.close()
+    exp = ref.criterion(prm, thr)
+    assert np.any(exp > 0), "the case exercises the sensor"
+    err = np.abs(got - exp)
+    assert np.all(err <= 1e-9 * np.maximum(1.0, np.abs(exp))), (name, float(err.max()))

@@ -105,3 +105,37 @@ def test_golden_fixture():
     topo, st, _ = _run(p, int(g["steps"]))
     assert np.max(np.abs(st.f - g["f"])) <= 1e-13 * np.max(np.abs(g["f"]))
     assert np.max(np.abs(st.w - g["w"])) <= 1e-13 * np.max(np.abs(g["w"]))
+
+
+def test_criterion_zero_on_a_uniform_state():
+    """update_criterion!: a uniform state trips no amplitude test, so every Löhner row is 0."""
+    p = _periodic_box(ic=lambda x: [1.0, 0.2, 0.1, 1.0])
+    topo, state = cases.build(p)
+    st = O.OracleState(topo, state)
+    lo = st.criterion(abi.make_params(p), 0.1)
+    assert np.all(lo == 0.0)
+
+
+def test_criterion_flags_a_density_jump_and_its_buffer_layer():
+    """A Sod jump (uniform mesh, zero slopes): the density sensor of the two cells at the jump
+    is the Löhner ratio of a step, |Δρ| / (|Δρ| + 0.2 ds (|l| + 2|c| + |r|)) (the reference's
+    eps = 0.2 ds is a length); the cells next to them carry the buffer value 2 * threshold;
+    cells away from the jump stay at 0."""
+    p = cases.sod(scale=0.125, max_level=0, nv=16)
+    topo, state = cases.build(p)
+    st = O.OracleState(topo, state)
+    thr = 0.1
+    lo = st.criterion(abi.make_params(p), thr, sw=np.zeros((topo["n_cells"], 2, 4)))
+    mid = np.asarray(topo["cell_midpoint"]).reshape(-1, 2)
+    sensor = np.maximum(lo[:, :, 0].max(1), lo[:, :, -1].max(1))
+    ds = topo["cell_ds"].reshape(-1, 2)[0, 0]
+    d = np.abs(mid[:, 0] - 0.5)
+    at = d < ds
+    assert np.all(sensor[at] > thr)
+    # density row of the cell just left of the jump: l = c = 1, r = 0.125
+    left = np.nonzero(at & (mid[:, 0] < 0.5))[0][0]
+    expect = 0.875 / (0.875 + 0.2 * ds * (1.0 + 2.0 + 0.125))
+    assert abs(lo[left, 0, 0] - expect) < 1e-14
+    near = (d > ds) & (d < 2 * ds)
+    assert np.all(lo[near] == 2 * thr)
+    assert np.all(lo[d > 3 * ds] == 0.0)
