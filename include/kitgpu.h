@@ -192,14 +192,59 @@ int kg_download_sw(kg_handle *h, double *sw);
 /* Physical-space refinement sensor of the adaptation step: PsData.lohner as
  * update_criterion! leaves it (Physical_space/AMR.jl:256-284; update_Lohner_inner_ps!,
  * Physical_space/Criteria.jl:95-158), including apply_amr_buffer!'s one-cell buffer layer
- * (AMR.jl:286-330) with threshold adapt_coeffi_ps (solver.ADAPT_COEFFI_PS).  Computed on
- * demand from the device state (w, prim and the sw of the last step's slopes) in FP64; the
- * host applies ps_refine_flag / ps_coarsen_flag (user-defined functions) to it, so only
+ * (AMR.jl:286-330) with threshold adapt_coeffi_ps (solver.ADAPT_COEFFI_PS).  As
+ * ps_adaptive_mesh_refinement! does (Physical_space/AMR.jl:1108-1116), the slopes are first
+ * recomputed from the current f (slope!), then sw and the sensor follow in FP64 from w, prim
+ * and that sw; the refreshed slopes stay on the device (kg_download_state's sdf, kg_download_sw,
+ * kg_adapt's refinement).  The host applies ps_refine_flag / ps_coarsen_flag (user-defined
+ * functions) to the sensor, so only
  * (dim+2) x dim doubles per cell cross the link at an adaptation instead of f.
  * lohner: n_cells blocks of (dim+2) x dim doubles, column-major (PsData.lohner memory);
  * solid cells get zeros.  A direction whose two sides are both coarser uses 1.5 ds on
  * both sides (the reference has no applicable method for that case).          */
 int kg_criterion(kg_handle *h, double adapt_coeffi_ps, double *lohner);
+
+/* ---- physical-space adaptation on the device --------------------------------
+ * The state moves of the refine / coarsen / balance callbacks (ps_replace!,
+ * Physical_space/AMR.jl:633-703), applied to the device state without sending f to the
+ * host.  The caller records, in its replacement callbacks, where every cell of the
+ * adapted mesh comes from and passes one kg_adapt_src per cell of the new topology (same
+ * order as topo's cells):
+ *   KG_ADAPT_KEEP     src[0]: the same cell in the previous topology (also the children a
+ *                     balance pass restores after a coarsening, BALANCE_FLAG);
+ *   KG_ADAPT_REFINE   src[0]: the parent; `depth` refinements (1..KG_ADAPT_MAX_DEPTH, more
+ *                     than one under recursive refinement) along path[0..depth-1], each a
+ *                     0-based child number in RMT order (Abstract/Types.jl:10: bit d set =
+ *                     upper half in dimension d).  Per velocity cell and level, with the
+ *                     child's ds (half the parent's):
+ *                     df += min(|df / (ds . |sdf| + EPS)|, 1) * (sdf . (ds/2 .* RMT[i]))
+ *                     with the parent's slopes; sdf is the parent's; w = calc_w0,
+ *                     prim = get_prim; qf = 0;
+ *   KG_ADAPT_COARSEN  src[0..2^dim-1]: the children in RMT order.  The parent's velocity
+ *                     grid must be the grid of the first child with the fewest velocity
+ *                     cells (ps_merge); df and sdf are the vs_merge! sums of the children
+ *                     over 2^dim, w the children's mean, prim = get_prim(w), qf = 0.
+ * Indices refer to the cells of the topology on the device before the call; KEEP and
+ * REFINE cells keep their source's velocity grid (equal content).  As
+ * ps_adaptive_mesh_refinement! does, the slopes of the current f are recomputed first
+ * (slope!).  After the call the handle holds the new topology and state (walls start
+ * from their donors' f, as after amr_recover!), exactly as kg_upload_topology +
+ * kg_upload_state with the interpolated state would leave it.  Device memory peaks at
+ * the previous plus the new pools during the call.  A rejected plan (KG_ERR_ARG: a source
+ * out of range, a bad depth or child number; KG_ERR_TOPOLOGY: a grid that breaks the rules
+ * above, or a new topology flatten rejects) leaves the handle as it was; a device failure
+ * after that (KG_ERR_NOMEM, KG_ERR_CUDA) leaves it without a state.                   */
+#define KG_ADAPT_KEEP       0
+#define KG_ADAPT_REFINE     1
+#define KG_ADAPT_COARSEN    2
+#define KG_ADAPT_MAX_DEPTH  8
+typedef struct {
+    int32_t kind;
+    int32_t depth;
+    int32_t src[8];
+    int8_t  path[KG_ADAPT_MAX_DEPTH];
+} kg_adapt_src;
+int kg_adapt(kg_handle *h, const kg_topology *topo, const kg_adapt_src *src);
 
 /* Advance `nsteps` steps with time step dt; `step` is status.step before the
  * first of them (drives the residual cadence).  One call = nsteps x
@@ -250,6 +295,9 @@ int kg_batch_step(kg_handle *h, int32_t nsteps, kg_step_report *reports, int32_t
 int kg_batch_download(kg_handle *h, int32_t slot, double *f, double *w, double *prim, double *qf);
 int kg_batch_download_sw(kg_handle *h, int32_t slot, double *sw);   /* kg_download_sw of one problem */
 int kg_batch_criterion(kg_handle *h, int32_t slot, double adapt_coeffi_ps, double *lohner);   /* kg_criterion of one problem */
+/* kg_adapt of one problem: its new slabs are placed while the previous ones are live, then
+ * the previous ones are released (KG_ERR_BUDGET when the pool cannot hold both).            */
+int kg_batch_adapt(kg_handle *h, int32_t slot, const kg_topology *topo, const kg_adapt_src *src);
 int kg_batch_info(const kg_handle *h, int32_t *n_live, int64_t *f_free_elems, int64_t *bytes_per_elem);
 int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
 

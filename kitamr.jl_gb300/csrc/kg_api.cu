@@ -19,6 +19,8 @@ template <int D, int NDF, typename T> struct Launch {
     static int flux_occupancy(const Dev&, int);
     static cudaError_t macro_slope(const Dev&, int, int, int, double*, cudaStream_t);
     static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
+    static cudaError_t adapt(const Dev&, int, const AdaptRec*, const void*, const void*, const double*, const double*,
+                             const double*, const int32_t*, const int8_t*, cudaStream_t);
 };
 cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
@@ -438,6 +440,19 @@ int autotune_flux(kg_handle* h) {
 }
 
 // One step of every live problem on the handle's stream (graph-capturable).
+// The level passes of slope! on the current f (the first phase of a step).
+cudaError_t enqueue_slopes(kg_handle* h, const Dev& P, cudaStream_t s) {
+    const Flat& F = h->M;
+    const int npass = (int)F.pass_cells_off.size() - 1;
+    for (int p = 0; p < npass; ++p) {
+        const int base = F.pass_cells_off[p], n = F.pass_cells_off[p + 1] - base;
+        if (n <= 0) continue;
+        cudaError_t e = dispatch(h, [&](auto L) { return decltype(L)::slope(P, base, n, s); });
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
     Flat& F = h->M;
     Dev P = h->dev;
@@ -571,6 +586,38 @@ void fill_report(const kg_handle* h, int slot, double ms, int64_t launches, kg_s
     r->status = st ? ((st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE) : KG_OK;
 }
 
+// SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298): one
+// launch for all walls of the problem in `slot`, within the f buffer at fa (the problem's
+// block of it).
+int init_wall_blocks(kg_handle* h, int slot, char* fa) {
+    const Flat& L = h->probs[slot].F;
+    const int nwall = (int)L.wall_ops.size();
+    if (nwall == 0) return KG_OK;
+    std::vector<int64_t> tri((size_t)nwall * 3);
+    for (int k = 0; k < nwall; ++k) {
+        const WallOp& wo = L.wall_ops[k];
+        tri[3 * k] = L.foff[wo.donor];
+        tri[3 * k + 1] = L.foff[wo.data];
+        tri[3 * k + 2] = L.foff[wo.data + 1] - L.foff[wo.data];
+    }
+    if (h->tri_cap < (int64_t)tri.size()) {
+        if (h->d_tri) cudaFree(h->d_tri);
+        h->d_tri = nullptr;
+        h->tri_cap = 0;
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, sizeof(int64_t) * tri.size());
+        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc wall copies");
+        h->d_tri = (int64_t*)p;
+        h->tri_cap = (int64_t)tri.size();
+    }
+    KG_CUDA(h, cudaMemcpyAsync(h->d_tri, tri.data(), sizeof(int64_t) * tri.size(), cudaMemcpyHostToDevice, h->stream));
+    if (h->prm.precision == KG_PREC_FP64) copy_blocks<double><<<nwall, 256, 0, h->stream>>>((double*)fa, h->d_tri);
+    else copy_blocks<float><<<nwall, 256, 0, h->stream>>>((float*)fa, h->d_tri);
+    KG_CUDA(h, cudaGetLastError());
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // tri is host memory the copy reads
+    return KG_OK;
+}
+
 // Uploads a placed problem's state into its slabs (both f buffers).
 int upload_problem_state(kg_handle* h, int slot, const double* f, const double* w, const double* prim, int64_t step) {
     Problem& pb = h->probs[slot];
@@ -590,31 +637,9 @@ int upload_problem_state(kg_handle* h, int slot, const double* f, const double* 
         to_storage<float><<<1024, 256, 0, h->stream>>>(st, (float*)fa, nfc);
         KG_CUDA(h, cudaGetLastError());
     }
-    // SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298): one
-    // launch for all walls of the problem
-    const int nwall = (int)L.wall_ops.size();
-    std::vector<int64_t> tri((size_t)nwall * 3);
-    for (int k = 0; k < nwall; ++k) {
-        const WallOp& wo = L.wall_ops[k];
-        tri[3 * k] = L.foff[wo.donor];
-        tri[3 * k + 1] = L.foff[wo.data];
-        tri[3 * k + 2] = L.foff[wo.data + 1] - L.foff[wo.data];
-    }
-    if (nwall > 0) {
-        if (h->tri_cap < (int64_t)tri.size()) {
-            if (h->d_tri) cudaFree(h->d_tri);
-            h->d_tri = nullptr;
-            h->tri_cap = 0;
-            void* p = nullptr;
-            cudaError_t e = cudaMalloc(&p, sizeof(int64_t) * tri.size());
-            if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc wall copies");
-            h->d_tri = (int64_t*)p;
-            h->tri_cap = (int64_t)tri.size();
-        }
-        KG_CUDA(h, cudaMemcpyAsync(h->d_tri, tri.data(), sizeof(int64_t) * tri.size(), cudaMemcpyHostToDevice, h->stream));
-        if (h->prm.precision == KG_PREC_FP64) copy_blocks<double><<<nwall, 256, 0, h->stream>>>((double*)fa, h->d_tri);
-        else copy_blocks<float><<<nwall, 256, 0, h->stream>>>((float*)fa, h->d_tri);
-        KG_CUDA(h, cudaGetLastError());
+    {
+        int rc = init_wall_blocks(h, slot, fa);
+        if (rc) return rc;
     }
     KG_CUDA(h, cudaMemsetAsync((char*)h->sdf + fb * D * ss, 0, nf * D * ss, h->stream));
     std::vector<double> pw((size_t)nd * MAXW, 0.0), pp((size_t)nd * MAXW, 0.0);
@@ -697,9 +722,10 @@ int download_problem(kg_handle* h, int slot, double* f, double* w, double* prim,
 
 // sw of the problem in `slot` (update_macro_slope!) from the slopes on the device, into a
 // device array of (dim+2) x dim doubles per data item of the problem (zero rows for items
-// without a fluid-list entry); optionally followed by the physical-space criterion with the
-// buffer layer (update_criterion! + apply_amr_buffer!) into a second such array.  The host
-// receives the rows of the problem's cells.
+// without a fluid-list entry); or, for the physical-space criterion, fresh slopes of the
+// current f, their sw and the criterion with the buffer layer (update_criterion! +
+// apply_amr_buffer!) into a second such array.  The host receives the rows of the problem's
+// cells.
 int sync_point_rows(kg_handle* h, int slot, double* sw_host, double thr, double* loh_host) {
     int rc = rebuild(h);
     if (rc) return rc;
@@ -714,8 +740,14 @@ int sync_point_rows(kg_handle* h, int slot, double* sw_host, double thr, double*
     double* dsw = d;
     double* dloh = d + bytes / sizeof(double);
     double* dout = dloh + bytes / sizeof(double);
-    const Dev P = h->dev;
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fA : h->fB;
+    P.f_out = h->parity == 0 ? h->fB : h->fA;
     e = cudaMemsetAsync(d, 0, 3 * bytes, h->stream);
+    // ps_adaptive_mesh_refinement! (Physical_space/AMR.jl:1108-1116) runs slope! on the current
+    // f before update_criterion!; the next step recomputes the same slopes, so the state a step
+    // sees is unchanged (in a batch the pass covers every live problem)
+    if (e == cudaSuccess && loh_host) e = enqueue_slopes(h, P, h->stream);
     if (e == cudaSuccess)
         e = dispatch(h, [&](auto L) { return decltype(L)::macro_slope(P, fb, n, (int)pb.dbase, dsw, h->stream); });
     if (e == cudaSuccess && loh_host)
@@ -727,6 +759,223 @@ int sync_point_rows(kg_handle* h, int slot, double* sw_host, double thr, double*
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     cudaFree(d);
     if (e != cudaSuccess) return cuda_fail(h, e, "sync-point rows");
+    return KG_OK;
+}
+
+// ---- physical-space adaptation (ps_replace!, Physical_space/AMR.jl:633-703) -----------
+// Same velocity grid content (levels, weights, midpoints) of grid ga of A and grid gb of B.
+bool same_grid(const Flat& A, int ga, const Flat& B, int gb) {
+    const int64_t na = A.g_off[ga + 1] - A.g_off[ga], nb = B.g_off[gb + 1] - B.g_off[gb];
+    if (na != nb) return false;
+    const int64_t a0 = A.g_off[ga], b0 = B.g_off[gb];
+    const int64_t PA = (int64_t)A.vw.size(), PB = (int64_t)B.vw.size();
+    if (std::memcmp(&A.vlev[a0], &B.vlev[b0], (size_t)na) != 0) return false;
+    if (std::memcmp(&A.vw[a0], &B.vw[b0], sizeof(double) * (size_t)na) != 0) return false;
+    for (int d = 0; d < A.dim; ++d)
+        if (std::memcmp(&A.vu[(size_t)d * PA + a0], &B.vu[(size_t)d * PB + b0], sizeof(double) * (size_t)na) != 0) return false;
+    return true;
+}
+
+struct AdaptPlan {
+    std::vector<AdaptRec> recs;
+    std::vector<int32_t> runs;   // (j0, count) pairs
+    std::vector<int8_t> lev;     // levels of the children's grids that need runs
+};
+
+// Checks the per-cell sources of the adapted mesh Fn (placed at data slot dbn) against the
+// previous mesh Fo (placed at fbo / dbo) and resolves them to pool positions.
+int build_adapt_plan(kg_handle* h, const Flat& Fo, int64_t fbo, int64_t dbo, const Flat& Fn, int64_t dbn,
+                     const kg_adapt_src* src, AdaptPlan& plan) {
+    const int D = Fn.dim, NC = Fn.n_cells, NCo = Fo.n_cells, nch = 1 << D;
+    std::map<std::pair<int, int>, bool> same;                 // (previous grid, new grid)
+    std::map<std::pair<int, int>, int64_t> run_of;            // (new grid, previous grid) -> first pair
+    std::map<int, int64_t> lev_of;                            // previous grid -> level table offset
+    auto is_same = [&](int go, int gn) {
+        auto key = std::make_pair(go, gn);
+        auto it = same.find(key);
+        if (it != same.end()) return it->second;
+        const bool r = same_grid(Fo, go, Fn, gn);
+        same[key] = r;
+        return r;
+    };
+    auto where = [](int c) { return " (new cell " + std::to_string(c) + ")"; };
+    std::vector<int32_t> tmp;
+    plan.recs.assign(NC, AdaptRec{});
+    for (int c = 0; c < NC; ++c) {
+        const kg_adapt_src& a = src[c];
+        AdaptRec& r = plan.recs[c];
+        r.cell = (int32_t)(dbn + c);
+        r.kind = a.kind;
+        const int gn = Fn.dgrid[c];
+        for (int q = 0; q < 8; ++q) r.run[q] = -1;
+        if (a.kind == KG_ADAPT_KEEP || a.kind == KG_ADAPT_REFINE) {
+            const int o = a.src[0];
+            if (o < 0 || o >= NCo) return fail(h, KG_ERR_ARG, "adapt source cell out of range" + where(c));
+            if (!is_same(Fo.dgrid[o], gn))
+                return fail(h, KG_ERR_TOPOLOGY, "a kept or refined cell must keep its source's velocity grid" + where(c));
+            r.nsrc = 1;
+            r.src_f[0] = fbo + Fo.foff[o];
+            r.src_nv[0] = Fo.dnv[o];
+            r.src_d[0] = (int32_t)(dbo + o);
+            if (a.kind == KG_ADAPT_REFINE) {
+                if (a.depth < 1 || a.depth > KG_ADAPT_MAX_DEPTH) return fail(h, KG_ERR_ARG, "refinement depth out of range" + where(c));
+                r.depth = a.depth;
+                for (int l = 0; l < a.depth; ++l) {
+                    if (a.path[l] < 0 || a.path[l] >= nch) return fail(h, KG_ERR_ARG, "child number out of range" + where(c));
+                    r.path[l] = a.path[l];
+                }
+                for (int d = 0; d < D; ++d) r.ds[d] = Fo.dds[(size_t)o * MAXD + d];
+            }
+        } else if (a.kind == KG_ADAPT_COARSEN) {
+            int best = 0;
+            for (int q = 0; q < nch; ++q) {
+                const int o = a.src[q];
+                if (o < 0 || o >= NCo) return fail(h, KG_ERR_ARG, "adapt source cell out of range" + where(c));
+                if (Fo.dnv[o] < Fo.dnv[a.src[best]]) best = q;
+            }
+            // ps_merge keeps the grid of the first child with the fewest velocity cells
+            if (!is_same(Fo.dgrid[a.src[best]], gn))
+                return fail(h, KG_ERR_TOPOLOGY, "a coarsened cell takes the grid of its first child with the fewest velocity cells" + where(c));
+            r.nsrc = nch;
+            for (int q = 0; q < nch; ++q) {
+                const int o = a.src[q], go = Fo.dgrid[o];
+                r.src_f[q] = fbo + Fo.foff[o];
+                r.src_nv[q] = Fo.dnv[o];
+                r.src_d[q] = (int32_t)(dbo + o);
+                if (is_same(go, gn)) continue;
+                auto key = std::make_pair(gn, go);
+                auto it = run_of.find(key);
+                if (it == run_of.end()) {
+                    const int64_t nn = Fn.g_off[gn + 1] - Fn.g_off[gn], no = Fo.g_off[go + 1] - Fo.g_off[go];
+                    if (!level_runs(&Fn.vlev[Fn.g_off[gn]], (int)nn, &Fo.vlev[Fo.g_off[go]], (int)no, D, tmp))
+                        return fail(h, KG_ERR_TOPOLOGY, "velocity grids of a coarsening do not tile the same root lattice" + where(c));
+                    it = run_of.emplace(key, (int64_t)plan.runs.size() / 2).first;
+                    plan.runs.insert(plan.runs.end(), tmp.begin(), tmp.end());
+                }
+                r.run[q] = it->second;
+                auto lt = lev_of.find(go);
+                if (lt == lev_of.end()) {
+                    lt = lev_of.emplace(go, (int64_t)plan.lev.size()).first;
+                    plan.lev.insert(plan.lev.end(), Fo.vlev.begin() + Fo.g_off[go], Fo.vlev.begin() + Fo.g_off[go + 1]);
+                }
+                r.lev[q] = lt->second;
+            }
+        } else {
+            return fail(h, KG_ERR_ARG, "unknown adapt kind" + where(c));
+        }
+    }
+    return KG_OK;
+}
+
+// Replaces the problem in `slot` by the adapted mesh `topo`, its state interpolated on the
+// device from the previous one.  Single handle: the previous pools stay alive until the new
+// ones are filled.  Batch: the new slabs are placed beside the previous ones in the shared
+// pools, then the previous ones are released.
+int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adapt_src* src) {
+    Flat Fn;
+    std::string err;
+    int rc = flatten(h->prm, *topo, Fn, err);
+    if (rc) return fail(h, rc, err);
+    if (Fn.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
+    // ps_adaptive_mesh_refinement! runs slope! before the replacements read the slopes
+    if ((rc = rebuild(h))) return rc;
+    {
+        Dev P = h->dev;
+        P.f_in = h->parity == 0 ? h->fA : h->fB;
+        P.f_out = h->parity == 0 ? h->fB : h->fA;
+        KG_CUDA(h, enqueue_slopes(h, P, h->stream));
+    }
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    // every check before the handle changes: a rejected adaptation leaves it as it was
+    AdaptPlan plan;
+    if ((rc = build_adapt_plan(h, h->probs[slot].F, h->probs[slot].fbase, h->probs[slot].dbase, Fn, 0, src, plan))) return rc;
+    Problem old = std::move(h->probs[slot]);
+    h->probs[slot] = Problem();
+    // the previous state: pointers into pools that stay alive until the end of this call
+    const void* of = h->parity == 0 ? h->fA : h->fB;
+    const void* osdf = h->sdf;
+    const double *ow = h->w, *oprim = h->prim, *oqf = h->qf;
+    std::vector<void*> old_pools;
+    const int64_t nf = Fn.foff.back(), nd = Fn.n_data;
+    if (!h->is_batch) {
+        // hand the previous pools over to this call, then size new ones for the new mesh
+        old_pools.swap(h->pool_allocs);
+        h->pool_bytes = 0;
+        h->fA = h->fB = h->sdf = nullptr;
+        h->w = h->prim = h->qf = h->staging = nullptr;
+        rc = make_pools(h, nf, nd);   // clears the slot table
+        if (rc) { for (void* p : old_pools) cudaFree(p); return rc; }
+        Problem& pn = h->probs[slot];
+        h->fslab.alloc(nf, &pn.fbase);
+        h->dslab.alloc(nd, &pn.dbase);
+    } else {
+        int64_t fb, db;
+        if (!h->fslab.alloc(nf, &fb)) { h->probs[slot] = std::move(old); return fail(h, KG_ERR_BUDGET, "f pool cannot hold the adapted problem beside the previous one"); }
+        if (!h->dslab.alloc(nd, &db)) {
+            h->fslab.release(fb, nf);
+            h->probs[slot] = std::move(old);
+            return fail(h, KG_ERR_BUDGET, "cell pool cannot hold the adapted problem beside the previous one");
+        }
+        h->probs[slot].fbase = fb; h->probs[slot].dbase = db;
+    }
+    Problem& pb = h->probs[slot];
+    pb.F = std::move(Fn);
+    pb.fsize = nf; pb.dsize = nd;
+    pb.pp = old.pp;
+    pb.live = true;
+    h->dirty = true;
+    for (AdaptRec& r : plan.recs) r.cell += (int32_t)pb.dbase;
+    rc = rebuild(h);
+    void* tab = nullptr;
+    if (rc == KG_OK) {
+        const size_t b_recs = sizeof(AdaptRec) * plan.recs.size();
+        const size_t b_runs = sizeof(int32_t) * std::max<size_t>(plan.runs.size(), 2);
+        const size_t b_lev = std::max<size_t>(plan.lev.size(), 16);
+        const size_t o_runs = (b_recs + 255) / 256 * 256, o_lev = o_runs + (b_runs + 255) / 256 * 256;
+        cudaError_t e = cudaMalloc(&tab, o_lev + b_lev);
+        if (e != cudaSuccess) { tab = nullptr; rc = fail(h, KG_ERR_NOMEM, "cudaMalloc adaptation tables"); }
+        else {
+            char* t = (char*)tab;
+            e = cudaMemcpyAsync(t, plan.recs.data(), b_recs, cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess && !plan.runs.empty())
+                e = cudaMemcpyAsync(t + o_runs, plan.runs.data(), sizeof(int32_t) * plan.runs.size(), cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess && !plan.lev.empty())
+                e = cudaMemcpyAsync(t + o_lev, plan.lev.data(), plan.lev.size(), cudaMemcpyHostToDevice, h->stream);
+            Dev P = h->dev;
+            P.f_in = h->parity == 0 ? h->fA : h->fB;
+            P.f_out = h->parity == 0 ? h->fB : h->fA;
+            if (e == cudaSuccess)
+                e = dispatch(h, [&](auto L) {
+                    return decltype(L)::adapt(P, (int)plan.recs.size(), (const AdaptRec*)t, of, osdf, ow, oprim, oqf,
+                                              (const int32_t*)(t + o_runs), (const int8_t*)(t + o_lev), h->stream);
+                });
+            if (e == cudaSuccess) e = cudaMemsetAsync(h->d_status + slot, 0, sizeof(int), h->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+            if (e != cudaSuccess) rc = cuda_fail(h, e, "adapt_kernel");
+        }
+    }
+    if (rc == KG_OK) {
+        char* fa = (char*)(h->parity == 0 ? h->fA : h->fB) + pb.fbase * storage_size(h);
+        rc = init_wall_blocks(h, slot, fa);
+    }
+    cudaStreamSynchronize(h->stream);
+    if (tab) cudaFree(tab);
+    if (!h->is_batch) {
+        for (void* p : old_pools) cudaFree(p);
+        if (rc) { free_pools(h); return rc; }
+        h->have_state = true;
+    } else {
+        h->fslab.release(old.fbase, old.fsize);
+        h->dslab.release(old.dbase, old.dsize);
+        if (rc) {
+            // the problem cannot continue in a half-built state: release it
+            h->fslab.release(pb.fbase, pb.fsize);
+            h->dslab.release(pb.dbase, pb.dsize);
+            pb = Problem();
+            h->dirty = true;
+            return rc;
+        }
+    }
     return KG_OK;
 }
 
@@ -857,6 +1106,15 @@ int kg_criterion(kg_handle* h, double adapt_coeffi_ps, double* lohner) {
     if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
     cudaSetDevice(h->device);
     return sync_point_rows(h, 0, nullptr, adapt_coeffi_ps, lohner);
+}
+
+int kg_adapt(kg_handle* h, const kg_topology* topo, const kg_adapt_src* src) {
+    if (!h) return KG_ERR_ARG;
+    if (!topo || !src) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_adapt");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return adapt_problem(h, 0, topo, src);
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
@@ -1024,6 +1282,14 @@ int kg_batch_criterion(kg_handle* h, int32_t slot, double adapt_coeffi_ps, doubl
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live || !lohner) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
     return sync_point_rows(h, slot, nullptr, adapt_coeffi_ps, lohner);
+}
+
+int kg_batch_adapt(kg_handle* h, int32_t slot, const kg_topology* topo, const kg_adapt_src* src) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    if (!topo || !src) return fail(h, KG_ERR_ARG, "null argument");
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    return adapt_problem(h, slot, topo, src);
 }
 
 int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {

@@ -24,6 +24,43 @@ struct Ctx {
 
 int grid_nv(const kg_topology& t, int g) { return (int)(t.grid_off[g + 1] - t.grid_off[g]); }
 
+}  // namespace
+
+// The reference's level merge walk (diff_vs!, Flux/Slope.jl:36-63; vs_merge!,
+// Physical_space/AMR.jl:343-366) defines, for every velocity cell i of grid A, the run of
+// grid-B cells that overlap it: one cell when B is as coarse or coarser there, the whole
+// covering run when B is finer.  runs receives (j0, count) per cell of A.
+bool level_runs(const int8_t* la, int na, const int8_t* lb, int nb, int D, std::vector<int32_t>& runs) {
+    runs.clear();
+    runs.reserve((size_t)2 * na);
+    int j = 0;
+    double flag = 0.0;
+    for (int i = 0; i < na; ++i) {
+        if (j >= nb) return false;
+        const int li = la[i];
+        if (li == lb[j]) {
+            runs.push_back(j); runs.push_back(1);
+            j += 1;
+        } else if (li < lb[j]) {
+            int j0 = j, cnt = 0;
+            while (flag != 1.0) {
+                if (j >= nb) return false;
+                flag += 1.0 / std::ldexp(1.0, D * (lb[j] - li));
+                j += 1; cnt += 1;
+            }
+            flag = 0.0;
+            runs.push_back(j0); runs.push_back(cnt);
+        } else {
+            runs.push_back(j); runs.push_back(1);
+            flag += 1.0 / std::ldexp(1.0, D * (li - lb[j]));
+            if (flag == 1.0) { j += 1; flag = 0.0; }
+        }
+    }
+    return j == nb;
+}
+
+namespace {
+
 // data index of a neighbour reference (cells first, then walls); -1 for none/inside
 int data_of(const Ctx& c, int32_t r) {
     if (r == KG_NBR_NONE || r == KG_NBR_INSIDE) return -1;
@@ -31,9 +68,6 @@ int data_of(const Ctx& c, int32_t r) {
     return c.t->n_cells + (-1 - r);
 }
 
-// The reference's level merge walk (e.g. diff_vs!, Flux/Slope.jl:36-63) defines, for
-// every velocity cell i of grid A, the run of grid-B cells that overlap it: one cell
-// when B is as coarse or coarser, the whole covering run when B is finer.
 int pairing(Ctx& c, int ga, int gb) {
     if (ga == gb) return -1;
     auto key = std::make_pair(ga, gb);
@@ -41,34 +75,13 @@ int pairing(Ctx& c, int ga, int gb) {
     if (it != c.pairs.end()) return it->second;
     const kg_topology& t = *c.t;
     Flat& F = *c.F;
-    int na = grid_nv(t, ga), nb = grid_nv(t, gb);
-    const int8_t* la = t.vs_level + t.grid_off[ga];
-    const int8_t* lb = t.vs_level + t.grid_off[gb];
-    int id = (int)F.p_off.size() - 1;
-    int j = 0;
-    double flag = 0.0;
-    for (int i = 0; i < na; ++i) {
-        if (j >= nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
-        int li = la[i];
-        if (li == lb[j]) {
-            F.p_j0.push_back(j); F.p_cnt.push_back(1);
-            j += 1;
-        } else if (li < lb[j]) {
-            int j0 = j, cnt = 0;
-            while (flag != 1.0) {
-                if (j >= nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
-                flag += 1.0 / std::ldexp(1.0, c.D * (lb[j] - li));
-                j += 1; cnt += 1;
-            }
-            flag = 0.0;
-            F.p_j0.push_back(j0); F.p_cnt.push_back(cnt);
-        } else {
-            F.p_j0.push_back(j); F.p_cnt.push_back(1);
-            flag += 1.0 / std::ldexp(1.0, c.D * (li - lb[j]));
-            if (flag == 1.0) { j += 1; flag = 0.0; }
-        }
+    std::vector<int32_t> runs;
+    if (!level_runs(t.vs_level + t.grid_off[ga], grid_nv(t, ga), t.vs_level + t.grid_off[gb], grid_nv(t, gb), c.D, runs)) {
+        *c.err = "velocity grids do not tile the same root lattice";
+        return -2;
     }
-    if (j != nb) { *c.err = "velocity grids do not tile the same root lattice"; return -2; }
+    int id = (int)F.p_off.size() - 1;
+    for (size_t q = 0; q < runs.size(); q += 2) { F.p_j0.push_back(runs[q]); F.p_cnt.push_back(runs[q + 1]); }
     F.p_off.push_back((int64_t)F.p_j0.size());
     c.pairs[key] = id;
     return id;

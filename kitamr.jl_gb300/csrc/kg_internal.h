@@ -177,6 +177,27 @@ struct Flat {
     int max_bcm = 0;                      // most Maxwellian-state domain faces (wall, inflow) of a cell
 };
 
+// One cell of an adapted mesh and the cells of the previous mesh its state comes from
+// (ps_replace!, Physical_space/AMR.jl:633-703), resolved to pool positions on the host.
+// kind: KG_ADAPT_KEEP (src 0), KG_ADAPT_REFINE (src 0 = the parent, `depth` refinements
+// along `path`), KG_ADAPT_COARSEN (srcs 0..2^dim-1 = the children in RMT order).
+struct AdaptRec {
+    int64_t src_f[8];      // f element offset of each source block in the previous pools
+    int64_t run[8];        // COARSEN: first (j0, count) pair of the child's runs; -1: same grid
+    int64_t lev[8];        // COARSEN: offset of the child's grid levels in the level table
+    double ds[MAXD];       // REFINE: the parent's ds
+    int32_t src_nv[8];     // velocity cells of each source
+    int32_t src_d[8];      // data index of each source in the previous pools (w, prim, qf rows)
+    int32_t cell;          // data index of the new cell (merged layout)
+    int32_t kind, depth, nsrc;
+    int8_t path[8];        // REFINE: child number (RMT order, bit d = upper half in dim d)
+};
+
+// The level merge walk of two velocity grids (diff_vs!, vs_merge!): per cell of grid A the
+// (first, count) run of grid-B cells overlapping it.  False when the grids do not tile the
+// same root lattice.
+bool level_runs(const int8_t* la, int na, const int8_t* lb, int nb, int D, std::vector<int32_t>& runs);
+
 // Builds the gather form; returns KG_OK or an error code with a message.
 int flatten(const kg_params& prm, const kg_topology& t, Flat& out, std::string& err);
 

@@ -1599,6 +1599,153 @@ __global__ void __launch_bounds__(BLOCK) residual_kernel(Dev P, const int32_t* l
 }
 
 // ---- launchers ------------------------------------------------------------------
+// ---- physical-space adaptation (ps_replace!, Physical_space/AMR.jl:633-703) ----------
+// One CTA per cell of the adapted mesh (layout P, state written into P.f_in / P.sdf / P.w /
+// P.prim / P.qf) from the pools of the previous mesh (V).  Arithmetic in the form's precision
+// (the refinement limiter and the merge sums); w of a refined cell is its calc_w0 (block
+// reduction), prim = get_prim of w.
+template <typename T> struct AdaptView {
+    const AdaptRec* recs;
+    const T* f;             // previous f (the buffer the next step would have read)
+    const T* sdf;           // previous slopes (recomputed from that f)
+    const double* w;
+    const double* prim;
+    const double* qf;
+    const int32_t* runs;    // (j0, count) pairs of the coarsening merges
+    const int8_t* lev;      // velocity levels of the children's grids
+};
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) adapt_kernel(Dev P, AdaptView<T> V) {
+    using A = typename Arith<T>::type;
+    __shared__ double sred[(D + 2) * (BLOCK / 32)];
+    const AdaptRec& R = V.recs[blockIdx.x];
+    const int cell = R.cell;
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const int64_t fo = P.foff[cell];
+    T* fn = (T*)P.f_in + fo;
+    T* sn = (T*)P.sdf + fo * D;
+    double* wn = P.w + (int64_t)cell * MAXW;
+    double* pn = P.prim + (int64_t)cell * MAXW;
+    double* qn = P.qf + (int64_t)cell * MAXD;
+    if (R.kind == KG_ADAPT_KEEP) {
+        const T* fs = V.f + R.src_f[0];
+        const T* ss = V.sdf + R.src_f[0] * D;
+        for (int64_t a = threadIdx.x; a < (int64_t)NDF * nv; a += BLOCK) fn[a] = fs[a];
+        for (int64_t a = threadIdx.x; a < (int64_t)D * NDF * nv; a += BLOCK) sn[a] = ss[a];
+        const int64_t od = R.src_d[0];
+        if (threadIdx.x < D + 2) {
+            wn[threadIdx.x] = V.w[od * MAXW + threadIdx.x];
+            pn[threadIdx.x] = V.prim[od * MAXW + threadIdx.x];
+        }
+        if (threadIdx.x < D) qn[threadIdx.x] = V.qf[od * MAXD + threadIdx.x];
+        return;
+    }
+    if (R.kind == KG_ADAPT_REFINE) {
+        const T* fs = V.f + R.src_f[0];
+        const T* ss = V.sdf + R.src_f[0] * D;
+        const A* VU = vel<A>(P);
+        const A* VW = wts<A>(P) + g.goff;
+        KSum<A> m[D + 2];
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A fv[NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                A x = (A)fs[(int64_t)k * nv + i];
+                A s[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) s[d] = (A)ss[((int64_t)d * NDF + k) * nv + i];
+                double dsl[D];
+#pragma unroll
+                for (int d = 0; d < D; ++d) dsl[d] = R.ds[d];
+                for (int l = 0; l < R.depth; ++l) {
+                    // the child's ds and its offset 0.5 ds .* RMT[child] from the parent centre
+                    A den = 0, dot = 0;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        dsl[d] *= 0.5;
+                        const A dd = (A)dsl[d];
+                        den += dd * fabs(s[d]);
+                        const A off = ((R.path[l] >> d) & 1) ? (A)0.5 * dd : -((A)0.5 * dd);
+                        dot += s[d] * off;
+                    }
+                    den += (A)EPS_REF;
+                    A th = fabs(x / den);
+                    th = th < (A)1 ? th : (A)1;
+                    x += th * dot;
+                }
+                fv[k] = x;
+                fn[(int64_t)k * nv + i] = (T)x;
+#pragma unroll
+                for (int d = 0; d < D; ++d) sn[((int64_t)d * NDF + k) * nv + i] = ss[((int64_t)d * NDF + k) * nv + i];
+            }
+            A u[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) u[d] = VU[(int64_t)d * P.PG + g.goff + i];
+            moments_add_a<D, NDF, A>(u, VW[i], fv, m);
+        }
+        double mw[D + 2];
+        block_sum_ks<D + 2>(m, mw, sred);
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int e = 0; e < D + 2; ++e) wn[e] = mw[e];
+            get_prim<D>(mw, P.probs[P.dprob[cell]].gamma, pn);
+#pragma unroll
+            for (int d = 0; d < D; ++d) qn[d] = 0.0;
+        }
+        return;
+    }
+    // KG_ADAPT_COARSEN: vs_merge! of every child onto this grid (in child order), over 2^D
+    const A inv_children = (A)1 / (A)(1 << D);
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const int li = P.vlev[g.goff + i];
+        A acc[(D + 1) * NDF];
+#pragma unroll
+        for (int q = 0; q < (D + 1) * NDF; ++q) acc[q] = 0;
+        for (int c = 0; c < R.nsrc; ++c) {
+            const T* fs = V.f + R.src_f[c];
+            const T* ss = V.sdf + R.src_f[c] * D;
+            const int nvc = R.src_nv[c];
+            int j0 = i, cnt = 1;
+            if (R.run[c] >= 0) { j0 = V.runs[2 * (R.run[c] + i)]; cnt = V.runs[2 * (R.run[c] + i) + 1]; }
+            for (int j = j0; j < j0 + cnt; ++j) {
+                const int sh = R.run[c] >= 0 ? D * ((int)V.lev[R.lev[c] + j] - li) : 0;
+                const A div = sh > 0 ? (A)(1 << sh) : (A)1;
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) {
+                    const A v = (A)fs[(int64_t)k * nvc + j];
+                    acc[k] += sh > 0 ? v / div : v;
+#pragma unroll
+                    for (int d = 0; d < D; ++d) {
+                        const A sv = (A)ss[((int64_t)d * NDF + k) * nvc + j];
+                        acc[NDF + d * NDF + k] += sh > 0 ? sv / div : sv;
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            fn[(int64_t)k * nv + i] = (T)(acc[k] * inv_children);
+#pragma unroll
+            for (int d = 0; d < D; ++d) sn[((int64_t)d * NDF + k) * nv + i] = (T)(acc[NDF + d * NDF + k] * inv_children);
+        }
+    }
+    if (threadIdx.x == 0) {
+        double mw[D + 2];
+#pragma unroll
+        for (int e = 0; e < D + 2; ++e) {
+            double s = 0.0;
+            for (int c = 0; c < R.nsrc; ++c) s += V.w[(int64_t)R.src_d[c] * MAXW + e];
+            mw[e] = s / (double)(1 << D);
+            wn[e] = mw[e];
+        }
+        get_prim<D>(mw, P.probs[P.dprob[cell]].gamma, pn);
+#pragma unroll
+        for (int d = 0; d < D; ++d) qn[d] = 0.0;
+    }
+}
+
 template <int D, int NDF, typename T>
 struct Launch {
     static cudaError_t slope(const Dev& P, int pc_base, int n, cudaStream_t s) {
@@ -1646,6 +1793,15 @@ struct Launch {
     }
     // physical-space criterion of the fluid cells [fbegin, fbegin + n): loh from sw, then
     // the buffer layer into out (both per data item from dbase on)
+    // adapted-mesh state from the previous pools, one CTA per cell record
+    static cudaError_t adapt(const Dev& P, int n, const AdaptRec* recs, const void* f, const void* sdf, const double* w,
+                             const double* prim, const double* qf, const int32_t* runs, const int8_t* lev,
+                             cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        AdaptView<T> V{recs, (const T*)f, (const T*)sdf, w, prim, qf, runs, lev};
+        adapt_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, V);
+        return cudaGetLastError();
+    }
     static cudaError_t criterion(const Dev& P, int fbegin, int n, int dbase, const double* sw, double thr,
                                  double* loh, double* out, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;

@@ -89,6 +89,30 @@ def sod(scale: float = 1.0, max_level: int = 2, nv: int = 28) -> Problem:
     return Problem("sod", case, Gas(Kn=1e-2, K=1.0, omega=0.81, omega_r=0.81), cfl=CFL)
 
 
+def collision(center: float = 0.5, scale: float = 0.125, max_level: int = 1, nv: int = 12) -> Problem:
+    """Two streams meeting in a tube ([0,1]x[0,0.1], outflow in x, periodic in y): left
+    [1, 0.8, 0, 0.5], right [0.5, -0.8, 0, 0.8] with the jump at x = 0.47 (inside a tree, so
+    the children of one parent can sit on either side), refinement around x = center, and per
+    state a velocity grid refined by one level around its bulk velocity -- two grids each
+    finer than the other somewhere.  Moving `center` gives a second mesh of the same case
+    with cells kept, refined and coarsened (the adaptation tests)."""
+    tx = max(4, int(round(128 * scale)))
+
+    def ic(x):
+        return [1.0, 0.8, 0.0, 0.5] if x[0] < 0.47 else [0.5, -0.8, 0.0, 0.8]
+
+    def refine(mid, ds, L):
+        return abs(mid[0] - center) < 2.0 * ds[0]
+
+    case = M.Case(
+        dim=2, geometry=[0.0, 1.0, 0.0, 0.1], trees_num=[tx, 4], max_level=max_level,
+        quadrature=[-5.0, 5.0, -5.0, 5.0], vs_trees_num=[nv, nv],
+        domain_bc=[(M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_PERIOD, None), (M.BC_PERIOD, None)],
+        ic=ic, refine=refine if max_level > 0 else None, vgrid_fn=lambda prim: tuple(prim), vs_maxlevel=1,
+        gamma=5.0 / 3.0, K=1.0)
+    return Problem("collision", case, Gas(Kn=1e-2, K=1.0, omega=0.81, omega_r=0.81), cfl=CFL, vs_maxlevel=1)
+
+
 def couette(n: int = 16, nv: int = 16) -> Problem:
     case = M.Case(
         dim=2, geometry=[-0.5, 0.5, -0.5, 0.5], trees_num=[n, n], max_level=0,

@@ -716,6 +716,9 @@ def build_topology(case: Case, dtype_check: bool = True) -> Dict[str, np.ndarray
         face_here=np.array(F["here"], np.int32), face_there=np.array(F["there"], np.int32),
         face_there_midpoint=np.array(F["there_mid"], np.float64).reshape(-1),
         face_bc_kind=np.array(F["bck"], np.int8), face_bc=np.array(F["bc"], np.float64).reshape(-1),
+        # per cell its forest leaf (level, index...): not part of kg_topology, it lets two
+        # meshes of one case be matched cell by cell (adapt_sources)
+        cell_leaf=np.array([order[i] for i in cells], np.int64).reshape(ncell, 1 + dim),
     )
     # initial state (initialize_ps!, Solver/Initialize.jl:343-380): w from prim, f = Maxwellian
     K = case.K
@@ -741,3 +744,74 @@ def f_offsets(topo) -> np.ndarray:
     off = np.zeros(topo["n_cells"] + 1, np.int64)
     off[1:] = np.cumsum(nv * topo["ndf"])
     return off
+
+
+# --------------------------------------------------------------------------
+# adaptation between two meshes of one case (the replacement callbacks' record)
+# --------------------------------------------------------------------------
+from .abi import ADAPT_SRC, KG_ADAPT_COARSEN as ADAPT_COARSEN, KG_ADAPT_KEEP as ADAPT_KEEP  # noqa: E402
+from .abi import KG_ADAPT_REFINE as ADAPT_REFINE  # noqa: E402
+
+
+def adapt_sources(old: Dict, new: Dict) -> np.ndarray:
+    """Per cell of ``new``, where ps_replace! (Physical_space/AMR.jl:633-703) takes its
+    state from in ``old`` (kg_adapt_src records), by matching the meshes' leaves: the same
+    leaf (KEEP), a leaf below an old one (REFINE, child numbers in RMT order from the old
+    leaf down), or the parent of 2^dim old leaves (COARSEN, children in RMT order)."""
+    dim = int(new["dim"])
+    lo = {tuple(int(v) for v in x): i for i, x in enumerate(old["cell_leaf"])}
+    out = np.zeros(int(new["n_cells"]), ADAPT_SRC)
+    for c, x in enumerate(new["cell_leaf"]):
+        lf = tuple(int(v) for v in x)
+        L, idx = lf[0], lf[1:]
+        if lf in lo:
+            out[c]["kind"] = ADAPT_KEEP
+            out[c]["src"][0] = lo[lf]
+            continue
+        done = False
+        for up in range(1, L + 1):
+            anc = (L - up, *[v >> up for v in idx])
+            if anc in lo:
+                if up > 8:
+                    raise ValueError("refinement deeper than 8 levels in one adaptation")
+                out[c]["kind"] = ADAPT_REFINE
+                out[c]["depth"] = up
+                out[c]["src"][0] = lo[anc]
+                for s in range(1, up + 1):
+                    out[c]["path"][s - 1] = sum(((idx[d] >> (up - s)) & 1) << d for d in range(dim))
+                done = True
+                break
+        if done:
+            continue
+        ch = [(L + 1, *[2 * idx[d] + ((q >> d) & 1) for d in range(dim)]) for q in range(2 ** dim)]
+        if all(k in lo for k in ch):
+            out[c]["kind"] = ADAPT_COARSEN
+            out[c]["src"][:2 ** dim] = [lo[k] for k in ch]
+            continue
+        raise ValueError(f"cell {c} (leaf {lf}) is neither kept, refined nor a one-level coarsening")
+    return out
+
+
+def adapt_grids(old: Dict, new: Dict, src: np.ndarray) -> Dict:
+    """``new`` with the velocity grids ps_replace! gives its cells: a kept or refined cell
+    keeps its source's grid (ps_copy), a coarsened one takes the grid of its first child with
+    the fewest velocity cells (ps_merge).  The grid table becomes ``old``'s.  For meshes
+    without immersed boundaries (wall cut cells depend on the donor's grid)."""
+    if int(new["n_walls"]) > 0:
+        raise ValueError("adapt_grids: meshes with immersed-boundary walls keep their own grids")
+    dim = int(new["dim"])
+    out = dict(new)
+    for k in ("n_grids", "grid_off", "vs_level", "vs_weight", "vs_midpoint"):
+        out[k] = old[k]
+    goff = np.asarray(old["grid_off"])
+    nvg = goff[1:] - goff[:-1]
+    ocg = np.asarray(old["cell_grid"])
+    cg = np.empty(int(new["n_cells"]), np.int32)
+    for c, r in enumerate(src):
+        if r["kind"] == ADAPT_COARSEN:
+            ch = r["src"][:2 ** dim]
+            cg[c] = ocg[ch[int(np.argmin(nvg[ocg[ch]]))]]
+        else:
+            cg[c] = ocg[r["src"][0]]
+    out["cell_grid"] = cg
+    return out

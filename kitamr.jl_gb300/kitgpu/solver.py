@@ -53,6 +53,8 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_download_sw.argtypes = [vp, i32, vp]
     L.kg_criterion.argtypes = [vp, dbl, vp]
     L.kg_batch_criterion.argtypes = [vp, i32, dbl, vp]
+    L.kg_adapt.argtypes = [vp, vp, vp]
+    L.kg_batch_adapt.argtypes = [vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     _lib = L
     return L
@@ -65,6 +67,7 @@ EXPORTS = [
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
+    "kg_adapt", "kg_batch_adapt",
 ]
 
 
@@ -158,6 +161,19 @@ class GpuStep:
         lo = np.empty(self.nc * self.dim * (self.dim + 2))
         _check(self.L, self.h, self.L.kg_criterion(self.h, float(adapt_coeffi_ps), lo.ctypes.data))
         return lo.reshape(self.nc, self.dim, self.dim + 2)
+
+    def adapt(self, topo: Dict, src: np.ndarray):
+        """Move the device state onto the adapted mesh ``topo`` (kg_adapt); ``src`` holds one
+        abi.ADAPT_SRC record per cell of ``topo``.  A rejected plan leaves the handle as it was."""
+        tref = abi.TopologyRef(topo)
+        src = np.ascontiguousarray(src, dtype=abi.ADAPT_SRC)
+        if src.size != int(topo["n_cells"]):
+            raise ValueError("one adaptation record per cell of the new topology")
+        _check(self.L, self.h, self.L.kg_adapt(self.h, C.cast(tref.ptr, C.c_void_p), src.ctypes.data))
+        from .mesh import f_offsets
+        self.topo, self._tref = topo, tref
+        self.foff = f_offsets(topo)
+        self.nc = int(topo["n_cells"])
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
@@ -256,6 +272,16 @@ class GpuBatch:
         lo = np.empty(nc * dim * (dim + 2))
         _check(self.L, self.h, self.L.kg_batch_criterion(self.h, slot, float(adapt_coeffi_ps), lo.ctypes.data))
         return lo.reshape(nc, dim, dim + 2)
+
+    def adapt(self, slot: int, topo: Dict, src: np.ndarray):
+        """kg_batch_adapt: move one problem's state onto its adapted mesh ``topo``."""
+        tref = abi.TopologyRef(topo)
+        src = np.ascontiguousarray(src, dtype=abi.ADAPT_SRC)
+        if src.size != int(topo["n_cells"]):
+            raise ValueError("one adaptation record per cell of the new topology")
+        _check(self.L, self.h, self.L.kg_batch_adapt(self.h, slot, C.cast(tref.ptr, C.c_void_p), src.ctypes.data))
+        from .mesh import f_offsets
+        self.meta[slot] = (topo, f_offsets(topo))
 
     def info(self):
         n, fr, bpe = C.c_int32(), C.c_int64(), C.c_int64()

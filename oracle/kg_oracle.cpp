@@ -1125,6 +1125,133 @@ int kgo_run(const kg_params* prm, const kg_topology* t, double dt, int64_t step0
     return KG_OK;
 }
 
+// slope! alone (Flux/Slope.jl:1047-1070) on the state as it stands: the pass that
+// ps_adaptive_mesh_refinement! (Physical_space/AMR.jl:1108-1116) runs before the criterion.
+// sdf is overwritten; wall_f (the SolidNeighbor distributions) is read only.
+int kgo_slope(const kg_params* prm, const kg_topology* t, const double* f, double* sdf, const double* wall_f,
+              int32_t nthreads) {
+    Model m;
+    int rc = setup(m, prm, t);
+    if (rc) return rc;
+    m.f = const_cast<double*>(f); m.sdf = sdf;
+    m.nthreads = nthreads < 1 ? 1 : nthreads;
+    m.wall_f.assign(wall_f, wall_f + m.wfoff[t->n_walls]);
+    m.wall_sdf.assign(m.wsoff[t->n_walls], 0.0);
+    try {
+        slope(m);
+    } catch (...) {
+        return KG_ERR_TOPOLOGY;
+    }
+    return KG_OK;
+}
+
+// ---- physical-space adaptation: the state moves of ps_replace! (Physical_space/AMR.jl:633-703)
+// vs_merge! (AMR.jl:343-366): the level merge walk adding the cells of grid n onto grid p --
+// one-to-one on equal levels, finer cells over 2^(dim*Δl), a coarser cell into each cell it
+// covers.  cols: the columns of the nv x cols block (ndf for df, ndf*dim for sdf).
+static void vs_merge(int D, double* dst, const Grid& gp, const double* src, const Grid& gn, int cols) {
+    int j = 0;
+    double flag = 0.0;
+    for (int i = 0; i < gp.nv; ++i) {
+        const int li = gp.level[i];
+        if (li == gn.level[j]) {
+            for (int q = 0; q < cols; ++q) dst[(size_t)q * gp.nv + i] += src[(size_t)q * gn.nv + j];
+            j += 1;
+        } else if (li < gn.level[j]) {
+            while (flag != 1.0) {
+                const double div = std::ldexp(1.0, D * (gn.level[j] - li));
+                for (int q = 0; q < cols; ++q) dst[(size_t)q * gp.nv + i] += src[(size_t)q * gn.nv + j] / div;
+                flag += 1.0 / div;
+                j += 1;
+            }
+            flag = 0.0;
+        } else {
+            for (int q = 0; q < cols; ++q) dst[(size_t)q * gp.nv + i] += src[(size_t)q * gn.nv + j];
+            flag += 1.0 / std::ldexp(1.0, D * (li - gn.level[j]));
+            if (flag == 1.0) { j += 1; flag = 0.0; }
+        }
+    }
+}
+
+// The adapted mesh's state from the previous one, per new cell as src[c] says (see
+// kg_adapt_src): KEEP copies; REFINE is ps_replace!(::Val{1}) applied depth times (ps_copy,
+// ds halved, df += min(|df/(ds.|sdf| + EPS)|, 1) * (sdf . (ds/2 .* RMT[i])) with the parent's
+// sdf, then calc_w0 and get_prim); COARSEN is ps_merge + vs_merge! of df and sdf over the
+// children and the division by 2^dim.  qf of a replaced cell is zero (PsData's default).
+// The *_old arrays are the previous state with the slopes of its current f (slope! runs
+// before the replacements).
+int kgo_adapt(const kg_params* prm, const kg_topology* told, const kg_topology* tnew, const kg_adapt_src* src,
+              const double* f_old, const double* sdf_old, const double* w_old, const double* prim_old,
+              const double* qf_old, double* f_new, double* sdf_new, double* w_new, double* prim_new, double* qf_new) {
+    Model mo, mn;
+    int rc = setup(mo, prm, told);
+    if (rc) return rc;
+    if ((rc = setup(mn, prm, tnew))) return rc;
+    const int D = mn.dim, NDF = mn.ndf, NW = D + 2, nch = 1 << D;
+    for (int c = 0; c < tnew->n_cells; ++c) {
+        const kg_adapt_src& a = src[c];
+        const Grid& g = mn.grids[tnew->cell_grid[c]];
+        double* fn = f_new + mn.foff[c];
+        double* sn = sdf_new + mn.soff[c];
+        const size_t nf = (size_t)g.nv * NDF, ns = nf * D;
+        if (a.kind == KG_ADAPT_KEEP) {
+            const int o = a.src[0];
+            std::copy(f_old + mo.foff[o], f_old + mo.foff[o] + nf, fn);
+            std::copy(sdf_old + mo.soff[o], sdf_old + mo.soff[o] + ns, sn);
+            for (int e = 0; e < NW; ++e) { w_new[(size_t)c * NW + e] = w_old[(size_t)o * NW + e]; prim_new[(size_t)c * NW + e] = prim_old[(size_t)o * NW + e]; }
+            for (int d = 0; d < D; ++d) qf_new[(size_t)c * D + d] = qf_old[(size_t)o * D + d];
+        } else if (a.kind == KG_ADAPT_REFINE) {
+            const int o = a.src[0];
+            std::copy(f_old + mo.foff[o], f_old + mo.foff[o] + nf, fn);
+            std::copy(sdf_old + mo.soff[o], sdf_old + mo.soff[o] + ns, sn);
+            double ds[3];
+            for (int d = 0; d < D; ++d) ds[d] = told->cell_ds[(size_t)o * D + d];
+            for (int l = 0; l < a.depth; ++l) {
+                for (int d = 0; d < D; ++d) ds[d] *= 0.5;
+                double off[3];
+                for (int d = 0; d < D; ++d) off[d] = 0.5 * ds[d] * (((a.path[l] >> d) & 1) ? 1.0 : -1.0);
+                for (int k = 0; k < NDF; ++k)
+                    for (int j = 0; j < g.nv; ++j) {
+                        double den = 0.0, dot = 0.0;
+                        for (int d = 0; d < D; ++d) {
+                            den += ds[d] * std::fabs(Model::S(sn, g.nv, NDF, j, k, d));
+                            dot += Model::S(sn, g.nv, NDF, j, k, d) * off[d];
+                        }
+                        double& x = Model::F(fn, g.nv, j, k);
+                        x += std::min(std::fabs(x / (den + EPS_REF)), 1.0) * dot;
+                    }
+            }
+            calc_w0(mn, g, fn, w_new + (size_t)c * NW);
+            get_prim(mn, w_new + (size_t)c * NW, prim_new + (size_t)c * NW);
+            for (int d = 0; d < D; ++d) qf_new[(size_t)c * D + d] = 0.0;
+        } else if (a.kind == KG_ADAPT_COARSEN) {
+            double wsum[5];
+            for (int e = 0; e < NW; ++e) {
+                double s = w_old[(size_t)a.src[0] * NW + e];
+                for (int q = 1; q < nch; ++q) s += w_old[(size_t)a.src[q] * NW + e];
+                wsum[e] = s / nch;
+                w_new[(size_t)c * NW + e] = wsum[e];
+            }
+            get_prim(mn, wsum, prim_new + (size_t)c * NW);
+            std::fill(fn, fn + nf, 0.0);
+            std::fill(sn, sn + ns, 0.0);
+            for (int q = 0; q < nch; ++q) {
+                const int o = a.src[q];
+                const Grid& go = mo.grids[told->cell_grid[o]];
+                vs_merge(D, sn, g, sdf_old + mo.soff[o], go, NDF * D);
+                vs_merge(D, fn, g, f_old + mo.foff[o], go, NDF);
+            }
+            for (size_t e = 0; e < nf; ++e) fn[e] /= nch;
+            for (size_t e = 0; e < ns; ++e) sn[e] /= nch;
+            for (int d = 0; d < D; ++d) qf_new[(size_t)c * D + d] = 0.0;
+        } else {
+            g_err = "unknown adapt kind";
+            return KG_ERR_ARG;
+        }
+    }
+    return KG_OK;
+}
+
 // Moments (ρ, ρU, ρE) and heat flux of every cell's f relative to its prim
 // (micro_to_macro / calc_qf), for the known-answer tests.
 int kgo_moments(const kg_params* prm, const kg_topology* t, const double* f, const double* prim, double* w_out, double* q_out) {

@@ -38,6 +38,8 @@ def lib():
                                            C.POINTER(C.c_int32), C.c_int32]
         L.kgo_moments.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4
         L.kgo_macro_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 2
+        L.kgo_adapt.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 10
+        L.kgo_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + [C.c_int32]
         L.kgo_criterion.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + \
             [C.c_double, C.POINTER(C.c_double)]
         L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
@@ -96,11 +98,22 @@ class OracleState:
             raise RuntimeError(f"oracle macro_slope failed: {rc}")
         return sw.reshape(nc, dim, dim + 2)
 
+    def slope(self, params, nthreads: int = 1):
+        """slope! on the state as it stands (overwrites self.sdf)."""
+        rc = lib().kgo_slope(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.f),
+                             abi.dptr(self.sdf), abi.dptr(self.wall_f), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle slope failed: {rc}")
+        return self
+
     def criterion(self, params, adapt_coeffi_ps, sw=None):
         """PsData.lohner of every cell (update_criterion! + buffer layer) from this state's
-        w, prim and sw (default: macro_slope of its sdf), shape (n_cells, dim, dim + 2)."""
+        w, prim and sw, shape (n_cells, dim, dim + 2).  Without sw it follows
+        ps_adaptive_mesh_refinement! (Physical_space/AMR.jl:1108-1116): slope! on the current
+        f, then the criterion on the macro slopes of those slopes."""
         nc, dim = self.topo["n_cells"], self.topo["dim"]
         if sw is None:
+            self.slope(params)
             sw = self.macro_slope(params)
         sw = np.ascontiguousarray(sw, dtype=np.float64).reshape(-1)
         lo = np.zeros(nc * dim * (dim + 2))
@@ -109,6 +122,33 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle criterion failed: {rc}")
         return lo.reshape(nc, dim, dim + 2)
+
+    def adapt(self, params, topo_new: Dict, src: np.ndarray) -> "OracleState":
+        """The state on the adapted mesh topo_new (ps_replace!): slope! on the current f, then
+        per new cell the move src says (a kg_adapt_src record array, abi.ADAPT_SRC).  Returns
+        a new OracleState whose walls start from their donors' f (amr_recover!)."""
+        self.slope(params)
+        src = np.ascontiguousarray(src, dtype=abi.ADAPT_SRC)
+        assert src.size == topo_new["n_cells"]
+        tnew = abi.TopologyRef(topo_new)
+        n = [C.c_int64() for _ in range(4)]
+        lib().kgo_sizes(C.cast(tnew.ptr, C.c_void_p), *[C.byref(x) for x in n])
+        nf, nsdf = n[0].value, n[1].value
+        nc, dim = topo_new["n_cells"], topo_new["dim"]
+        f = np.zeros(max(nf, 1)); sdf = np.zeros(max(nsdf, 1))
+        w = np.zeros(nc * (dim + 2)); prim = np.zeros(nc * (dim + 2)); qf = np.zeros(max(nc * dim, 1))
+        rc = lib().kgo_adapt(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), C.cast(tnew.ptr, C.c_void_p),
+                             C.c_void_p(src.ctypes.data), abi.dptr(self.f), abi.dptr(self.sdf), abi.dptr(self.w),
+                             abi.dptr(self.prim), abi.dptr(self.qf), abi.dptr(f), abi.dptr(sdf), abi.dptr(w),
+                             abi.dptr(prim), abi.dptr(qf))
+        if rc != 0:
+            buf = C.create_string_buffer(512)
+            lib().kgo_last_error(buf, 512)
+            raise RuntimeError(f"oracle adapt failed: {abi.ERRORS.get(rc, rc)}: {buf.value.decode()}")
+        out = OracleState(topo_new, dict(f=f[:nf], w=w, prim=prim))
+        out.sdf[:] = sdf
+        out.qf[:] = qf
+        return out
 
     def moments(self, params):
         nc, nw = self.topo["n_cells"], self.topo["dim"] + 2

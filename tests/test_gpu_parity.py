@@ -143,8 +143,17 @@ def test_criterion_matches_oracle(name, make, nsteps):
     g.step(p.dt(), 0, nsteps)
     thr = 0.05
     got = g.criterion(thr)
+    sdf = g.download_state(sdf=True)["sdf"]
     g.close()
     exp = ref.criterion(prm, thr)
     assert np.any(exp > 0), "the case exercises the sensor"
     err = np.abs(got - exp)
     assert np.all(err <= 1e-9 * np.maximum(1.0, np.abs(exp))), (name, float(err.max()))
+    # the criterion ran on fresh slopes of the current f (slope! before update_criterion!),
+    # and they stay on the device
+    from kitgpu import mesh
+    off, dim = mesh.f_offsets(topo), topo["dim"]
+    mask = np.zeros(ref.sdf.size, bool)
+    for c in np.nonzero(np.asarray(topo["cell_bound_enc"]) >= 0)[0]:
+        mask[off[c] * dim:off[c + 1] * dim] = True
+    assert float(np.max(np.abs(sdf[mask] - ref.sdf[mask]))) <= 1e-12 * float(np.max(np.abs(ref.sdf[mask])))

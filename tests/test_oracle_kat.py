@@ -139,3 +139,106 @@ def test_criterion_flags_a_density_jump_and_its_buffer_layer():
     near = (d > ds) & (d < 2 * ds)
     assert np.all(lo[near] == 2 * thr)
     assert np.all(lo[d > 3 * ds] == 0.0)
+
+
+# ---- physical-space adaptation (ps_replace!) ----------------------------------------------
+def _adapt_pair(center_old=0.5, center_new=0.62, steps=3):
+    pa, pb = cases.collision(center=center_old), cases.collision(center=center_new)
+    ta, sa = cases.build(pa)
+    tb, _ = cases.build(pb)
+    src = mesh.adapt_sources(ta, tb)
+    tb = mesh.adapt_grids(ta, tb, src)
+    prm = abi.make_params(pa)
+    st = O.OracleState(ta, sa)
+    if steps:
+        st.run(prm, pa.dt(), 0, steps)
+    return pa, prm, ta, tb, src, st
+
+
+def _wmoments(prm, topo, f):
+    st = O.OracleState(topo, dict(f=f, w=np.zeros(topo["n_cells"] * (topo["dim"] + 2)),
+                                  prim=np.ones(topo["n_cells"] * (topo["dim"] + 2))))
+    return st.moments(prm)[0]
+
+
+def test_adapt_sources_follow_the_leaves():
+    _, _, ta, tb, src, _ = _adapt_pair(steps=0)
+    kinds = np.bincount(src["kind"], minlength=3)
+    assert kinds[abi.KG_ADAPT_KEEP] > 0 and kinds[abi.KG_ADAPT_REFINE] > 0 and kinds[abi.KG_ADAPT_COARSEN] > 0
+    la, lb = ta["cell_leaf"], tb["cell_leaf"]
+    for c, r in enumerate(src):
+        L, idx = lb[c][0], lb[c][1:]
+        if r["kind"] == abi.KG_ADAPT_KEEP:
+            assert tuple(la[r["src"][0]]) == tuple(lb[c])
+        elif r["kind"] == abi.KG_ADAPT_REFINE:
+            p = la[r["src"][0]]
+            assert p[0] == L - r["depth"] and all(p[1:] == idx >> r["depth"])
+        else:
+            for q in range(4):
+                ch = la[r["src"][q]]
+                assert ch[0] == L + 1 and all(ch[1:] == 2 * idx + np.array([(q >> d) & 1 for d in range(2)]))
+    # ps_merge: the coarsened cell keeps the grid of its first child with the fewest cells
+    goff = ta["grid_off"]
+    nvg = goff[1:] - goff[:-1]
+    for c in np.nonzero(src["kind"] == abi.KG_ADAPT_COARSEN)[0]:
+        ch = src[c]["src"][:4]
+        assert tb["cell_grid"][c] == ta["cell_grid"][ch[int(np.argmin(nvg[ta["cell_grid"][ch]]))]]
+
+
+def test_adapt_keep_everything_is_the_identity():
+    _, prm, ta, _, _, st = _adapt_pair()
+    src = mesh.adapt_sources(ta, ta)
+    assert np.all(src["kind"] == abi.KG_ADAPT_KEEP)
+    out = st.adapt(prm, ta, src)
+    assert np.array_equal(out.f, st.f) and np.array_equal(out.w, st.w) and np.array_equal(out.prim, st.prim)
+    assert np.array_equal(out.sdf, st.sdf) and np.array_equal(out.qf, st.qf)
+
+
+def test_adapt_refinement_offsets_cancel_over_the_children():
+    # one level everywhere: per velocity cell the 2^dim children share the limiter (same df,
+    # same |sdf|) and their offsets +-ds/4 cancel, so their mean is the parent's df
+    p = cases.collision(center=0.5, max_level=0)
+    ta, sa = cases.build(p)
+    p2 = cases.collision(center=0.5, max_level=0)
+    p2.case.max_level, p2.case.refine = 1, (lambda mid, ds, L: True)
+    tb, _ = cases.build(p2)
+    src = mesh.adapt_sources(ta, tb)
+    assert np.all(src["kind"] == abi.KG_ADAPT_REFINE)
+    tb = mesh.adapt_grids(ta, tb, src)
+    prm = abi.make_params(p)
+    st = O.OracleState(ta, sa).run(prm, p.dt(), 0, 4)
+    out = st.adapt(prm, tb, src)
+    offa, offb = mesh.f_offsets(ta), mesh.f_offsets(tb)
+    worst = 0.0
+    for parent in range(ta["n_cells"]):
+        kids = np.nonzero(src["src"][:, 0] == parent)[0]
+        assert kids.size == 4
+        mean = sum(out.f[offb[k]:offb[k + 1]] for k in kids) / 4
+        ref = st.f[offa[parent]:offa[parent + 1]]
+        worst = max(worst, np.max(np.abs(mean - ref)) / np.max(np.abs(ref)))
+    assert worst < 1e-14
+    # the slopes did move the children apart (near the jump)
+    spread = max(np.max(np.abs(out.f[offb[k]:offb[k + 1]] - out.f[offb[k + 1]:offb[k + 2]]))
+                 for k in range(0, tb["n_cells"], 4))
+    assert spread > 1e-3 * np.max(np.abs(st.f))
+    # ... and coarsening them back returns the parent's df
+    back_src = mesh.adapt_sources(tb, ta)
+    assert np.all(back_src["kind"] == abi.KG_ADAPT_COARSEN)
+    back = out.adapt(prm, mesh.adapt_grids(tb, ta, back_src), back_src)
+    assert np.max(np.abs(back.f - st.f)) / np.max(np.abs(st.f)) < 1e-14
+
+
+def test_adapt_coarsening_conserves_each_childs_mass_across_grids():
+    # vs_merge! onto another grid moves weight * df unchanged (a finer child cell adds df/2^(dΔl)
+    # to a cell 2^(dΔl) times heavier; a coarser one is injected into the cells it covers)
+    pa, prm, ta, tb, src, st = _adapt_pair()
+    out = st.adapt(prm, tb, src)
+    mixed = 0
+    wa, wb = _wmoments(prm, ta, st.f), _wmoments(prm, tb, out.f)
+    for c in np.nonzero(src["kind"] == abi.KG_ADAPT_COARSEN)[0]:
+        ch = src[c]["src"][:4]
+        mixed += len(set(ta["cell_grid"][ch])) > 1
+        assert abs(wb[c, 0] - wa[ch, 0].mean()) <= 1e-14 * abs(wb[c, 0])
+        # w of a coarsened cell is the children's mean (not the moments of the merged df)
+        assert np.allclose(out.w.reshape(-1, 4)[c], st.w.reshape(-1, 4)[ch].mean(axis=0), rtol=0, atol=1e-15)
+    assert mixed > 0, "the case must coarsen children that sit on different velocity grids"
