@@ -5,7 +5,7 @@ Workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x6
 synthetic initial state; 61 M phase cells, so f is far larger than L2 between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-  python bench.py --mode sphere | batched | serve   (the other workloads, one line each)
+  python bench.py --mode sphere | batched | serve | adapt   (the other workloads, one line each)
 
 Metric: phase-cell updates/s of the mixed-precision form (FP32 f, compensated moments,
 FP64 conserved update), with the plain FP64 form, the roofline of the dominant kernel, the
@@ -15,6 +15,8 @@ Other modes:
 * sphere: the 3D Ma 3 sphere at half its base mesh (183 M phase cells).
 * batched: 256 Sod / cavity problems in one batch handle.
 * serve: Poisson arrivals solved to residual < 1e-6.
+* adapt: one physical-space adaptation of the cylinder on the device (criterion, then the
+  refine / coarsen moves of f) against the host route (f down, new topology and f up).
 """
 from __future__ import annotations
 
@@ -299,6 +301,108 @@ def run_serve(args):
             "forms": out}
 
 
+def cylinder_after_adaptation():
+    """The cylinder mesh after one physical-space adaptation: a band refined downstream and
+    the outer level-1 ring coarsened upstream; the cells at the wall are unchanged."""
+    p = make_problem(1.0)
+    base = p.case.refine
+
+    def refine(mid, ds, L):
+        if L == 0 and mid[0] > 5.0 and abs(mid[1]) < 2.0:
+            return True
+        if L == 1 and mid[0] < -3.0:
+            return False
+        return base(mid, ds, L)
+    p.case.refine = refine
+    return p
+
+
+def run_adapt(args):
+    """Cost of one physical-space adaptation of the cylinder (mixed form): the device route
+    (kg_criterion, then kg_adapt with the new topology and the per-cell sources) against the
+    host route it replaces (f down, the new topology and f up)."""
+    import torch
+    from kitgpu import abi, cases, mesh
+    from kitgpu.solver import GpuStep
+    pa = make_problem(1.0)
+    ta, sa = cases.build(pa)
+    tb, _ = cases.build(cylinder_after_adaptation())
+    fwd = mesh.adapt_sources(ta, tb)
+    tb = mesh.adapt_grids(ta, tb, fwd)
+    back = mesh.adapt_sources(tb, ta)
+    ta2 = mesh.adapt_grids(tb, ta, back)
+    kinds = np.bincount(fwd["kind"], minlength=3)
+    prm = abi.make_params(pa, precision=abi.KG_PREC_MIXED, st_check_interval=100)
+    dt = pa.dt()
+    g = GpuStep(prm, ta)
+    g.upload_state(sa["f"], sa["w"], sa["prim"])
+    g.step(dt, 0, args.warmup)
+    step = args.warmup
+    crit, adapt = [], []
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.criterion(0.05)
+        t1 = time.perf_counter()
+        g.adapt(tb, fwd) if k % 2 == 0 else g.adapt(ta2, back)
+        t2 = time.perf_counter()
+        crit.append((t1 - t0) * 1e3)
+        adapt.append((t2 - t1) * 1e3)
+        g.step(dt, step, 1)
+        step += 1
+    g.close()
+    # flattening alone (host), the part of kg_adapt that is not device work
+    from kitgpu.solver import load_library
+    import ctypes as C
+    L = load_library()
+    tref = abi.TopologyRef(tb)
+    b = C.c_int64()
+    t0 = time.perf_counter()
+    L.kg_topology_footprint(C.byref(prm), C.cast(tref.ptr, C.c_void_p), C.byref(b))
+    flatten_ms = (time.perf_counter() - t0) * 1e3
+    # host route: download f / w / prim, upload the new topology and a state of its size
+    h = GpuStep(prm, ta)
+    h.upload_state(sa["f"], sa["w"], sa["prim"])
+    h.step(dt, 0, 1)
+    nfb = int(mesh.f_offsets(tb)[-1])
+    fb = np.ones(nfb)
+    wb = np.tile(sa["w"][:4], tb["n_cells"])
+    host = []
+    for k in range(max(3, args.steps // 4)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = h.download_state()
+        t1 = time.perf_counter()
+        if k % 2 == 0:
+            L.kg_upload_topology(h.h, C.cast(tref.ptr, C.c_void_p))
+            h.L.kg_upload_state(h.h, fb.ctypes.data, wb.ctypes.data, wb.ctypes.data)
+            h.nc, h.foff = int(tb["n_cells"]), mesh.f_offsets(tb)
+        else:
+            ta_ref = abi.TopologyRef(ta)
+            L.kg_upload_topology(h.h, C.cast(ta_ref.ptr, C.c_void_p))
+            h.L.kg_upload_state(h.h, sa["f"].ctypes.data, sa["w"].ctypes.data, sa["prim"].ctypes.data)
+            h.nc, h.foff = int(ta["n_cells"]), mesh.f_offsets(ta)
+        t2 = time.perf_counter()
+        host.append(((t1 - t0) * 1e3, (t2 - t1) * 1e3, out["f"].nbytes))
+    h.close()
+    med = lambda v: float(np.median(v))
+    dev_total = med([a + b_ for a, b_ in zip(crit, adapt)])
+    host_total = med([a + b_ for a, b_, _ in host])
+    return {"metric": "physical-space adaptation time (criterion + refine/coarsen of the state)", "value": dev_total,
+            "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32-f/f64-moments", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " adapted: band refined downstream, ring coarsened upstream",
+                       "cells": [int(ta["n_cells"]), int(tb["n_cells"])], "kept": int(kinds[0]),
+                       "refined": int(kinds[1]), "coarsened": int(kinds[2]),
+                       "phase_cells": [mesh.phase_cells(ta), mesh.phase_cells(tb)]},
+            "device_route": {"criterion_ms": med(crit), "adapt_ms": med(adapt), "flatten_ms": flatten_ms,
+                             "lohner_bytes_down": int(ta["n_cells"]) * 8 * 8},
+            "host_route": {"download_ms": med([x[0] for x in host]), "upload_ms": med([x[1] for x in host]),
+                           "total_ms": host_total, "f_bytes_down": int(host[0][2]),
+                           "note": "transfers and re-upload only; the host-side interpolation itself is extra"},
+            "device_over_host": dev_total / host_total}
+
+
 def cpu_baseline(threads, budget_s=12.0, mode="cylinder"):
     import oracle as O
     from kitgpu import abi, cases, mesh
@@ -328,7 +432,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=None,
                     help="scale of the base mesh (default: the workload's own; smaller for profiling captures)")
-    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "batched", "serve"])
+    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "batched", "serve", "adapt"])
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
@@ -380,6 +484,11 @@ def main():
         return
     if args.mode == "serve":
         line = run_serve(args)
+        if rank == 0:
+            print(json.dumps(line))
+        return
+    if args.mode == "adapt":
+        line = run_adapt(args)
         if rank == 0:
             print(json.dumps(line))
         return

@@ -795,10 +795,8 @@ def adapt_sources(old: Dict, new: Dict) -> np.ndarray:
 def adapt_grids(old: Dict, new: Dict, src: np.ndarray) -> Dict:
     """``new`` with the velocity grids ps_replace! gives its cells: a kept or refined cell
     keeps its source's grid (ps_copy), a coarsened one takes the grid of its first child with
-    the fewest velocity cells (ps_merge).  The grid table becomes ``old``'s.  For meshes
-    without immersed boundaries (wall cut cells depend on the donor's grid)."""
-    if int(new["n_walls"]) > 0:
-        raise ValueError("adapt_grids: meshes with immersed-boundary walls keep their own grids")
+    the fewest velocity cells (ps_merge).  The grid table becomes ``old``'s.  A wall's cut
+    cells were computed on its donor's grid in ``new``, so every donor must keep that grid."""
     dim = int(new["dim"])
     out = dict(new)
     for k in ("n_grids", "grid_off", "vs_level", "vs_weight", "vs_midpoint"):
@@ -814,4 +812,14 @@ def adapt_grids(old: Dict, new: Dict, src: np.ndarray) -> Dict:
         else:
             cg[c] = ocg[r["src"][0]]
     out["cell_grid"] = cg
+
+    def grid_arrays(t, g):
+        o = np.asarray(t["grid_off"])
+        a, b = int(o[g]), int(o[g + 1])
+        return (np.asarray(t["vs_level"])[a:b], np.asarray(t["vs_weight"])[a:b],
+                np.asarray(t["vs_midpoint"])[a * dim:b * dim])
+    for dn in np.unique(np.asarray(new["wall_donor"], np.int64)):
+        ga, gb = grid_arrays(old, int(cg[dn])), grid_arrays(new, int(new["cell_grid"][dn]))
+        if not all(np.array_equal(x, y) for x, y in zip(ga, gb)):
+            raise ValueError(f"wall donor {dn} changes its velocity grid; its cut cells would not match")
     return out

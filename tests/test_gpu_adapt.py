@@ -15,8 +15,7 @@ def _meshes(make_old, make_new):
     ta, sa = cases.build(pa)
     tb, _ = cases.build(pb)
     src = mesh.adapt_sources(ta, tb)
-    if tb["n_walls"] == 0:
-        tb = mesh.adapt_grids(ta, tb, src)
+    tb = mesh.adapt_grids(ta, tb, src)
     return pa, ta, sa, tb, src
 
 
