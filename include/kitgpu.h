@@ -246,6 +246,23 @@ typedef struct {
 } kg_adapt_src;
 int kg_adapt(kg_handle *h, const kg_topology *topo, const kg_adapt_src *src);
 
+/* ---- checkpoint payload from the device (save_for_restart / restart, IO/Restart.jl) --------
+ * kg_download_restart fills the per-rank arrays of restart_<rank>.jld2 that come from the
+ * state (IO/Restart.jl:81-117), in FP64:
+ *   vs_df  the Nv x ndf column-major matrix of every cell's VsData.df stacked in cell order
+ *          (Nv = the sum of the cells' velocity-cell counts; column k holds df[:, k]);
+ *   ws     the n_quads x (dim+2) column-major matrix of PsData.w, row quad_index[c] for cell
+ *          c; rows of quadrants without a distribution function (InsideSolidData) are zero.
+ * quad_index may be NULL (row c for cell c; n_quads must then equal n_cells); either output
+ * may be NULL.  vs_nums, bound_encs, vs_levels and vs_midpoints are topology the caller holds.
+ * kg_upload_restart is the inverse as restart() builds its PsData (IO/Restart.jl:300-325):
+ * f from vs_df, w from ws, prim = get_prim(w) (on the device), qf and slopes zero, walls from
+ * their donors; the topology must be uploaded first.  Together they resume a run bit for bit
+ * in the FP64 form (the mixed form stores f in FP32).                                     */
+int kg_download_restart(kg_handle *h, const int32_t *quad_index, int32_t n_quads, double *vs_df, double *ws);
+int kg_upload_restart(kg_handle *h, const int32_t *quad_index, int32_t n_quads, const double *vs_df,
+                      const double *ws);
+
 /* Advance `nsteps` steps with time step dt; `step` is status.step before the
  * first of them (drives the residual cadence).  One call = nsteps x
  * (slope -> flux -> iterate).                                               */
@@ -298,6 +315,8 @@ int kg_batch_criterion(kg_handle *h, int32_t slot, double adapt_coeffi_ps, doubl
 /* kg_adapt of one problem: its new slabs are placed while the previous ones are live, then
  * the previous ones are released (KG_ERR_BUDGET when the pool cannot hold both).            */
 int kg_batch_adapt(kg_handle *h, int32_t slot, const kg_topology *topo, const kg_adapt_src *src);
+int kg_batch_download_restart(kg_handle *h, int32_t slot, const int32_t *quad_index, int32_t n_quads,
+                              double *vs_df, double *ws);   /* kg_download_restart of one problem */
 int kg_batch_info(const kg_handle *h, int32_t *n_live, int64_t *f_free_elems, int64_t *bytes_per_elem);
 int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
 

@@ -53,6 +53,33 @@ __global__ void copy_blocks(T* f, const int64_t* tri) {
     const int64_t src = t[0], dst = t[1], len = t[2];
     for (int64_t i = threadIdx.x; i < len; i += blockDim.x) f[dst + i] = f[src + i];
 }
+// The checkpoint layout of save_for_restart (IO/Restart.jl:100-117): column k of the
+// nv_total x ndf matrix vs_df stacks VsData.df[:, k] of every cell in cell order.  foff:
+// the cells' f offsets (ndf * nv blocks, k-major), so a cell's first row is foff[c] / ndf.
+template <typename T>
+__global__ void restart_gather(const T* __restrict__ f, const int64_t* __restrict__ foff, int ncell, int ndf,
+                               int64_t nv_total, double* __restrict__ out) {
+    for (int c = blockIdx.x; c < ncell; c += gridDim.x) {
+        const int64_t o = foff[c], nv = (foff[c + 1] - o) / ndf, r0 = o / ndf;
+        for (int k = 0; k < ndf; ++k)
+            for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) out[k * nv_total + r0 + i] = (double)f[o + k * nv + i];
+    }
+}
+template <typename T>
+__global__ void restart_scatter(const double* __restrict__ in, const int64_t* __restrict__ foff, int ncell, int ndf,
+                                int64_t nv_total, T* __restrict__ f) {
+    for (int c = blockIdx.x; c < ncell; c += gridDim.x) {
+        const int64_t o = foff[c], nv = (foff[c + 1] - o) / ndf, r0 = o / ndf;
+        for (int k = 0; k < ndf; ++k)
+            for (int64_t i = threadIdx.x; i < nv; i += blockDim.x) f[o + k * nv + i] = (T)in[k * nv_total + r0 + i];
+    }
+}
+// prim = get_prim(w) of data items [0, n) (rows of MAXW), as restart() builds its PsData
+template <int D>
+__global__ void prim_of_w(const double* __restrict__ w, double* __restrict__ prim, int n, double gamma) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c < n) get_prim<D>(w + (int64_t)c * MAXW, gamma, prim + (int64_t)c * MAXW);
+}
 }  // namespace
 
 void kg::set_global_error(const std::string& msg) { g_create_err = msg; }
@@ -979,6 +1006,125 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     return KG_OK;
 }
 
+// ---- checkpoint payload (save_for_restart / restart, IO/Restart.jl) ----------------------
+int check_quads(kg_handle* h, const Flat& L, const int32_t* quad_index, int32_t n_quads) {
+    if (!quad_index) {
+        if (n_quads != L.n_cells) return fail(h, KG_ERR_ARG, "without quad_index, n_quads must equal the number of cells");
+        return KG_OK;
+    }
+    if (n_quads < L.n_cells) return fail(h, KG_ERR_ARG, "n_quads is smaller than the number of cells");
+    std::vector<char> seen((size_t)n_quads, 0);
+    for (int c = 0; c < L.n_cells; ++c) {
+        const int32_t q = quad_index[c];
+        if (q < 0 || q >= n_quads || seen[q]) return fail(h, KG_ERR_ARG, "quad_index out of range or repeated");
+        seen[q] = 1;
+    }
+    return KG_OK;
+}
+
+// A device buffer of n doubles for the checkpoint matrix: the problem's staging slab in the
+// mixed form, a temporary allocation in FP64 (*tmp is then set and must be freed).
+int restart_buffer(kg_handle* h, const Problem& pb, int64_t n, double** buf, void** tmp) {
+    *tmp = nullptr;
+    if (h->staging && n <= pb.fsize) { *buf = h->staging + pb.fbase; return KG_OK; }
+    cudaError_t e = cudaMalloc(tmp, sizeof(double) * (size_t)std::max<int64_t>(n, 1));
+    if (e != cudaSuccess) { *tmp = nullptr; return fail(h, KG_ERR_NOMEM, "cudaMalloc checkpoint buffer"); }
+    *buf = (double*)*tmp;
+    return KG_OK;
+}
+
+int download_restart(kg_handle* h, int slot, const int32_t* quad_index, int32_t n_quads, double* vs_df, double* ws) {
+    int rc;
+    Problem& pb = h->probs[slot];
+    const Flat& L = pb.F;
+    if ((rc = check_quads(h, L, quad_index, n_quads))) return rc;
+    const int D = h->prm.dim, NDF = h->prm.ndf, NW = D + 2, NC = L.n_cells;
+    const int64_t nv_total = L.foff[NC] / NDF;
+    if (vs_df) {
+        double* buf = nullptr;
+        void* tmp = nullptr;
+        if ((rc = restart_buffer(h, pb, NDF * nv_total, &buf, &tmp))) return rc;
+        const int64_t* dfo = nullptr;
+        void* fo = nullptr;
+        cudaError_t e = cudaMalloc(&fo, sizeof(int64_t) * (NC + 1));
+        if (e == cudaSuccess) {
+            dfo = (const int64_t*)fo;
+            e = cudaMemcpyAsync(fo, L.foff.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, h->stream);
+        }
+        const size_t ss = storage_size(h);
+        const char* fin = (const char*)(h->parity == 0 ? h->fA : h->fB) + pb.fbase * ss;
+        const int grid = std::min(NC, 152 * 8);
+        if (e == cudaSuccess) {
+            if (h->prm.precision == KG_PREC_FP64) restart_gather<double><<<grid, 256, 0, h->stream>>>((const double*)fin, dfo, NC, NDF, nv_total, buf);
+            else restart_gather<float><<<grid, 256, 0, h->stream>>>((const float*)fin, dfo, NC, NDF, nv_total, buf);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(vs_df, buf, sizeof(double) * NDF * nv_total, cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (fo) cudaFree(fo);
+        if (tmp) cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(h, e, "restart gather");
+    }
+    if (ws) {
+        std::vector<double> pw((size_t)pb.dsize * MAXW);
+        KG_CUDA(h, cudaMemcpyAsync(pw.data(), h->w + pb.dbase * MAXW, sizeof(double) * pw.size(), cudaMemcpyDeviceToHost, h->stream));
+        KG_CUDA(h, cudaStreamSynchronize(h->stream));
+        std::fill(ws, ws + (size_t)n_quads * NW, 0.0);
+        for (int c = 0; c < NC; ++c) {
+            const int64_t q = quad_index ? quad_index[c] : c;
+            for (int e = 0; e < NW; ++e) ws[(size_t)e * n_quads + q] = pw[(size_t)c * MAXW + e];
+        }
+    }
+    return KG_OK;
+}
+
+int upload_restart(kg_handle* h, int slot, const int32_t* quad_index, int32_t n_quads, const double* vs_df,
+                   const double* ws, int64_t step) {
+    int rc;
+    Problem& pb = h->probs[slot];
+    const Flat& L = pb.F;
+    if ((rc = check_quads(h, L, quad_index, n_quads))) return rc;
+    const int D = h->prm.dim, NDF = h->prm.ndf, NW = D + 2, NC = L.n_cells;
+    const int64_t nv_total = L.foff[NC] / NDF;
+    const size_t ss = storage_size(h);
+    char* fa = (char*)(h->parity == 0 ? h->fA : h->fB) + pb.fbase * ss;
+    double* buf = nullptr;
+    void* tmp = nullptr;
+    if ((rc = restart_buffer(h, pb, NDF * nv_total, &buf, &tmp))) return rc;
+    void* fo = nullptr;
+    cudaError_t e = cudaMalloc(&fo, sizeof(int64_t) * (NC + 1));
+    if (e == cudaSuccess) e = cudaMemcpyAsync(fo, L.foff.data(), sizeof(int64_t) * (NC + 1), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf, vs_df, sizeof(double) * NDF * nv_total, cudaMemcpyHostToDevice, h->stream);
+    const int grid = std::min(NC, 152 * 8);
+    if (e == cudaSuccess) {
+        if (h->prm.precision == KG_PREC_FP64) restart_scatter<double><<<grid, 256, 0, h->stream>>>(buf, (const int64_t*)fo, NC, NDF, nv_total, (double*)fa);
+        else restart_scatter<float><<<grid, 256, 0, h->stream>>>(buf, (const int64_t*)fo, NC, NDF, nv_total, (float*)fa);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (fo) cudaFree(fo);
+    if (tmp) cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(h, e, "restart scatter");
+    if ((rc = init_wall_blocks(h, slot, fa))) return rc;
+    // w from ws; prim = get_prim(w) on the device; slopes and qf zero (restart's PsData)
+    std::vector<double> pw((size_t)pb.dsize * MAXW, 0.0);
+    for (int c = 0; c < NC; ++c) {
+        const int64_t q = quad_index ? quad_index[c] : c;
+        for (int k = 0; k < NW; ++k) pw[(size_t)c * MAXW + k] = ws[(size_t)k * n_quads + q];
+    }
+    KG_CUDA(h, cudaMemcpyAsync(h->w + pb.dbase * MAXW, pw.data(), sizeof(double) * pw.size(), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->prim + pb.dbase * MAXW, 0, sizeof(double) * pb.dsize * MAXW, h->stream));
+    if (D == 2) prim_of_w<2><<<(NC + 127) / 128, 128, 0, h->stream>>>(h->w + pb.dbase * MAXW, h->prim + pb.dbase * MAXW, NC, pb.pp.gamma);
+    else prim_of_w<3><<<(NC + 127) / 128, 128, 0, h->stream>>>(h->w + pb.dbase * MAXW, h->prim + pb.dbase * MAXW, NC, pb.pp.gamma);
+    KG_CUDA(h, cudaGetLastError());
+    KG_CUDA(h, cudaMemsetAsync((char*)h->sdf + pb.fbase * D * ss, 0, pb.fsize * D * ss, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->qf + pb.dbase * MAXD, 0, sizeof(double) * pb.dsize * MAXD, h->stream));
+    KG_CUDA(h, cudaMemcpyAsync(h->d_step + slot, &step, sizeof(int64_t), cudaMemcpyHostToDevice, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->d_status + slot, 0, sizeof(int), h->stream));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));   // host temporaries
+    return KG_OK;
+}
+
 int check_params(const kg_params* params, std::string& err) {
     if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) { err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1"; return KG_ERR_ARG; }
     if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { err = "bad precision"; return KG_ERR_ARG; }
@@ -1115,6 +1261,28 @@ int kg_adapt(kg_handle* h, const kg_topology* topo, const kg_adapt_src* src) {
     if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
     cudaSetDevice(h->device);
     return adapt_problem(h, 0, topo, src);
+}
+
+int kg_download_restart(kg_handle* h, const int32_t* quad_index, int32_t n_quads, double* vs_df, double* ws) {
+    if (!h) return KG_ERR_ARG;
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_download_restart");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return download_restart(h, 0, quad_index, n_quads, vs_df, ws);
+}
+
+int kg_upload_restart(kg_handle* h, const int32_t* quad_index, int32_t n_quads, const double* vs_df, const double* ws) {
+    if (!h || !vs_df || !ws) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch || h->probs.empty() || h->probs[0].F.n_data == 0) return fail(h, KG_ERR_STATE, "upload a topology first");
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    Problem& pb = h->probs[0];
+    const bool was_live = pb.live;
+    if (!pb.live) { pb.live = true; h->dirty = true; }
+    int rc = upload_restart(h, 0, quad_index, n_quads, vs_df, ws, 0);
+    if (rc) { if (!was_live) pb.live = false; return rc; }
+    h->have_state = true;
+    return KG_OK;
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
@@ -1290,6 +1458,12 @@ int kg_batch_adapt(kg_handle* h, int32_t slot, const kg_topology* topo, const kg
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
     return adapt_problem(h, slot, topo, src);
+}
+
+int kg_batch_download_restart(kg_handle* h, int32_t slot, const int32_t* quad_index, int32_t n_quads, double* vs_df, double* ws) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    cudaSetDevice(h->device);
+    return download_restart(h, slot, quad_index, n_quads, vs_df, ws);
 }
 
 int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {

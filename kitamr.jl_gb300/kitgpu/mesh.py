@@ -719,6 +719,9 @@ def build_topology(case: Case, dtype_check: bool = True) -> Dict[str, np.ndarray
         # per cell its forest leaf (level, index...): not part of kg_topology, it lets two
         # meshes of one case be matched cell by cell (adapt_sources)
         cell_leaf=np.array([order[i] for i in cells], np.int64).reshape(ncell, 1 + dim),
+        # per cell its position among all leaves (InsideSolidData included), and their count:
+        # the quadrant order of the reference's per-rank checkpoint arrays
+        cell_quad=np.array(cells, np.int32), n_quads=nleaf,
     )
     # initial state (initialize_ps!, Solver/Initialize.jl:343-380): w from prim, f = Maxwellian
     K = case.K

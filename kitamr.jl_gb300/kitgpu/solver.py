@@ -55,6 +55,9 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_criterion.argtypes = [vp, i32, dbl, vp]
     L.kg_adapt.argtypes = [vp, vp, vp]
     L.kg_batch_adapt.argtypes = [vp, i32, vp, vp]
+    L.kg_download_restart.argtypes = [vp, vp, i32, vp, vp]
+    L.kg_upload_restart.argtypes = [vp, vp, i32, vp, vp]
+    L.kg_batch_download_restart.argtypes = [vp, i32, vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     _lib = L
     return L
@@ -67,7 +70,7 @@ EXPORTS = [
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
-    "kg_adapt", "kg_batch_adapt",
+    "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
 ]
 
 
@@ -174,6 +177,25 @@ class GpuStep:
         self.topo, self._tref = topo, tref
         self.foff = f_offsets(topo)
         self.nc = int(topo["n_cells"])
+
+    def download_restart(self, quad_index: Optional[np.ndarray] = None, n_quads: Optional[int] = None):
+        """The state arrays of save_for_restart: vs_df (Nv x ndf) and ws (n_quads x dim+2)."""
+        ndf = int(self.topo["ndf"])
+        nq = self.nc if n_quads is None else int(n_quads)
+        qi = None if quad_index is None else np.ascontiguousarray(quad_index, dtype=np.int32)
+        vs_df = np.empty(int(self.foff[self.nc]), dtype=np.float64)
+        ws = np.empty(nq * (self.dim + 2))
+        _check(self.L, self.h, self.L.kg_download_restart(self.h, None if qi is None else qi.ctypes.data, nq,
+                                                            vs_df.ctypes.data, ws.ctypes.data))
+        return vs_df.reshape(ndf, -1).T, ws.reshape(self.dim + 2, nq).T
+
+    def upload_restart(self, vs_df: np.ndarray, ws: np.ndarray, quad_index: Optional[np.ndarray] = None):
+        """restart(): f from vs_df, w from ws, prim = get_prim(w)."""
+        vs = np.asfortranarray(vs_df, dtype=np.float64)
+        wsf = np.asfortranarray(ws, dtype=np.float64)
+        qi = None if quad_index is None else np.ascontiguousarray(quad_index, dtype=np.int32)
+        _check(self.L, self.h, self.L.kg_upload_restart(self.h, None if qi is None else qi.ctypes.data,
+                                                          int(wsf.shape[0]), vs.ctypes.data, wsf.ctypes.data))
 
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
@@ -282,6 +304,17 @@ class GpuBatch:
         _check(self.L, self.h, self.L.kg_batch_adapt(self.h, slot, C.cast(tref.ptr, C.c_void_p), src.ctypes.data))
         from .mesh import f_offsets
         self.meta[slot] = (topo, f_offsets(topo))
+
+    def download_restart(self, slot: int, quad_index: Optional[np.ndarray] = None, n_quads: Optional[int] = None):
+        topo, foff = self.meta[slot]
+        nc, dim, ndf = int(topo["n_cells"]), int(topo["dim"]), int(topo["ndf"])
+        nq = nc if n_quads is None else int(n_quads)
+        qi = None if quad_index is None else np.ascontiguousarray(quad_index, dtype=np.int32)
+        vs_df = np.empty(int(foff[nc]), dtype=np.float64)
+        ws = np.empty(nq * (dim + 2))
+        _check(self.L, self.h, self.L.kg_batch_download_restart(self.h, slot, None if qi is None else qi.ctypes.data,
+                                                                  nq, vs_df.ctypes.data, ws.ctypes.data))
+        return vs_df.reshape(ndf, -1).T, ws.reshape(dim + 2, nq).T
 
     def info(self):
         n, fr, bpe = C.c_int32(), C.c_int64(), C.c_int64()
