@@ -339,6 +339,7 @@ def run_adapt(args):
     g.step(dt, 0, args.warmup)
     step = args.warmup
     crit, adapt = [], []
+    g.profile(True)         # host phase times of kg_adapt (the steps between run untimed)
     for k in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -350,6 +351,7 @@ def run_adapt(args):
         adapt.append((t2 - t1) * 1e3)
         g.step(dt, step, 1)
         step += 1
+    phases = {k: v[0] / max(v[1], 1) for k, v in g.profile_read().items() if k.startswith("adapt:")}
     g.close()
     # flattening alone (host), the part of kg_adapt that is not device work
     from kitgpu.solver import load_library
@@ -396,6 +398,7 @@ def run_adapt(args):
                        "refined": int(kinds[1]), "coarsened": int(kinds[2]),
                        "phase_cells": [mesh.phase_cells(ta), mesh.phase_cells(tb)]},
             "device_route": {"criterion_ms": med(crit), "adapt_ms": med(adapt), "flatten_ms": flatten_ms,
+                             "adapt_phases_ms": phases,
                              "lohner_bytes_down": int(ta["n_cells"]) * 8 * 8},
             "host_route": {"download_ms": med([x[0] for x in host]), "upload_ms": med([x[1] for x in host]),
                            "total_ms": host_total, "f_bytes_down": int(host[0][2]),

@@ -1,6 +1,7 @@
 // kg_api.cu -- the C-ABI of libkitgpu.so (include/kitgpu.h).
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -898,10 +899,26 @@ int build_adapt_plan(kg_handle* h, const Flat& Fo, int64_t fbo, int64_t dbo, con
 // device from the previous one.  Single handle: the previous pools stay alive until the new
 // ones are filled.  Batch: the new slabs are placed beside the previous ones in the shared
 // pools, then the previous ones are released.
+// With profiling on, host wall time of the phases of an adaptation (ms, into the profile table).
+struct PhaseClock {
+    kg_handle* h;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char* name) {
+        if (!h->prof) return;
+        const auto n = std::chrono::steady_clock::now();
+        const int k = prof_slot(h, name);
+        h->pms[k] += std::chrono::duration<double, std::milli>(n - t).count();
+        h->pcount[k] += 1;
+        t = n;
+    }
+};
+
 int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adapt_src* src) {
+    PhaseClock clk{h};
     Flat Fn;
     std::string err;
     int rc = flatten(h->prm, *topo, Fn, err);
+    clk.mark("adapt:flatten");
     if (rc) return fail(h, rc, err);
     if (Fn.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
     // ps_adaptive_mesh_refinement! runs slope! before the replacements read the slopes
@@ -913,9 +930,11 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
         KG_CUDA(h, enqueue_slopes(h, P, h->stream));
     }
     KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    clk.mark("adapt:slopes");
     // every check before the handle changes: a rejected adaptation leaves it as it was
     AdaptPlan plan;
     if ((rc = build_adapt_plan(h, h->probs[slot].F, h->probs[slot].fbase, h->probs[slot].dbase, Fn, 0, src, plan))) return rc;
+    clk.mark("adapt:plan");
     Problem old = std::move(h->probs[slot]);
     h->probs[slot] = Problem();
     // the previous state: pointers into pools that stay alive until the end of this call
@@ -952,7 +971,9 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     pb.live = true;
     h->dirty = true;
     for (AdaptRec& r : plan.recs) r.cell += (int32_t)pb.dbase;
+    clk.mark("adapt:pools");
     rc = rebuild(h);
+    clk.mark("adapt:rebuild");
     void* tab = nullptr;
     if (rc == KG_OK) {
         const size_t b_recs = sizeof(AdaptRec) * plan.recs.size();
@@ -986,14 +1007,17 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
         rc = init_wall_blocks(h, slot, fa);
     }
     cudaStreamSynchronize(h->stream);
+    clk.mark("adapt:move");
     if (tab) cudaFree(tab);
     if (!h->is_batch) {
         for (void* p : old_pools) cudaFree(p);
+        clk.mark("adapt:release");
         if (rc) { free_pools(h); return rc; }
         h->have_state = true;
     } else {
         h->fslab.release(old.fbase, old.fsize);
         h->dslab.release(old.dbase, old.dsize);
+        clk.mark("adapt:release");
         if (rc) {
             // the problem cannot continue in a half-built state: release it
             h->fslab.release(pb.fbase, pb.fsize);

@@ -20,6 +20,8 @@ struct Ctx {
     Flat* F;
     std::map<std::pair<int, int>, int> pairs;  // (my grid, other grid) -> id
     std::string* err;
+    std::vector<int32_t> dense;                 // the same for up to 1024 grids: G x G, -3 unknown
+    int G = 0;
 };
 
 int grid_nv(const kg_topology& t, int g) { return (int)(t.grid_off[g + 1] - t.grid_off[g]); }
@@ -70,9 +72,11 @@ int data_of(const Ctx& c, int32_t r) {
 
 int pairing(Ctx& c, int ga, int gb) {
     if (ga == gb) return -1;
+    int32_t* slot = c.dense.empty() ? nullptr : &c.dense[(size_t)ga * c.G + gb];
+    if (slot && *slot != -3) return *slot;
     auto key = std::make_pair(ga, gb);
     auto it = c.pairs.find(key);
-    if (it != c.pairs.end()) return it->second;
+    if (it != c.pairs.end()) { if (slot) *slot = it->second; return it->second; }
     const kg_topology& t = *c.t;
     Flat& F = *c.F;
     std::vector<int32_t> runs;
@@ -84,6 +88,7 @@ int pairing(Ctx& c, int ga, int gb) {
     for (size_t q = 0; q < runs.size(); q += 2) { F.p_j0.push_back(runs[q]); F.p_cnt.push_back(runs[q + 1]); }
     F.p_off.push_back((int64_t)F.p_j0.size());
     c.pairs[key] = id;
+    if (slot) *slot = id;
     return id;
 }
 
@@ -107,7 +112,8 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         { err = "null topology array"; return KG_ERR_ARG; }
     const int D = t.dim, NDF = t.ndf, NC = t.n_cells, NWL = t.n_walls;
     F.dim = D; F.ndf = NDF; F.n_cells = NC; F.n_walls = NWL; F.n_data = NC + NWL;
-    Ctx c{&t, D, NDF, &F, {}, &err};
+    Ctx c{&t, D, NDF, &F, {}, &err, {}, t.n_grids};
+    if (t.n_grids <= 1024) c.dense.assign((size_t)t.n_grids * t.n_grids, -3);
     F.p_off.push_back(0);
 
     // ---- velocity grids ------------------------------------------------------
@@ -362,7 +368,20 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
     }
 
     // ---- flux incidences (flux!, Flux/Flux.jl:19-111,458-503) -----------------------------
-    std::vector<std::vector<Incidence>> per(NC);
+    // Per cell its incidences in face order, in one array: count them, then place them.
+    std::vector<int32_t> nper(NC + 1, 0);
+    for (int fi = 0; fi < t.n_faces; ++fi) {
+        const int here = t.face_here[fi];
+        if (here < 0 || here >= NC) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
+        nper[here + 1] += 1;
+        if (t.face_kind[fi] != KG_FACE_DOMAIN) {
+            const int od = data_of(c, t.face_there[fi]);
+            if (od >= 0 && od < NC && F.dbe[od] >= 0) nper[od + 1] += 1;
+        }
+    }
+    for (int i = 0; i < NC; ++i) nper[i + 1] += nper[i];
+    std::vector<Incidence> incs((size_t)nper[NC]);
+    std::vector<int32_t> fill(nper.begin(), nper.end() - 1);
     for (int fi = 0; fi < t.n_faces; ++fi) {
         Incidence a{};
         int dir = t.face_dir[fi];
@@ -386,7 +405,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
                 for (int e = 0; e < MAXW; ++e) F.bc_hl.push_back((float)b[e]);
                 for (int e = 0; e < MAXW; ++e) F.bc_hl.push_back((float)(b[e] - (double)(float)b[e]));
             }
-            per[here].push_back(a);
+            incs[fill[here]++] = a;
             continue;
         }
         int od = data_of(c, t.face_there[fi]);
@@ -398,7 +417,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         a.pair = pairing(c, t.cell_grid[here], F.dgrid[od]);
         if (a.pair == -2) return KG_ERR_TOPOLOGY;
         if (solid && od >= NC && F.dgrid[od] != t.cell_grid[here]) { err = "wall grid differs from donor grid"; return KG_ERR_TOPOLOGY; }
-        per[here].push_back(a);
+        incs[fill[here]++] = a;
         if (!solid && od < NC) {
             // the there side receives the same flux with the opposite sign
             Incidence b{};
@@ -412,26 +431,32 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
             }
             b.pair = pairing(c, t.cell_grid[od], t.cell_grid[here]);
             if (b.pair == -2) return KG_ERR_TOPOLOGY;
-            per[od].push_back(b);
+            incs[fill[od]++] = b;
         }
     }
+    // cells with bound_enc < 0 hold no incidences (a face's here side is fluid, and only a
+    // fluid there side is updated), so the per-cell runs in cell order are the fluid list's
+    F.inc = std::move(incs);
     F.inc_off.push_back(0);
     for (int i = 0; i < NC; ++i) {
         if (t.cell_bound_enc[i] < 0) continue;
         F.fluid_cells.push_back(i);
         int nbcm = 0;
-        for (auto& a : per[i]) {
-            F.inc.push_back(a);
+        const Incidence* pi = F.inc.data() + nper[i];
+        const int ni = nper[i + 1] - nper[i];
+        for (int q = 0; q < ni; ++q) {
+            const Incidence& a = pi[q];
             if (a.kind == INC_DOMAIN && (a.bc_kind == KG_BC_MAXWELL || a.bc_kind == KG_BC_INFLOW)) ++nbcm;
         }
-        F.max_inc = std::max(F.max_inc, (int)per[i].size());
+        F.max_inc = std::max(F.max_inc, ni);
         F.max_bcm = std::max(F.max_bcm, nbcm);
         // regular cell: per direction one face at -ds/2 and one at +ds/2, each an inner face to
         // a same-sized fluid neighbour on this cell's velocity grid, oriented so that a velocity
         // leaves through the face it points at (the flux kernel's fast path relies on all of it)
-        bool reg = (int)per[i].size() == 2 * D;
+        bool reg = ni == 2 * D;
         int seen[2 * MAXD] = {0};
-        for (auto& a : per[i]) {
+        for (int q = 0; q < ni; ++q) {
+            const Incidence& a = pi[q];
             if (!reg) break;
             const int d = a.dir;
             const double h = 0.5 * t.cell_ds[(size_t)i * D + d];
@@ -447,7 +472,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         }
         for (int e = 0; reg && e < 2 * D; ++e) reg = seen[e] == 1;
         F.fluid_reg.push_back(reg ? 1 : 0);
-        F.inc_off.push_back((int32_t)F.inc.size());
+        F.inc_off.push_back(nper[i + 1]);
     }
 
     // ---- immersed boundary (Boundary/Immersed_boundary.jl:122-146,367-500) -----------------
@@ -543,6 +568,18 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
     M.dinvv.assign(dcap, 0.0);
     M.dmid.assign((size_t)dcap * MAXD, 0.0); M.dds.assign((size_t)dcap * MAXD, 0.0);
     M.inc_off.push_back(0);
+    {
+        size_t ninc = 0, nfl = 0, nso = 0, nsn = 0, np = 0, npo = 0, nco = 0, ncn = 0;
+        for (auto& p : parts) {
+            ninc += p.F->inc.size(); nfl += p.F->fluid_cells.size(); nso += p.F->slope_ops.size();
+            nsn += p.F->slope_nbr.size(); np += p.F->p_j0.size(); npo += p.F->p_off.size();
+            nco += p.F->crit_ops.size(); ncn += p.F->crit_nbr.size();
+        }
+        M.inc.reserve(ninc); M.fcrec.reserve(nfl); M.fluid_cells.reserve(nfl); M.fluid_reg.reserve(nfl);
+        M.inc_off.reserve(nfl + 1); M.slope_ops.reserve(nso); M.slope_nbr.reserve(nsn);
+        M.p_j0.reserve(np); M.p_cnt.reserve(np); M.p_off.reserve(npo + 1);
+        M.crit_ops.reserve(nco); M.crit_nbr.reserve(ncn);
+    }
     size_t npass = 0;
     for (auto& p : parts) npass = std::max(npass, p.F->pass_cells_off.size() - 1);
     int64_t PGacc = 0;
