@@ -157,6 +157,7 @@ struct kg_handle {
     std::vector<void*> topo_allocs;
     int64_t topo_bytes = 0;
     Flat M;
+    Flat spare;                    // a previous problem's arrays, reused by the next flattening
     Dev dev{};
     std::vector<int32_t> live;
     int32_t* d_live = nullptr;
@@ -915,7 +916,7 @@ struct PhaseClock {
 
 int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adapt_src* src) {
     PhaseClock clk{h};
-    Flat Fn;
+    Flat Fn = std::move(h->spare);
     std::string err;
     int rc = flatten(h->prm, *topo, Fn, err);
     clk.mark("adapt:flatten");
@@ -1009,6 +1010,7 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     cudaStreamSynchronize(h->stream);
     clk.mark("adapt:move");
     if (tab) cudaFree(tab);
+    h->spare = std::move(old.F);
     if (!h->is_batch) {
         for (void* p : old_pools) cudaFree(p);
         clk.mark("adapt:release");
@@ -1218,10 +1220,11 @@ int kg_upload_topology(kg_handle* h, const kg_topology* topo) {
     if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle admits problems with kg_batch_admit");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
-    Flat F;
+    Flat F = std::move(h->spare);
     std::string err;
     int rc = flatten(h->prm, *topo, F, err);
     if (rc) { free_pools(h); return fail(h, rc, err); }
+    if (!h->probs.empty()) h->spare = std::move(h->probs[0].F);
     if (F.max_inc > MAX_INC) { free_pools(h); return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported (" + std::to_string(F.max_inc) + ")"); }
     if ((rc = make_pools(h, F.foff.back(), F.n_data))) return rc;
     Problem& pb = h->probs[0];

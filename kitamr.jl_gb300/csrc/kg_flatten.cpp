@@ -96,8 +96,29 @@ const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 
 }  // namespace
 
+// Empties a gather form but keeps the capacity of its arrays: rebuilding one of a similar size
+// (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
+// cost more than filling ~20 MB of records.
+void reset(Flat& F) {
+    static_assert(sizeof(Flat) == 46 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
+    F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
+    F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
+    F.ax_off.clear(); F.ax_val.clear(); F.ax_hi.clear(); F.ax_lo.clear(); F.vidx.clear();
+    F.foff.clear(); F.dgrid.clear(); F.dbe.clear(); F.dinvv.clear(); F.dnv.clear(); F.dprob.clear();
+    F.dmid.clear(); F.dds.clear();
+    F.p_off.clear(); F.p_j0.clear(); F.p_cnt.clear();
+    F.pass_off.clear(); F.slope_ops.clear(); F.pass_cells_off.clear(); F.pass_cells.clear();
+    F.cell_slope_op.clear(); F.slope_nbr.clear();
+    F.fluid_cells.clear(); F.fcrec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
+    F.fluid_reg.clear();
+    F.inc_off.clear(); F.inc.clear(); F.bc_prim.clear(); F.bc_hl.clear();
+    F.solid_ops.clear(); F.wall_ops.clear(); F.ib_nbr.clear(); F.ib_dx.clear(); F.cut_idx.clear();
+    F.cut_gw.clear(); F.cut_sw.clear(); F.cvcw.clear();
+}
+
 int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& err) {
-    F = Flat();
+    reset(F);
     if (t.dim != 2 && t.dim != 3) { err = "dim must be 2 or 3"; return KG_ERR_ARG; }
     if (t.ndf != (t.dim == 2 ? 2 : 1)) { err = "ndf must be 2 in 2D and 1 in 3D"; return KG_ERR_ARG; }
     if (prm.dim != t.dim || prm.ndf != t.ndf) { err = "params and topology disagree on dim/ndf"; return KG_ERR_ARG; }
@@ -380,7 +401,8 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         }
     }
     for (int i = 0; i < NC; ++i) nper[i + 1] += nper[i];
-    std::vector<Incidence> incs((size_t)nper[NC]);
+    F.inc.resize((size_t)nper[NC]);
+    Incidence* incs = F.inc.data();
     std::vector<int32_t> fill(nper.begin(), nper.end() - 1);
     for (int fi = 0; fi < t.n_faces; ++fi) {
         Incidence a{};
@@ -436,7 +458,6 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
     }
     // cells with bound_enc < 0 hold no incidences (a face's here side is fluid, and only a
     // fluid there side is updated), so the per-cell runs in cell order are the fluid list's
-    F.inc = std::move(incs);
     F.inc_off.push_back(0);
     for (int i = 0; i < NC; ++i) {
         if (t.cell_bound_enc[i] < 0) continue;
@@ -551,7 +572,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
 }
 
 void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges) {
-    M = Flat();
+    reset(M);
     if (parts.empty()) return;
     const int D = parts[0].F->dim;
     M.dim = D; M.ndf = parts[0].F->ndf;

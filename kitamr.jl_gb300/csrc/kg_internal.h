@@ -198,6 +198,9 @@ struct AdaptRec {
 // same root lattice.
 bool level_runs(const int8_t* la, int na, const int8_t* lb, int nb, int D, std::vector<int32_t>& runs);
 
+// Empties a gather form, keeping the capacity of its arrays for the next build.
+void reset(Flat& F);
+
 // Builds the gather form; returns KG_OK or an error code with a message.
 int flatten(const kg_params& prm, const kg_topology& t, Flat& out, std::string& err);
 
