@@ -346,7 +346,9 @@ int rebuild(kg_handle* h) {
         cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
         // dynamic shared memory of the flux and wall kernels plus a reserve for their static arrays
         const size_t sa = storage_size(h);
-        const size_t sflux = ((size_t)M.ndf * M.max_nv + (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis) * sa + 16384;
+        // the flux kernel's convected f can move to global memory; its tables and the wall
+        // kernel's cannot
+        const size_t sflux = (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis * sa + 16384;
         const size_t swall = (size_t)M.dim * M.max_axis * sa + M.max_nv + 4096;
         const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
@@ -367,6 +369,20 @@ int rebuild(kg_handle* h) {
 #undef UP
     P.max_axis = M.max_axis;
     P.max_bcm = M.max_bcm;
+    if (M.n_fluid > 0) {
+        // stage the flux kernel's convected f in global memory when shared memory would cost
+        // resident CTAs (or not fit at all)
+        int dev_smem = 0;
+        cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+        const size_t sa = storage_size(h);
+        const size_t full = ((size_t)M.ndf * M.max_nv + (size_t)std::max(2, M.max_bcm) * M.dim * M.max_axis) * sa + 16384;
+        P.fst_global = 0;
+        const int occ_smem = full <= (size_t)dev_smem
+            ? (int)dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, M.max_nv); }) : 0;
+        P.fst_global = 1;
+        const int occ_glob = (int)dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, M.max_nv); });
+        P.fst_global = occ_glob > occ_smem ? 1 : 0;
+    }
     {
         std::vector<int32_t> order(M.fluid_cells.size());
         for (size_t q = 0; q < order.size(); ++q) order[q] = (int32_t)q;

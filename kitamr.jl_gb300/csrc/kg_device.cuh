@@ -62,6 +62,8 @@ struct Dev {
     const double* bc_prim;
     const float* bc_hl;                // bc_prim as FP32 hi (MAXW) then lo (MAXW) per entry
     int max_bcm;                       // most Maxwellian-state domain faces of a cell
+    int fst_global;                    // flux kernel: convected f staged in the cell's output
+                                       // block (L2) instead of shared memory
     // ib
     const SolidOp* solid_ops;
     const WallOp* wall_ops;

@@ -762,11 +762,12 @@ __device__ __forceinline__ void get_prim_r(const double* w, double gamma, double
     prim[D + 1] = 0.5 * w[0] / ((gamma - 1.0) * (w[D + 1] - 0.5 * m2 * inv));
 }
 
-// dynamic shared memory of the flux kernel: convected f, then the factor tables (two
-// collision Maxwellians, or one per Maxwellian-state domain face earlier in the step)
+// dynamic shared memory of the flux kernel: convected f (unless it is staged in the cell's
+// output block), then the factor tables (two collision Maxwellians, or one per
+// Maxwellian-state domain face earlier in the step)
 template <int D, int NDF, typename A>
-__host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, int max_bcm) {
-    return ((size_t)NDF * max_nv + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
+__host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, int max_bcm, int fst_global) {
+    return ((fst_global ? (size_t)0 : (size_t)NDF * max_nv) + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
 }
 
 // the faces of a regular cell (fluid_reg), by direction and side (2*dir + (face at +ds/2))
@@ -878,8 +879,12 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     for (int d = 0; d < D; ++d) myds[d] = sc[C_DS0 + d];
     const A s_dt = sc[C_SDT];
     const A adt = sc[C_ADT];
-    A* fst = (A*)sh_raw;                                  // NDF * nv
-    A* Ec = fst + (size_t)NDF * nv;                       // factor tables (flux_smem)
+    // convected f, NDF * nv: in shared memory, or -- when that would cost resident CTAs (large
+    // 3D grids) -- in the cell's output block, which stays in L2 until the relaxation
+    // overwrites it; every access below is by the thread that owns velocity i, at k * nv + i
+    static_assert(sizeof(A) == sizeof(T), "the staging block holds the arithmetic type");
+    A* fst = P.fst_global ? (A*)fnew : (A*)sh_raw;
+    A* Ec = P.fst_global ? (A*)sh_raw : fst + (size_t)NDF * nv;   // factor tables (flux_smem)
     const bool caidvm = P.flux == KG_FLUX_CAIDVM;
 
     const int MA = P.max_axis;
@@ -1768,7 +1773,7 @@ struct Launch {
     }
     static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
-        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
@@ -1778,7 +1783,7 @@ struct Launch {
     static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,
                                        cudaStream_t s) {
         using A = typename Arith<T>::type;
-        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
         cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(counter, 0, sizeof(int), s);
@@ -1813,7 +1818,7 @@ struct Launch {
     // resident CTAs per SM the flux kernel reaches (for the persistent grid size)
     static int flux_occupancy(const Dev& P, int max_nv) {
         using A = typename Arith<T>::type;
-        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm);
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
         cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, flux_collide_kernel<D, NDF, T>, BLOCK, smem);

@@ -53,7 +53,11 @@ def test_fp64_chunked_calls_and_graph_match_single_call():
     assert f_error(topo, ref.f, out1["f"]) <= TOL_FP64
 
 
-MIXED = CASES_FP64[:4] + CASES_FP64[5:]
+MIXED = CASES_FP64[:4] + CASES_FP64[5:] + [
+    # a 24^3 velocity grid: the mixed flux kernel stages its convected f in the cells' output
+    # blocks (shared memory would cost a resident CTA per SM)
+    ("sphere3d_v24_global_staging", lambda: cases.sphere(scale=0.25, nv=24), 2),
+]
 
 
 @pytest.mark.parametrize("name,make,nsteps", MIXED, ids=[c[0] for c in MIXED])
