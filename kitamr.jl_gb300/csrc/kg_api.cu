@@ -383,6 +383,7 @@ int rebuild(kg_handle* h) {
         const int occ_glob = (int)dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, M.max_nv); });
         P.fst_global = occ_glob > occ_smem ? 1 : 0;
     }
+
     {
         std::vector<int32_t> order(M.fluid_cells.size());
         for (size_t q = 0; q < order.size(); ++q) order[q] = (int32_t)q;

@@ -141,8 +141,8 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
     if (SC.regular) {
         // regular cell (one record, no shared-memory setup): in every direction
         // minmod((f - f_A)/ds_A, (f - f_B)/ds_B) -- slope_side with its loops and unit factors
-        // resolved.  Two velocity cells per thread and pass: all their loads are issued
-        // before any store, so each thread keeps twice the loads in flight.
+        // resolved.  Several velocity cells per thread and pass: all their loads are issued
+        // before any store, so each thread keeps that many sets of loads in flight.
         const int nv = SC.nv;
         const T* fcell = (const T*)P.f_in + SC.foff;
         T* scell = (T*)P.sdf + SC.foff * D;
@@ -157,32 +157,39 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
             if constexpr (sizeof(A) == 4) { ia[dir] = SC.inv_f[2 * dir]; ib[dir] = SC.inv_f[2 * dir + 1]; }
             else { ia[dir] = SC.inv_d[2 * dir]; ib[dir] = SC.inv_d[2 * dir + 1]; }
         }
-        for (int i0 = threadIdx.x; i0 < nv; i0 += 2 * BLOCK) {
-            const int i1 = i0 + BLOCK;
-            const bool two = i1 < nv;
-            const int j1 = two ? i1 : i0;    // a valid index for the second set of loads
-            A fc0[NDF], fc1[NDF], a0[D][NDF], a1[D][NDF], b0[D][NDF], b1[D][NDF];
+        // velocity cells per thread and pass (measured on the 3D sphere, mixed form: 2 beats 3
+        // and 4, whose registers cost resident CTAs)
+        constexpr int VPT = 2;
+        for (int i0 = threadIdx.x; i0 < nv; i0 += VPT * BLOCK) {
+            int iv[VPT], jv[VPT];
 #pragma unroll
-            for (int k = 0; k < NDF; ++k) { fc0[k] = (A)fcell[k * nv + i0]; fc1[k] = (A)fcell[k * nv + j1]; }
+            for (int v = 0; v < VPT; ++v) {
+                iv[v] = i0 + v * BLOCK;
+                jv[v] = iv[v] < nv ? iv[v] : i0;    // a valid index for the loads
+            }
+            A fc[VPT][NDF], a[VPT][D][NDF], b[VPT][D][NDF];
 #pragma unroll
-            for (int dir = 0; dir < D; ++dir) {
+            for (int v = 0; v < VPT; ++v) {
 #pragma unroll
-                for (int k = 0; k < NDF; ++k) {
-                    a0[dir][k] = (A)fa[dir][k * nv + i0];
-                    b0[dir][k] = (A)fb[dir][k * nv + i0];
-                    a1[dir][k] = (A)fa[dir][k * nv + j1];
-                    b1[dir][k] = (A)fb[dir][k * nv + j1];
+                for (int k = 0; k < NDF; ++k) fc[v][k] = (A)fcell[k * nv + jv[v]];
+#pragma unroll
+                for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) {
+                        a[v][dir][k] = (A)fa[dir][k * nv + jv[v]];
+                        b[v][dir][k] = (A)fb[dir][k * nv + jv[v]];
+                    }
                 }
             }
 #pragma unroll
-            for (int dir = 0; dir < D; ++dir) {
+            for (int v = 0; v < VPT; ++v) {
+                if (v > 0 && iv[v] >= nv) break;
 #pragma unroll
-                for (int k = 0; k < NDF; ++k) {
-                    scell[(dir * NDF + k) * nv + i0] =
-                        (T)minmod((fc0[k] - a0[dir][k]) * ia[dir], (fc0[k] - b0[dir][k]) * ib[dir]);
-                    if (two)
-                        scell[(dir * NDF + k) * nv + i1] =
-                            (T)minmod((fc1[k] - a1[dir][k]) * ia[dir], (fc1[k] - b1[dir][k]) * ib[dir]);
+                for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k)
+                        scell[(dir * NDF + k) * nv + iv[v]] =
+                            (T)minmod((fc[v][k] - a[v][dir][k]) * ia[dir], (fc[v][k] - b[v][dir][k]) * ib[dir]);
                 }
             }
         }
