@@ -263,6 +263,12 @@ def run_batched(args):
         ms = next(iter(reps.values())).device_ms
         forms[form] = {"value": P * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "phase_cells": P,
                        "launches_per_call": int(next(iter(reps.values())).kernel_launches)}
+        if form == "mixed":
+            # per-kernel device times (CUDA events on the handle's stream), a separate pass
+            b.profile(True)
+            b.step(2)
+            forms[form]["kernels_ms_per_step"] = {k: v[0] / 2 for k, v in b.profile_read().items()}
+            b.profile(False)
         b.close()
     m = forms["mixed"]
     return {"metric": METRIC + " (batched)", "value": m["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,

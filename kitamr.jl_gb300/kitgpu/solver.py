@@ -330,6 +330,15 @@ class GpuBatch:
     def profile(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
 
+    def profile_read(self):
+        cap = 16
+        names = (C.c_char_p * cap)()
+        ms = (C.c_double * cap)()
+        cnt = (C.c_int64 * cap)()
+        n = C.c_int32()
+        _check(self.L, self.h, self.L.kg_profile_read(self.h, names, ms, cnt, cap, C.byref(n)))
+        return {names[i].decode(): (ms[i], cnt[i]) for i in range(min(n.value, cap))}
+
     def autotune(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
 
