@@ -785,8 +785,10 @@ template <typename A, typename T> struct RegFace {
     A sarea;
 };
 
-// flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part)
-template <int D, int NDF, typename T>
+// flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part).
+// FG: the convected f is staged in the cell's output block instead of shared memory (a
+// compile-time choice, so that the shared-memory variant keeps shared-memory instructions)
+template <int D, int NDF, typename T, bool FG>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -890,8 +892,8 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     // 3D grids) -- in the cell's output block, which stays in L2 until the relaxation
     // overwrites it; every access below is by the thread that owns velocity i, at k * nv + i
     static_assert(sizeof(A) == sizeof(T), "the staging block holds the arithmetic type");
-    A* fst = P.fst_global ? (A*)fnew : (A*)sh_raw;
-    A* Ec = P.fst_global ? (A*)sh_raw : fst + (size_t)NDF * nv;   // factor tables (flux_smem)
+    A* fst = FG ? (A*)fnew : (A*)sh_raw;
+    A* Ec = FG ? (A*)sh_raw : fst + (size_t)NDF * nv;   // factor tables (flux_smem)
     const bool caidvm = P.flux == KG_FLUX_CAIDVM;
 
     const int MA = P.max_axis;
@@ -1363,7 +1365,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 //  * persistent: `gridDim.x` resident CTAs take cells from the work counter (in `order`,
 //    when given), so a batch of uneven problems keeps every SM busy to the end of the
 //    sub-step.  The counter must be zero at launch.
-template <int D, int NDF, typename T>
+template <int D, int NDF, typename T, bool FG>
 __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_kernel(Dev P, int* counter,
                                                                                   const int32_t* order, int n) {
     __shared__ int item;
@@ -1376,7 +1378,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_ke
             __syncthreads();
         }
         if (it >= n) break;
-        flux_collide_cell<D, NDF, T>(P, order ? order[it] : it);
+        flux_collide_cell<D, NDF, T, FG>(P, order ? order[it] : it);
         if (!counter) break;
         __syncthreads();
     }
@@ -1778,12 +1780,18 @@ struct Launch {
         wall_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
         return cudaGetLastError();
     }
+    // the flux kernel of the layout's staging choice
+    using FluxFn = void (*)(Dev, int*, const int32_t*, int);
+    static FluxFn flux_fn(const Dev& P) {
+        return P.fst_global ? flux_collide_kernel<D, NDF, T, true> : flux_collide_kernel<D, NDF, T, false>;
+    }
     static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
-        cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const FluxFn fn = flux_fn(P);
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        flux_collide_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
+        fn<<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
         return cudaGetLastError();
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
@@ -1791,11 +1799,12 @@ struct Launch {
                                        cudaStream_t s) {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
-        cudaError_t e = cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const FluxFn fn = flux_fn(P);
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(counter, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
-        flux_collide_kernel<D, NDF, T><<<grid, BLOCK, smem, s>>>(P, counter, order, n);
+        fn<<<grid, BLOCK, smem, s>>>(P, counter, order, n);
         return cudaGetLastError();
     }
     static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {
@@ -1803,8 +1812,6 @@ struct Launch {
         macro_slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, fbegin, dbase, out);
         return cudaGetLastError();
     }
-    // physical-space criterion of the fluid cells [fbegin, fbegin + n): loh from sw, then
-    // the buffer layer into out (both per data item from dbase on)
     // adapted-mesh state from the previous pools, one CTA per cell record
     static cudaError_t adapt(const Dev& P, int n, const AdaptRec* recs, const void* f, const void* sdf, const double* w,
                              const double* prim, const double* qf, const int32_t* runs, const int8_t* lev,
@@ -1814,6 +1821,8 @@ struct Launch {
         adapt_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, V);
         return cudaGetLastError();
     }
+    // physical-space criterion of the fluid cells [fbegin, fbegin + n): loh from sw, then
+    // the buffer layer into out (both per data item from dbase on)
     static cudaError_t criterion(const Dev& P, int fbegin, int n, int dbase, const double* sw, double thr,
                                  double* loh, double* out, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
@@ -1826,9 +1835,10 @@ struct Launch {
     static int flux_occupancy(const Dev& P, int max_nv) {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
-        cudaFuncSetAttribute(flux_collide_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        const FluxFn fn = flux_fn(P);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, flux_collide_kernel<D, NDF, T>, BLOCK, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, BLOCK, smem);
         return nb;
     }
 };
