@@ -382,6 +382,11 @@ int rebuild(kg_handle* h) {
         P.fst_global = 1;
         const int occ_glob = (int)dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, M.max_nv); });
         P.fst_global = occ_glob > occ_smem ? 1 : 0;
+        // small velocity grids: the per-cell fixed work (setup, reductions, the scalar chain)
+        // outweighs the per-velocity work, and 128-thread CTAs keep twice the cells in flight
+        const double mean_nv = (double)M.phase_cells / (double)M.n_fluid;
+        P.flux_nt = (!P.fst_global && mean_nv < 1024.0) ? 128 : BLOCK;
+        P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
     }
 
     {

@@ -64,6 +64,9 @@ struct Dev {
     int max_bcm;                       // most Maxwellian-state domain faces of a cell
     int fst_global;                    // flux kernel: convected f staged in the cell's output
                                        // block (L2) instead of shared memory
+    int flux_nt;                       // flux kernel threads per CTA: 256, or 128 for layouts of
+                                       // small velocity grids (twice the cells in flight)
+    int slope_nt;                      // slope kernel threads per CTA (the same choice)
     // ib
     const SolidOp* solid_ops;
     const WallOp* wall_ops;
@@ -94,10 +97,10 @@ struct Dev {
 // Block sums with a fixed combination order (deterministic run to run): a butterfly
 // within each warp, then warp 0 combines the warp partials and broadcasts the result
 // through shared memory, so every thread sees the same bits.
-template <int N>
+template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum(double (&v)[N], double* sred) {
-    // sred: shared scratch of N * (BLOCK/32) doubles
-    constexpr int NWARP = BLOCK / 32;
+    // sred: shared scratch of N * (NT/32) doubles; NT: threads of the block
+    constexpr int NWARP = NT / 32;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int e = 0; e < N; ++e) {
@@ -139,10 +142,10 @@ __device__ __forceinline__ void two_sum_acc(float& h, float& l, float h2, float 
     l = l + l2 + err;
     h = sum;
 }
-template <int N>
+template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], double (&out)[N], double* sred) {
-    // sred: shared scratch of at least N * (BLOCK/32) doubles
-    constexpr int NWARP = BLOCK / 32;
+    // sred: shared scratch of at least N * (NT/32) doubles; NT: threads of the block
+    constexpr int NWARP = NT / 32;
     static_assert(NWARP == 4 || NWARP == 8, "the warp-0 stage maps NWARP lanes per element");
     constexpr int GROUPS = 32 / NWARP;            // elements per round of warp 0
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;

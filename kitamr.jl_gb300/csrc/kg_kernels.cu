@@ -133,8 +133,10 @@ __device__ __forceinline__ void slope_side(int i, int li, const typename Arith<T
     for (int k = 0; k < NDF; ++k) s[k] = acc[k] * inv_cnt;
 }
 
-template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
+// NT: threads per CTA (128 for layouts of small velocity grids, whose cells would leave half
+// of a 256-thread CTA idle)
+template <int D, int NDF, typename T, int NT>
+__global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
     using A = typename Arith<T>::type;
     const int pc = pc_base + blockIdx.x;
     const SlopeCell& SC = P.screc[pc];
@@ -160,11 +162,11 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
         // velocity cells per thread and pass (measured on the 3D sphere, mixed form: 2 beats 3
         // and 4, whose registers cost resident CTAs)
         constexpr int VPT = 2;
-        for (int i0 = threadIdx.x; i0 < nv; i0 += VPT * BLOCK) {
+        for (int i0 = threadIdx.x; i0 < nv; i0 += VPT * NT) {
             int iv[VPT], jv[VPT];
 #pragma unroll
             for (int v = 0; v < VPT; ++v) {
-                iv[v] = i0 + v * BLOCK;
+                iv[v] = i0 + v * NT;
                 jv[v] = iv[v] < nv ? iv[v] : i0;    // a valid index for the loads
             }
             A fc[VPT][NDF], a[VPT][D][NDF], b[VPT][D][NDF];
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(BLOCK) slope_kernel(Dev P, int pc_base) {
         snb[e] = c;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+    for (int i = threadIdx.x; i < nv; i += NT) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
 #pragma unroll
@@ -305,19 +307,19 @@ template <> struct KSum<double> {
     __device__ __forceinline__ double value() const { return s; }
 };
 
-// Block sum of compensated per-thread accumulators into FP64 results.
-template <int N>
+// Block sum of compensated per-thread accumulators into FP64 results (NT: threads of the block).
+template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum_ks(const KSum<double> (&v)[N], double (&out)[N], double* sred) {
 #pragma unroll
     for (int e = 0; e < N; ++e) out[e] = v[e].s;
-    block_sum<N>(out, sred);
+    block_sum<N, NT>(out, sred);
 }
-template <int N>
+template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum_ks(const KSum<float> (&v)[N], double (&out)[N], double* sred) {
     float hi[N], lo[N];
 #pragma unroll
     for (int e = 0; e < N; ++e) { hi[e] = v[e].s; lo[e] = -v[e].c; }
-    block_sum_ff<N>(hi, lo, out, sred);
+    block_sum_ff<N, NT>(hi, lo, out, sred);
 }
 
 // limiter ratio: exact division in FP64; the fast FP32 division (2 ulp) in the mixed form,
@@ -733,12 +735,12 @@ template <typename A, typename T> struct IncA {
 // Factor tables E[d][a] = exp(-lam (x_a - U_d)^2) of a Maxwellian at the distinct axis
 // coordinates x_a of grid gid (exp(-lam|u-U|^2) = Π_d E[d][axis index of u_d]); every thread
 // of the block takes entries.  FP64 form: FP64 exponents.
-template <int D>
+template <int D, int NT = BLOCK>
 __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const double* U, double lam, double* E) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
-        for (int a = threadIdx.x; a < na; a += BLOCK) {
+        for (int a = threadIdx.x; a < na; a += NT) {
             const double cu = P.ax_val[a0 + a] - U[d];
             E[d * P.max_axis + a] = exp(-lam * cu * cu);
         }
@@ -746,13 +748,13 @@ __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const double*
 }
 // Mixed form: FP32 tables whose exponents are formed in float-float arithmetic from the
 // FP32 hi + lo pairs of x, U and lam, so no FP64 instruction runs per entry.
-template <int D>
+template <int D, int NT = BLOCK>
 __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const float* Uh, const float* Ul, float lh,
                                             float ll, float* E) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
-        for (int a = threadIdx.x; a < na; a += BLOCK)
+        for (int a = threadIdx.x; a < na; a += NT)
             E[d * P.max_axis + a] = exp_gauss_ff(P.ax_hi[a0 + a], P.ax_lo[a0 + a], Uh[d], Ul[d], lh, ll);
     }
 }
@@ -788,7 +790,7 @@ template <typename A, typename T> struct RegFace {
 // flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part).
 // FG: the convected f is staged in the cell's output block instead of shared memory (a
 // compile-time choice, so that the shared-memory variant keeps shared-memory instructions)
-template <int D, int NDF, typename T, bool FG>
+template <int D, int NDF, typename T, bool FG, int NT>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -797,7 +799,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     __shared__ RegFace<A, T> srf[2 * MAXD];
     __shared__ int8_t sbt[MAX_INC];             // incidence -> its Maxwellian factor table, -1 none
     __shared__ A sbpre[MAX_INC], sbk[MAX_INC];  // ρ (λ/π)^{D/2} and K/(2λ) of that Maxwellian
-    __shared__ double sred[2 * (D + 2) * (BLOCK / 32)];
+    __shared__ double sred[2 * (D + 2) * (NT / 32)];
     __shared__ double sscal[4 * MAXW];
     // per-CTA scalars in the arithmetic precision, computed once by thread 0
     enum { C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
@@ -820,7 +822,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const int check_interval = PP.check;
     const int i0 = FC.inc0, ninc = FC.ninc;
     const bool reg = FC.reg != 0;
-    for (int e = threadIdx.x; e < ninc; e += BLOCK) {
+    for (int e = threadIdx.x; e < ninc; e += NT) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
         IncA<A, T> ia;
@@ -913,10 +915,10 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         A* Eb = Ec + (size_t)nbt * D * MA;
         if constexpr (sizeof(A) == 8) {
             const double* bc = P.bc_prim + (int64_t)I.bc * MAXW;
-            gauss_table<D>(P, gid, bc + 1, bc[D + 1], (double*)Eb);
+            gauss_table<D, NT>(P, gid, bc + 1, bc[D + 1], (double*)Eb);
         } else {
             const float* hl = P.bc_hl + (int64_t)I.bc * 2 * MAXW;
-            gauss_table<D>(P, gid, hl + 1, hl + MAXW + 1, hl[D + 1], hl[MAXW + D + 1], (float*)Eb);
+            gauss_table<D, NT>(P, gid, hl + 1, hl + MAXW + 1, hl[D + 1], hl[MAXW + D + 1], (float*)Eb);
         }
         ++nbt;
     }
@@ -930,7 +932,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             if (I.bc_kind == KG_BC_MAXWELL) {
                 const A* Eb = Ec + (size_t)b * D * MA;
                 KSum<A> red[2];
-                for (int i = threadIdx.x; i < nv; i += BLOCK) {
+                for (int i = threadIdx.x; i < nv; i += NT) {
                     const A ud = VU[(int64_t)I.dir * PG + g.goff + i];
                     if (sia[e].orient * ud <= (A)0) {
                         const A fk = (A)fcell[i];
@@ -949,7 +951,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
                     }
                 }
                 double rs[2];
-                block_sum_ks<2>(red, rs, sred);
+                block_sum_ks<2, NT>(red, rs, sred);
                 if (threadIdx.x == 0) {
                     const double lam = bc[D + 1];
                     const double pre = D == 2 ? lam / PI : pow(lam / PI, 1.5);
@@ -968,7 +970,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 
     // ---- 1. fluxes gathered over the incidences; convected f into shared memory ----
     KSum<A> wacc[D + 2], wfc[D + 2];
-    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+    for (int i = threadIdx.x; i < nv; i += NT) {
         const int li = P.vlev[g.goff + i];
         A u[D];
 #pragma unroll
@@ -1121,7 +1123,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             const T* of = sia[e].of;
             const T* os = sia[e].os;
             const int mode = sia[e].mode_in;
-            for (int j = threadIdx.x; j < onv; j += BLOCK) {
+            for (int j = threadIdx.x; j < onv; j += NT) {
                 A uj[D];
 #pragma unroll
                 for (int d = 0; d < D; ++d) uj[d] = VU[(int64_t)d * PG + go.goff + j];
@@ -1148,7 +1150,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             KSum<A> both[2 * (D + 2)];
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) { both[q] = wacc[q]; both[D + 2 + q] = wfc[q]; }
-            block_sum_ks<2 * (D + 2)>(both, red, sred);
+            block_sum_ks<2 * (D + 2), NT>(both, red, sred);
         }
         // Two lanes recover the two sets of primitives in one FP64 instruction stream (on
         // GB300 an FP64 warp instruction costs the same for one lane or 32): lane 0 the
@@ -1234,12 +1236,12 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const bool need_n = P.marching == KG_MARCH_CAIDVM;
     A* En = Ec + (size_t)D * MA;
     if constexpr (sizeof(A) == 8) {
-        gauss_table<D>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
-        if (need_n) gauss_table<D>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
+        gauss_table<D, NT>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
+        if (need_n) gauss_table<D, NT>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
     } else {
-        gauss_table<D>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
+        gauss_table<D, NT>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
         if (need_n)
-            gauss_table<D>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
+            gauss_table<D, NT>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
     }
     __syncthreads();
     const A prec = sc[C_PREC], pren = sc[C_PREN];
@@ -1263,7 +1265,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     };
     if (need_n) {
         // conservation correction f += M(prim_c) - M(prim)  (Theory/Iterate.jl:117), then q
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        for (int i = threadIdx.x; i < nv; i += NT) {
             A mc = prec, mn = pren;
 #pragma unroll
             for (int d = 0; d < D; ++d) {
@@ -1280,7 +1282,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
     } else {
         // Euler: q of f before convection (Theory/Iterate.jl:153)
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        for (int i = threadIdx.x; i < nv; i += NT) {
             A fv[NDF];
 #pragma unroll
             for (int k = 0; k < NDF; ++k) fv[k] = (A)fcell[k * nv + i];
@@ -1288,7 +1290,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
     }
     double qv[D];
-    block_sum_ks<D>(qs, qv, sred);
+    block_sum_ks<D, NT>(qs, qv, sred);
     if (threadIdx.x == 0)
         for (int d = 0; d < D; ++d) sc[C_QA + d] = (A)(0.5 * qv[d]);
     __syncthreads();
@@ -1321,7 +1323,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     };
     if (P.marching == KG_MARCH_CAIDVM) {
         // f = f tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:121-122)
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        for (int i = threadIdx.x; i < nv; i += NT) {
             A gp[NDF];
             gplus(i, gp);
 #pragma unroll
@@ -1329,7 +1331,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
     } else {
         // f = (f + dt/V flux) tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:156)
-        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        for (int i = threadIdx.x; i < nv; i += NT) {
             A gp[NDF];
             gplus(i, gp);
 #pragma unroll
@@ -1365,9 +1367,9 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 //  * persistent: `gridDim.x` resident CTAs take cells from the work counter (in `order`,
 //    when given), so a batch of uneven problems keeps every SM busy to the end of the
 //    sub-step.  The counter must be zero at launch.
-template <int D, int NDF, typename T, bool FG>
-__global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_kernel(Dev P, int* counter,
-                                                                                  const int32_t* order, int n) {
+template <int D, int NDF, typename T, bool FG, int NT>
+__global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) flux_collide_kernel(Dev P, int* counter,
+                                                                                             const int32_t* order, int n) {
     __shared__ int item;
     int it = blockIdx.x;
     for (;;) {
@@ -1378,7 +1380,7 @@ __global__ void __launch_bounds__(BLOCK, sizeof(T) == 4 ? 4 : 2) flux_collide_ke
             __syncthreads();
         }
         if (it >= n) break;
-        flux_collide_cell<D, NDF, T, FG>(P, order ? order[it] : it);
+        flux_collide_cell<D, NDF, T, FG, NT>(P, order ? order[it] : it);
         if (!counter) break;
         __syncthreads();
     }
@@ -1764,7 +1766,8 @@ template <int D, int NDF, typename T>
 struct Launch {
     static cudaError_t slope(const Dev& P, int pc_base, int n, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, pc_base);
+        if (P.slope_nt == 128) slope_kernel<D, NDF, T, 128><<<n, 128, 0, s>>>(P, pc_base);
+        else slope_kernel<D, NDF, T, BLOCK><<<n, BLOCK, 0, s>>>(P, pc_base);
         return cudaGetLastError();
     }
     static cudaError_t solid(const Dev& P, int n, cudaStream_t s) {
@@ -1783,15 +1786,17 @@ struct Launch {
     // the flux kernel of the layout's staging choice
     using FluxFn = void (*)(Dev, int*, const int32_t*, int);
     static FluxFn flux_fn(const Dev& P) {
-        return P.fst_global ? flux_collide_kernel<D, NDF, T, true> : flux_collide_kernel<D, NDF, T, false>;
+        if (P.fst_global) return flux_collide_kernel<D, NDF, T, true, BLOCK>;
+        return P.flux_nt == 128 ? flux_collide_kernel<D, NDF, T, false, 128> : flux_collide_kernel<D, NDF, T, false, BLOCK>;
     }
+    static int flux_threads(const Dev& P) { return P.fst_global ? BLOCK : (P.flux_nt == 128 ? 128 : BLOCK); }
     static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
         const FluxFn fn = flux_fn(P);
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        fn<<<n, BLOCK, smem, s>>>(P, nullptr, nullptr, n);
+        fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, nullptr, n);
         return cudaGetLastError();
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
@@ -1804,7 +1809,7 @@ struct Launch {
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(counter, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
-        fn<<<grid, BLOCK, smem, s>>>(P, counter, order, n);
+        fn<<<grid, flux_threads(P), smem, s>>>(P, counter, order, n);
         return cudaGetLastError();
     }
     static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {
@@ -1838,7 +1843,7 @@ struct Launch {
         const FluxFn fn = flux_fn(P);
         cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, BLOCK, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, flux_threads(P), smem);
         return nb;
     }
 };
