@@ -156,6 +156,10 @@ struct kg_handle {
     int64_t version = 0;
     std::vector<void*> topo_allocs;
     int64_t topo_bytes = 0;
+    // the read-only topology arrays of a layout in one allocation
+    char* arena = nullptr;
+    size_t arena_cap = 0, arena_used = 0;
+    bool arena_measure = false;    // first pass: only sum the sizes
     Flat M;
     Flat spare;                    // a previous problem's arrays, reused by the next flattening
     Dev dev{};
@@ -207,14 +211,21 @@ size_t storage_size(const kg_handle* h) { return h->prm.precision == KG_PREC_FP6
 template <typename V>
 int upload_vec(kg_handle* h, const std::vector<V>& v, const V** out) {
     size_t n = std::max<size_t>(v.size(), 1) * sizeof(V);
+    const size_t n256 = (n + 255) / 256 * 256;
+    if (h->arena_measure) { h->arena_used += n256; *out = nullptr; return KG_OK; }
     void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    h->topo_allocs.push_back(p);
-    h->topo_bytes += (int64_t)n;
+    if (h->arena && h->arena_used + n256 <= h->arena_cap) {
+        p = h->arena + h->arena_used;
+        h->arena_used += n256;
+    } else {
+        cudaError_t e = cudaMalloc(&p, n);
+        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+        h->topo_allocs.push_back(p);
+        h->topo_bytes += (int64_t)n;
+    }
     if (!v.empty()) {
         // on the handle's stream: a non-blocking stream is not ordered after the legacy one
-        e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, h->stream);
+        cudaError_t e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, h->stream);
         if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync topology");
     }
     *out = (const V*)p;
@@ -240,7 +251,11 @@ void free_topology(kg_handle* h) {
     for (void* p : h->topo_allocs) cudaFree(p);
     h->topo_allocs.clear();
     h->topo_bytes = 0;
+    if (h->arena) cudaFree(h->arena);
+    h->arena = nullptr;
+    h->arena_cap = h->arena_used = 0;
 }
+
 void free_pools(kg_handle* h) {
     free_topology(h);
     for (void* p : h->pool_allocs) cudaFree(p);
@@ -357,16 +372,33 @@ int rebuild(kg_handle* h) {
     P = Dev{};
     P.dim = h->prm.dim; P.ndf = h->prm.ndf; P.n_cells = M.n_cells; P.n_walls = M.n_walls;
     P.PG = (int64_t)M.vw.size();
+    // the read-only arrays: sizes first, then one arena, then the copies
+    auto upload_all = [&]() -> int {
 #define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
-    UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
-    UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
-    UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
-    UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
-    UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-    UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
-    UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
-    UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
+        UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
+        UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
+        UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
+        UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
+        UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
+        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+        UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
+        UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
+        return KG_OK;
+    };
+    h->arena_measure = true;
+    h->arena_used = 0;
+    upload_all();
+    h->arena_measure = false;
+    {
+        void* a = nullptr;
+        if (cudaMalloc(&a, h->arena_used) != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc topology");
+        h->arena = (char*)a;
+        h->arena_cap = h->arena_used;
+        h->topo_bytes += (int64_t)h->arena_cap;
+        h->arena_used = 0;
+    }
+    { int r = upload_all(); if (r) return r; }
     P.max_axis = M.max_axis;
     P.max_bcm = M.max_bcm;
     if (M.n_fluid > 0) {

@@ -14,6 +14,9 @@ CASES_FP64 = [
     ("cylinder_ib_adapted", lambda: cases.cylinder(scale=0.25, nv=24, vs_levels=2), 4),
     ("box3d_levels", lambda: cases.box3d(n=(6, 4, 4), nv=8, levels=1), 4),
     ("sphere3d_ib", lambda: cases.sphere(scale=0.25, nv=8), 3),
+    # 36^2 velocity grids (mean above 1024 velocity cells): the 256-thread flux and slope
+    # kernels; the cases above run the 128-thread ones
+    ("sod_v36_256_threads", lambda: cases.sod(scale=0.125, nv=36), 4),
 ]
 
 
