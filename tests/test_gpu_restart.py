@@ -86,3 +86,25 @@ def test_restart_rejects_bad_quadrant_maps():
     with pytest.raises(KitGpuError):
         g.download_restart(None, nc + 1)                         # n_quads without a map
     g.close()
+
+
+def test_batch_checkpoint_payload_equals_the_single_handle():
+    from kitgpu.solver import GpuBatch, GpuStep
+    p = cases.cylinder(scale=0.125, max_level=2, nv=16, vs_levels=1)
+    topo, state = cases.build(p)
+    q = cases.cavity(n=8, nv=12)
+    tq, sq = cases.build(q)
+    prm = abi.make_params(p, precision=abi.KG_PREC_MIXED)
+    g = GpuStep(prm, topo)
+    g.upload_state(state["f"], state["w"], state["prim"])
+    g.step(p.dt(), 0, 2)
+    exp_df, exp_ws = g.download_restart(topo["cell_quad"], topo["n_quads"])
+    g.close()
+    b = GpuBatch(prm, pool_bytes=256 << 20)
+    s0 = b.admit(abi.make_params(q, precision=abi.KG_PREC_MIXED), tq, sq["f"], sq["w"], sq["prim"], q.dt())
+    s1 = b.admit(prm, topo, state["f"], state["w"], state["prim"], p.dt())
+    b.step(2)
+    vs_df, ws = b.download_restart(s1, topo["cell_quad"], topo["n_quads"])
+    b.close()
+    assert s0 != s1
+    assert np.array_equal(vs_df, exp_df) and np.array_equal(ws, exp_ws)
