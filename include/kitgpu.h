@@ -246,6 +246,43 @@ typedef struct {
 } kg_adapt_src;
 int kg_adapt(kg_handle *h, const kg_topology *topo, const kg_adapt_src *src);
 
+/* ---- velocity-space adaptation flags on the device ---------------------------------------
+ * The per-velocity-cell decisions of vs_refine! / vs_coarsen! (Velocity_space/AMR.jl:26-118)
+ * computed from the device state, so the host's loops over every phase cell become one
+ * download of Nv bytes:
+ *   bit 0  refine:     level < maxlevel and, in KG_VS_LOHNER mode, the Löhner indicator
+ *                      (vs_lohner_indicator, Velocity_space/Criteria.jl:253-283) above
+ *                      coeffi_lohner or local_contribution_refine_flag; in KG_VS_CONTRIBUTION
+ *                      mode contribution_refine_flag (local or global, Criteria.jl:4-58);
+ *   bit 1  coarsen_ok: the indicator below 0.3 coeffi_lohner (VS_LOHNER_COARSEN_RATIO) and
+ *                      local_contribution_coarsen_flag (Löhner mode), or the local and global
+ *                      coarsen flags (contribution mode), for the cell's single velocity cell.
+ * The contribution flags read the criterion distribution df + max_d |sdf ds_d| of
+ * _criterion_cell! (the slopes on the device, as the reference reads PsData's) and, for the
+ * global ones, the Velocity_Resolution of vs_resolution (AMR.jl:135-166), returned in vr[2].
+ * Both bits are those of the grid on the device: the reference evaluates coarsening after its
+ * refinement pass, so bit 1 is final for cells with no bit 0 set.  Every cell with a
+ * distribution (solid ghost cells included, as vs_refine! visits them) gets its nv bytes, in
+ * cell order (Σ nv bytes); eta (optional) receives the indicator per velocity cell (Löhner
+ * mode; zeros otherwise).  Face neighbours in velocity space are the same-or-coarser leaves of
+ * vs_face_neighbor (Velocity_space/Neighbor.jl:181-204), the domain edge counting as vacuum.
+ * Arithmetic in FP64 from the stored f (FP32 in the mixed form).                         */
+#define KG_VS_LOHNER        0   /* ADAPT_VS_MODE = :lohner (the reference's default)     */
+#define KG_VS_CONTRIBUTION  1   /* any other mode: the contribution flags                 */
+typedef struct {
+    double  quadrature[6];     /* config.quadrature: (lower, upper) per dimension            */
+    int32_t vs_trees_num[3];
+    int32_t maxlevel;          /* solver.AMR_VS_MAXLEVEL                                    */
+    int32_t mode;              /* KG_VS_*                                                    */
+    int32_t pad;
+    double  coeffi_lohner;     /* solver.ADAPT_COEFFI_VS_LOHNER (default 0.6)               */
+    double  coeffi_local;      /* solver.ADAPT_COEFFI_VS_LOCAL (default 1e-2)               */
+    double  coeffi_global;     /* solver.ADAPT_COEFFI_VS_GLOBAL (default 0.125)             */
+} kg_vs_config;
+int kg_vs_flags(kg_handle *h, const kg_vs_config *cfg, uint8_t *flags, double *eta, double *vr);
+int kg_batch_vs_flags(kg_handle *h, int32_t slot, const kg_vs_config *cfg, uint8_t *flags, double *eta,
+                      double *vr);   /* kg_vs_flags of one problem (vr over that problem) */
+
 /* ---- checkpoint payload from the device (save_for_restart / restart, IO/Restart.jl) --------
  * kg_download_restart fills the per-rank arrays of restart_<rank>.jld2 that come from the
  * state (IO/Restart.jl:81-117), in FP64:

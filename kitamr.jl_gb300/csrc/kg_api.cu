@@ -22,6 +22,8 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
     static cudaError_t adapt(const Dev&, int, const AdaptRec*, const void*, const void*, const double*, const double*,
                              const double*, const int32_t*, const int8_t*, cudaStream_t);
+    static cudaError_t vs_resolution(const Dev&, int, int, double*, cudaStream_t);
+    static cudaError_t vs_flags(const Dev&, int, int, const VsFlagArgs&, cudaStream_t);
 };
 cudaError_t launch_residual(const Dev&, const int32_t*, int, double*, cudaStream_t);
 }  // namespace kg
@@ -1205,6 +1207,80 @@ int upload_restart(kg_handle* h, int slot, const int32_t* quad_index, int32_t n_
     return KG_OK;
 }
 
+// ---- velocity-space adaptation flags (vs_refine! / vs_coarsen!) -----------------------------
+int vs_flags(kg_handle* h, int slot, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr_out) {
+    const int D = h->prm.dim, NDF = h->prm.ndf;
+    if (cfg->maxlevel < 0 || cfg->maxlevel > 12) return fail(h, KG_ERR_ARG, "maxlevel out of range");
+    if (cfg->mode != KG_VS_LOHNER && cfg->mode != KG_VS_CONTRIBUTION) return fail(h, KG_ERR_ARG, "bad mode");
+    double vmin[MAXD] = {0, 0, 0}, du[MAXD] = {0, 0, 0}, hf[MAXD] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+        if (cfg->vs_trees_num[d] <= 0 || !(cfg->quadrature[2 * d + 1] > cfg->quadrature[2 * d]))
+            return fail(h, KG_ERR_ARG, "bad quadrature or vs_trees_num");
+        if (((int64_t)cfg->vs_trees_num[d] << cfg->maxlevel) >= (int64_t(1) << 20))
+            return fail(h, KG_ERR_ARG, "more than 2^20 finest velocity cells along a dimension");
+        vmin[d] = cfg->quadrature[2 * d];
+        du[d] = cfg->quadrature[2 * d + 1] - cfg->quadrature[2 * d];
+        hf[d] = du[d] / cfg->vs_trees_num[d] / std::ldexp(1.0, cfg->maxlevel);
+    }
+    int rc = rebuild(h);
+    if (rc) return rc;
+    Problem& pb = h->probs[slot];
+    const Flat& L = pb.F;
+    const int c0 = (int)pb.dbase, nc = L.n_cells;
+    const int64_t nv_total = L.foff[nc] / NDF;
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fA : h->fB;
+    P.f_out = h->parity == 0 ? h->fB : h->fA;
+    // vs_resolution: per-cell maxima on the device, the maximum over the fluid cells here
+    std::vector<double> res((size_t)nc * 2);
+    double* d_res = nullptr;
+    KG_CUDA(h, cudaMalloc(&d_res, sizeof(double) * std::max(nc, 1) * 2));
+    cudaError_t e = dispatch(h, [&](auto Lc) { return decltype(Lc)::vs_resolution(P, c0, nc, d_res, h->stream); });
+    if (e == cudaSuccess) e = cudaMemcpyAsync(res.data(), d_res, sizeof(double) * nc * 2, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_res);
+    if (e != cudaSuccess) return cuda_fail(h, e, "vs_resolution_kernel");
+    double pdu = du[0], ptn = cfg->vs_trees_num[0];
+    for (int d = 1; d < D; ++d) { pdu *= du[d]; ptn *= cfg->vs_trees_num[d]; }
+    const double rweight = pdu / ptn / std::ldexp(1.0, D * cfg->maxlevel);
+    double dens_res = 0.0, en_res = 0.0;
+    for (int c = 0; c < nc; ++c) {
+        if (L.dbe[c] < 0) continue;
+        dens_res = std::max(res[2 * c] * rweight, dens_res);
+        en_res = std::max(0.5 * res[2 * c + 1] * rweight, en_res);
+    }
+    if (vr_out) { vr_out[0] = dens_res; vr_out[1] = en_res; }
+    // face neighbours of every grid of the layout (host), then the flags (device)
+    const bool lohner = cfg->mode == KG_VS_LOHNER;
+    std::vector<int32_t> nbr;
+    if (lohner) vs_face_table(h->M, vmin, hf, cfg->vs_trees_num, cfg->maxlevel, nbr);
+    else nbr.assign(1, -1);
+    void* buf = nullptr;
+    const size_t b_nbr = sizeof(int32_t) * nbr.size(), b_fl = (size_t)std::max<int64_t>(nv_total, 1);
+    const size_t b_eta = eta ? sizeof(double) * std::max<int64_t>(nv_total, 1) : 0;
+    const size_t o_fl = (b_nbr + 255) / 256 * 256, o_eta = o_fl + (b_fl + 255) / 256 * 256;
+    KG_CUDA(h, cudaMalloc(&buf, o_eta + b_eta));
+    char* bb = (char*)buf;
+    VsFlagArgs A{};
+    A.nbr = (const int32_t*)bb;
+    A.flags = (uint8_t*)(bb + o_fl);
+    A.eta = eta ? (double*)(bb + o_eta) : nullptr;
+    A.row0 = h->M.foff[c0];
+    for (int d = 0; d < MAXD; ++d) A.hf[d] = hf[d];
+    A.dens_res = dens_res; A.en_res = en_res;
+    A.tau_l = cfg->coeffi_lohner; A.tau_c = 0.3 * cfg->coeffi_lohner;   // VS_LOHNER_COARSEN_RATIO
+    A.c_local = cfg->coeffi_local; A.c_global = cfg->coeffi_global;
+    A.maxlevel = cfg->maxlevel; A.lohner = lohner ? 1 : 0;
+    e = cudaMemcpyAsync(bb, nbr.data(), b_nbr, cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = dispatch(h, [&](auto Lc) { return decltype(Lc)::vs_flags(P, c0, nc, A, h->stream); });
+    if (e == cudaSuccess) e = cudaMemcpyAsync(flags, A.flags, (size_t)nv_total, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess && eta) e = cudaMemcpyAsync(eta, A.eta, sizeof(double) * nv_total, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(h, e, "vs_flags_kernel");
+    return KG_OK;
+}
+
 int check_params(const kg_params* params, std::string& err) {
     if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) { err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1"; return KG_ERR_ARG; }
     if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { err = "bad precision"; return KG_ERR_ARG; }
@@ -1364,6 +1440,15 @@ int kg_upload_restart(kg_handle* h, const int32_t* quad_index, int32_t n_quads, 
     if (rc) { if (!was_live) pb.live = false; return rc; }
     h->have_state = true;
     return KG_OK;
+}
+
+int kg_vs_flags(kg_handle* h, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr) {
+    if (!h) return KG_ERR_ARG;
+    if (!cfg || !flags) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_vs_flags");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return vs_flags(h, 0, cfg, flags, eta, vr);
 }
 
 int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_report* report) {
@@ -1545,6 +1630,13 @@ int kg_batch_download_restart(kg_handle* h, int32_t slot, const int32_t* quad_in
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
     return download_restart(h, slot, quad_index, n_quads, vs_df, ws);
+}
+
+int kg_batch_vs_flags(kg_handle* h, int32_t slot, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    if (!cfg || !flags) return fail(h, KG_ERR_ARG, "null argument");
+    cudaSetDevice(h->device);
+    return vs_flags(h, slot, cfg, flags, eta, vr);
 }
 
 int kg_batch_info(const kg_handle* h, int32_t* n_live, int64_t* f_free_elems, int64_t* bytes_per_elem) {

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <utility>
 #include "kg_internal.h"
 
@@ -790,6 +791,65 @@ int64_t device_bytes(const Flat& F, int precision) {
     b += (int64_t)F.wall_ops.size() * sizeof(WallOp) + (int64_t)F.cvcw.size() * 8;
     b += (int64_t)F.n_data * 64;
     return b;
+}
+
+}  // namespace kg
+
+namespace kg {
+
+// Leaves are keyed by (level, index of their lower corner at that level); the leaf containing
+// a finest-level point is the key found first from the finest level down.  The corner and the
+// probe are computed with the reference's arithmetic (round of the corner, floor of the probe
+// across the face at the face-centre line), so the answers are the leaves its sorted-key search
+// returns.
+void vs_face_table(const Flat& M, const double* vmin, const double* hf, const int32_t* trees, int maxlevel,
+                   std::vector<int32_t>& nbr) {
+    const int D = M.dim;
+    const int64_t PG = (int64_t)M.vw.size();
+    nbr.assign((size_t)PG * 2 * D, -1);
+    const int G = (int)M.g_off.size() - 1;
+    std::unordered_map<uint64_t, int32_t> leaf;
+    auto key = [&](int L, const int64_t* g) {
+        uint64_t k = (uint64_t)L;
+        for (int d = 0; d < D; ++d) k = (k << 20) | (uint64_t)(g[d] >> (maxlevel - L));
+        return k;
+    };
+    for (int gi = 0; gi < G; ++gi) {
+        const int64_t o = M.g_off[gi], nv = M.g_off[gi + 1] - o;
+        leaf.clear();
+        leaf.reserve((size_t)nv * 2);
+        for (int64_t i = 0; i < nv; ++i) {
+            const int L = M.vlev[o + i];
+            int64_t g[MAXD];
+            for (int d = 0; d < D; ++d) {
+                const double cell = hf[d] * (double)(1L << (maxlevel - L));
+                g[d] = (int64_t)std::nearbyint((M.vu[(size_t)d * PG + o + i] - 0.5 * cell - vmin[d]) / hf[d]);
+            }
+            leaf[key(L, g)] = (int32_t)i;
+        }
+        for (int64_t i = 0; i < nv; ++i) {
+            const int L = M.vlev[o + i];
+            for (int dim = 0; dim < D; ++dim) {
+                for (int side = 0; side < 2; ++side) {
+                    const int dir = side == 0 ? -1 : 1;
+                    const double cell = hf[dim] * (double)(1L << (maxlevel - L));
+                    int64_t g[MAXD];
+                    bool inside = true;
+                    for (int d = 0; d < D && inside; ++d) {
+                        double coord = M.vu[(size_t)d * PG + o + i];
+                        if (d == dim) coord += dir * (0.5 * cell + 0.5 * hf[d]);
+                        g[d] = (int64_t)std::floor((coord - vmin[d]) / hf[d]);
+                        inside = g[d] >= 0 && g[d] < ((int64_t)trees[d] << maxlevel);
+                    }
+                    if (!inside) continue;
+                    for (int l = maxlevel; l >= 0; --l) {
+                        auto it = leaf.find(key(l, g));
+                        if (it != leaf.end()) { nbr[(size_t)(o + i) * 2 * D + 2 * dim + side] = it->second; break; }
+                    }
+                }
+            }
+        }
+    }
 }
 
 }  // namespace kg

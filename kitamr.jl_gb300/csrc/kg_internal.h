@@ -193,6 +193,24 @@ struct AdaptRec {
     int8_t path[8];        // REFINE: child number (RMT order, bit d = upper half in dim d)
 };
 
+// Arguments of the velocity-space flag kernel (see kg_vs_flags).
+struct VsFlagArgs {
+    const int32_t* nbr;      // per velocity cell of every grid: 2*dim face neighbours (grid-local, -1: none)
+    uint8_t* flags;          // per velocity cell of the problem's cells, in cell order
+    double* eta;             // the same rows, or null
+    int64_t row0;            // f offset of the problem's first cell (rows = f offset / ndf)
+    double hf[MAXD];         // finest velocity-cell size per dimension
+    double dens_res, en_res; // Velocity_Resolution
+    double tau_l, tau_c, c_local, c_global;
+    int maxlevel, lohner;
+};
+
+// Same-or-coarser face neighbours in velocity space (vs_face_neighbor,
+// Velocity_space/Neighbor.jl:181-204) of every velocity cell of the layout's grids: 2*dim
+// grid-local leaf indices per cell (-1 across the velocity-domain edge).
+void vs_face_table(const Flat& M, const double* vmin, const double* hf, const int32_t* trees, int maxlevel,
+                   std::vector<int32_t>& nbr);
+
 // The level merge walk of two velocity grids (diff_vs!, vs_merge!): per cell of grid A the
 // (first, count) run of grid-B cells overlapping it.  False when the grids do not tile the
 // same root lattice.

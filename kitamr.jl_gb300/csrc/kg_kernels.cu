@@ -1615,6 +1615,150 @@ __global__ void __launch_bounds__(BLOCK) residual_kernel(Dev P, const int32_t* l
 }
 
 // ---- launchers ------------------------------------------------------------------
+// ---- velocity-space adaptation flags (vs_refine! / vs_coarsen!, Velocity_space/AMR.jl:26-118)
+// Block maximum of N doubles (every thread sees the result); sred: N * (BLOCK/32) doubles.
+template <int N>
+__device__ __forceinline__ void block_max(double (&v)[N], double* sred) {
+    constexpr int NWARP = BLOCK / 32;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+        double x = v[e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x = fmax(x, __shfl_xor_sync(0xffffffffu, x, o));
+        v[e] = x;
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int e = 0; e < N; ++e) sred[e * NWARP + wid] = v[e];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int e = 0; e < N; ++e) {
+        double x = sred[e * NWARP];
+        for (int q = 1; q < NWARP; ++q) x = fmax(x, sred[e * NWARP + q]);
+        v[e] = x;
+    }
+    __syncthreads();
+}
+
+// vs_resolution (Velocity_space/AMR.jl:153-166) of the cells [c0, c0 + gridDim.x): the largest
+// df entry and the largest h|U-u|^2 + b (3D: f|U-u|^2) of each, into out[2 * (cell - c0)]
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) vs_resolution_kernel(Dev P, int c0, double* out) {
+    __shared__ double sred[2 * (BLOCK / 32)];
+    const int cell = c0 + blockIdx.x;
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const T* fc = (const T*)P.f_in + P.foff[cell];
+    const double* U = P.prim + (int64_t)cell * MAXW + 1;
+    double m[2] = {-INFINITY, -INFINITY};
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        double c2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { const double x = U[d] - P.vu[(int64_t)d * P.PG + g.goff + i]; c2 += x * x; }
+        const double h = (double)fc[i];
+        m[0] = fmax(m[0], h);
+        if (NDF == 2) {
+            const double b = (double)fc[nv + i];
+            m[0] = fmax(m[0], b);
+            m[1] = fmax(m[1], h * c2 + b);
+        } else {
+            m[1] = fmax(m[1], h * c2);
+        }
+    }
+    block_max<2>(m, sred);
+    if (threadIdx.x == 0) { out[2 * blockIdx.x] = m[0]; out[2 * blockIdx.x + 1] = m[1]; }
+}
+
+
+// _lohner_ratio (Velocity_space/Criteria.jl:221-227)
+__device__ __forceinline__ double vs_lohner_ratio(double L, double C, double R, double dsL, double dsR, double scale) {
+    const double num = fabs(dsR * L - (dsL + dsR) * C + dsL * R);
+    const double den = dsR * fabs(L - C) + dsL * fabs(R - C) +
+                       1e-2 * (dsR * fabs(L) + (dsL + dsR) * fabs(C) + dsL * fabs(R)) + 1e-3 * scale * (dsL + dsR);
+    return den > 0 ? num / den : 0.0;
+}
+
+// The flags of vs_refine! / vs_coarsen! for the cells [c0, c0 + gridDim.x), one CTA each, in
+// FP64: the criterion distribution and contribution flags (_criterion_cell!,
+// local_/global_contribution_*_flag, Criteria.jl:18-78) and the Löhner indicator
+// (vs_lohner_indicator, Criteria.jl:253-283) over the face-neighbour table.
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) vs_flags_kernel(Dev P, int c0, VsFlagArgs A) {
+    __shared__ double sred[2 * (BLOCK / 32)];
+    const int cell = c0 + blockIdx.x;
+    const VGridView g = grid_view(P, cell);
+    const int nv = g.nv;
+    const int64_t fo = P.foff[cell];
+    const T* fc = (const T*)P.f_in + fo;
+    const T* sc = (const T*)P.sdf + fo * D;
+    const double* wc = P.w + (int64_t)cell * MAXW;
+    const double* U = P.prim + (int64_t)cell * MAXW + 1;
+    const double* ds = P.dds + (int64_t)cell * MAXD;
+    const int32_t* nb = A.nbr + (g.goff) * 2 * D;
+    const int8_t* lev = P.vlev + g.goff;
+    // vs_lohner_scales: the largest |h| and |b| of the cell
+    double s[2] = {0.0, 0.0};
+    if (A.lohner) {
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            s[0] = fmax(s[0], fabs((double)fc[i]));
+            if (NDF == 2) s[1] = fmax(s[1], fabs((double)fc[nv + i]));
+        }
+        block_max<2>(s, sred);
+    }
+    double U2 = 0.0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) U2 += U[d] * U[d];
+    const double den = wc[D + 1] - 0.5 * wc[0] * U2;
+    const double nch = (double)(1 << D);
+    const int64_t row = (fo - A.row0) / NDF;
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        double cdf[NDF];
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) {
+            double mm = 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) mm = fmax(mm, fabs((double)sc[((int64_t)d * NDF + k) * nv + i] * ds[d]));
+            cdf[k] = (double)fc[(int64_t)k * nv + i] + mm;
+        }
+        double S = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { const double x = U[d] - P.vu[(int64_t)d * P.PG + g.goff + i]; S += x * x; }
+        const double wt = P.vw[g.goff + i];
+        const double en = NDF == 2 ? 0.5 * (S * cdf[0] + cdf[NDF - 1]) * wt : 0.5 * S * cdf[0] * wt;
+        const double rho = cdf[0] * wt;
+        const bool loc_ref = fmax(fabs(en) / den, rho / wc[0]) > A.c_local;
+        const bool loc_coa = fmax(en / den, rho / wc[0]) < A.c_local / nch;
+        const bool glo_ref = rho > A.c_global * A.dens_res || en > A.en_res * A.c_global;
+        const bool glo_coa = rho < A.c_global * A.dens_res / nch && en < A.en_res * A.c_global / nch;
+        double e = 0.0;
+        if (A.lohner) {
+            const int li = lev[i];
+            const double h0 = (double)fc[i];
+            const double b0 = NDF == 2 ? (double)fc[nv + i] : 0.0;
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const double hi = A.hf[d] * (double)(1 << (A.maxlevel - li));
+                const int Ln = nb[(int64_t)i * 2 * D + 2 * d], Rn = nb[(int64_t)i * 2 * D + 2 * d + 1];
+                const double dsL = Ln < 0 ? hi : 0.5 * (hi + A.hf[d] * (double)(1 << (A.maxlevel - lev[Ln])));
+                const double dsR = Rn < 0 ? hi : 0.5 * (hi + A.hf[d] * (double)(1 << (A.maxlevel - lev[Rn])));
+                const double hL = Ln < 0 ? 0.0 : (double)fc[Ln], hR = Rn < 0 ? 0.0 : (double)fc[Rn];
+                e = fmax(e, vs_lohner_ratio(hL, h0, hR, dsL, dsR, s[0]));
+                if (NDF == 2) {
+                    const double bL = Ln < 0 ? 0.0 : (double)fc[nv + Ln], bR = Rn < 0 ? 0.0 : (double)fc[nv + Rn];
+                    e = fmax(e, vs_lohner_ratio(bL, b0, bR, dsL, dsR, s[1]));
+                }
+            }
+        }
+        const bool refine = lev[i] < A.maxlevel && (A.lohner ? (e > A.tau_l || loc_ref) : (loc_ref || glo_ref));
+        const bool coarsen = A.lohner ? (e < A.tau_c && loc_coa) : (loc_coa && glo_coa);
+        A.flags[row + i] = (uint8_t)((refine ? 1 : 0) | (coarsen ? 2 : 0));
+        if (A.eta) A.eta[row + i] = e;
+    }
+}
+
 // ---- physical-space adaptation (ps_replace!, Physical_space/AMR.jl:633-703) ----------
 // One CTA per cell of the adapted mesh (layout P, state written into P.f_in / P.sdf / P.w /
 // P.prim / P.qf) from the pools of the previous mesh (V).  Arithmetic in the form's precision
@@ -1815,6 +1959,17 @@ struct Launch {
     static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
         macro_slope_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, fbegin, dbase, out);
+        return cudaGetLastError();
+    }
+    // velocity-space adaptation: resolution terms, then flags, of the cells [c0, c0 + n)
+    static cudaError_t vs_resolution(const Dev& P, int c0, int n, double* out, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        vs_resolution_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, c0, out);
+        return cudaGetLastError();
+    }
+    static cudaError_t vs_flags(const Dev& P, int c0, int n, const VsFlagArgs& A, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        vs_flags_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, c0, A);
         return cudaGetLastError();
     }
     // adapted-mesh state from the previous pools, one CTA per cell record

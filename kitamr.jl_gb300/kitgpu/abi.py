@@ -108,6 +108,28 @@ ADAPT_SRC = np.dtype([("kind", "<i4"), ("depth", "<i4"), ("src", "<i4", (8,)), (
 assert ADAPT_SRC.itemsize == 48
 
 
+KG_VS_LOHNER, KG_VS_CONTRIBUTION = 0, 1
+
+
+class KgVsConfig(C.Structure):
+    _fields_ = [
+        ("quadrature", C.c_double * 6), ("vs_trees_num", C.c_int32 * 3), ("maxlevel", C.c_int32),
+        ("mode", C.c_int32), ("pad", C.c_int32), ("coeffi_lohner", C.c_double), ("coeffi_local", C.c_double),
+        ("coeffi_global", C.c_double),
+    ]
+
+
+def make_vs_config(problem, maxlevel=None, mode=KG_VS_LOHNER, coeffi_lohner=0.6, coeffi_local=1e-2,
+                   coeffi_global=0.125) -> KgVsConfig:
+    """The velocity-space adaptation settings of a case (solver defaults of Solver/Types.jl:97-100)."""
+    c = problem.case
+    q = list(c.quadrature) + [0.0] * (6 - len(c.quadrature))
+    tn = list(c.vs_trees_num) + [1] * (3 - len(c.vs_trees_num))
+    ml = problem.vs_maxlevel if maxlevel is None else maxlevel
+    return KgVsConfig(quadrature=(C.c_double * 6)(*q), vs_trees_num=(C.c_int32 * 3)(*tn), maxlevel=ml, mode=mode,
+                      pad=0, coeffi_lohner=coeffi_lohner, coeffi_local=coeffi_local, coeffi_global=coeffi_global)
+
+
 def dptr(a: np.ndarray):
     assert a.dtype == np.float64 and a.flags.c_contiguous
     return a.ctypes.data_as(C.POINTER(C.c_double))

@@ -56,6 +56,8 @@ def load_library(path: Optional[str] = None):
     L.kg_adapt.argtypes = [vp, vp, vp]
     L.kg_batch_adapt.argtypes = [vp, i32, vp, vp]
     L.kg_download_restart.argtypes = [vp, vp, i32, vp, vp]
+    L.kg_vs_flags.argtypes = [vp, vp, vp, vp, vp]
+    L.kg_batch_vs_flags.argtypes = [vp, i32, vp, vp, vp, vp]
     L.kg_upload_restart.argtypes = [vp, vp, i32, vp, vp]
     L.kg_batch_download_restart.argtypes = [vp, i32, vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
@@ -71,6 +73,7 @@ EXPORTS = [
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
     "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
+    "kg_vs_flags", "kg_batch_vs_flags",
 ]
 
 
@@ -177,6 +180,17 @@ class GpuStep:
         self.topo, self._tref = topo, tref
         self.foff = f_offsets(topo)
         self.nc = int(topo["n_cells"])
+
+    def vs_flags(self, vs_cfg: abi.KgVsConfig, eta: bool = True):
+        """vs_refine! / vs_coarsen!'s per-velocity flags (bit 0 refine, bit 1 coarsen on the
+        current grid), the Löhner indicator (or None) and the Velocity_Resolution."""
+        nv_total = int(self.foff[self.nc]) // int(self.topo["ndf"])
+        fl = np.empty(max(nv_total, 1), np.uint8)
+        et = np.empty(max(nv_total, 1)) if eta else None
+        vr = np.empty(2)
+        _check(self.L, self.h, self.L.kg_vs_flags(self.h, C.byref(vs_cfg), fl.ctypes.data,
+                                                    et.ctypes.data if eta else None, vr.ctypes.data))
+        return fl[:nv_total], (et[:nv_total] if eta else None), vr
 
     def download_restart(self, quad_index: Optional[np.ndarray] = None, n_quads: Optional[int] = None):
         """The state arrays of save_for_restart: vs_df (Nv x ndf) and ws (n_quads x dim+2)."""
@@ -304,6 +318,16 @@ class GpuBatch:
         _check(self.L, self.h, self.L.kg_batch_adapt(self.h, slot, C.cast(tref.ptr, C.c_void_p), src.ctypes.data))
         from .mesh import f_offsets
         self.meta[slot] = (topo, f_offsets(topo))
+
+    def vs_flags(self, slot: int, vs_cfg: abi.KgVsConfig, eta: bool = True):
+        topo, foff = self.meta[slot]
+        nv_total = int(foff[int(topo["n_cells"])]) // int(topo["ndf"])
+        fl = np.empty(max(nv_total, 1), np.uint8)
+        et = np.empty(max(nv_total, 1)) if eta else None
+        vr = np.empty(2)
+        _check(self.L, self.h, self.L.kg_batch_vs_flags(self.h, slot, C.byref(vs_cfg), fl.ctypes.data,
+                                                          et.ctypes.data if eta else None, vr.ctypes.data))
+        return fl[:nv_total], (et[:nv_total] if eta else None), vr
 
     def download_restart(self, slot: int, quad_index: Optional[np.ndarray] = None, n_quads: Optional[int] = None):
         topo, foff = self.meta[slot]

@@ -1405,3 +1405,193 @@ int kgo_last_error(char* buf, size_t cap) {
 }
 
 }  // extern "C"
+
+// ---- velocity-space adaptation flags: vs_refine! / vs_coarsen!'s per-velocity decisions
+// (Velocity_space/AMR.jl:26-118, Criteria.jl:4-78,212-283, Neighbor.jl:74-204), restated on
+// the topology arrays with the reference's own sorted-key index.
+namespace {
+constexpr int VS_INDEX_BITS = 24;
+constexpr uint64_t VS_INDEX_MASK = (uint64_t(1) << VS_INDEX_BITS) - 1;
+struct VsIndex {
+    int D = 2, maxlevel = 0, mortonbits = 0;
+    double vmin[3] = {0, 0, 0}, hf[3] = {0, 0, 0};
+    long tn[3] = {1, 1, 1}, stride[3] = {1, 1, 1};
+    std::vector<uint64_t> keys;
+};
+// build_vs_index! (Neighbor.jl:74-137)
+void vs_build(VsIndex& ix, const Grid& g, int D, const double* vmin, const double* ds0, const int32_t* tn, int maxlevel) {
+    ix.D = D; ix.maxlevel = maxlevel; ix.mortonbits = D * maxlevel;
+    long s = 1;
+    for (int d = 0; d < D; ++d) {
+        ix.vmin[d] = vmin[d];
+        ix.hf[d] = ds0[d] / std::ldexp(1.0, maxlevel);
+        ix.tn[d] = tn[d];
+        ix.stride[d] = s;
+        s *= tn[d];
+    }
+    const long mask = (1L << maxlevel) - 1;
+    ix.keys.resize(g.nv);
+    for (int i = 0; i < g.nv; ++i) {
+        const int L = g.level[i];
+        long root_lin = 0;
+        uint64_t morton = 0;
+        for (int d = 0; d < D; ++d) {
+            const double cell = ix.hf[d] * (double)(1L << (maxlevel - L));
+            const long gi = (long)std::nearbyint((g.u(i, d) - 0.5 * cell - ix.vmin[d]) / ix.hf[d]);   // round, ties to even
+            root_lin += (gi >> maxlevel) * ix.stride[d];
+            const long q = gi & mask;
+            for (int b = 0; b < maxlevel; ++b) morton |= (uint64_t)((q >> b) & 1) << (b * D + d);
+        }
+        const uint64_t cellkey = ((uint64_t)root_lin << ix.mortonbits) | morton;
+        ix.keys[i] = (cellkey << VS_INDEX_BITS) | (uint64_t)(i + 1);
+    }
+    std::sort(ix.keys.begin(), ix.keys.end());
+}
+// _vs_locate_code (Neighbor.jl:139-151): 0-based leaf, or -1
+int vs_locate_code(const VsIndex& ix, const Grid& g, uint64_t code) {
+    const uint64_t packed = (code << VS_INDEX_BITS) | VS_INDEX_MASK;
+    auto it = std::upper_bound(ix.keys.begin(), ix.keys.end(), packed);   // searchsortedlast
+    if (it == ix.keys.begin()) return -1;
+    --it;
+    const uint64_t corner = *it >> VS_INDEX_BITS;
+    const int leaf = (int)(*it & VS_INDEX_MASK) - 1;
+    const uint64_t span = uint64_t(1) << (ix.D * (ix.maxlevel - g.level[leaf]));
+    return (code >= corner && code < corner + span) ? leaf : -1;
+}
+// vs_face_neighbor (Neighbor.jl:181-204)
+int vs_face_neighbor(const VsIndex& ix, const Grid& g, int i, int dim, int dir) {
+    const long mask = (1L << ix.maxlevel) - 1;
+    long root_lin = 0;
+    uint64_t morton = 0;
+    const int L = g.level[i];
+    const double cell = ix.hf[dim] * (double)(1L << (ix.maxlevel - L));
+    for (int d = 0; d < ix.D; ++d) {
+        double coord = g.u(i, d);
+        if (d == dim) coord += dir * (0.5 * cell + 0.5 * ix.hf[d]);
+        const long gi = (long)std::floor((coord - ix.vmin[d]) / ix.hf[d]);
+        if (gi < 0 || gi >= (ix.tn[d] << ix.maxlevel)) return -1;
+        root_lin += (gi >> ix.maxlevel) * ix.stride[d];
+        const long q = gi & mask;
+        for (int b = 0; b < ix.maxlevel; ++b) morton |= (uint64_t)((q >> b) & 1) << (b * ix.D + d);
+    }
+    return vs_locate_code(ix, g, ((uint64_t)root_lin << ix.mortonbits) | morton);
+}
+double vs_cell_size(const VsIndex& ix, const Grid& g, int j, int d) { return ix.hf[d] * (double)(1L << (ix.maxlevel - g.level[j])); }
+// _lohner_ratio (Criteria.jl:221-227)
+double vs_lohner_ratio(double L, double C, double R, double dsL, double dsR, double eflt, double eabs, double scale) {
+    const double num = std::fabs(dsR * L - (dsL + dsR) * C + dsL * R);
+    const double den = dsR * std::fabs(L - C) + dsL * std::fabs(R - C) +
+                       eflt * (dsR * std::fabs(L) + (dsL + dsR) * std::fabs(C) + dsL * std::fabs(R)) +
+                       eabs * scale * (dsL + dsR);
+    return den > 0 ? num / den : 0.0;
+}
+}  // namespace
+
+extern "C" int kgo_vs_flags(const kg_params* prm, const kg_topology* t, const double* f, const double* sdf,
+                            const double* w, const double* prim, const kg_vs_config* cfg, uint8_t* flags,
+                            double* eta, double* vr_out) {
+    Model m;
+    int rc = setup(m, prm, t);
+    if (rc) return rc;
+    const int D = m.dim, NDF = m.ndf, NW = D + 2;
+    double vmin[3] = {0, 0, 0}, ds0[3] = {0, 0, 0}, du[3] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) {
+        vmin[d] = cfg->quadrature[2 * d];
+        du[d] = cfg->quadrature[2 * d + 1] - cfg->quadrature[2 * d];
+        ds0[d] = du[d] / cfg->vs_trees_num[d];
+    }
+    const int maxlevel = cfg->maxlevel;
+    // vs_resolution (AMR.jl:139-166)
+    double pdu = du[0], ptn = cfg->vs_trees_num[0];
+    for (int d = 1; d < D; ++d) { pdu *= du[d]; ptn *= cfg->vs_trees_num[d]; }
+    const double rweight = pdu / ptn / std::ldexp(1.0, D * maxlevel);
+    double dens_res = 0.0, en_res = 0.0;
+    for (int c = 0; c < t->n_cells; ++c) {
+        if (t->cell_bound_enc[c] < 0) continue;
+        const Grid& g = m.grids[t->cell_grid[c]];
+        const double* fc = f + m.foff[c];
+        const double* U = prim + (size_t)c * NW + 1;
+        double dmax = -INFINITY, emax = -INFINITY;
+        for (int k = 0; k < NDF; ++k)
+            for (int i = 0; i < g.nv; ++i) dmax = std::max(dmax, fc[(size_t)k * g.nv + i]);
+        for (int i = 0; i < g.nv; ++i) {
+            double c2 = 0.0;
+            for (int d = 0; d < D; ++d) { const double x = U[d] - g.u(i, d); c2 += x * x; }
+            const double e = NDF == 1 ? fc[i] * c2 : fc[i] * c2 + fc[g.nv + i];
+            emax = std::max(emax, e);
+        }
+        dens_res = std::max(dmax * rweight, dens_res);
+        en_res = std::max(0.5 * emax * rweight, en_res);
+    }
+    if (vr_out) { vr_out[0] = dens_res; vr_out[1] = en_res; }
+    const bool lohner = cfg->mode == KG_VS_LOHNER;
+    const double tauL = cfg->coeffi_lohner, tauC = 0.3 * cfg->coeffi_lohner;
+    const double cl = cfg->coeffi_local, cg = cfg->coeffi_global;
+    const double nch = std::ldexp(1.0, D);
+    VsIndex ix;
+    int64_t row = 0;
+    for (int c = 0; c < t->n_cells; ++c) {
+        const Grid& g = m.grids[t->cell_grid[c]];
+        const double* fc = f + m.foff[c];
+        const double* sc = sdf + m.soff[c];
+        const double* wc = w + (size_t)c * NW;
+        const double* U = prim + (size_t)c * NW + 1;
+        const double* ds = t->cell_ds + (size_t)c * D;
+        double s1 = 0.0, s2 = 0.0;
+        if (lohner) {
+            vs_build(ix, g, D, vmin, ds0, cfg->vs_trees_num, maxlevel);
+            for (int i = 0; i < g.nv; ++i) {
+                const double a1 = std::fabs(fc[i]);
+                if (a1 > s1) s1 = a1;
+                if (NDF == 2) { const double a2 = std::fabs(fc[g.nv + i]); if (a2 > s2) s2 = a2; }
+            }
+        }
+        double U2 = 0.0;
+        for (int d = 0; d < D; ++d) U2 += U[d] * U[d];
+        const double den = wc[NW - 1] - 0.5 * wc[0] * U2;
+        for (int i = 0; i < g.nv; ++i) {
+            // _criterion_cell! (AMR.jl:8-20)
+            double cdf[2];
+            for (int k = 0; k < NDF; ++k) {
+                double mm = 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double a = std::fabs(Model::S(const_cast<double*>(sc), g.nv, NDF, i, k, d) * ds[d]);
+                    if (a > mm) mm = a;
+                }
+                cdf[k] = fc[(size_t)k * g.nv + i] + mm;
+            }
+            double S = 0.0;
+            for (int d = 0; d < D; ++d) { const double x = U[d] - g.u(i, d); S += x * x; }
+            const double wt = g.weight[i];
+            const double en = NDF == 2 ? 0.5 * (S * cdf[0] + cdf[1]) * wt : 0.5 * S * cdf[0] * wt;
+            const double rho = cdf[0] * wt;
+            const bool loc_ref = std::max(std::fabs(en) / den, rho / wc[0]) > cl;
+            const bool loc_coa = std::max(en / den, rho / wc[0]) < cl / nch;
+            const bool glo_ref = rho > cg * dens_res || en > en_res * cg;
+            const bool glo_coa = rho < cg * dens_res / nch && en < en_res * cg / nch;
+            double e = 0.0;
+            if (lohner) {
+                // vs_lohner_indicator (Criteria.jl:253-283)
+                const double h0 = fc[i], b0 = NDF == 2 ? fc[g.nv + i] : 0.0;
+                for (int d = 0; d < D; ++d) {
+                    const double hi = vs_cell_size(ix, g, i, d);
+                    const int Ln = vs_face_neighbor(ix, g, i, d, -1), Rn = vs_face_neighbor(ix, g, i, d, +1);
+                    const double dsL = Ln < 0 ? hi : 0.5 * (hi + vs_cell_size(ix, g, Ln, d));
+                    const double dsR = Rn < 0 ? hi : 0.5 * (hi + vs_cell_size(ix, g, Rn, d));
+                    const double hL = Ln < 0 ? 0.0 : fc[Ln], hR = Rn < 0 ? 0.0 : fc[Rn];
+                    e = std::max(e, vs_lohner_ratio(hL, h0, hR, dsL, dsR, 1e-2, 1e-3, s1));
+                    if (NDF == 2) {
+                        const double bL = Ln < 0 ? 0.0 : fc[g.nv + Ln], bR = Rn < 0 ? 0.0 : fc[g.nv + Rn];
+                        e = std::max(e, vs_lohner_ratio(bL, b0, bR, dsL, dsR, 1e-2, 1e-3, s2));
+                    }
+                }
+            }
+            const bool refine = g.level[i] < maxlevel && (lohner ? (e > tauL || loc_ref) : (loc_ref || glo_ref));
+            const bool coarsen = lohner ? (e < tauC && loc_coa) : (loc_coa && glo_coa);
+            flags[row + i] = (uint8_t)((refine ? 1 : 0) | (coarsen ? 2 : 0));
+            if (eta) eta[row + i] = e;
+        }
+        row += g.nv;
+    }
+    return KG_OK;
+}

@@ -39,6 +39,8 @@ def lib():
         L.kgo_moments.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4
         L.kgo_macro_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 2
         L.kgo_adapt.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 10
+        L.kgo_vs_flags.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 4 + \
+            [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.kgo_slope.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + [C.c_int32]
         L.kgo_criterion.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + \
             [C.c_double, C.POINTER(C.c_double)]
@@ -149,6 +151,21 @@ class OracleState:
         out.sdf[:] = sdf
         out.qf[:] = qf
         return out
+
+    def vs_flags(self, params, vs_cfg):
+        """vs_refine! / vs_coarsen!'s per-velocity flags on this state (bit 0 refine, bit 1
+        coarsen on the current grid), the Löhner indicator and the Velocity_Resolution."""
+        from kitgpu.mesh import f_offsets
+        nv_total = int(f_offsets(self.topo)[-1]) // int(self.topo["ndf"])
+        flags = np.zeros(max(nv_total, 1), np.uint8)
+        eta = np.zeros(max(nv_total, 1))
+        vr = np.zeros(2)
+        rc = lib().kgo_vs_flags(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.f),
+                                abi.dptr(self.sdf), abi.dptr(self.w), abi.dptr(self.prim), C.byref(vs_cfg),
+                                C.c_void_p(flags.ctypes.data), C.c_void_p(eta.ctypes.data), C.c_void_p(vr.ctypes.data))
+        if rc != 0:
+            raise RuntimeError(f"oracle vs_flags failed: {rc}")
+        return flags[:nv_total], eta[:nv_total], vr
 
     def moments(self, params):
         nc, nw = self.topo["n_cells"], self.topo["dim"] + 2

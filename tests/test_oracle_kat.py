@@ -242,3 +242,45 @@ def test_adapt_coarsening_conserves_each_childs_mass_across_grids():
         # w of a coarsened cell is the children's mean (not the moments of the merged df)
         assert np.allclose(out.w.reshape(-1, 4)[c], st.w.reshape(-1, 4)[ch].mean(axis=0), rtol=0, atol=1e-15)
     assert mixed > 0, "the case must coarsen children that sit on different velocity grids"
+
+
+# ---- velocity-space adaptation flags -------------------------------------------------------
+def _vs_case_with(p, fn):
+    topo, state = cases.build(p)
+    off, goff = mesh.f_offsets(topo), topo["grid_off"]
+    q = p.case.quadrature
+    ds0 = [(q[2 * d + 1] - q[2 * d]) / p.case.vs_trees_num[d] for d in range(2)]
+    f = np.empty(int(off[-1]))
+    inner = []
+    for c in range(topo["n_cells"]):
+        g = topo["cell_grid"][c]
+        nv = int(goff[g + 1] - goff[g])
+        mid = np.asarray(topo["vs_midpoint"][goff[g] * 2:goff[g + 1] * 2]).reshape(2, nv)
+        lev = np.asarray(topo["vs_level"][goff[g]:goff[g + 1]])
+        h, b = fn(mid[0], mid[1])
+        f[off[c]:off[c] + nv] = h
+        f[off[c] + nv:off[c + 1]] = b
+        ok = np.ones(nv, bool)
+        for d in range(2):
+            half = 0.5 * ds0[d] / 2.0 ** lev
+            ok &= (mid[d] - q[2 * d] > 3 * half) & (q[2 * d + 1] - mid[d] > 3 * half)
+        inner.append(ok)
+    st = O.OracleState(topo, dict(f=f, w=state["w"], prim=state["prim"]))
+    fl, eta, vr = st.vs_flags(abi.make_params(p), abi.make_vs_config(p, maxlevel=max(p.vs_maxlevel, 1)))
+    return np.concatenate(inner), fl, eta
+
+
+def test_vs_lohner_indicator_vanishes_on_linear_and_uniform_distributions():
+    # The non-uniform second difference of a linear function is zero for any spacing: on a
+    # uniform velocity grid a distribution linear in u has η = 0 at every velocity cell whose
+    # face neighbours exist, so each neighbour found must be the cell across that face; the
+    # vacuum beyond the domain edge is a jump (η > 0 there).
+    inner, fl, eta = _vs_case_with(cases.sod(scale=0.125, nv=16),
+                                   lambda u, v: (2.0 + 0.1 * u + 0.05 * v, 1.0 + 0.02 * u - 0.03 * v))
+    assert inner.sum() > 0.5 * inner.size
+    assert np.max(eta[inner]) < 1e-12
+    assert np.max(eta[~inner]) > 1e-2
+    # on adapted (two-level) grids a constant has no structure: η = 0 away from the edge
+    inner, fl, eta = _vs_case_with(cases.collision(center=0.5), lambda u, v: (np.ones_like(u), 0.5 * np.ones_like(u)))
+    assert np.max(eta[inner]) < 1e-12
+    assert np.max(eta[~inner]) > 1e-2
