@@ -381,7 +381,7 @@ int rebuild(kg_handle* h) {
         UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
         UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
         UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
-        UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
+        UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(slope_items, slope_items); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
         UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
         UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
         UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
@@ -528,9 +528,9 @@ int autotune_flux(kg_handle* h) {
 // The level passes of slope! on the current f (the first phase of a step).
 cudaError_t enqueue_slopes(kg_handle* h, const Dev& P, cudaStream_t s) {
     const Flat& F = h->M;
-    const int npass = (int)F.pass_cells_off.size() - 1;
+    const int npass = (int)F.pass_items_off.size() - 1;
     for (int p = 0; p < npass; ++p) {
-        const int base = F.pass_cells_off[p], n = F.pass_cells_off[p + 1] - base;
+        const int base = F.pass_items_off[p], n = F.pass_items_off[p + 1] - base;
         if (n <= 0) continue;
         cudaError_t e = dispatch(h, [&](auto L) { return decltype(L)::slope(P, base, n, s); });
         if (e != cudaSuccess) return e;
@@ -562,9 +562,9 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         cudaEventDestroy(e0); cudaEventDestroy(e1);
     };
     cudaError_t e;
-    int npass = (int)F.pass_cells_off.size() - 1;
+    int npass = (int)F.pass_items_off.size() - 1;
     for (int p = 0; p < npass; ++p) {
-        int base = F.pass_cells_off[p], n = F.pass_cells_off[p + 1] - base;
+        int base = F.pass_items_off[p], n = F.pass_items_off[p + 1] - base;
         if (n <= 0) continue;
         begin();
         e = dispatch(h, [&](auto L) { return decltype(L)::slope(P, base, n, s); });

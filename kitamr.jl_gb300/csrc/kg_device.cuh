@@ -48,6 +48,7 @@ struct Dev {
     // slope
     const SlopeOp* slope_ops;
     const int32_t* pass_cells;
+    const int32_t* slope_items;        // (pass-cell entry, velocity chunk) per slope CTA
     const int32_t* cell_slope_op;
     const NbrRef* slope_nbr;
     // flux

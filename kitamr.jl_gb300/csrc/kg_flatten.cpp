@@ -101,7 +101,7 @@ const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 // (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
 // cost more than filling ~20 MB of records.
 void reset(Flat& F) {
-    static_assert(sizeof(Flat) == 46 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    static_assert(sizeof(Flat) == 48 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
     F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
     F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
     F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
@@ -110,7 +110,7 @@ void reset(Flat& F) {
     F.dmid.clear(); F.dds.clear();
     F.p_off.clear(); F.p_j0.clear(); F.p_cnt.clear();
     F.pass_off.clear(); F.slope_ops.clear(); F.pass_cells_off.clear(); F.pass_cells.clear();
-    F.cell_slope_op.clear(); F.slope_nbr.clear();
+    F.cell_slope_op.clear(); F.slope_nbr.clear(); F.slope_items.clear(); F.pass_items_off.clear();
     F.fluid_cells.clear(); F.fcrec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
     F.fluid_reg.clear();
     F.inc_off.clear(); F.inc.clear(); F.bc_prim.clear(); F.bc_hl.clear();
@@ -773,6 +773,15 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         }
         c.regular = reg ? 1 : 0;
         M.screc[k] = c;
+    }
+    // work items of the slope passes: a pass cell per SLOPE_CHUNK velocity cells
+    M.pass_items_off.push_back(0);
+    for (size_t ps = 0; ps + 1 < M.pass_cells_off.size(); ++ps) {
+        for (int32_t k = M.pass_cells_off[ps]; k < M.pass_cells_off[ps + 1]; ++k) {
+            const int nch = (M.dnv[M.pass_cells[k]] + SLOPE_CHUNK - 1) / SLOPE_CHUNK;
+            for (int c = 0; c < nch; ++c) { M.slope_items.push_back(k); M.slope_items.push_back(c); }
+        }
+        M.pass_items_off.push_back((int32_t)(M.slope_items.size() / 2));
     }
     if (M.p_j0.empty()) { M.p_j0.push_back(0); M.p_cnt.push_back(0); }
 }

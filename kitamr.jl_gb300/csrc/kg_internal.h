@@ -17,6 +17,9 @@ namespace kg {
 
 constexpr int MAXD = 3;
 constexpr int MAXW = MAXD + 2;
+// velocity cells of one slope work item: a multiple of the cells a CTA covers per pass (two
+// per thread at 128 or 256 threads), so a large grid spreads over several CTAs
+constexpr int SLOPE_CHUNK = 4096;
 
 // ---- slope operations (one per fluid cell and direction) -------------------
 enum SlopeKind : int8_t { SLOPE_ZERO = 0, SLOPE_SKIP = 1, SLOPE_ONE = 2, SLOPE_TWO = 3 };
@@ -152,6 +155,8 @@ struct Flat {
     std::vector<int32_t> pass_cells_off;  // per pass: cells [pass_cells_off[p], ...) in pass_cells
     std::vector<int32_t> pass_cells;
     std::vector<int32_t> cell_slope_op;   // per pass-cell entry: first op index (dim ops each)
+    std::vector<int32_t> slope_items;     // merged layout: (pass-cell entry, velocity chunk) pairs
+    std::vector<int32_t> pass_items_off;  // merged layout: per pass its items (one CTA each)
     std::vector<NbrRef> slope_nbr;
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order

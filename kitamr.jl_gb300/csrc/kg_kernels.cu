@@ -135,10 +135,14 @@ __device__ __forceinline__ void slope_side(int i, int li, const typename Arith<T
 
 // NT: threads per CTA (128 for layouts of small velocity grids, whose cells would leave half
 // of a 256-thread CTA idle)
+// One CTA per work item: a pass cell and a chunk of SLOPE_CHUNK of its velocity cells (every
+// velocity cell's slope is independent of the others').
 template <int D, int NDF, typename T, int NT>
-__global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
+__global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
     using A = typename Arith<T>::type;
-    const int pc = pc_base + blockIdx.x;
+    static_assert(SLOPE_CHUNK % (2 * NT) == 0, "a chunk is whole passes of the CTA");
+    const int pc = P.slope_items[2 * (item_base + blockIdx.x)];
+    const int v0 = P.slope_items[2 * (item_base + blockIdx.x) + 1] * SLOPE_CHUNK;
     const SlopeCell& SC = P.screc[pc];
     if (SC.regular) {
         // regular cell (one record, no shared-memory setup): in every direction
@@ -146,9 +150,10 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
         // resolved.  Several velocity cells per thread and pass: all their loads are issued
         // before any store, so each thread keeps that many sets of loads in flight.
         const int nv = SC.nv;
+        const int v1 = min(nv, v0 + SLOPE_CHUNK);
         const T* fcell = (const T*)P.f_in + SC.foff;
         T* scell = (T*)P.sdf + SC.foff * D;
-        if (threadIdx.x == 0) prefetch_l2(fcell, sizeof(T) * (size_t)NDF * nv);
+        if (threadIdx.x < NDF) prefetch_l2(fcell + (int64_t)threadIdx.x * nv + v0, sizeof(T) * (size_t)(v1 - v0));
         const T* fa[D];
         const T* fb[D];
         A ia[D], ib[D];
@@ -162,12 +167,12 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
         // velocity cells per thread and pass (measured on the 3D sphere, mixed form: 2 beats 3
         // and 4, whose registers cost resident CTAs)
         constexpr int VPT = 2;
-        for (int i0 = threadIdx.x; i0 < nv; i0 += VPT * NT) {
+        for (int i0 = v0 + threadIdx.x; i0 < v1; i0 += VPT * NT) {
             int iv[VPT], jv[VPT];
 #pragma unroll
             for (int v = 0; v < VPT; ++v) {
                 iv[v] = i0 + v * NT;
-                jv[v] = iv[v] < nv ? iv[v] : i0;    // a valid index for the loads
+                jv[v] = iv[v] < v1 ? iv[v] : i0;    // a valid index for the loads
             }
             A fc[VPT][NDF], a[VPT][D][NDF], b[VPT][D][NDF];
 #pragma unroll
@@ -185,7 +190,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
             }
 #pragma unroll
             for (int v = 0; v < VPT; ++v) {
-                if (v > 0 && iv[v] >= nv) break;
+                if (v > 0 && iv[v] >= v1) break;
 #pragma unroll
                 for (int dir = 0; dir < D; ++dir) {
 #pragma unroll
@@ -263,7 +268,8 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int pc_base) {
         snb[e] = c;
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < nv; i += NT) {
+    const int v1 = min(nv, v0 + SLOPE_CHUNK);
+    for (int i = v0 + threadIdx.x; i < v1; i += NT) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
 #pragma unroll
@@ -1908,10 +1914,11 @@ __global__ void __launch_bounds__(BLOCK) adapt_kernel(Dev P, AdaptView<T> V) {
 
 template <int D, int NDF, typename T>
 struct Launch {
-    static cudaError_t slope(const Dev& P, int pc_base, int n, cudaStream_t s) {
+    // the slope work items [item_base, item_base + n) of one pass
+    static cudaError_t slope(const Dev& P, int item_base, int n, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        if (P.slope_nt == 128) slope_kernel<D, NDF, T, 128><<<n, 128, 0, s>>>(P, pc_base);
-        else slope_kernel<D, NDF, T, BLOCK><<<n, BLOCK, 0, s>>>(P, pc_base);
+        if (P.slope_nt == 128) slope_kernel<D, NDF, T, 128><<<n, 128, 0, s>>>(P, item_base);
+        else slope_kernel<D, NDF, T, BLOCK><<<n, BLOCK, 0, s>>>(P, item_base);
         return cudaGetLastError();
     }
     static cudaError_t solid(const Dev& P, int n, cudaStream_t s) {
