@@ -403,6 +403,7 @@ int rebuild(kg_handle* h) {
     { int r = upload_all(); if (r) return r; }
     P.max_axis = M.max_axis;
     P.max_bcm = M.max_bcm;
+    P.slope_split = (int64_t)M.slope_items.size() / 2 != (int64_t)M.pass_cells.size();
     if (M.n_fluid > 0) {
         // stage the flux kernel's convected f in global memory when shared memory would cost
         // resident CTAs (or not fit at all)

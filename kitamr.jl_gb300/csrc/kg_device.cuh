@@ -49,6 +49,7 @@ struct Dev {
     const SlopeOp* slope_ops;
     const int32_t* pass_cells;
     const int32_t* slope_items;        // (pass-cell entry, velocity chunk) per slope CTA
+    int slope_split;                   // 0: one item per pass cell, item == pass-cell entry
     const int32_t* cell_slope_op;
     const NbrRef* slope_nbr;
     // flux

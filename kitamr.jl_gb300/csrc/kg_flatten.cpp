@@ -774,11 +774,15 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         c.regular = reg ? 1 : 0;
         M.screc[k] = c;
     }
-    // work items of the slope passes: a pass cell per SLOPE_CHUNK velocity cells
+    // work items of the slope passes: when some grid exceeds two chunks, a pass cell per
+    // SLOPE_CHUNK velocity cells (large 3D grids: fewer cells than resident CTAs per level);
+    // otherwise one item per pass cell, in order, and the kernel indexes directly
+    bool split = false;
+    for (int32_t m : M.pass_cells) split |= M.dnv[m] > 2 * SLOPE_CHUNK;
     M.pass_items_off.push_back(0);
     for (size_t ps = 0; ps + 1 < M.pass_cells_off.size(); ++ps) {
         for (int32_t k = M.pass_cells_off[ps]; k < M.pass_cells_off[ps + 1]; ++k) {
-            const int nch = (M.dnv[M.pass_cells[k]] + SLOPE_CHUNK - 1) / SLOPE_CHUNK;
+            const int nch = split ? (M.dnv[M.pass_cells[k]] + SLOPE_CHUNK - 1) / SLOPE_CHUNK : 1;
             for (int c = 0; c < nch; ++c) { M.slope_items.push_back(k); M.slope_items.push_back(c); }
         }
         M.pass_items_off.push_back((int32_t)(M.slope_items.size() / 2));

@@ -141,8 +141,11 @@ template <int D, int NDF, typename T, int NT>
 __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
     using A = typename Arith<T>::type;
     static_assert(SLOPE_CHUNK % (2 * NT) == 0, "a chunk is whole passes of the CTA");
-    const int pc = P.slope_items[2 * (item_base + blockIdx.x)];
-    const int v0 = P.slope_items[2 * (item_base + blockIdx.x) + 1] * SLOPE_CHUNK;
+    int pc = item_base + blockIdx.x, v0 = 0;
+    if (P.slope_split) {
+        pc = P.slope_items[2 * pc];
+        v0 = P.slope_items[2 * (item_base + blockIdx.x) + 1] * SLOPE_CHUNK;
+    }
     const SlopeCell& SC = P.screc[pc];
     if (SC.regular) {
         // regular cell (one record, no shared-memory setup): in every direction
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
         // resolved.  Several velocity cells per thread and pass: all their loads are issued
         // before any store, so each thread keeps that many sets of loads in flight.
         const int nv = SC.nv;
-        const int v1 = min(nv, v0 + SLOPE_CHUNK);
+        const int v1 = P.slope_split ? min(nv, v0 + SLOPE_CHUNK) : nv;
         const T* fcell = (const T*)P.f_in + SC.foff;
         T* scell = (T*)P.sdf + SC.foff * D;
         if (threadIdx.x < NDF) prefetch_l2(fcell + (int64_t)threadIdx.x * nv + v0, sizeof(T) * (size_t)(v1 - v0));
@@ -268,7 +271,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
         snb[e] = c;
     }
     __syncthreads();
-    const int v1 = min(nv, v0 + SLOPE_CHUNK);
+    const int v1 = P.slope_split ? min(nv, v0 + SLOPE_CHUNK) : nv;
     for (int i = v0 + threadIdx.x; i < v1; i += NT) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
