@@ -17,6 +17,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t wall(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
+    static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t macro_slope(const Dev&, int, int, int, double*, cudaStream_t);
     static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
@@ -134,6 +135,13 @@ struct kg_handle {
     kg_params prm{};
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a step's immersed-boundary kernels run on `aux` beside the flux of the fluid cells that
+    // read none of their output (fork / join through the two events)
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    const int32_t* d_indep = nullptr;  // fluid-list entries without a solid / wall incidence
+    const int32_t* d_dep = nullptr;    // the others
+    int n_indep = 0, n_dep = 0;
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -433,6 +441,20 @@ int rebuild(kg_handle* h) {
         int r = upload_vec(h, order, &h->d_order);
         if (r) return r;
     }
+    {
+        // fluid cells whose flux reads no solid cell or wall record (the IB kernels' output)
+        std::vector<int32_t> indep, dep;
+        for (int q = 0; q < M.n_fluid; ++q) {
+            bool d = false;
+            for (int e = M.inc_off[q]; e < M.inc_off[q + 1] && !d; ++e) d = M.inc[e].kind == INC_SOLID;
+            (d ? dep : indep).push_back(q);
+        }
+        h->n_indep = (int)indep.size();
+        h->n_dep = (int)dep.size();
+        int r = upload_vec(h, indep, &h->d_indep);
+        if (!r) r = upload_vec(h, dep, &h->d_dep);
+        if (r) return r;
+    }
     const int32_t* dl;
     { int r = upload_vec(h, h->live, &dl); if (r) return r; }
     h->d_live = const_cast<int32_t*>(dl);
@@ -572,6 +594,36 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         if (e != cudaSuccess) return cuda_fail(h, e, "slope_kernel");
         end("slope_kernel");
         ++*launches;
+    }
+    const bool ib = !F.solid_ops.empty() || !F.wall_ops.empty();
+    if (!timed && ib && h->sched == 0 && h->n_dep > 0 && h->n_indep > 0) {
+        // the IB kernels on the second stream, beside the flux of the cells that read none of
+        // their output; the flux of the others after the join
+        cudaStream_t a = h->aux;
+        KG_CUDA(h, cudaEventRecord(h->ev_fork, s));
+        KG_CUDA(h, cudaStreamWaitEvent(a, h->ev_fork, 0));
+        if (!F.solid_ops.empty()) {
+            e = dispatch(h, [&](auto L) { return decltype(L)::solid(P, (int)F.solid_ops.size(), a); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "solid_kernel");
+            ++*launches;
+        }
+        if (!F.wall_ops.empty()) {
+            e = dispatch(h, [&](auto L) { return decltype(L)::wall(P, (int)F.wall_ops.size(), F.max_nv, a); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "wall_kernel");
+            ++*launches;
+        }
+        KG_CUDA(h, cudaEventRecord(h->ev_join, a));
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_indep, h->n_indep, F.max_nv, s); });
+        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_dep, h->n_dep, F.max_nv, s); });
+        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        *launches += 2;
+        e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
+        if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
+        ++*launches;
+        h->parity ^= 1;
+        return KG_OK;
     }
     if (!F.solid_ops.empty()) {
         begin();
@@ -1310,9 +1362,19 @@ int create_handle(const kg_params* params, int device, kg_handle** out) {
     cudaGetDevice(&h->device);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); delete h; return KG_ERR_CUDA; }
+    e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
+    if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); cudaStreamDestroy(h->stream); delete h; return KG_ERR_CUDA; }
     e = cudaMallocHost(&h->h_res, sizeof(double) * MAX_SLOTS * RES_STRIDE);
     if (e == cudaSuccess) e = cudaMallocHost(&h->h_status, sizeof(int) * MAX_SLOTS);
-    if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); cudaStreamDestroy(h->stream); delete h; return KG_ERR_NOMEM; }
+    if (e != cudaSuccess) {
+        g_create_err = cudaGetErrorString(e);
+        cudaEventDestroy(h->ev_fork); cudaEventDestroy(h->ev_join);
+        cudaStreamDestroy(h->aux); cudaStreamDestroy(h->stream);
+        delete h;
+        return KG_ERR_NOMEM;
+    }
     *out = h;
     return KG_OK;
 }
@@ -1327,10 +1389,14 @@ int kg_destroy(kg_handle* h) {
     if (!h) return KG_ERR_ARG;
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
+    cudaStreamSynchronize(h->aux);
     free_pools(h);
     if (h->d_tri) cudaFree(h->d_tri);
     if (h->h_res) cudaFreeHost(h->h_res);
     if (h->h_status) cudaFreeHost(h->h_status);
+    cudaEventDestroy(h->ev_fork);
+    cudaEventDestroy(h->ev_join);
+    cudaStreamDestroy(h->aux);
     cudaStreamDestroy(h->stream);
     delete h;
     return KG_OK;

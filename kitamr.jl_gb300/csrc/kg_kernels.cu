@@ -1953,6 +1953,17 @@ struct Launch {
         fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, nullptr, n);
         return cudaGetLastError();
     }
+    // one CTA per listed fluid-list entry
+    static cudaError_t flux_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        using A = typename Arith<T>::type;
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
+        const FluxFn fn = flux_fn(P);
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, list, n);
+        return cudaGetLastError();
+    }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
     static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,
                                        cudaStream_t s) {
