@@ -597,8 +597,9 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
     }
     const bool ib = !F.solid_ops.empty() || !F.wall_ops.empty();
     if (!timed && ib && h->sched == 0 && h->n_dep > 0 && h->n_indep > 0) {
-        // the IB kernels on the second stream, beside the flux of the cells that read none of
-        // their output; the flux of the others after the join
+        // the IB kernels and then the flux of the cells that read their output on the second
+        // stream (higher priority: its CTAs take SM slots first as they free up), beside the
+        // flux of the cells that read none of it; the step ends on one tail
         cudaStream_t a = h->aux;
         KG_CUDA(h, cudaEventRecord(h->ev_fork, s));
         KG_CUDA(h, cudaStreamWaitEvent(a, h->ev_fork, 0));
@@ -612,12 +613,12 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
             if (e != cudaSuccess) return cuda_fail(h, e, "wall_kernel");
             ++*launches;
         }
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_dep, h->n_dep, F.max_nv, a); });
+        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaEventRecord(h->ev_join, a));
         e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_indep, h->n_indep, F.max_nv, s); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_dep, h->n_dep, F.max_nv, s); });
-        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         *launches += 2;
         e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
@@ -1362,7 +1363,9 @@ int create_handle(const kg_params* params, int device, kg_handle** out) {
     cudaGetDevice(&h->device);
     e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); delete h; return KG_ERR_CUDA; }
-    e = cudaStreamCreateWithFlags(&h->aux, cudaStreamNonBlocking);
+    int lo_prio = 0, hi_prio = 0;
+    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
+    e = cudaStreamCreateWithPriority(&h->aux, cudaStreamNonBlocking, hi_prio);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming);
     if (e != cudaSuccess) { g_create_err = cudaGetErrorString(e); cudaStreamDestroy(h->stream); delete h; return KG_ERR_CUDA; }
