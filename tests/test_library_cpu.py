@@ -110,3 +110,79 @@ def test_reference_arm_prints_the_contract_line():
     assert line["impl"] == "reference" and line["metric"] == "phase-cell updates/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def _footprint_error(p, topo, **prm):
+    with pytest.raises(S.KitGpuError) as e:
+        S.topology_footprint(abi.make_params(p, **prm), topo)
+    return e.value
+
+
+@pytest.mark.parametrize("mutate,code,words", [
+    # a grid whose levels cannot tile the root lattice next to another grid (the merge walk)
+    ("ragged_grid", 2, "tile"),
+    # cell_grid out of range
+    ("bad_cell_grid", 2, "cell_grid"),
+    # an empty velocity grid
+    ("empty_grid", 2, "empty"),
+    # a face whose direction is not a dimension
+    ("bad_face_dir", 2, "face_dir"),
+    # an unknown domain boundary kind
+    ("bad_bc_kind", 2, "boundary kind"),
+    # no cells at all
+    ("no_cells", 2, "empty"),
+])
+def test_flattener_rejects_malformed_topologies(lib, mutate, code, words):
+    p = cases.collision(center=0.5)        # two velocity grids, hanging faces, outflow + periodic
+    topo, _ = cases.build(p)
+    bad = dict(topo)
+    if mutate == "ragged_grid":
+        # drop the last velocity cell of grid 1: its leaves no longer cover the root lattice
+        goff = np.asarray(topo["grid_off"]).copy()
+        cut = int(goff[2]) - 1
+        keep = np.ones(int(goff[-1]), bool)
+        keep[cut] = False
+        bad["vs_level"] = np.asarray(topo["vs_level"])[keep]
+        bad["vs_weight"] = np.asarray(topo["vs_weight"])[keep]
+        mid = np.asarray(topo["vs_midpoint"])
+        parts = []
+        for g in range(int(topo["n_grids"])):
+            a, b = int(goff[g]), int(goff[g + 1])
+            blk = mid[a * 2:b * 2].reshape(2, b - a)
+            if g == 1:
+                blk = blk[:, :-1]
+            parts.append(blk.reshape(-1))
+        bad["vs_midpoint"] = np.concatenate(parts)
+        goff[2:] -= 1
+        bad["grid_off"] = goff
+    elif mutate == "bad_cell_grid":
+        bad["cell_grid"] = np.asarray(topo["cell_grid"]).copy()
+        bad["cell_grid"][3] = int(topo["n_grids"])
+    elif mutate == "empty_grid":
+        goff = np.asarray(topo["grid_off"]).copy()
+        bad["grid_off"] = np.concatenate([goff[:1], goff])   # grid 0 now holds no cells
+        bad["n_grids"] = int(topo["n_grids"]) + 1
+    elif mutate == "bad_face_dir":
+        bad["face_dir"] = np.asarray(topo["face_dir"]).copy()
+        bad["face_dir"][0] = 7
+    elif mutate == "bad_bc_kind":
+        kinds = np.asarray(topo["face_kind"])
+        j = int(np.nonzero(kinds == abi.KG_FACE_DOMAIN if hasattr(abi, "KG_FACE_DOMAIN") else kinds == 1)[0][0])
+        bad["face_bc_kind"] = np.asarray(topo["face_bc_kind"]).copy()
+        bad["face_bc_kind"][j] = 9
+    elif mutate == "no_cells":
+        bad["n_cells"] = 0
+    err = _footprint_error(p, bad)
+    assert err.code == code, (mutate, err.code, str(err))
+    assert words in str(err), (mutate, str(err))
+
+
+def test_flattener_rejects_mismatched_params(lib):
+    p = cases.collision(center=0.5)
+    topo, _ = cases.build(p)
+    prm = abi.make_params(p)
+    prm.dim = 3
+    prm.ndf = 1
+    with pytest.raises(S.KitGpuError) as e:
+        S.topology_footprint(prm, topo)
+    assert e.value.code == 1
