@@ -290,7 +290,8 @@ def run_serve(args):
         from kitgpu import cases
         r.topo, r.state = cases.build(r.problem)
     out = {}
-    for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
+    allforms = (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64))
+    for form, prec in [x for x in allforms if x[0] in args.forms.split(",")]:
         for r in reqs:
             r.slot, r.admitted, r.finished, r.steps, r.residual, r.converged = -1, -1.0, -1.0, 0, float("inf"), False
         free = torch.cuda.mem_get_info()[0]
@@ -445,6 +446,7 @@ def main():
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
+    ap.add_argument("--forms", default="mixed,fp64", help="serve: precision forms to run (mixed, fp64)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.scale is None:
