@@ -5,7 +5,7 @@ Workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x6
 synthetic initial state; 61 M phase cells, so f is far larger than L2 between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-  python bench.py --mode sphere | batched | serve | adapt   (the other workloads, one line each)
+  python bench.py --mode sphere | sod | batched | serve | adapt   (the other workloads, one line each)
 
 Metric: phase-cell updates/s of the mixed-precision form (FP32 f, compensated moments,
 FP64 conserved update), with the plain FP64 form, the roofline of the dominant kernel, the
@@ -13,6 +13,7 @@ oracle CPU baseline and the end-to-end rate through the C-ABI with host buffers 
 N > 1: independent replicas, one per GPU (the path has no exchange on one device).
 Other modes:
 * sphere: the 3D Ma 3 sphere at half its base mesh (183 M phase cells).
+* sod: the 2D Sod tube of the reference's Riemann example (inputs inside L2).
 * batched: 256 Sod / cavity problems in one batch handle.
 * serve: Poisson arrivals solved to residual < 1e-6.
 * adapt: one physical-space adaptation of the cylinder on the device (criterion, then the
@@ -44,6 +45,9 @@ SINGLE = {
     # the 3D sphere (Ma 3, Kn 0.05, 32^3 trees, 2 levels, 24^3 velocity grid) at half the base
     # mesh by default: 13,536 cells, 183 M phase cells (the full mesh needs a 22 GB host state)
     "sphere": ("sphere_ma3_kn0.05_32x32x32_L2_v24x24x24", 0.5, "seeded sphere buffer state on a generated octree"),
+    # the 2D Shakhov Sod tube ([0,1]x[0,0.1], 128x4 trees, 2 levels at the jump, 28^2 velocity
+    # grid): small enough that f stays in L2 between kernels
+    "sod": ("sod_2d_128x4_L2_v28x28", 1.0, "Sod left/right states on a generated forest"),
 }
 
 
@@ -51,6 +55,8 @@ def make_problem(scale=1.0, mode="cylinder"):
     from kitgpu import cases
     if mode == "sphere":
         return cases.sphere(scale=scale)
+    if mode == "sod":
+        return cases.sod(scale=scale)
     return cases.cylinder(scale=scale, nv=48, vs_levels=2)
 
 
@@ -442,7 +448,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=None,
                     help="scale of the base mesh (default: the workload's own; smaller for profiling captures)")
-    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "batched", "serve", "adapt"])
+    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "sod", "batched", "serve", "adapt"])
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
@@ -528,7 +534,9 @@ def main():
         "data": f"synthetic ({wdata})",
         "config": {"workload": wname if args.scale == wscale else f"{wname} at scale {args.scale}",
                    "phase_cells": P, "form": "mixed",
-                   "l2": f"inputs > L2 (f is {P * ndf * 4 / 1e6:.0f} MB FP32, sdf {P * ndf * 4 * (2 if ndf == 2 else 3) / 1e6:.0f} MB)",
+                   "l2": (f"inputs > L2 (f is {P * ndf * 4 / 1e6:.0f} MB FP32, sdf {P * ndf * 4 * (2 if ndf == 2 else 3) / 1e6:.0f} MB)"
+                          if P * ndf * 4 * (3 if ndf == 2 else 4) > 129e6 else
+                          f"inputs inside L2 (f {P * ndf * 4 / 1e6:.0f} MB FP32), not flushed between steps: the workload is this small"),
                    "parallelism": f"replicas{world}"},
         "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
                   "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
