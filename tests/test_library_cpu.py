@@ -99,7 +99,7 @@ def test_flattens_3d_topologies(lib, make):
 
 def test_reference_arm_prints_the_contract_line():
     """bench.py --impl reference: the reference's CPU path (the oracle port) on the bench's
-    workload, one JSON line with the keys the driver reads."""
+    workload, one JSON line with the keys of the benchmark contract."""
     import json
     import subprocess
     import sys
