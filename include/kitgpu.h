@@ -48,6 +48,11 @@ extern "C" {
 #define KG_FLUX_DVM         1   /* DVM: micro flux only                              */
 #define KG_MARCH_CAIDVM     0   /* iterate!(::Type{CAIDVM_Marching})  Iterate.jl:96  */
 #define KG_MARCH_EULER      1   /* iterate!(::Type{Euler})            Iterate.jl:131 */
+#define KG_MARCH_CIP        2   /* iterate!(::Type{CIP_Marching}) I-projection.jl:161:
+                                   convection, then the conservative I-projection of f
+                                   onto w (a Newton solve per cell) before relaxation;
+                                   meshes without immersed-boundary cells
+                                   (positivity_preserving_ib! is not provided)       */
 #define KG_PREC_FP64        0   /* f, sdf, fluxes in FP64 (plain form)               */
 #define KG_PREC_MIXED       1   /* f, sdf, micro fluxes in FP32; moments compensated;
                                    w, prim, exponents, wall density in FP64          */

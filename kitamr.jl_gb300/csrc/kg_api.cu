@@ -19,6 +19,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
+    static cudaError_t cip(const Dev&, int, cudaStream_t);
     static cudaError_t macro_slope(const Dev&, int, int, int, double*, cudaStream_t);
     static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
     static cudaError_t adapt(const Dev&, int, const AdaptRec*, const void*, const void*, const double*, const double*,
@@ -596,7 +597,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         ++*launches;
     }
     const bool ib = !F.solid_ops.empty() || !F.wall_ops.empty();
-    if (!timed && ib && h->sched == 0 && h->n_dep > 0 && h->n_indep > 0) {
+    if (!timed && ib && h->sched == 0 && h->n_dep > 0 && h->n_indep > 0 && h->prm.marching != KG_MARCH_CIP) {
         // the IB kernels and then the flux of the cells that read their output on the second
         // stream (higher priority: its CTAs take SM slots first as they free up), beside the
         // flux of the cells that read none of it; the step ends on one tail
@@ -646,6 +647,13 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         end("flux_collide_kernel");
         ++*launches;
+        if (h->prm.marching == KG_MARCH_CIP) {
+            begin();
+            e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "cip_kernel");
+            end("cip_kernel");
+            ++*launches;
+        }
     }
     e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
     if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
@@ -1339,7 +1347,7 @@ int check_params(const kg_params* params, std::string& err) {
     if (!(params->dim == 2 && params->ndf == 2) && !(params->dim == 3 && params->ndf == 1)) { err = "supported forms: dim 2 / ndf 2 and dim 3 / ndf 1"; return KG_ERR_ARG; }
     if (params->precision != KG_PREC_FP64 && params->precision != KG_PREC_MIXED) { err = "bad precision"; return KG_ERR_ARG; }
     if (params->flux != KG_FLUX_CAIDVM && params->flux != KG_FLUX_DVM) { err = "bad flux"; return KG_ERR_ARG; }
-    if (params->marching != KG_MARCH_CAIDVM && params->marching != KG_MARCH_EULER) { err = "bad marching"; return KG_ERR_ARG; }
+    if (params->marching != KG_MARCH_CAIDVM && params->marching != KG_MARCH_EULER && params->marching != KG_MARCH_CIP) { err = "bad marching"; return KG_ERR_ARG; }
     if (params->st_check_interval <= 0) { err = "st_check_interval must be positive"; return KG_ERR_ARG; }
     return KG_OK;
 }

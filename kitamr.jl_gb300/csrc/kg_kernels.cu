@@ -1169,7 +1169,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             const int ln = threadIdx.x;
             double* w = P.w + (int64_t)cell * MAXW;
             const double dtV = dt * invV;
-            const bool lane_mom = P.marching == KG_MARCH_CAIDVM ? ln == 1 : P.flux == KG_FLUX_DVM;
+            const bool lane_mom = P.marching != KG_MARCH_EULER ? ln == 1 : P.flux == KG_FLUX_DVM;
             double wv[MAXW], pv[MAXW];
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) wv[q] = lane_mom ? red[D + 2 + q] : fma(red[q], dtV, w[q]);
@@ -1289,6 +1289,14 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             for (int k = 0; k < NDF; ++k) fst[k * nv + i] = fv[k];
             qadd(i, fv);
         }
+    } else if (P.marching == KG_MARCH_CIP) {
+        // CIP: q of the convected f (Theory/I-projection.jl:178)
+        for (int i = threadIdx.x; i < nv; i += NT) {
+            A fv[NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) fv[k] = fst[k * nv + i];
+            qadd(i, fv);
+        }
     } else {
         // Euler: q of f before convection (Theory/Iterate.jl:153)
         for (int i = threadIdx.x; i < nv; i += NT) {
@@ -1330,7 +1338,13 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             gp[0] = mc + sk * cq * ((A)2 * lc * c2 - (A)5) * mc;
         }
     };
-    if (P.marching == KG_MARCH_CAIDVM) {
+    if (P.marching == KG_MARCH_CIP) {
+        // the I-projection and the relaxation follow in cip_kernel, from the convected f
+        if (!FG)
+            for (int i = threadIdx.x; i < nv; i += NT)
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) fnew[k * nv + i] = (T)fst[k * nv + i];
+    } else if (P.marching == KG_MARCH_CAIDVM) {
         // f = f tau/(tau+dt) + dt/(tau+dt) g+   (Theory/Iterate.jl:121-122)
         for (int i = threadIdx.x; i < nv; i += NT) {
             A gp[NDF];
@@ -1915,6 +1929,303 @@ __global__ void __launch_bounds__(BLOCK) adapt_kernel(Dev P, AdaptView<T> V) {
     }
 }
 
+// ---- CIP_Marching: conservative I-projection and relaxation ------------------------------
+// iterate!(CIP_Marching) (Theory/I-projection.jl:161-193) after the flux kernel, which leaves
+// in f_out the convected f of every fluid cell, in w the conserved update, in prim prim_c and
+// in qf the heat flux of the convected f.  One CTA per fluid cell:
+//  1. conserved_I_porjection! (:144-158): W = w (2D2F: less the energy Σ ω f₂ / 2 of the second
+//     distribution); solve_I_projection (:55-141) on f₁ -- the negative-value shave, then Newton
+//     iterations on G(λ) = Σ ω f e^{λ·ψ} ψ - W, ψ = (1, ξ, |ξ|²/2), with the stall test and the
+//     Armijo backtracking on Φ(λ) = Σ ω f e^{λ·ψ} - λ·W.  Every sum is a block reduction
+//     (compensated in the mixed form); thread 0 takes the decisions and solves the symmetric
+//     (dim+2)² Newton system in FP64 (Gaussian elimination, partial pivoting);
+//  2. f₁ *= e^{λ·ψ}; f = f τ/(τ+Δt) + Δt/(τ+Δt) g⁺, g⁺ = M(prim_c)(1 + Shakhov(q)) (:181-185).
+template <int D, typename A>
+__device__ __forceinline__ void cip_psi(const A* VU, int64_t PG, int64_t goff, int i, A* ps) {
+    ps[0] = (A)1;
+    A s = 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const A x = VU[(int64_t)d * PG + goff + i];
+        ps[1 + d] = x;
+        s += x * x;
+    }
+    ps[D + 1] = s / (A)2;
+}
+template <int M, typename A>
+__device__ __forceinline__ A cip_dot(const A* lam, const A* ps) {
+    A d = 0;
+#pragma unroll
+    for (int m = 0; m < M; ++m) d += lam[m] * ps[m];
+    return d;
+}
+__device__ __forceinline__ double cip_exp(double x) { return exp(x); }
+__device__ __forceinline__ float cip_exp(float x) { return expf(x); }
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
+    using A = typename Arith<T>::type;
+    constexpr int M = D + 2, NJ = M * (M + 1) / 2, NS = M + NJ, MAXIT = 10;
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    __shared__ double sred[NS * (BLOCK / 32)];
+    __shared__ double slam[M], strial[M];
+    __shared__ A slA[M];
+    __shared__ int sctl;
+    enum { C_PREC = 0, C_BFC, C_R1, C_R2, C_SK, C_LC, C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
+    __shared__ A sc[C_N];
+    __shared__ float sUl[MAXD], sUh[MAXD], slh, sll;
+    const FluxCell FC = P.fcrec[blockIdx.x];
+    const int cell = FC.cell, slot = FC.slot, nv = FC.nv;
+    const ProbParams& PP = P.probs[slot];
+    const int64_t PG = P.PG, goff = FC.goff;
+    const A* VU = vel<A>(P);
+    const A* VW = wts<A>(P) + goff;
+    T* f = (T*)P.f_out + FC.foff;
+
+    // ---- W, and the shave of negative values of f₁ (I-projection.jl:78-88) ----------------
+    {
+        KSum<A> ei[1];
+        double mn[2] = {-INFINITY, -INFINITY};   // -min f₁, -min of the positive f₁
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            const double x = (double)f[i];
+            mn[0] = fmax(mn[0], -x);
+            if (x > 0.0) mn[1] = fmax(mn[1], -x);
+            if (NDF == 2) ei[0].add(VW[i] * (A)f[nv + i]);
+        }
+        double e[1];
+        block_sum_ks<1, BLOCK>(ei, e, sred);
+        block_max<2>(mn, sred);
+        const double f_min = 1.1 * -mn[0], fp_min = -mn[1];
+        if (f_min < 0.0 && fp_min < INFINITY) {
+            const double dd = fp_min - f_min;
+            for (int i = threadIdx.x; i < nv; i += BLOCK) {
+                const double x = (double)f[i];
+                if (x < 0.0) f[i] = (T)((x - f_min) / dd * fp_min);
+            }
+        }
+        if (threadIdx.x == 0) {
+            const double* w = P.w + (int64_t)cell * MAXW;
+            for (int m = 0; m < M; ++m) { slam[m] = 0.0; strial[m] = w[m]; }
+            if (NDF == 2) strial[M - 1] -= e[0] / 2;
+        }
+        __syncthreads();
+    }
+    // ---- Newton iterations (thread 0 keeps the state; the block evaluates the sums) ----------
+    double W[M], dl[M], gprev = INFINITY, tol = 0.0, phi0 = 0.0, slope = 0.0, alpha = 1.0;
+    int stall = 0;
+#pragma unroll
+    for (int m = 0; m < M; ++m) W[m] = strial[m];
+    {
+        double wn = 0.0;
+#pragma unroll
+        for (int m = 0; m < M; ++m) wn += W[m] * W[m];
+        tol = 1e-10 * fmax(1.0, sqrt(wn));
+    }
+    for (int it = 0; it < MAXIT; ++it) {
+        if (threadIdx.x < M) slA[threadIdx.x] = (A)slam[threadIdx.x];
+        __syncthreads();
+        A lam[M];
+#pragma unroll
+        for (int m = 0; m < M; ++m) lam[m] = slA[m];
+        KSum<A> acc[NS];
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            A ps[M];
+            cip_psi<D, A>(VU, PG, goff, i, ps);
+            const A c = VW[i] * (A)f[i] * cip_exp(cip_dot<M, A>(lam, ps));
+            int q = M;
+#pragma unroll
+            for (int a = 0; a < M; ++a) {
+                const A ca = c * ps[a];
+                acc[a].add(ca);
+#pragma unroll
+                for (int b = a; b < M; ++b) acc[q++].add(ca * ps[b]);
+            }
+        }
+        double red[NS];
+        block_sum_ks<NS, BLOCK>(acc, red, sred);
+        if (threadIdx.x == 0) {
+            double G[M], gn = 0.0;
+#pragma unroll
+            for (int m = 0; m < M; ++m) { G[m] = red[m] - W[m]; gn += G[m] * G[m]; }
+            gn = sqrt(gn);
+            int stop = 0;
+            if (!(gn >= tol)) stop = 1;   // converged (or not a number)
+            else if (gn > 0.9 * gprev) { if (++stall >= 2) stop = 1; }
+            else stall = 0;
+            if (!stop) {
+                gprev = gn;
+                double J[M][M], b[M];
+                int q = M;
+                for (int a = 0; a < M; ++a)
+                    for (int c = a; c < M; ++c) { J[a][c] = red[q]; J[c][a] = red[q]; ++q; }
+                for (int a = 0; a < M; ++a) b[a] = -G[a];
+                for (int c = 0; c < M; ++c) {
+                    int p = c;
+                    for (int r = c + 1; r < M; ++r)
+                        if (fabs(J[r][c]) > fabs(J[p][c])) p = r;
+                    if (p != c) {
+                        for (int j = 0; j < M; ++j) { const double t = J[c][j]; J[c][j] = J[p][j]; J[p][j] = t; }
+                        const double t = b[c]; b[c] = b[p]; b[p] = t;
+                    }
+                    for (int r = c + 1; r < M; ++r) {
+                        const double l = J[r][c] / J[c][c];
+                        for (int j = c; j < M; ++j) J[r][j] -= l * J[c][j];
+                        b[r] -= l * b[c];
+                    }
+                }
+                for (int r = M - 1; r >= 0; --r) {
+                    double sacc = b[r];
+                    for (int j = r + 1; j < M; ++j) sacc -= J[r][j] * dl[j];
+                    dl[r] = sacc / J[r][r];
+                }
+                double lw = 0.0;
+                slope = 0.0;
+                for (int m = 0; m < M; ++m) { lw += slam[m] * W[m]; slope += G[m] * dl[m]; }
+                phi0 = red[0] - lw;   // Σ ω f e^{λ·ψ} is G's first sum (ψ₀ = 1)
+                alpha = 1.0;
+                for (int m = 0; m < M; ++m) strial[m] = slam[m] + dl[m];
+            }
+            sctl = stop;
+        }
+        __syncthreads();
+        if (sctl) break;
+        for (int ls = 0; ls < MAXIT; ++ls) {
+            // FP64: Φ at the trial point, as the reference evaluates it.  Mixed form: the
+            // difference Φ(λ + αΔλ) - Φ(λ) = Σ ω f e^{λ·ψ} expm1(αΔλ·ψ) - αΔλ·W, the same test in
+            // exact arithmetic; FP32 terms could not resolve Φ's decrease near convergence
+            // (~|G|²), and the solve would stall at |G| ~ 1e-4 |W|
+            if (threadIdx.x < M) slA[threadIdx.x] = (A)(sizeof(A) == 8 ? strial[threadIdx.x] : strial[threadIdx.x] - slam[threadIdx.x]);
+            __syncthreads();
+            A dlt[M];
+#pragma unroll
+            for (int m = 0; m < M; ++m) dlt[m] = slA[m];
+            KSum<A> a1[1];
+            for (int i = threadIdx.x; i < nv; i += BLOCK) {
+                A ps[M];
+                cip_psi<D, A>(VU, PG, goff, i, ps);
+                if constexpr (sizeof(A) == 8) {
+                    a1[0].add(VW[i] * (A)f[i] * cip_exp(cip_dot<M, A>(dlt, ps)));
+                } else {
+                    const A c = VW[i] * (A)f[i] * cip_exp(cip_dot<M, A>(lam, ps));
+                    a1[0].add(c * expm1f(cip_dot<M, A>(dlt, ps)));
+                }
+            }
+            double r1[1];
+            block_sum_ks<1, BLOCK>(a1, r1, sred);
+            if (threadIdx.x == 0) {
+                double lw = 0.0;
+                bool ok;
+                if constexpr (sizeof(A) == 8) {
+                    for (int m = 0; m < M; ++m) lw += strial[m] * W[m];
+                    ok = r1[0] - lw <= phi0 + 1e-4 * alpha * slope;
+                } else {
+                    for (int m = 0; m < M; ++m) lw += (strial[m] - slam[m]) * W[m];
+                    ok = r1[0] - lw <= 1e-4 * alpha * slope;
+                }
+                if (ok) {
+                    sctl = 1;
+                } else {
+                    alpha *= 0.5;
+                    for (int m = 0; m < M; ++m) strial[m] = slam[m] + alpha * dl[m];
+                    sctl = 0;
+                }
+            }
+            __syncthreads();
+            if (sctl) break;
+        }
+        if (threadIdx.x == 0)
+            for (int m = 0; m < M; ++m) slam[m] += alpha * dl[m];
+        __syncthreads();
+    }
+    // ---- collision constants of prim_c (the flux kernel's expressions) ----------------------
+    A* Ec = (A*)sh_raw;
+    const double* pc = P.prim + (int64_t)cell * MAXW;
+    if (threadIdx.x == 0) {
+        bool bad = false;
+        for (int m = 0; m < M; ++m) {
+            slA[m] = (A)slam[m];
+            bad |= !isfinite(slam[m]);
+        }
+        if (bad) atomicOr(&P.status[slot], ST_NONFINITE);
+        const double lc = pc[D + 1];
+        for (int d = 0; d < D; ++d) {
+            const double x = pc[1 + d];
+            sUh[d] = (float)x;
+            sUl[d] = (float)(x - (double)sUh[d]);
+            sc[C_UH + d] = (A)(sizeof(A) == 4 ? (double)sUh[d] : x);
+            sc[C_UL + d] = (A)(sizeof(A) == 4 ? (double)sUl[d] : 0.0);
+            sc[C_QA + d] = (A)P.qf[(int64_t)cell * MAXD + d];
+        }
+        slh = (float)lc;
+        sll = (float)(lc - (double)slh);
+        if constexpr (sizeof(A) == 8) {
+            const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
+            sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
+            sc[C_BFC] = PP.K / (2.0 * lc);
+            sc[C_R1] = tau / (tau + PP.dt);
+            sc[C_R2] = PP.dt / (tau + PP.dt);
+            sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
+            sc[C_LC] = lc;
+        } else {
+            const float rc = (float)pc[0], lcf = slh, dtf = PP.dtf;
+            const float tau = PP.mu2f * powf(lcf, PP.omf) / rc;
+            constexpr float IPI = (float)(1.0 / PI);
+            sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
+            sc[C_BFC] = PP.Kf / (2.f * lcf);
+            sc[C_R1] = tau / (tau + dtf);
+            sc[C_R2] = dtf / (tau + dtf);
+            sc[C_SK] = PP.shkf * lcf * lcf / rc;
+            sc[C_LC] = lcf;
+        }
+    }
+    __syncthreads();
+    if constexpr (sizeof(A) == 8) {
+        double U[D];
+        for (int d = 0; d < D; ++d) U[d] = pc[1 + d];
+        gauss_table<D, BLOCK>(P, FC.gid, U, pc[D + 1], (double*)Ec);
+    } else {
+        gauss_table<D, BLOCK>(P, FC.gid, sUh, sUl, slh, sll, (float*)Ec);
+    }
+    __syncthreads();
+    // ---- f₁ e^{λ·ψ}, then the relaxation towards g⁺ ----------------------------------------
+    const int MA = P.max_axis;
+    const uint16_t* vx = P.vidx + goff;
+    const A prec = sc[C_PREC], bfc = sc[C_BFC], r1 = sc[C_R1], r2 = sc[C_R2], sk = sc[C_SK], lc = sc[C_LC];
+    const A Kk = (A)PP.K;
+    A lam[M], Uh[D], Ul[D], qa[D];
+#pragma unroll
+    for (int m = 0; m < M; ++m) lam[m] = slA[m];
+#pragma unroll
+    for (int d = 0; d < D; ++d) { Uh[d] = sc[C_UH + d]; Ul[d] = sc[C_UL + d]; qa[d] = sc[C_QA + d]; }
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        A ps[M];
+        cip_psi<D, A>(VU, PG, goff, i, ps);
+        A fv[NDF];
+        fv[0] = (A)f[i] * cip_exp(cip_dot<M, A>(lam, ps));
+        if (NDF == 2) fv[NDF - 1] = (A)f[nv + i];
+        A mc = prec;
+#pragma unroll
+        for (int d = 0; d < D; ++d) mc *= Ec[d * MA + vx[(int64_t)d * PG + i]];
+        A c2 = 0, cq = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const A cd = (VU[(int64_t)d * PG + goff + i] - Uh[d]) - Ul[d];
+            c2 += cd * cd;
+            cq += cd * qa[d];
+        }
+        A gp[NDF];
+        if (NDF == 2) {
+            const A mb = mc * bfc;
+            gp[0] = mc + sk * cq * ((A)2 * lc * c2 + Kk - (A)5) * mc;
+            gp[NDF - 1] = mb + sk * cq * ((A)2 * lc * c2 + Kk - (A)3) * mb;
+        } else {
+            gp[0] = mc + sk * cq * ((A)2 * lc * c2 - (A)5) * mc;
+        }
+#pragma unroll
+        for (int k = 0; k < NDF; ++k) f[k * nv + i] = (T)(fv[k] * r1 + r2 * gp[k]);
+    }
+}
+
 template <int D, int NDF, typename T>
 struct Launch {
     // the slope work items [item_base, item_base + n) of one pass
@@ -1975,6 +2286,16 @@ struct Launch {
         e = cudaMemsetAsync(counter, 0, sizeof(int), s);
         if (e != cudaSuccess) return e;
         fn<<<grid, flux_threads(P), smem, s>>>(P, counter, order, n);
+        return cudaGetLastError();
+    }
+    // CIP_Marching's I-projection and relaxation of the fluid cells (after the flux kernel)
+    static cudaError_t cip(const Dev& P, int n, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        using A = typename Arith<T>::type;
+        const size_t smem = (size_t)D * P.max_axis * sizeof(A);
+        cudaError_t e = cudaFuncSetAttribute(cip_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        cip_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
         return cudaGetLastError();
     }
     static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {

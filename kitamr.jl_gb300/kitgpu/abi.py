@@ -9,7 +9,7 @@ import numpy as np
 
 KG_OK = 0
 KG_FLUX_CAIDVM, KG_FLUX_DVM = 0, 1
-KG_MARCH_CAIDVM, KG_MARCH_EULER = 0, 1
+KG_MARCH_CAIDVM, KG_MARCH_EULER, KG_MARCH_CIP = 0, 1, 2
 KG_PREC_FP64, KG_PREC_MIXED = 0, 1
 
 ERRORS = {

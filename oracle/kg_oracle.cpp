@@ -939,8 +939,148 @@ void flux(Model& m) {
         if (is_ib(fi)) inner_face(m, fi);
 }
 
+// ---------------------------------------------------------- I-projection --------
+// solve_I_projection (Theory/I-projection.jl:55-141): Newton iterations on the dual equation
+// G(λ) = Σ_k ω_k f_k exp(λ·ψ_k) ψ_k - W = 0, ψ_k = (1, ξ_k, |ξ_k|²/2), from λ = 0, with the
+// reference's negative-value shave of f (in place), its stall test and its Armijo
+// backtracking on the dual objective Φ(λ) = Σ_k ω_k f_k exp(λ·ψ_k) - λ·W.  The symmetric
+// Newton system is solved by Gaussian elimination with partial pivoting (the reference calls
+// a symmetric factorisation; the two agree to rounding).  Returns the iterations taken.
+static void iproj_psi(int D, const double* mid, int nv, int k, double* psi) {
+    psi[0] = 1.0;
+    double s = 0.0;
+    for (int d = 0; d < D; ++d) {
+        const double x = mid[(size_t)d * nv + k];
+        psi[1 + d] = x;
+        s += x * x;
+    }
+    psi[D + 1] = s / 2;
+}
+static double iproj_dual(int D, const double* mid, const double* wt, const double* f, int nv, const double* W,
+                         const double* lam) {
+    const int M = D + 2;
+    double acc = 0.0, psi[5];
+    for (int k = 0; k < nv; ++k) {
+        iproj_psi(D, mid, nv, k, psi);
+        double dot = 0.0;
+        for (int i = 0; i < M; ++i) dot += lam[i] * psi[i];
+        acc += wt[k] * f[k] * std::exp(dot);
+    }
+    double lw = 0.0;
+    for (int i = 0; i < M; ++i) lw += lam[i] * W[i];
+    return acc - lw;
+}
+// x = A⁻¹ b for a small dense system (n ≤ 5), partial pivoting
+static void small_solve(int n, double (*A)[5], double* b, double* x) {
+    for (int c = 0; c < n; ++c) {
+        int p = c;
+        for (int r = c + 1; r < n; ++r)
+            if (std::fabs(A[r][c]) > std::fabs(A[p][c])) p = r;
+        if (p != c) {
+            for (int j = 0; j < n; ++j) std::swap(A[c][j], A[p][j]);
+            std::swap(b[c], b[p]);
+        }
+        for (int r = c + 1; r < n; ++r) {
+            const double l = A[r][c] / A[c][c];
+            for (int j = c; j < n; ++j) A[r][j] -= l * A[c][j];
+            b[r] -= l * b[c];
+        }
+    }
+    for (int r = n - 1; r >= 0; --r) {
+        double s = b[r];
+        for (int j = r + 1; j < n; ++j) s -= A[r][j] * x[j];
+        x[r] = s / A[r][r];
+    }
+}
+int solve_iprojection(int D, const double* mid, double* f, const double* W, const double* wt, int nv, double* lam) {
+    const int M = D + 2, maxiter = 10;
+    double wn = 0.0;
+    for (int i = 0; i < M; ++i) wn += W[i] * W[i];
+    const double tol_eff = 1e-10 * std::max(1.0, std::sqrt(wn));
+    for (int i = 0; i < M; ++i) lam[i] = 0.0;
+    // shave negative distribution
+    double fmn = INFINITY;
+    for (int k = 0; k < nv; ++k) fmn = std::min(fmn, f[k]);
+    const double f_min = 1.1 * fmn;
+    if (f_min < 0) {
+        double fp_min = INFINITY;
+        for (int k = 0; k < nv; ++k)
+            if (f[k] > 0) fp_min = std::min(fp_min, f[k]);
+        if (fp_min < INFINITY) {
+            const double d = fp_min - f_min;
+            for (int k = 0; k < nv; ++k)
+                if (f[k] < 0) f[k] = (f[k] - f_min) / d * fp_min;
+        }
+    }
+    double Gprev = INFINITY;
+    int stall = 0, it = 0;
+    for (; it < maxiter; ++it) {
+        double G[5] = {0, 0, 0, 0, 0}, J[5][5] = {}, psi[5];
+        for (int k = 0; k < nv; ++k) {
+            iproj_psi(D, mid, nv, k, psi);
+            double dot = 0.0;
+            for (int i = 0; i < M; ++i) dot += lam[i] * psi[i];
+            const double c = wt[k] * f[k] * std::exp(dot);
+            for (int i = 0; i < M; ++i) {
+                const double ci = c * psi[i];
+                G[i] += ci;
+                for (int j = i; j < M; ++j) J[i][j] += ci * psi[j];
+            }
+        }
+        double gn = 0.0;
+        for (int i = 0; i < M; ++i) { G[i] -= W[i]; gn += G[i] * G[i]; }
+        gn = std::sqrt(gn);
+        if (gn < tol_eff) return it;
+        if (gn > 0.9 * Gprev) {
+            if (++stall >= 2) return it;
+        } else {
+            stall = 0;
+        }
+        Gprev = gn;
+        for (int i = 0; i < M; ++i)
+            for (int j = 0; j < i; ++j) J[i][j] = J[j][i];
+        double rhs[5], dl[5];
+        for (int i = 0; i < M; ++i) rhs[i] = -G[i];
+        small_solve(M, J, rhs, dl);
+        const double phi0 = iproj_dual(D, mid, wt, f, nv, W, lam);
+        double slope = 0.0;
+        for (int i = 0; i < M; ++i) slope += G[i] * dl[i];
+        double alpha = 1.0, trial[5];
+        for (int ls = 0; ls < maxiter; ++ls) {
+            for (int i = 0; i < M; ++i) trial[i] = lam[i] + alpha * dl[i];
+            if (iproj_dual(D, mid, wt, f, nv, W, trial) <= phi0 + 1e-4 * alpha * slope) break;
+            alpha *= 0.5;
+        }
+        for (int i = 0; i < M; ++i) lam[i] += alpha * dl[i];
+    }
+    return it;
+}
+// conserved_I_porjection! (Theory/I-projection.jl:144-158): 2D2F projects df[:,1] onto w with
+// the energy of df[:,2] taken out; 3D1F projects df onto w
+void conserved_iprojection(int D, int NDF, const double* mid, const double* wt, int nv, double* df, const double* w,
+                           double* lam) {
+    if (D != 2 && D != 3) return;
+    const int M = D + 2;
+    double W[5];
+    for (int i = 0; i < M; ++i) W[i] = w[i];
+    if (NDF == 2) {
+        double e = 0.0;
+        for (int k = 0; k < nv; ++k) e += wt[k] * df[nv + k];
+        W[M - 1] -= e / 2;
+    }
+    solve_iprojection(D, mid, df, W, wt, nv, lam);
+    double psi[5];
+    for (int k = 0; k < nv; ++k) {
+        iproj_psi(D, mid, nv, k, psi);
+        double dot = 0.0;
+        for (int i = 0; i < M; ++i) dot += lam[i] * psi[i];
+        df[k] *= std::exp(dot);
+    }
+}
+
 // ------------------------------------------------------------- iterate --------
-// iterate!(CAIDVM_Marching) (Theory/Iterate.jl:96-130) and iterate!(Euler) (:131-162)
+// iterate!(CAIDVM_Marching) (Theory/Iterate.jl:96-130), iterate!(Euler) (:131-162) and
+// iterate!(CIP_Marching) (Theory/I-projection.jl:161-193)
 void iterate(Model& m, int64_t step, double* sum_res, double* sum_avg) {
     const kg_topology* t = m.t;
     int D = m.dim, NDF = m.ndf, NW = m.nw();
@@ -988,6 +1128,27 @@ void iterate(Model& m, int64_t step, double* sum_res, double* sum_avg) {
                     double gplus = Fc[k] + Sp[k];
                     double v = Model::F(fp, nv, i, k) * r1;
                     Model::F(fp, nv, i, k) = v + r2 * gplus;
+                }
+            }
+        } else if (m.prm.marching == KG_MARCH_CIP) {
+            // w update, convection, q of the convected f, I-projection of f onto w, relaxation
+            for (int e = 0; e < NW; ++e) w[e] += wf[e] * dt / area;
+            get_prim(m, w, prim_c);
+            double s = dt / area;
+            for (size_t a = 0; a < (size_t)nv * NDF; ++a) fp[a] += s * vf[a];
+            heat_flux(m, g, fp, prim_c, q);
+            for (int e = 0; e < D; ++e) m.qf[(size_t)c * D + e] = q[e];
+            double lam[5];
+            conserved_iprojection(D, NDF, g.mid, g.weight, nv, fp, w, lam);
+            double tau = get_tau(m, prim_c);
+            double r1 = tau / (tau + dt), r2 = dt / (tau + dt);
+            double Fc[2], Sp[2];
+            for (int i = 0; i < nv; ++i) {
+                maxwell(m, g, i, prim_c, Fc);
+                shakhov(m, g, i, Fc, prim_c, q, Sp);
+                for (int k = 0; k < NDF; ++k) {
+                    double v = Model::F(fp, nv, i, k) * r1;
+                    Model::F(fp, nv, i, k) = v + r2 * (Fc[k] + Sp[k]);
                 }
             }
         } else {
@@ -1402,6 +1563,16 @@ int kgo_macro_slope(const kg_params* prm, const kg_topology* t, const double* sd
 int kgo_last_error(char* buf, size_t cap) {
     std::snprintf(buf, cap, "%s", g_err.c_str());
     return 0;
+}
+
+// conserved_I_porjection! of one velocity grid: df (column-major nv x ndf) in place, the
+// multipliers λ (dim+2) out.  mid: column-major nv x dim midpoints, weight: nv.
+int kgo_iprojection(int dim, int ndf, int nv, const double* mid, const double* weight, double* df, const double* w,
+                    double* lam) {
+    if ((dim != 2 || ndf != 2) && (dim != 3 || ndf != 1)) { g_err = "dim/ndf"; return KG_ERR_ARG; }
+    if (nv <= 0 || !mid || !weight || !df || !w || !lam) { g_err = "null argument"; return KG_ERR_ARG; }
+    conserved_iprojection(dim, ndf, mid, weight, nv, df, w, lam);
+    return KG_OK;
 }
 
 }  // extern "C"

@@ -45,6 +45,7 @@ def lib():
         L.kgo_criterion.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + \
             [C.c_double, C.POINTER(C.c_double)]
         L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.kgo_iprojection.argtypes = [C.c_int, C.c_int, C.c_int] + [C.POINTER(C.c_double)] * 5
         _lib = L
     return _lib
 
@@ -174,3 +175,20 @@ class OracleState:
         lib().kgo_moments(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.f),
                           abi.dptr(self.prim), abi.dptr(w), abi.dptr(q))
         return w.reshape(nc, nw), q.reshape(nc, self.topo["dim"])
+
+
+def iprojection(dim: int, ndf: int, mid: np.ndarray, weight: np.ndarray, df: np.ndarray, w: np.ndarray):
+    """conserved_I_porjection! of one velocity grid (Theory/I-projection.jl:144-158).
+
+    mid: nv x dim midpoints, weight: nv, df: nv x ndf, w: dim+2 conserved variables.
+    Returns the projected df (nv x ndf) and the multipliers λ (dim+2)."""
+    nv = weight.size
+    m = np.ascontiguousarray(np.asarray(mid, np.float64).reshape(nv, dim).T).ravel()
+    wt = np.ascontiguousarray(weight, np.float64)
+    f = np.ascontiguousarray(np.asarray(df, np.float64).reshape(nv, ndf).T).ravel()
+    ww = np.ascontiguousarray(w, np.float64)
+    lam = np.zeros(dim + 2)
+    rc = lib().kgo_iprojection(dim, ndf, nv, abi.dptr(m), abi.dptr(wt), abi.dptr(f), abi.dptr(ww), abi.dptr(lam))
+    if rc != 0:
+        raise RuntimeError(f"oracle iprojection failed: {rc}")
+    return f.reshape(ndf, nv).T.copy(), lam
