@@ -206,31 +206,32 @@ def run_ours(args, rank, world, dist):
             step += 3
             res[form]["kernels"] = g.profile_read()
             g.profile(False)
-            # end to end through the C-ABI with pinned host buffers: every step uploads f, w,
-            # prim and downloads f, w, prim, qf
-            f_h = pinned_empty(state["f"].size, torch)
-            f_h[:] = state["f"]
-            w_h = pinned_empty(state["w"].size, torch); w_h[:] = state["w"]
-            p_h = pinned_empty(state["prim"].size, torch); p_h[:] = state["prim"]
-            q_h = pinned_empty(topo["n_cells"] * topo["dim"], torch)
-            import ctypes as C
-            g.use_graph(False)   # one step per call, each from freshly uploaded host state
+            # end to end through the C-ABI with pinned host buffers: kg_serve runs e2e_steps
+            # requests of one step each; every request uploads f, w, prim from the host and
+            # downloads f, w, prim, qf (the upload of the next and the download of the previous
+            # request overlap the step, both link directions at once)
+            ins = {"f": pinned_empty(state["f"].size, torch), "w": pinned_empty(state["w"].size, torch),
+                   "prim": pinned_empty(state["prim"].size, torch)}
+            for k in ins:
+                ins[k][:] = state[k]
+            outs = [{"f": pinned_empty(state["f"].size, torch), "w": pinned_empty(state["w"].size, torch),
+                     "prim": pinned_empty(state["prim"].size, torch),
+                     "qf": pinned_empty(topo["n_cells"] * topo["dim"], torch)} for _ in range(2)]
+            g.use_graph(False)
             e2e_steps = max(1, min(args.steps, 10))
+            requests = [ins] * e2e_steps
+            req_out = [outs[r % 2] for r in range(e2e_steps)]
             barrier()
             t0 = time.perf_counter()
-            for s in range(e2e_steps):
-                g.L.kg_upload_state(g.h, f_h.ctypes.data, w_h.ctypes.data, p_h.ctypes.data)
-                r = abi.KgStepReport()
-                g.L.kg_step(g.h, dt, step + s, 1, C.byref(r))
-                g.L.kg_download_state(g.h, f_h.ctypes.data, w_h.ctypes.data, p_h.ctypes.data, q_h.ctypes.data, None)
+            g.serve(requests, dt, step, 1, outputs=req_out)
             barrier()
             el = time.perf_counter() - t0
             if dist is not None:
                 t = torch.tensor([el], dtype=torch.float64)
                 dist.all_reduce(t, op=dist.ReduceOp.MAX)
                 el = float(t.item())
-            h2d = f_h.nbytes + w_h.nbytes + p_h.nbytes
-            d2h = f_h.nbytes + w_h.nbytes + p_h.nbytes + q_h.nbytes
+            h2d = sum(a.nbytes for a in ins.values())
+            d2h = sum(a.nbytes for a in outs[0].values())
             res[form]["e2e"] = {"value": P * world * e2e_steps / el, "unit": UNIT,
                                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
         g.close()

@@ -310,6 +310,21 @@ int kg_upload_restart(kg_handle *h, const int32_t *quad_index, int32_t n_quads, 
  * (slope -> flux -> iterate).                                               */
 int kg_step(kg_handle *h, double dt, int64_t step, int32_t nsteps, kg_step_report *report);
 
+/* Pipelined serving of independent requests on the uploaded topology (single-problem
+ * handle).  Request r starts from the host state f_in[r], w_in[r], prim_in[r] (layouts of
+ * kg_upload_state), advances nsteps steps from step counter step0 with time step dt, and
+ * writes its final state to f_out[r], w_out[r], prim_out[r], qf_out[r] (layouts of
+ * kg_download_state; an output array or entry may be NULL) and its report to reports[r].
+ * The result equals kg_upload_state + kg_step + kg_download_state per request, bit for bit;
+ * the upload of request r+1 and the download of request r-1 run on two copy streams while
+ * request r steps, so with pinned host buffers the link carries both directions at once.
+ * Returns when every output is written; the handle then holds the last request's state.
+ * No counterpart in the reference (a serving loop over its step).                      */
+int kg_serve(kg_handle *h, int32_t n_requests, const double *const *f_in, const double *const *w_in,
+             const double *const *prim_in, double dt, int64_t step0, int32_t nsteps,
+             double *const *f_out, double *const *w_out, double *const *prim_out, double *const *qf_out,
+             kg_step_report *reports);
+
 /* Optional per-kernel device timing (CUDA events on the handle's stream).
  * kg_profile_read fills up to `cap` entries; names are static strings.       */
 int kg_profile_enable(kg_handle *h, int enable);

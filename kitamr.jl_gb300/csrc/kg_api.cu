@@ -85,6 +85,23 @@ __global__ void prim_of_w(const double* __restrict__ w, double* __restrict__ pri
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c < n) get_prim<D>(w + (int64_t)c * MAXW, gamma, prim + (int64_t)c * MAXW);
 }
+// Rows between the caller's packed layout (n_src rows of sw doubles) and the library's padded
+// one (n_dst rows of dw >= sw doubles); padding and the rows past n_src (wall data items) are
+// zero.  rows_pack is the inverse for the first n rows.
+__global__ void rows_unpack(const double* __restrict__ src, int sw, int n_src, double* __restrict__ dst, int dw, int n_dst) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n_dst * dw) return;
+    const int64_t c = i / dw;
+    const int e = (int)(i - c * dw);
+    dst[i] = (c < n_src && e < sw) ? src[c * sw + e] : 0.0;
+}
+__global__ void rows_pack(const double* __restrict__ src, int sw, double* __restrict__ dst, int dw, int n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * dw) return;
+    const int64_t c = i / dw;
+    dst[i] = src[c * sw + (i - c * dw)];
+}
+__global__ void set_step_counter(int64_t* p, int64_t v) { *p = v; }
 }  // namespace
 
 void kg::set_global_error(const std::string& msg) { g_create_err = msg; }
@@ -194,6 +211,10 @@ struct kg_handle {
     const int32_t* d_order = nullptr;
     int64_t* d_tri = nullptr;      // wall-initialisation copies of an upload (grown on demand)
     int64_t tri_cap = 0;
+    // pipelined serving (kg_serve): two copy streams and FP64 staging, made on first use
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    double* sv_buf = nullptr;
+    int64_t sv_cap = 0;            // doubles
     // graph
     bool use_graph = false;
     cudaGraphExec_t gexec = nullptr;
@@ -733,10 +754,154 @@ void fill_report(const kg_handle* h, int slot, double ms, int64_t launches, kg_s
     r->status = st ? ((st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE) : KG_OK;
 }
 
+// Pipelined serving of independent requests on the single problem (kg_serve).  Three streams:
+// s_in uploads request r+1 into FP64 staging while the handle's stream steps request r and
+// s_out downloads request r-1 from one of two FP64 output stagings; events order the reuse of
+// each staging.  Request r: f, w, prim from the host -> the steps -> f, w, prim, qf to the
+// host, the same device work as kg_upload_state + kg_step + kg_download_state.
+int prepare_wall_copies(kg_handle* h, int slot);
+cudaError_t launch_wall_copies(const kg_handle* h, int nwall, char* fa, cudaStream_t s);
+int enqueue_step(kg_handle* h, bool timed, int64_t* launches);
+int serve(kg_handle* h, int32_t n, const double* const* f_in, const double* const* w_in, const double* const* prim_in,
+          double dt, int64_t step0, int32_t nsteps, double* const* f_out, double* const* w_out,
+          double* const* prim_out, double* const* qf_out, kg_step_report* reports) {
+    Problem& pb = h->probs[0];
+    if (!pb.live) { pb.live = true; h->dirty = true; }
+    int rc = rebuild(h);
+    if (rc) return rc;
+    if (h->autotune && h->tuned_version != h->version && (rc = autotune_flux(h))) return rc;
+    if (pb.pp.dt != dt && (rc = set_prob_dt(h, 0, dt))) return rc;
+    const Flat& L = pb.F;
+    const int D = h->prm.dim, NW = D + 2, NC = L.n_cells;
+    const int64_t nfc = L.foff[NC], nd = pb.dsize, fb = pb.fbase, db = pb.dbase;
+    const size_t ss = storage_size(h);
+    // staging: f in, two f out, rows in (w, prim), two rows out (w, prim, qf)
+    const int64_t rin = 2LL * NC * NW, rout = 2LL * NC * NW + (int64_t)NC * D;
+    const int64_t need = 3 * nfc + rin + 2 * rout;
+    if (h->sv_cap < need) {
+        if (h->sv_buf) cudaFree(h->sv_buf);
+        h->sv_buf = nullptr;
+        h->sv_cap = 0;
+        if (cudaMalloc(&h->sv_buf, sizeof(double) * need) != cudaSuccess) {
+            h->sv_buf = nullptr;
+            return fail(h, KG_ERR_NOMEM, "cudaMalloc serving staging");
+        }
+        h->sv_cap = need;
+    }
+    if (!h->s_in) KG_CUDA(h, cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking));
+    if (!h->s_out) KG_CUDA(h, cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking));
+    double* d_fin = h->sv_buf;
+    double* d_fout[2] = {d_fin + nfc, d_fin + 2 * nfc};
+    double* d_rin = d_fin + 3 * nfc;
+    double* d_rout[2] = {d_rin + rin, d_rin + rin + rout};
+    if ((rc = prepare_wall_copies(h, 0))) return rc;
+    const int nwall = (int)L.wall_ops.size();
+    // per request: residual row and status word, copied on the device, read at the end
+    double* d_rep = nullptr;
+    if (cudaMalloc(&d_rep, sizeof(double) * (size_t)n * (RES_STRIDE + 1)) != cudaSuccess)
+        return fail(h, KG_ERR_NOMEM, "cudaMalloc serving reports");
+    std::vector<cudaEvent_t> ev((size_t)n * 6, nullptr);   // h2d, in_free, done, out_free, t0, t1
+    struct Cleanup {
+        std::vector<cudaEvent_t>& ev;
+        double* rep;
+        ~Cleanup() {
+            for (cudaEvent_t e : ev) if (e) cudaEventDestroy(e);
+            if (rep) cudaFree(rep);
+        }
+    } cleanup{ev, d_rep};
+    for (int32_t r = 0; r < n; ++r)
+        for (int k = 0; k < 6; ++k)
+            KG_CUDA(h, cudaEventCreateWithFlags(&ev[(size_t)r * 6 + k], k < 4 ? cudaEventDisableTiming : cudaEventDefault));
+    auto E = [&](int32_t r, int k) { return ev[(size_t)r * 6 + k]; };
+    std::vector<int64_t> launches((size_t)n, 0);
+    const int tb = 256;
+    auto blocks = [&](int64_t m) { return (int)std::min<int64_t>((m + tb - 1) / tb, 1 << 20); };
+    for (int32_t r = 0; r < n; ++r) {
+        // upload (s_in), once the previous request has consumed the input staging
+        if (r > 0) KG_CUDA(h, cudaStreamWaitEvent(h->s_in, E(r - 1, 1), 0));
+        KG_CUDA(h, cudaMemcpyAsync(d_fin, f_in[r], sizeof(double) * nfc, cudaMemcpyHostToDevice, h->s_in));
+        KG_CUDA(h, cudaMemcpyAsync(d_rin, w_in[r], sizeof(double) * NC * NW, cudaMemcpyHostToDevice, h->s_in));
+        KG_CUDA(h, cudaMemcpyAsync(d_rin + NC * NW, prim_in[r], sizeof(double) * NC * NW, cudaMemcpyHostToDevice, h->s_in));
+        KG_CUDA(h, cudaEventRecord(E(r, 0), h->s_in));
+        // state (handle stream)
+        cudaStream_t s = h->stream;
+        KG_CUDA(h, cudaStreamWaitEvent(s, E(r, 0), 0));
+        char* fa = (char*)(h->parity == 0 ? h->fA : h->fB) + fb * ss;
+        if (h->prm.precision == KG_PREC_FP64)
+            KG_CUDA(h, cudaMemcpyAsync(fa, d_fin, sizeof(double) * nfc, cudaMemcpyDeviceToDevice, s));
+        else
+            to_storage<float><<<1024, 256, 0, s>>>(d_fin, (float*)fa, nfc);
+        rows_unpack<<<blocks(nd * MAXW), tb, 0, s>>>(d_rin, NW, NC, h->w + db * MAXW, MAXW, (int)nd);
+        rows_unpack<<<blocks(nd * MAXW), tb, 0, s>>>(d_rin + NC * NW, NW, NC, h->prim + db * MAXW, MAXW, (int)nd);
+        KG_CUDA(h, cudaGetLastError());
+        KG_CUDA(h, cudaEventRecord(E(r, 1), s));
+        KG_CUDA(h, launch_wall_copies(h, nwall, fa, s));
+        KG_CUDA(h, cudaMemsetAsync((char*)h->sdf + fb * D * ss, 0, pb.fsize * D * ss, s));
+        KG_CUDA(h, cudaMemsetAsync(h->qf + db * MAXD, 0, sizeof(double) * nd * MAXD, s));
+        set_step_counter<<<1, 1, 0, s>>>(h->d_step, step0);
+        KG_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), s));
+        KG_CUDA(h, cudaMemsetAsync(h->res_out + 2 * MAXW + 1, 0, sizeof(double), s));
+        KG_CUDA(h, cudaEventRecord(E(r, 4), s));
+        for (int32_t k = 0; k < nsteps; ++k)
+            if ((rc = enqueue_step(h, false, &launches[r]))) return rc;
+        KG_CUDA(h, cudaEventRecord(E(r, 5), s));
+        KG_CUDA(h, cudaMemcpyAsync(d_rep + (int64_t)r * (RES_STRIDE + 1), h->res_out, sizeof(double) * RES_STRIDE, cudaMemcpyDeviceToDevice, s));
+        KG_CUDA(h, cudaMemcpyAsync(d_rep + (int64_t)r * (RES_STRIDE + 1) + RES_STRIDE, h->d_status, sizeof(int), cudaMemcpyDeviceToDevice, s));
+        // result into output staging r % 2, once request r-2 has left it
+        if (r >= 2) KG_CUDA(h, cudaStreamWaitEvent(s, E(r - 2, 3), 0));
+        const char* fr = (const char*)(h->parity == 0 ? h->fA : h->fB) + fb * ss;
+        double* fo = d_fout[r % 2];
+        double* ro = d_rout[r % 2];
+        if (h->prm.precision == KG_PREC_FP64)
+            KG_CUDA(h, cudaMemcpyAsync(fo, fr, sizeof(double) * nfc, cudaMemcpyDeviceToDevice, s));
+        else
+            from_storage<float><<<1024, 256, 0, s>>>((const float*)fr, fo, nfc);
+        rows_pack<<<blocks((int64_t)NC * NW), tb, 0, s>>>(h->w + db * MAXW, MAXW, ro, NW, NC);
+        rows_pack<<<blocks((int64_t)NC * NW), tb, 0, s>>>(h->prim + db * MAXW, MAXW, ro + NC * NW, NW, NC);
+        rows_pack<<<blocks((int64_t)NC * D), tb, 0, s>>>(h->qf + db * MAXD, MAXD, ro + 2 * NC * NW, D, NC);
+        KG_CUDA(h, cudaGetLastError());
+        KG_CUDA(h, cudaEventRecord(E(r, 2), s));
+        // download (s_out)
+        KG_CUDA(h, cudaStreamWaitEvent(h->s_out, E(r, 2), 0));
+        if (f_out && f_out[r]) KG_CUDA(h, cudaMemcpyAsync(f_out[r], fo, sizeof(double) * nfc, cudaMemcpyDeviceToHost, h->s_out));
+        if (w_out && w_out[r]) KG_CUDA(h, cudaMemcpyAsync(w_out[r], ro, sizeof(double) * NC * NW, cudaMemcpyDeviceToHost, h->s_out));
+        if (prim_out && prim_out[r]) KG_CUDA(h, cudaMemcpyAsync(prim_out[r], ro + NC * NW, sizeof(double) * NC * NW, cudaMemcpyDeviceToHost, h->s_out));
+        if (qf_out && qf_out[r]) KG_CUDA(h, cudaMemcpyAsync(qf_out[r], ro + 2 * NC * NW, sizeof(double) * NC * D, cudaMemcpyDeviceToHost, h->s_out));
+        KG_CUDA(h, cudaEventRecord(E(r, 3), h->s_out));
+    }
+    KG_CUDA(h, cudaStreamSynchronize(h->s_out));
+    KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::vector<double> rep((size_t)n * (RES_STRIDE + 1));
+    KG_CUDA(h, cudaMemcpy(rep.data(), d_rep, sizeof(double) * rep.size(), cudaMemcpyDeviceToHost));
+    h->have_state = true;
+    int worst = KG_OK;
+    for (int32_t r = 0; r < n; ++r) {
+        const double* o = rep.data() + (size_t)r * (RES_STRIDE + 1);
+        kg_step_report R;
+        std::memset(&R, 0, sizeof(R));
+        R.checked = o[2 * MAXW + 1] != 0.0;
+        R.checked_step = R.checked ? (int64_t)o[2 * MAXW] : -1;
+        for (int e = 0; e < 5; ++e) { R.sum_res[e] = o[e]; R.sum_avg[e] = o[MAXW + e]; }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, E(r, 4), E(r, 5));
+        R.device_ms = ms;
+        R.phase_cells = L.phase_cells;
+        R.kernel_launches = (int32_t)launches[r];
+        int st = 0;
+        std::memcpy(&st, o + RES_STRIDE, sizeof(int));
+        R.status = st ? ((st & ST_NONFINITE) ? KG_ERR_NONFINITE : KG_ERR_NEGATIVE) : KG_OK;
+        if (R.status && !worst) worst = R.status;
+        if (reports) reports[r] = R;
+    }
+    if (worst) return fail(h, worst, worst == KG_ERR_NONFINITE ? "non-finite primitive variables" : "rho <= 0 or lambda <= 0");
+    return KG_OK;
+}
+
 // SolidNeighbor df starts as a copy of the donor df (Immersed_boundary.jl:290-298): one
 // launch for all walls of the problem in `slot`, within the f buffer at fa (the problem's
 // block of it).
-int init_wall_blocks(kg_handle* h, int slot, char* fa) {
+// The (donor, wall, length) copies of the problem in `slot` into h->d_tri (host-synchronous).
+int prepare_wall_copies(kg_handle* h, int slot) {
     const Flat& L = h->probs[slot].F;
     const int nwall = (int)L.wall_ops.size();
     if (nwall == 0) return KG_OK;
@@ -758,10 +923,20 @@ int init_wall_blocks(kg_handle* h, int slot, char* fa) {
         h->tri_cap = (int64_t)tri.size();
     }
     KG_CUDA(h, cudaMemcpyAsync(h->d_tri, tri.data(), sizeof(int64_t) * tri.size(), cudaMemcpyHostToDevice, h->stream));
-    if (h->prm.precision == KG_PREC_FP64) copy_blocks<double><<<nwall, 256, 0, h->stream>>>((double*)fa, h->d_tri);
-    else copy_blocks<float><<<nwall, 256, 0, h->stream>>>((float*)fa, h->d_tri);
-    KG_CUDA(h, cudaGetLastError());
     KG_CUDA(h, cudaStreamSynchronize(h->stream));   // tri is host memory the copy reads
+    return KG_OK;
+}
+// The copies prepared above, within the f buffer at fa (the problem's block of it).
+cudaError_t launch_wall_copies(const kg_handle* h, int nwall, char* fa, cudaStream_t s) {
+    if (nwall == 0) return cudaSuccess;
+    if (h->prm.precision == KG_PREC_FP64) copy_blocks<double><<<nwall, 256, 0, s>>>((double*)fa, h->d_tri);
+    else copy_blocks<float><<<nwall, 256, 0, s>>>((float*)fa, h->d_tri);
+    return cudaGetLastError();
+}
+int init_wall_blocks(kg_handle* h, int slot, char* fa) {
+    int rc = prepare_wall_copies(h, slot);
+    if (rc) return rc;
+    KG_CUDA(h, launch_wall_copies(h, (int)h->probs[slot].F.wall_ops.size(), fa, h->stream));
     return KG_OK;
 }
 
@@ -1403,6 +1578,9 @@ int kg_destroy(kg_handle* h) {
     cudaStreamSynchronize(h->aux);
     free_pools(h);
     if (h->d_tri) cudaFree(h->d_tri);
+    if (h->sv_buf) cudaFree(h->sv_buf);
+    if (h->s_in) { cudaStreamSynchronize(h->s_in); cudaStreamDestroy(h->s_in); }
+    if (h->s_out) { cudaStreamSynchronize(h->s_out); cudaStreamDestroy(h->s_out); }
     if (h->h_res) cudaFreeHost(h->h_res);
     if (h->h_status) cudaFreeHost(h->h_status);
     cudaEventDestroy(h->ev_fork);
@@ -1549,6 +1727,21 @@ int kg_step(kg_handle* h, double dt, int64_t step, int32_t nsteps, kg_step_repor
     if (report) *report = r;
     if (r.status) return fail(h, r.status, r.status == KG_ERR_NONFINITE ? "non-finite primitive variables" : "rho <= 0 or lambda <= 0");
     return KG_OK;
+}
+
+int kg_serve(kg_handle* h, int32_t n_requests, const double* const* f_in, const double* const* w_in,
+             const double* const* prim_in, double dt, int64_t step0, int32_t nsteps, double* const* f_out,
+             double* const* w_out, double* const* prim_out, double* const* qf_out, kg_step_report* reports) {
+    if (!h) return KG_ERR_ARG;
+    if (h->is_batch || h->probs.empty() || h->probs[0].F.n_data == 0) return fail(h, KG_ERR_STATE, "upload a topology first");
+    if (n_requests < 0 || nsteps < 0 || !(dt > 0.0)) return fail(h, KG_ERR_ARG, "n_requests and nsteps must be >= 0 and dt > 0");
+    if (n_requests == 0) return KG_OK;
+    if (!f_in || !w_in || !prim_in) return fail(h, KG_ERR_ARG, "null argument");
+    for (int32_t r = 0; r < n_requests; ++r)
+        if (!f_in[r] || !w_in[r] || !prim_in[r]) return fail(h, KG_ERR_ARG, "null input state");
+    cudaSetDevice(h->device);
+    cudaStreamSynchronize(h->stream);
+    return serve(h, n_requests, f_in, w_in, prim_in, dt, step0, nsteps, f_out, w_out, prim_out, qf_out, reports);
 }
 
 int kg_profile_enable(kg_handle* h, int enable) {

@@ -61,6 +61,7 @@ def load_library(path: Optional[str] = None):
     L.kg_upload_restart.argtypes = [vp, vp, i32, vp, vp]
     L.kg_batch_download_restart.argtypes = [vp, i32, vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
+    L.kg_serve.argtypes = [vp, i32, vp, vp, vp, dbl, i64, i32, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -73,7 +74,7 @@ EXPORTS = [
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
     "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
-    "kg_vs_flags", "kg_batch_vs_flags",
+    "kg_vs_flags", "kg_batch_vs_flags", "kg_serve",
 ]
 
 
@@ -144,6 +145,26 @@ class GpuStep:
         rep = abi.KgStepReport()
         _check(self.L, self.h, self.L.kg_step(self.h, dt, step0, nsteps, C.byref(rep)))
         return rep
+
+    def serve(self, states, dt: float, step0: int, nsteps: int, outputs=None):
+        """kg_serve: every state dict (f, w, prim: float64 arrays, pinned for overlapped copies)
+        is advanced nsteps steps from step0; returns (outputs, reports).  `outputs`: optional
+        list of dicts of preallocated f, w, prim, qf arrays (entries may be shared between
+        requests)."""
+        n = len(states)
+        nf, nw = int(self.foff[-1]), self.nc * (self.dim + 2)
+        ins = [{k: np.ascontiguousarray(st[k], dtype=np.float64) for k in ("f", "w", "prim")} for st in states]
+        for st in ins:
+            assert st["f"].size == nf and st["w"].size == nw and st["prim"].size == nw
+        if outputs is None:
+            outputs = [dict(f=np.empty(nf), w=np.empty(nw), prim=np.empty(nw), qf=np.empty(self.nc * self.dim))
+                       for _ in range(n)]
+        ptrs = lambda key, lst: (C.c_void_p * n)(*[a[key].ctypes.data if a.get(key) is not None else None for a in lst])
+        reports = (abi.KgStepReport * max(n, 1))()
+        _check(self.L, self.h, self.L.kg_serve(self.h, n, ptrs("f", ins), ptrs("w", ins), ptrs("prim", ins), dt, step0,
+                                               nsteps, ptrs("f", outputs), ptrs("w", outputs), ptrs("prim", outputs),
+                                               ptrs("qf", outputs), reports))
+        return outputs, [reports[r] for r in range(n)]
 
     def download_state(self, sdf: bool = False) -> Dict[str, np.ndarray]:
         nf = int(self.foff[-1])
