@@ -366,6 +366,51 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         F.pass_off.push_back((int32_t)F.slope_ops.size());
         F.pass_cells_off.push_back((int32_t)F.pass_cells.size());
     }
+    // The passes by dependency depth instead of by level: only a transverse projection reads
+    // other cells' slopes of this step (those of its coarser neighbours, computed by an earlier
+    // pass of the level sweep, Slope.jl:908-941); every other cell reads f alone and joins the
+    // first pass.  A cell's pass follows the passes of the cells whose slopes it reads, so every
+    // cell computes the same values as in the level order, in fewer, fuller launches.
+    {
+        const size_t npc = F.pass_cells.size();
+        std::vector<int32_t> entry((size_t)NC, -1), depth(npc, 0);
+        for (size_t k = 0; k < npc; ++k) entry[F.pass_cells[k]] = (int32_t)k;
+        bool ok = true;
+        int maxd = 0;
+        for (size_t k = 0; k < npc && ok; ++k) {
+            int dk = 0;
+            for (int dir = 0; dir < D; ++dir) {
+                const SlopeOp& op = F.slope_ops[(size_t)F.cell_slope_op[k] + dir];
+                if (op.kind != SLOPE_ONE && op.kind != SLOPE_TWO) continue;
+                for (int side = 0; side < 2; ++side) {
+                    const bool proj = side == 0 ? op.projA : (op.kind == SLOPE_TWO && op.projB);
+                    if (!proj) continue;
+                    const int32_t l0 = side == 0 ? op.listA : op.listB, n = side == 0 ? op.cntA : op.cntB;
+                    for (int32_t j = 0; j < n; ++j) {
+                        const int32_t dn = F.slope_nbr[(size_t)l0 + j].data;
+                        if (dn >= NC || entry[dn] < 0) continue;   // walls, solid cells: no slope pass
+                        if ((size_t)entry[dn] >= k) { ok = false; break; }   // not coarser: keep the level passes
+                        dk = std::max(dk, depth[entry[dn]] + 1);
+                    }
+                }
+            }
+            depth[k] = dk;
+            maxd = std::max(maxd, dk);
+        }
+        if (ok) {
+            std::vector<int32_t> cells, ops;
+            cells.reserve(npc);
+            ops.reserve(npc);
+            F.pass_cells_off.assign(1, 0);
+            for (int d = 0; d <= maxd; ++d) {
+                for (size_t k = 0; k < npc; ++k)
+                    if (depth[k] == d) { cells.push_back(F.pass_cells[k]); ops.push_back(F.cell_slope_op[k]); }
+                F.pass_cells_off.push_back((int32_t)cells.size());
+            }
+            F.pass_cells.swap(cells);
+            F.cell_slope_op.swap(ops);
+        }
+    }
 
     // ---- physical-space criterion (update_criterion!, Physical_space/AMR.jl:1-284) --------
     for (int i = 0; i < NC; ++i) {

@@ -149,9 +149,9 @@ struct Flat {
     // pairing tables
     std::vector<int64_t> p_off;    // n_pairs + 1 (offsets into p_j0 / p_cnt)
     std::vector<int32_t> p_j0, p_cnt;
-    // slope: passes (levels) and ops
-    std::vector<int32_t> pass_off;   // n_passes + 1 into slope_ops (grouped by pass)
-    std::vector<SlopeOp> slope_ops;  // ordered by pass, then cell, then dir
+    // slope: passes (by dependency depth: the first holds every cell that reads f alone) and ops
+    std::vector<int32_t> pass_off;   // per level + 1 into slope_ops (the ops' build order)
+    std::vector<SlopeOp> slope_ops;  // ordered by level, then cell, then dir
     std::vector<int32_t> pass_cells_off;  // per pass: cells [pass_cells_off[p], ...) in pass_cells
     std::vector<int32_t> pass_cells;
     std::vector<int32_t> cell_slope_op;   // per pass-cell entry: first op index (dim ops each)
