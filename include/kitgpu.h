@@ -285,6 +285,15 @@ typedef struct {
     double  coeffi_global;     /* solver.ADAPT_COEFFI_VS_GLOBAL (default 0.125)             */
 } kg_vs_config;
 int kg_vs_flags(kg_handle *h, const kg_vs_config *cfg, uint8_t *flags, double *eta, double *vr);
+
+/* vs_conserved_correction! (Velocity_space/AMR.jl:122-137) on the device state: for every cell
+ * c with cell_flags[c] != 0 (n_cells bytes; solid cells are skipped), conserved_I_porjection!
+ * (Theory/I-projection.jl:144-158) of its f onto its w -- the Newton solve of
+ * solve_I_projection (:55-141) with the negative-value shave, then f₁ *= exp(λ·ψ).  For a
+ * caller that rebuilt velocity grids (vs_refine! / vs_coarsen!) and uploaded the new state, or
+ * any state whose moments must be made to match w.                                        */
+int kg_vs_conserve(kg_handle *h, const uint8_t *cell_flags);
+int kg_batch_vs_conserve(kg_handle *h, int32_t slot, const uint8_t *cell_flags);   /* kg_vs_conserve of one problem */
 int kg_batch_vs_flags(kg_handle *h, int32_t slot, const kg_vs_config *cfg, uint8_t *flags, double *eta,
                       double *vr);   /* kg_vs_flags of one problem (vr over that problem) */
 

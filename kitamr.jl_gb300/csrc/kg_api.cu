@@ -20,6 +20,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t cip(const Dev&, int, cudaStream_t);
+    static cudaError_t conserve(const Dev&, const int32_t*, int, cudaStream_t);
     static cudaError_t macro_slope(const Dev&, int, int, int, double*, cudaStream_t);
     static cudaError_t criterion(const Dev&, int, int, int, const double*, double, double*, double*, cudaStream_t);
     static cudaError_t adapt(const Dev&, int, const AdaptRec*, const void*, const void*, const double*, const double*,
@@ -1445,6 +1446,36 @@ int upload_restart(kg_handle* h, int slot, const int32_t* quad_index, int32_t n_
 }
 
 // ---- velocity-space adaptation flags (vs_refine! / vs_coarsen!) -----------------------------
+// vs_conserved_correction! (Velocity_space/AMR.jl:122-137): the I-projection of every flagged
+// fluid cell of the problem in `slot` onto its w, on the device state.
+int vs_conserve(kg_handle* h, int slot, const uint8_t* cell_flags) {
+    int rc = rebuild(h);
+    if (rc) return rc;
+    const Problem& pb = h->probs[slot];
+    const Flat& M = h->M;
+    std::vector<int32_t> list;
+    for (int k = pb.pp.fluid_begin; k < pb.pp.fluid_end; ++k) {
+        const int64_t c = (int64_t)M.fluid_cells[k] - pb.dbase;
+        if (c >= 0 && c < pb.F.n_cells && cell_flags[c]) list.push_back(k);
+    }
+    if (list.empty()) return KG_OK;
+    int32_t* d_list = nullptr;
+    KG_CUDA(h, cudaMalloc(&d_list, sizeof(int32_t) * list.size()));
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fA : h->fB;
+    P.f_out = h->parity == 0 ? h->fB : h->fA;
+    cudaError_t e = cudaMemcpyAsync(d_list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, h->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->d_status + slot, 0, sizeof(int), h->stream);
+    if (e == cudaSuccess) e = dispatch(h, [&](auto L) { return decltype(L)::conserve(P, d_list, (int)list.size(), h->stream); });
+    int st = 0;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, h->d_status + slot, sizeof(int), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    cudaFree(d_list);
+    if (e != cudaSuccess) return cuda_fail(h, e, "conserve_kernel");
+    if (st) return fail(h, KG_ERR_NONFINITE, "non-finite I-projection multipliers");
+    return KG_OK;
+}
+
 int vs_flags(kg_handle* h, int slot, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr_out) {
     const int D = h->prm.dim, NDF = h->prm.ndf;
     if (cfg->maxlevel < 0 || cfg->maxlevel > 12) return fail(h, KG_ERR_ARG, "maxlevel out of range");
@@ -1676,6 +1707,15 @@ int kg_adapt(kg_handle* h, const kg_topology* topo, const kg_adapt_src* src) {
     return adapt_problem(h, 0, topo, src);
 }
 
+int kg_vs_conserve(kg_handle* h, const uint8_t* cell_flags) {
+    if (!h) return KG_ERR_ARG;
+    if (!cell_flags) return fail(h, KG_ERR_ARG, "null argument");
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_vs_conserve");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    return vs_conserve(h, 0, cell_flags);
+}
+
 int kg_download_restart(kg_handle* h, const int32_t* quad_index, int32_t n_quads, double* vs_df, double* ws) {
     if (!h) return KG_ERR_ARG;
     if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: use kg_batch_download_restart");
@@ -1901,6 +1941,13 @@ int kg_batch_download_restart(kg_handle* h, int32_t slot, const int32_t* quad_in
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
     return download_restart(h, slot, quad_index, n_quads, vs_df, ws);
+}
+
+int kg_batch_vs_conserve(kg_handle* h, int32_t slot, const uint8_t* cell_flags) {
+    if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
+    if (!cell_flags) return fail(h, KG_ERR_ARG, "null argument");
+    cudaSetDevice(h->device);
+    return vs_conserve(h, slot, cell_flags);
 }
 
 int kg_batch_vs_flags(kg_handle* h, int32_t slot, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr) {

@@ -1962,25 +1962,23 @@ __device__ __forceinline__ A cip_dot(const A* lam, const A* ps) {
 __device__ __forceinline__ double cip_exp(double x) { return exp(x); }
 __device__ __forceinline__ float cip_exp(float x) { return expf(x); }
 
+// conserved_I_porjection!'s solve for the cell of record FC (one CTA; every thread of the
+// block takes part): f (the cell's block, in the storage type) has its negative values of f₁
+// shaved in place; lam receives the multipliers λ in every thread.  w: the cell's conserved
+// variables (FP64, padded to MAXW).
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
+__device__ __forceinline__ void iprojection_solve(const Dev& P, const FluxCell& FC, T* f, const double* wc,
+                                                  double (&lamd)[D + 2]) {
     using A = typename Arith<T>::type;
     constexpr int M = D + 2, NJ = M * (M + 1) / 2, NS = M + NJ, MAXIT = 10;
-    extern __shared__ __align__(16) unsigned char sh_raw[];
     __shared__ double sred[NS * (BLOCK / 32)];
     __shared__ double slam[M], strial[M];
     __shared__ A slA[M];
     __shared__ int sctl;
-    enum { C_PREC = 0, C_BFC, C_R1, C_R2, C_SK, C_LC, C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
-    __shared__ A sc[C_N];
-    __shared__ float sUl[MAXD], sUh[MAXD], slh, sll;
-    const FluxCell FC = P.fcrec[blockIdx.x];
-    const int cell = FC.cell, slot = FC.slot, nv = FC.nv;
-    const ProbParams& PP = P.probs[slot];
+    const int nv = FC.nv;
     const int64_t PG = P.PG, goff = FC.goff;
     const A* VU = vel<A>(P);
     const A* VW = wts<A>(P) + goff;
-    T* f = (T*)P.f_out + FC.foff;
 
     // ---- W, and the shave of negative values of f₁ (I-projection.jl:78-88) ----------------
     {
@@ -2004,8 +2002,7 @@ __global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
             }
         }
         if (threadIdx.x == 0) {
-            const double* w = P.w + (int64_t)cell * MAXW;
-            for (int m = 0; m < M; ++m) { slam[m] = 0.0; strial[m] = w[m]; }
+            for (int m = 0; m < M; ++m) { slam[m] = 0.0; strial[m] = wc[m]; }
             if (NDF == 2) strial[M - 1] -= e[0] / 2;
         }
         __syncthreads();
@@ -2137,6 +2134,29 @@ __global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
             for (int m = 0; m < M; ++m) slam[m] += alpha * dl[m];
         __syncthreads();
     }
+    __syncthreads();
+#pragma unroll
+    for (int m = 0; m < M; ++m) lamd[m] = slam[m];
+    __syncthreads();
+}
+
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
+    using A = typename Arith<T>::type;
+    constexpr int M = D + 2;
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    __shared__ A slA[M];
+    enum { C_PREC = 0, C_BFC, C_R1, C_R2, C_SK, C_LC, C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_N = C_QA + MAXD };
+    __shared__ A sc[C_N];
+    __shared__ float sUl[MAXD], sUh[MAXD], slh, sll;
+    const FluxCell FC = P.fcrec[blockIdx.x];
+    const int cell = FC.cell, slot = FC.slot, nv = FC.nv;
+    const ProbParams& PP = P.probs[slot];
+    const int64_t PG = P.PG, goff = FC.goff;
+    const A* VU = vel<A>(P);
+    T* f = (T*)P.f_out + FC.foff;
+    double slam[M];
+    iprojection_solve<D, NDF, T>(P, FC, f, P.w + (int64_t)cell * MAXW, slam);
     // ---- collision constants of prim_c (the flux kernel's expressions) ----------------------
     A* Ec = (A*)sh_raw;
     const double* pc = P.prim + (int64_t)cell * MAXW;
@@ -2226,6 +2246,29 @@ __global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
     }
 }
 
+// vs_conserved_correction! (Velocity_space/AMR.jl:122-137): conserved_I_porjection! of the
+// listed fluid-list entries on the current f (in place) and w, one CTA each.
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) conserve_kernel(Dev P, const int32_t* list) {
+    using A = typename Arith<T>::type;
+    constexpr int M = D + 2;
+    const FluxCell FC = P.fcrec[list[blockIdx.x]];
+    T* f = (T*)P.f_in + FC.foff;
+    double lam[M];
+    iprojection_solve<D, NDF, T>(P, FC, f, P.w + (int64_t)FC.cell * MAXW, lam);
+    A la[M];
+    bool bad = false;
+#pragma unroll
+    for (int m = 0; m < M; ++m) { la[m] = (A)lam[m]; bad |= !isfinite(lam[m]); }
+    if (bad && threadIdx.x == 0) atomicOr(&P.status[FC.slot], ST_NONFINITE);
+    const A* VU = vel<A>(P);
+    for (int i = threadIdx.x; i < FC.nv; i += BLOCK) {
+        A ps[M];
+        cip_psi<D, A>(VU, P.PG, FC.goff, i, ps);
+        f[i] = (T)((A)f[i] * cip_exp(cip_dot<M, A>(la, ps)));
+    }
+}
+
 template <int D, int NDF, typename T>
 struct Launch {
     // the slope work items [item_base, item_base + n) of one pass
@@ -2296,6 +2339,12 @@ struct Launch {
         cudaError_t e = cudaFuncSetAttribute(cip_kernel<D, NDF, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         cip_kernel<D, NDF, T><<<n, BLOCK, smem, s>>>(P);
+        return cudaGetLastError();
+    }
+    // vs_conserved_correction! of n listed fluid-list entries
+    static cudaError_t conserve(const Dev& P, const int32_t* list, int n, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        conserve_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, list);
         return cudaGetLastError();
     }
     static cudaError_t macro_slope(const Dev& P, int fbegin, int n, int dbase, double* out, cudaStream_t s) {

@@ -62,6 +62,8 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_download_restart.argtypes = [vp, i32, vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     L.kg_serve.argtypes = [vp, i32, vp, vp, vp, dbl, i64, i32, vp, vp, vp, vp, vp]
+    L.kg_vs_conserve.argtypes = [vp, vp]
+    L.kg_batch_vs_conserve.argtypes = [vp, i32, vp]
     _lib = L
     return L
 
@@ -74,7 +76,7 @@ EXPORTS = [
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
     "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
-    "kg_vs_flags", "kg_batch_vs_flags", "kg_serve",
+    "kg_vs_flags", "kg_batch_vs_flags", "kg_serve", "kg_vs_conserve", "kg_batch_vs_conserve",
 ]
 
 
@@ -165,6 +167,12 @@ class GpuStep:
                                                nsteps, ptrs("f", outputs), ptrs("w", outputs), ptrs("prim", outputs),
                                                ptrs("qf", outputs), reports))
         return outputs, [reports[r] for r in range(n)]
+
+    def vs_conserve(self, cell_flags: np.ndarray):
+        """kg_vs_conserve: I-projection of the flagged cells' f onto their w (in place on the device)."""
+        fl = np.ascontiguousarray(cell_flags, dtype=np.uint8)
+        assert fl.size == self.nc
+        _check(self.L, self.h, self.L.kg_vs_conserve(self.h, fl.ctypes.data))
 
     def download_state(self, sdf: bool = False) -> Dict[str, np.ndarray]:
         nf = int(self.foff[-1])
