@@ -228,7 +228,15 @@ int kg_criterion(kg_handle *h, double adapt_coeffi_ps, double *lohner);
  *   KG_ADAPT_COARSEN  src[0..2^dim-1]: the children in RMT order.  The parent's velocity
  *                     grid must be the grid of the first child with the fewest velocity
  *                     cells (ps_merge); df and sdf are the vs_merge! sums of the children
- *                     over 2^dim, w the children's mean, prim = get_prim(w), qf = 0.
+ *                     over 2^dim, w the children's mean, prim = get_prim(w), qf = 0;
+ *   KG_ADAPT_VS       src[0]: the same cell before a velocity-space adaptation
+ *                     (vs_refine! / vs_coarsen!, Velocity_space/AMR.jl:26-118) that gave
+ *                     it a new velocity grid, or the same one: refine_grid_stream! and
+ *                     coarsen_grid_stream! (Rebuild.jl:44-163) move df -- a refined
+ *                     velocity cell's children take its df, 2^dim coarsened siblings their
+ *                     mean -- along the level merge walk of the two grids; sdf is zero (both
+ *                     streams reset it), w, prim and qf are kept.  The conservative
+ *                     correction that follows is kg_vs_conserve.
  * Indices refer to the cells of the topology on the device before the call; KEEP and
  * REFINE cells keep their source's velocity grid (equal content).  As
  * ps_adaptive_mesh_refinement! does, the slopes of the current f are recomputed first
@@ -242,6 +250,7 @@ int kg_criterion(kg_handle *h, double adapt_coeffi_ps, double *lohner);
 #define KG_ADAPT_KEEP       0
 #define KG_ADAPT_REFINE     1
 #define KG_ADAPT_COARSEN    2
+#define KG_ADAPT_VS         3
 #define KG_ADAPT_MAX_DEPTH  8
 typedef struct {
     int32_t kind;

@@ -1183,6 +1183,32 @@ int build_adapt_plan(kg_handle* h, const Flat& Fo, int64_t fbo, int64_t dbo, con
                 }
                 r.lev[q] = lt->second;
             }
+        } else if (a.kind == KG_ADAPT_VS) {
+            const int o = a.src[0];
+            if (o < 0 || o >= NCo) return fail(h, KG_ERR_ARG, "adapt source cell out of range" + where(c));
+            const int go = Fo.dgrid[o];
+            r.nsrc = 1;
+            r.src_f[0] = fbo + Fo.foff[o];
+            r.src_nv[0] = Fo.dnv[o];
+            r.src_d[0] = (int32_t)(dbo + o);
+            if (!is_same(go, gn)) {
+                auto key = std::make_pair(gn, go);
+                auto it = run_of.find(key);
+                if (it == run_of.end()) {
+                    const int64_t nn = Fn.g_off[gn + 1] - Fn.g_off[gn], no = Fo.g_off[go + 1] - Fo.g_off[go];
+                    if (!level_runs(&Fn.vlev[Fn.g_off[gn]], (int)nn, &Fo.vlev[Fo.g_off[go]], (int)no, D, tmp))
+                        return fail(h, KG_ERR_TOPOLOGY, "a rebuilt velocity grid does not tile its source grid's root lattice" + where(c));
+                    it = run_of.emplace(key, (int64_t)plan.runs.size() / 2).first;
+                    plan.runs.insert(plan.runs.end(), tmp.begin(), tmp.end());
+                }
+                r.run[0] = it->second;
+                auto lt = lev_of.find(go);
+                if (lt == lev_of.end()) {
+                    lt = lev_of.emplace(go, (int64_t)plan.lev.size()).first;
+                    plan.lev.insert(plan.lev.end(), Fo.vlev.begin() + Fo.g_off[go], Fo.vlev.begin() + Fo.g_off[go + 1]);
+                }
+                r.lev[0] = lt->second;
+            }
         } else {
             return fail(h, KG_ERR_ARG, "unknown adapt kind" + where(c));
         }

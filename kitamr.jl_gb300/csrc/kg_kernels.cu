@@ -1825,6 +1825,37 @@ __global__ void __launch_bounds__(BLOCK) adapt_kernel(Dev P, AdaptView<T> V) {
         if (threadIdx.x < D) qn[threadIdx.x] = V.qf[od * MAXD + threadIdx.x];
         return;
     }
+    if (R.kind == KG_ADAPT_VS) {
+        // refine_grid_stream! / coarsen_grid_stream! (Velocity_space/Rebuild.jl:44-163): each
+        // velocity cell of the new grid from the run of source cells it overlaps -- a coarser
+        // source cell (refinement) copied, 2^dim finer siblings (coarsening) summed over 2^dim
+        // (the same bits as their sum over 2^dim); slopes zero, w, prim and qf kept
+        const T* fs = V.f + R.src_f[0];
+        const int nvs = R.src_nv[0];
+        for (int i = threadIdx.x; i < nv; i += BLOCK) {
+            const int li = P.vlev[g.goff + i];
+            int j0 = i, cnt = 1;
+            if (R.run[0] >= 0) { j0 = V.runs[2 * (R.run[0] + i)]; cnt = V.runs[2 * (R.run[0] + i) + 1]; }
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                A acc = 0;
+                for (int j = j0; j < j0 + cnt; ++j) {
+                    const int sh = R.run[0] >= 0 ? D * ((int)V.lev[R.lev[0] + j] - li) : 0;
+                    const A v = (A)fs[(int64_t)k * nvs + j];
+                    acc += sh > 0 ? v / (A)(1 << sh) : v;
+                }
+                fn[(int64_t)k * nv + i] = (T)acc;
+            }
+        }
+        for (int64_t a = threadIdx.x; a < (int64_t)D * NDF * nv; a += BLOCK) sn[a] = (T)0;
+        const int64_t od = R.src_d[0];
+        if (threadIdx.x < D + 2) {
+            wn[threadIdx.x] = V.w[od * MAXW + threadIdx.x];
+            pn[threadIdx.x] = V.prim[od * MAXW + threadIdx.x];
+        }
+        if (threadIdx.x < D) qn[threadIdx.x] = V.qf[od * MAXD + threadIdx.x];
+        return;
+    }
     if (R.kind == KG_ADAPT_REFINE) {
         const T* fs = V.f + R.src_f[0];
         const T* ss = V.sdf + R.src_f[0] * D;

@@ -101,7 +101,7 @@ def make_params(problem, precision=KG_PREC_FP64, flux=KG_FLUX_CAIDVM, marching=K
                     gamma=g.gamma, K=g.K, Pr=g.Pr, omega=g.omega, mu_ref=g.mu_ref())
 
 
-KG_ADAPT_KEEP, KG_ADAPT_REFINE, KG_ADAPT_COARSEN = 0, 1, 2
+KG_ADAPT_KEEP, KG_ADAPT_REFINE, KG_ADAPT_COARSEN, KG_ADAPT_VS = 0, 1, 2, 3
 KG_ADAPT_MAX_DEPTH = 8
 # kg_adapt_src: where a cell of an adapted mesh takes its state from
 ADAPT_SRC = np.dtype([("kind", "<i4"), ("depth", "<i4"), ("src", "<i4", (8,)), ("path", "i1", (KG_ADAPT_MAX_DEPTH,))])

@@ -104,6 +104,46 @@ def refine_vgrid(g: VGrid, flags: np.ndarray, root_ds: Sequence[float]) -> VGrid
     return VGrid(np.array(lev, np.int8), np.array(wt), np.array(mid, dtype=np.float64).reshape(-1, dim))
 
 
+def coarsen_vgrid(g: VGrid, ok: np.ndarray, root_ds: Sequence[float], maxlevel: int) -> VGrid:
+    """Streaming coarsening of Velocity_space/Rebuild.jl:96-163 (the grid part): walking the
+    depth-first grid with the reference's alignment bookkeeping, a 2^D-aligned group of
+    same-level siblings merges into its parent (level - 1, weight x 2^D, the midpoint half a
+    child step from the first child's) when every member is willing (``ok``)."""
+    dim = g.midpoint.shape[1]
+    nc = 2 ** dim
+    n = g.nv
+    flag = [0.0] * (maxlevel + 1)
+    lev, wt, mid = [], [], []
+
+    def copy(i):
+        lev.append(int(g.level[i])); wt.append(g.weight[i]); mid.append(list(g.midpoint[i]))
+    index = 0
+    while index < n:
+        fl = int(g.level[index])
+        if fl > 0:
+            if (flag[fl] % 1 == 0.0 and index + nc - 1 < n
+                    and all(int(g.level[index + k]) == fl for k in range(1, nc))):
+                if all(bool(ok[index + k]) for k in range(nc)):
+                    lev.append(fl - 1)
+                    wt.append(g.weight[index] * nc)
+                    mid.append([g.midpoint[index, d] + 0.5 * (root_ds[d] / 2 ** fl) for d in range(dim)])
+                else:
+                    for k in range(nc):
+                        copy(index + k)
+                index += nc
+                for i in range(1, fl):
+                    flag[i] += 1 / 2 ** (dim * (fl - i))
+            else:
+                copy(index)
+                for i in range(1, fl + 1):
+                    flag[i] += 1 / 2 ** (dim * (fl - i + 1))
+                index += 1
+        else:
+            copy(index)
+            index += 1
+    return VGrid(np.array(lev, np.int8), np.array(wt), np.array(mid, dtype=np.float64).reshape(-1, dim))
+
+
 def adapted_vgrid(dim, quadrature, vs_trees_num, prim, maxlevel: int, radius=(2.4, 1.2)) -> VGrid:
     """A velocity grid refined around the bulk velocity of ``prim`` (a static stand-in for
     the reference's velocity-space AMR, which stays on the host)."""
@@ -825,4 +865,57 @@ def adapt_grids(old: Dict, new: Dict, src: np.ndarray) -> Dict:
         ga, gb = grid_arrays(old, int(cg[dn])), grid_arrays(new, int(new["cell_grid"][dn]))
         if not all(np.array_equal(x, y) for x, y in zip(ga, gb)):
             raise ValueError(f"wall donor {dn} changes its velocity grid; its cut cells would not match")
+    return out
+
+
+def cell_vgrid(topo: Dict, cell: int) -> VGrid:
+    """The velocity grid of ``cell`` in a topology."""
+    dim = int(topo["dim"])
+    g = int(topo["cell_grid"][cell])
+    o = np.asarray(topo["grid_off"])
+    a, b = int(o[g]), int(o[g + 1])
+    return VGrid(np.asarray(topo["vs_level"])[a:b].astype(np.int8), np.asarray(topo["vs_weight"])[a:b].copy(),
+                 np.asarray(topo["vs_midpoint"])[a * dim:b * dim].reshape(dim, b - a).T.copy())
+
+
+def with_cell_vgrids(topo: Dict, grids: Dict[int, VGrid]) -> Dict:
+    """``topo`` with new velocity grids for some cells (a velocity-space adaptation): grids are
+    appended to the grid table (or shared with an equal one).  A wall donor may not change its
+    grid: its wall's cut cells index that grid."""
+    dim = int(topo["dim"])
+    out = dict(topo)
+    donors = set(int(x) for x in np.asarray(topo.get("wall_donor", np.zeros(0, np.int32))))
+    level = [np.asarray(topo["vs_level"])]
+    weight = [np.asarray(topo["vs_weight"])]
+    mid = [np.asarray(topo["vs_midpoint"])]
+    goff = list(np.asarray(topo["grid_off"], np.int64))
+    known = {}
+    for g in range(int(topo["n_grids"])):
+        a, b = goff[g], goff[g + 1]
+        known[level[0][a:b].tobytes() + mid[0][a * dim:b * dim].tobytes()] = g
+    cg = np.asarray(topo["cell_grid"], np.int32).copy()
+    for c, vg in grids.items():
+        key = vg.level.astype(np.int8).tobytes() + vg.midpoint.reshape(-1, order="F").tobytes()
+        g = known.get(key)
+        if g is None:
+            g = len(goff) - 1
+            known[key] = g
+            level.append(vg.level.astype(np.int8)); weight.append(vg.weight)
+            mid.append(vg.midpoint.reshape(-1, order="F"))
+            goff.append(goff[-1] + vg.nv)
+        if c in donors and g != cg[c]:
+            raise ValueError(f"wall donor {c} changes its velocity grid; its cut cells would not match")
+        cg[c] = g
+    out.update(n_grids=len(goff) - 1, grid_off=np.array(goff, np.int64),
+               vs_level=np.concatenate(level).astype(np.int8), vs_weight=np.concatenate(weight),
+               vs_midpoint=np.concatenate(mid), cell_grid=cg)
+    return out
+
+
+def vs_sources(topo: Dict) -> np.ndarray:
+    """One KG_ADAPT_VS record per cell (each cell its own source)."""
+    from .abi import KG_ADAPT_VS
+    out = np.zeros(int(topo["n_cells"]), ADAPT_SRC)
+    out["kind"] = KG_ADAPT_VS
+    out["src"][:, 0] = np.arange(int(topo["n_cells"]))
     return out

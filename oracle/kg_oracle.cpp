@@ -1334,6 +1334,46 @@ static void vs_merge(int D, double* dst, const Grid& gp, const double* src, cons
     }
 }
 
+// refine_grid_stream! / coarsen_grid_stream! (Velocity_space/Rebuild.jl:44-163), the df part:
+// the new grid gn walked against the source grid go -- a velocity cell on both copied, the
+// children of a refined cell each given its df, and 2^dim coarsened siblings merged as
+// (Σ df) / 2^dim.  (A cover of mixed levels, which the streams never produce, is weighted by
+// volume.)
+static void vs_rebuild_df(int D, double* dst, const Grid& gn, const double* src, const Grid& go, int ndf) {
+    int i = 0;
+    for (int j = 0; j < gn.nv;) {
+        const int ln = gn.level[j], lo = go.level[i];
+        if (ln == lo) {
+            for (int k = 0; k < ndf; ++k) dst[(size_t)k * gn.nv + j] = src[(size_t)k * go.nv + i];
+            ++i; ++j;
+        } else if (ln > lo) {
+            double filled = 0.0;
+            while (filled < 1.0) {
+                for (int k = 0; k < ndf; ++k) dst[(size_t)k * gn.nv + j] = src[(size_t)k * go.nv + i];
+                filled += 1.0 / std::ldexp(1.0, D * (gn.level[j] - lo));
+                ++j;
+            }
+            ++i;
+        } else {
+            int i1 = i;
+            bool same = true;
+            double filled = 0.0;
+            while (filled < 1.0) {
+                same = same && go.level[i1] == ln + 1;
+                filled += 1.0 / std::ldexp(1.0, D * (go.level[i1] - ln));
+                ++i1;
+            }
+            for (int k = 0; k < ndf; ++k) {
+                double s = 0.0;
+                for (int q = i; q < i1; ++q)
+                    s += same ? src[(size_t)k * go.nv + q] : src[(size_t)k * go.nv + q] / std::ldexp(1.0, D * (go.level[q] - ln));
+                dst[(size_t)k * gn.nv + j] = same ? s / (1 << D) : s;
+            }
+            i = i1; ++j;
+        }
+    }
+}
+
 // The adapted mesh's state from the previous one, per new cell as src[c] says (see
 // kg_adapt_src): KEEP copies; REFINE is ps_replace!(::Val{1}) applied depth times (ps_copy,
 // ds halved, df += min(|df/(ds.|sdf| + EPS)|, 1) * (sdf . (ds/2 .* RMT[i])) with the parent's
@@ -1405,6 +1445,13 @@ int kgo_adapt(const kg_params* prm, const kg_topology* told, const kg_topology* 
             for (size_t e = 0; e < nf; ++e) fn[e] /= nch;
             for (size_t e = 0; e < ns; ++e) sn[e] /= nch;
             for (int d = 0; d < D; ++d) qf_new[(size_t)c * D + d] = 0.0;
+        } else if (a.kind == KG_ADAPT_VS) {
+            const int o = a.src[0];
+            const Grid& go = mo.grids[told->cell_grid[o]];
+            vs_rebuild_df(D, fn, g, f_old + mo.foff[o], go, NDF);
+            std::fill(sn, sn + ns, 0.0);
+            for (int e = 0; e < NW; ++e) { w_new[(size_t)c * NW + e] = w_old[(size_t)o * NW + e]; prim_new[(size_t)c * NW + e] = prim_old[(size_t)o * NW + e]; }
+            for (int d = 0; d < D; ++d) qf_new[(size_t)c * D + d] = qf_old[(size_t)o * D + d];
         } else {
             g_err = "unknown adapt kind";
             return KG_ERR_ARG;

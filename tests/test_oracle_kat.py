@@ -358,3 +358,35 @@ def test_cip_marching_conserves_in_periodic_box():
     # relaxation towards the discrete Maxwellian of the same state)
     w_f, _ = st.moments(abi.make_params(p, marching=abi.KG_MARCH_CIP))
     assert np.max(np.abs(w_f - st.w.reshape(-1, 4))) < 1e-3 * np.max(np.abs(st.w))
+
+
+def test_vs_rebuild_refine_then_coarsen_returns_the_grid_and_f():
+    """refine_grid_stream! then coarsen_grid_stream! (Rebuild.jl:44-163) of the same velocity
+    cells: the grid comes back, and f to rounding (children inherit df, siblings average)."""
+    p = cases.sod(scale=0.125, nv=16)
+    topo, state = cases.build(p)
+    prm = abi.make_params(p)
+    st = O.OracleState(topo, state)
+    st.run(prm, p.dt(), 0, 2)
+    root = mesh.vgrid_root_ds(p.case.quadrature, p.case.vs_trees_num, 2)
+    fine = {}
+    for c in range(0, topo["n_cells"], 3):
+        g = mesh.cell_vgrid(topo, c)
+        fine[c] = mesh.refine_vgrid(g, np.linalg.norm(g.midpoint, axis=1) < 2.0, root)
+    t1 = mesh.with_cell_vgrids(topo, fine)
+    s1 = st.adapt(prm, t1, mesh.vs_sources(t1))
+    off0, off1 = mesh.f_offsets(topo), mesh.f_offsets(t1)
+    for c in fine:
+        g0, g1 = mesh.cell_vgrid(topo, c), mesh.cell_vgrid(t1, c)
+        f0 = st.f[off0[c]:off0[c + 1]].reshape(2, -1).T
+        f1 = s1.f[off1[c]:off1[c + 1]].reshape(2, -1).T
+        # the children carry the parent's df: density unchanged
+        assert abs(np.sum(g1.weight * f1[:, 0]) - np.sum(g0.weight * f0[:, 0])) <= 1e-14 * np.sum(g0.weight * f0[:, 0])
+    assert np.all(s1.sdf == 0.0) and np.array_equal(s1.w, st.w)
+    coarse = {c: mesh.coarsen_vgrid(mesh.cell_vgrid(t1, c), mesh.cell_vgrid(t1, c).level > 0, root, 2) for c in fine}
+    for c in fine:
+        g0, g2 = mesh.cell_vgrid(topo, c), coarse[c]
+        assert np.array_equal(g0.level, g2.level) and np.allclose(g0.midpoint, g2.midpoint, rtol=0, atol=1e-15)
+    t2 = mesh.with_cell_vgrids(t1, coarse)
+    s2 = s1.adapt(prm, t2, mesh.vs_sources(t2))
+    assert np.allclose(s2.f, st.f, rtol=4e-16, atol=0)
