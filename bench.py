@@ -342,6 +342,79 @@ def cylinder_after_adaptation():
     return p
 
 
+def run_vsadapt(args):
+    """Cost of one velocity-space adaptation of the cylinder (mixed form) on the device: the
+    flags (kg_vs_flags), the df moves onto refined grids (kg_adapt with KG_ADAPT_VS: the host
+    flattening of the new topology plus the device move) and the conservative correction of
+    the changed cells (kg_vs_conserve), then the same back onto the original grids.  The new
+    grids (every non-donor fluid cell's grid refined where |u| < 1.5) are built before the
+    timed region: that is the caller's host work.  Compared with the route that keeps f on
+    the host (f down and up around the reference's own host adaptation)."""
+    import torch
+    from kitgpu import abi, cases, mesh
+    from kitgpu.solver import GpuStep
+    pa = make_problem(1.0)
+    ta, sa = cases.build(pa)
+    dim = ta["dim"]
+    root = mesh.vgrid_root_ds(pa.case.quadrature, pa.case.vs_trees_num, dim)
+    donors = set(int(x) for x in np.asarray(ta["wall_donor"]))
+    be = ta["cell_bound_enc"]
+    by_grid = {}
+    for g in np.unique(ta["cell_grid"]):
+        c0 = int(np.nonzero(ta["cell_grid"] == g)[0][0])
+        vg = mesh.cell_vgrid(ta, c0)
+        ok = (np.linalg.norm(vg.midpoint, axis=1) < 1.5) & (vg.level < pa.vs_maxlevel)
+        by_grid[int(g)] = mesh.refine_vgrid(vg, ok, root)
+    changed = [c for c in range(ta["n_cells"]) if be[c] >= 0 and c not in donors]
+    tb = mesh.with_cell_vgrids(ta, {c: by_grid[int(ta["cell_grid"][c])] for c in changed})
+    src_b, src_a = mesh.vs_sources(tb), mesh.vs_sources(ta)
+    flags = np.zeros(ta["n_cells"], np.uint8)
+    flags[changed] = 1
+    prm = abi.make_params(pa, precision=abi.KG_PREC_MIXED, st_check_interval=100)
+    cfg = abi.make_vs_config(pa)
+    dt = pa.dt()
+    g = GpuStep(prm, ta)
+    g.upload_state(sa["f"], sa["w"], sa["prim"])
+    g.step(dt, 0, args.warmup)
+    step = args.warmup
+    t_flags, t_move, t_cons = [], [], []
+    for k in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.vs_flags(cfg, eta=False)
+        t1 = time.perf_counter()
+        g.adapt(tb, src_b) if k % 2 == 0 else g.adapt(ta, src_a)
+        t2 = time.perf_counter()
+        g.vs_conserve(flags)
+        t3 = time.perf_counter()
+        t_flags.append((t1 - t0) * 1e3); t_move.append((t2 - t1) * 1e3); t_cons.append((t3 - t2) * 1e3)
+        g.step(dt, step, 1)
+        step += 1
+    g.close()
+    # host route: f (and sdf for the flags' criterion) down, a state of the new size up
+    h = GpuStep(prm, ta)
+    h.upload_state(sa["f"], sa["w"], sa["prim"])
+    h.step(dt, 0, 1)
+    host = []
+    for k in range(max(3, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = h.download_state(sdf=True)
+        h.upload_state(out["f"], out["w"], out["prim"])
+        host.append((time.perf_counter() - t0) * 1e3)
+    h.close()
+    med = lambda v: float(np.median(v))
+    total = med([a + b + c for a, b, c in zip(t_flags, t_move, t_cons)])
+    return {"metric": "velocity-space adaptation time (flags + grid moves + conservative correction)",
+            "value": total, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32-f/f64-moments",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD + " velocity grids refined where |u| < 1.5 and back",
+                       "changed_cells": len(changed), "phase_cells": [mesh.phase_cells(ta), mesh.phase_cells(tb)]},
+            "device_route": {"vs_flags_ms": med(t_flags), "adapt_vs_ms": med(t_move), "vs_conserve_ms": med(t_cons)},
+            "host_route_transfer_ms": med(host), "gpu_launches": None}
+
+
 def run_adapt(args):
     """Cost of one physical-space adaptation of the cylinder (mixed form): the device route
     (kg_criterion, then kg_adapt with the new topology and the per-cell sources) against the
@@ -460,7 +533,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=None,
                     help="scale of the base mesh (default: the workload's own; smaller for profiling captures)")
-    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "sod", "batched", "serve", "adapt"])
+    ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "sod", "batched", "serve", "adapt", "vsadapt"])
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
@@ -516,8 +589,8 @@ def main():
         if rank == 0:
             print(json.dumps(line))
         return
-    if args.mode == "adapt":
-        line = run_adapt(args)
+    if args.mode in ("adapt", "vsadapt"):
+        line = run_adapt(args) if args.mode == "adapt" else run_vsadapt(args)
         if rank == 0:
             print(json.dumps(line))
         return
