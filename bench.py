@@ -170,7 +170,8 @@ def run_ours(args, rank, world, dist):
         torch.cuda.synchronize()
 
     for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
-        prm = abi.make_params(prob, precision=prec, st_check_interval=100)
+        march = {"caidvm": abi.KG_MARCH_CAIDVM, "cip": abi.KG_MARCH_CIP}[args.march]
+        prm = abi.make_params(prob, precision=prec, st_check_interval=100, marching=march)
         g = GpuStep(prm, topo, device=dev)
         g.upload_state(state["f"], state["w"], state["prim"])
         # the timed call replays a CUDA graph of `steps` steps (captured by the last warm-up
@@ -538,6 +539,8 @@ def main():
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     ap.add_argument("--forms", default="mixed,fp64", help="serve: precision forms to run (mixed, fp64)")
+    ap.add_argument("--march", default="caidvm", choices=["caidvm", "cip"],
+                    help="single-problem modes: time marching (cip: CIP_Marching, meshes without walls)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.scale is None:
@@ -622,7 +625,7 @@ def main():
                    "l2": (f"inputs > L2 (f is {P * ndf * 4 / 1e6:.0f} MB FP32, sdf {P * ndf * 4 * (2 if ndf == 2 else 3) / 1e6:.0f} MB)"
                           if P * ndf * 4 * (3 if ndf == 2 else 4) > 129e6 else
                           f"inputs inside L2 (f {P * ndf * 4 / 1e6:.0f} MB FP32), not flushed between steps: the workload is this small"),
-                   "parallelism": f"replicas{world}", "cuda_graph": True},
+                   "parallelism": f"replicas{world}", "cuda_graph": True, "marching": args.march},
         "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
                   "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
         "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
