@@ -2171,8 +2171,9 @@ __device__ __forceinline__ void iprojection_solve(const Dev& P, const FluxCell& 
     __syncthreads();
 }
 
+// (2D mixed form: three CTAs per SM, with 4 bytes of spills, instead of two)
 template <int D, int NDF, typename T>
-__global__ void __launch_bounds__(BLOCK) cip_kernel(Dev P) {
+__global__ void __launch_bounds__(BLOCK, (D == 2 && sizeof(T) == 4) ? 3 : 1) cip_kernel(Dev P) {
     using A = typename Arith<T>::type;
     constexpr int M = D + 2;
     extern __shared__ __align__(16) unsigned char sh_raw[];
