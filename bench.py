@@ -1,23 +1,28 @@
 """Benchmark of the phase-space step (slope -> flux incl. IB wall -> Shakhov collision).
 
-Workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x64 trees,
-3 levels near the wall, 48^2 velocity roots on [-15,15]^2 adapted by 2 levels), seeded
+Headline workload: the 2D Ma 5 / Kn 0.1 cylinder (diffuse isothermal wall, [-8,8]^2, 64x64
+trees, 3 levels near the wall, 48^2 velocity roots on [-15,15]^2 adapted by 2 levels), seeded
 synthetic initial state; 61 M phase cells, so f is far larger than L2 between steps.
 
-  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-  python bench.py --mode sphere | sod | batched | serve | adapt   (the other workloads, one line each)
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--no-sub]
+  python bench.py --mode sphere | sod | batched | serve | adapt | vsadapt   (one workload per line)
 
 Metric: phase-cell updates/s of the mixed-precision form (FP32 f, compensated moments,
-FP64 conserved update), with the plain FP64 form, the roofline of the dominant kernel, the
+FP64 conserved update), with the plain FP64 form, the accuracy of the mixed form against the
+FP64 form and of both against the FP64 oracle, the roofline of the dominant kernel, the
 oracle CPU baseline and the end-to-end rate through the C-ABI with host buffers beside it.
+The default line also carries one compact record per other workload (`sub`): the Sod tube,
+the sphere at its benchmark size, the batched form (autotuned) and serving.
 N > 1: independent replicas, one per GPU (the path has no exchange on one device).
 Other modes:
-* sphere: the 3D Ma 3 sphere at half its base mesh (183 M phase cells).
+* sphere: the 3D Ma 3 sphere (``--scale``: base mesh scale of the generator's default
+  refinement; without it, the benchmark configuration of about 2.1e5 cells).
 * sod: the 2D Sod tube of the reference's Riemann example (inputs inside L2).
 * batched: 256 Sod / cavity problems in one batch handle.
 * serve: Poisson arrivals solved to residual < 1e-6.
 * adapt: one physical-space adaptation of the cylinder on the device (criterion, then the
   refine / coarsen moves of f) against the host route (f down, new topology and f up).
+* vsadapt: one velocity-space adaptation of the cylinder on the device.
 """
 from __future__ import annotations
 
@@ -42,9 +47,10 @@ UNIT = "updates/s"
 # single-problem workloads: name, default scale, generator note
 SINGLE = {
     "cylinder": (WORKLOAD, 1.0, "seeded cylinder_buffer_IC state on a generated forest"),
-    # the 3D sphere (Ma 3, Kn 0.05, 32^3 trees, 2 levels, 24^3 velocity grid) at half the base
-    # mesh by default: 13,536 cells, 183 M phase cells (the full mesh needs a 22 GB host state)
-    "sphere": ("sphere_ma3_kn0.05_32x32x32_L2_v24x24x24", 0.5, "seeded sphere buffer state on a generated octree"),
+    # the 3D sphere (Ma 3, Kn 0.05, 32^3 trees, 2 levels, 24^3 velocity grid) at its benchmark
+    # size: refinement within 3.5 / 1.8 of the wall, about 2.1e5 cells and 2.9e9 phase cells
+    # (scale None); a --scale gives the generator's default refinement on a scaled base mesh
+    "sphere": ("sphere_ma3_kn0.05_32x32x32_L2_v24x24x24", None, "seeded sphere buffer state on a generated octree"),
     # the 2D Shakhov Sod tube ([0,1]x[0,0.1], 128x4 trees, 2 levels at the jump, 28^2 velocity
     # grid): small enough that f stays in L2 between kernels
     "sod": ("sod_2d_128x4_L2_v28x28", 1.0, "Sod left/right states on a generated forest"),
@@ -54,7 +60,7 @@ SINGLE = {
 def make_problem(scale=1.0, mode="cylinder"):
     from kitgpu import cases
     if mode == "sphere":
-        return cases.sphere(scale=scale)
+        return cases.sphere_config() if scale is None else cases.sphere(scale=scale)
     if mode == "sod":
         return cases.sod(scale=scale)
     return cases.cylinder(scale=scale, nv=48, vs_levels=2)
@@ -149,7 +155,11 @@ def pinned_empty(n, torch):
     return torch.empty(n, dtype=torch.float64, pin_memory=True).numpy()
 
 
-def run_ours(args, rank, world, dist):
+def run_single(args, mode, scale, rank, world, dist, e2e=True, march="caidvm"):
+    """Timed steps of one single-problem workload in both forms (mixed, then FP64), each on
+    a fresh handle, the timed call replaying a CUDA graph; for the mixed form also the
+    per-kernel times (a separate pass) and, with e2e, the end-to-end rate through kg_serve.
+    Returns (phase cells, per-form results, launches in the timed call, problem, topo, state)."""
     import torch
     from kitgpu import abi, mesh
     from kitgpu.solver import GpuStep
@@ -157,7 +167,7 @@ def run_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     from kitgpu import cases
-    prob = make_problem(args.scale, args.mode)
+    prob = make_problem(scale, mode)
     topo, state = cases.build(prob)
     P = mesh.phase_cells(topo)
     dt = prob.dt()
@@ -170,8 +180,8 @@ def run_ours(args, rank, world, dist):
         torch.cuda.synchronize()
 
     for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
-        march = {"caidvm": abi.KG_MARCH_CAIDVM, "cip": abi.KG_MARCH_CIP}[args.march]
-        prm = abi.make_params(prob, precision=prec, st_check_interval=100, marching=march)
+        mcode = {"caidvm": abi.KG_MARCH_CAIDVM, "cip": abi.KG_MARCH_CIP}[march]
+        prm = abi.make_params(prob, precision=prec, st_check_interval=100, marching=mcode)
         g = GpuStep(prm, topo, device=dev)
         g.upload_state(state["f"], state["w"], state["prim"])
         # the timed call replays a CUDA graph of `steps` steps (captured by the last warm-up
@@ -207,6 +217,7 @@ def run_ours(args, rank, world, dist):
             step += 3
             res[form]["kernels"] = g.profile_read()
             g.profile(False)
+        if form == "mixed" and e2e:
             # end to end through the C-ABI with pinned host buffers: kg_serve runs one request
             # of one step per timed step; every request uploads f, w, prim from the host and
             # downloads f, w, prim, qf (the upload of the next and the download of the previous
@@ -235,9 +246,72 @@ def run_ours(args, rank, world, dist):
             d2h = sum(a.nbytes for a in outs[0].values())
             res[form]["e2e"] = {"value": P * world * e2e_steps / el, "unit": UNIT,
                                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+            del ins, outs, requests, req_out
         g.close()
     res["graph"] = True
-    return P, res, launches_total
+    return P, res, launches_total, prob, topo, state
+
+
+def accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_f=True, march="caidvm"):
+    """The accuracy statement of one workload, from its initial state:
+    * mixed_vs_fp64: the mixed form against the FP64 form, both on the GPU, after acc_steps;
+    * fp64_vs_oracle / mixed_vs_oracle: each form against the FP64 CPU oracle after
+      oracle_steps (0: not run), with f's error too when oracle_f.
+    L-infinity relative errors of ρ, U, T and q over the fluid cells (kitgpu.accuracy)."""
+    import torch
+    from kitgpu import abi
+    from kitgpu.accuracy import f_error, moment_errors, summary
+    from kitgpu.solver import GpuStep
+    dev = torch.cuda.current_device()
+    dt = prob.dt()
+    mcode = {"caidvm": abi.KG_MARCH_CAIDVM, "cip": abi.KG_MARCH_CIP}[march]
+    snaps = {}
+    for form, prec in (("fp64", abi.KG_PREC_FP64), ("mixed", abi.KG_PREC_MIXED)):
+        g = GpuStep(abi.make_params(prob, precision=prec, st_check_interval=100, marching=mcode), topo, device=dev)
+        g.upload_state(state["f"], state["w"], state["prim"])
+        done = 0
+        if oracle_steps:
+            g.step(dt, 0, oracle_steps)
+            done = oracle_steps
+            snaps[(form, "oracle")] = g.download_state(f=oracle_f)
+        if acc_steps > done:
+            g.step(dt, done, acc_steps - done)
+        snaps[(form, "acc")] = snaps[(form, "oracle")] if acc_steps == done else g.download_state(f=False)
+        g.close()
+    a, b = snaps[("fp64", "acc")], snaps[("mixed", "acc")]
+    out = {"mixed_vs_fp64": dict(summary(moment_errors(topo, a["w"], a["prim"], a["qf"], b["w"], b["prim"], b["qf"])),
+                                 steps=acc_steps)}
+    if oracle_steps:
+        import oracle as O
+        prm64 = abi.make_params(prob, precision=abi.KG_PREC_FP64, st_check_interval=100, marching=mcode)
+        ref = O.OracleState(topo, state).run(prm64, dt, 0, oracle_steps, nthreads=threads)
+        for form in ("fp64", "mixed"):
+            g = snaps[(form, "oracle")]
+            e = moment_errors(topo, ref.w, ref.prim, ref.qf, g["w"], g["prim"], g["qf"])
+            if oracle_f:
+                e["f"] = f_error(topo, ref.f, g["f"])
+            out[f"{form}_vs_oracle"] = dict(summary(e), steps=oracle_steps)
+        del ref
+    out["tolerance"] = {"mixed": 1e-5, "fp64_vs_oracle": 1e-12}
+    out["mixed_form"] = ("FP32 f / sdf and per-velocity arithmetic, compensated FP32 moment sums reduced to FP64, "
+                         "FP64 conserved update and primitive recovery; the Maxwellian exponent formed in float-float "
+                         "(~44 bits) and tau / Shakhov / relaxation constants in FP32 from the FP64 primitives (a "
+                         "departure from an all-FP64 exponent, held to the same 1e-5)")
+    return out
+
+
+def roofline_of(kern, P, ndf, peak, peak_kind, traffic=None):
+    """Roofline of the flux kernel from its per-launch CUDA-event time: 2 * NDF * 4 B per phase
+    cell (one read, one write of f in FP32) over that time, against the measured HBM peak."""
+    if "flux_collide_kernel" not in kern:
+        return None
+    ms, cnt = kern["flux_collide_kernel"]
+    avg_s = ms / cnt / 1e3
+    b_alg = 2 * ndf * 4 * P
+    ach = b_alg / avg_s / 1e9
+    return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+            "traffic": traffic, "kernel": "flux_collide_kernel", "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": b_alg, "launch_ms": avg_s * 1e3}
 
 
 def batch_shapes():
@@ -255,26 +329,33 @@ def batch_shapes():
     return out
 
 
-def run_batched(args):
-    import math
+def run_batched(args, autotune=True):
+    """Config 4: 256 problems in one batch handle, CUDA-graph replay, the flux schedule chosen
+    by kg_autotune (one CTA per cell, or persistent CTAs in natural or largest-first order).
+    Accuracy: one problem of each shape, mixed against FP64, after the same steps."""
     import torch
-    from kitgpu import abi, cases, mesh
+    from kitgpu import abi, mesh
+    from kitgpu.accuracy import moment_errors, summary
     from kitgpu.solver import GpuBatch
-    rng = np.random.default_rng(20261203 + 4)
     shapes = batch_shapes()
     forms = {}
+    snaps = {}
     for form, prec in (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64)):
+        rng = np.random.default_rng(20261203 + 4)
         base = abi.make_params(shapes[0][1], precision=prec, st_check_interval=100)
         free = torch.cuda.mem_get_info()[0]
         b = GpuBatch(base, int(free * 0.85))
         b.use_graph(True)
         P = 0
+        slots = []
         for k in range(args.problems):
             name, prob, (topo, state) = shapes[k % len(shapes)]
             prob.gas.Kn = float(10 ** rng.uniform(-3, 0))
             prm = abi.make_params(prob, precision=prec, st_check_interval=100)
-            b.admit(prm, topo, state["f"], state["w"], state["prim"], prob.dt(), 0)
+            slots.append(b.admit(prm, topo, state["f"], state["w"], state["prim"], prob.dt(), 0))
             P += mesh.phase_cells(topo)
+        if autotune:
+            b.autotune(True)
         for _ in range(args.warmup):
             b.step(1)
         reps = b.step(args.steps)       # graph capture of `steps` steps
@@ -282,48 +363,66 @@ def run_batched(args):
         ms = next(iter(reps.values())).device_ms
         forms[form] = {"value": P * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps, "phase_cells": P,
                        "launches_per_call": int(next(iter(reps.values())).kernel_launches)}
+        if autotune:
+            forms[form]["autotune"] = b.autotune_result()
+        for k in range(len(shapes)):
+            snaps[(form, k)] = b.download(slots[k])
         if form == "mixed":
             # per-kernel device times (CUDA events on the handle's stream), a separate pass
             b.profile(True)
             b.step(2)
             forms[form]["kernels_ms_per_step"] = {k: v[0] / 2 for k, v in b.profile_read().items()}
+            forms[form]["kernels"] = b.profile_read()
             b.profile(False)
         b.close()
+    acc = {}
+    for k in range(len(shapes)):
+        topo = shapes[k][2][0]
+        a, m = snaps[("fp64", k)], snaps[("mixed", k)]
+        e = summary(moment_errors(topo, a["w"], a["prim"], a["qf"], m["w"], m["prim"], m["qf"]))
+        for q, v in e.items():
+            acc[q] = max(acc.get(q, 0.0), v)
+    acc["steps"] = args.warmup + 2 * args.steps
+    acc["problems_compared"] = len(shapes)
     m = forms["mixed"]
     return {"metric": METRIC + " (batched)", "value": m["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-f/f64-moments", "data": "synthetic",
             "config": {"workload": f"batched_{args.problems}_sod_cavity_8_shapes", "phase_cells": m["phase_cells"],
-                       "graph": True},
+                       "graph": True, "autotune": autotune},
             "forms": forms, "mixed_over_fp64": forms["mixed"]["value"] / forms["fp64"]["value"],
-            "gpu_launches": m["launches_per_call"]}
+            "accuracy": {"mixed_vs_fp64": acc}, "gpu_launches": m["launches_per_call"]}
 
 
-def run_serve(args):
+def run_serve(args, requests=None, rate=None, forms=None):
+    """Config 5: Poisson arrivals of cylinder / cavity steady solves, continuous batching,
+    each request to a density residual below 1e-6 (or the step cap, counted as unconverged).
+    Latency percentiles over all requests and over the converged ones."""
     import torch
-    from kitgpu import abi, serve
+    from kitgpu import abi, cases, serve
+    nreq = requests or args.requests
+    lam = rate or args.rate
     rng = np.random.default_rng(20261203 + 5)
-    arrivals = serve.poisson_arrivals(rng, args.rate, args.requests)
+    arrivals = serve.poisson_arrivals(rng, lam, nreq)
     reqs = [serve.random_request(rng, i, a, small=False) for i, a in enumerate(arrivals)]
     for r in reqs:   # generate before the clock starts
-        from kitgpu import cases
         r.topo, r.state = cases.build(r.problem)
     out = {}
     allforms = (("mixed", abi.KG_PREC_MIXED), ("fp64", abi.KG_PREC_FP64))
-    for form, prec in [x for x in allforms if x[0] in args.forms.split(",")]:
+    for form, prec in [x for x in allforms if x[0] in (forms or args.forms).split(",")]:
         for r in reqs:
             r.slot, r.admitted, r.finished, r.steps, r.residual, r.converged = -1, -1.0, -1.0, 0, float("inf"), False
         free = torch.cuda.mem_get_info()[0]
-        srv = serve.Server(precision=prec, pool_bytes=int(free * 0.8), chunk=50, tol=1e-6, max_steps=args.steps * 50)
+        srv = serve.Server(precision=prec, pool_bytes=int(free * 0.8), chunk=50, tol=1e-6, max_steps=args.max_steps)
         st = srv.run(reqs)
         srv.close()
         out[form] = st.summary()
-        out[form]["converged"] = sum(1 for r in reqs if r.converged)
     m = out["mixed"]
     return {"metric": "serve p50/p99 time-to-steady-state", "value": m["p99_ms"], "unit": "ms", "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-f/f64-moments", "data": "synthetic",
-            "config": {"workload": f"serve_poisson_{args.rate}_per_s_{args.requests}_requests", "tol": 1e-6},
+            "config": {"workload": f"serve_poisson_{lam}_per_s_{nreq}_requests", "tol": 1e-6,
+                       "step_cap": args.max_steps, "cfl": 0.4},
             "forms": out}
 
 
@@ -505,24 +604,49 @@ def run_adapt(args):
             "device_over_host": dev_total / host_total}
 
 
-def cpu_baseline(threads, budget_s=12.0, mode="cylinder"):
+def cpu_baseline(threads, budget_s=12.0, mode="cylinder", scale=1.0, built=None):
+    """The FP64 oracle on the host cores (OpenMP, `threads`), on the same workload as the GPU
+    line, for about budget_s seconds of steps (at least one)."""
     import oracle as O
     from kitgpu import abi, cases, mesh
-    prob = make_problem(scale=0.25, mode=mode)
-    topo, state = cases.build(prob)
+    if built is None:
+        prob = make_problem(scale=scale, mode=mode)
+        topo, state = cases.build(prob)
+    else:
+        prob, topo, state = built
     P = mesh.phase_cells(topo)
     st = O.OracleState(topo, state)
     prm = abi.make_params(prob, st_check_interval=100)
-    st.run(prm, prob.dt(), 0, 1, nthreads=threads)  # warm-up
     n, t0 = 0, time.perf_counter()
     while True:
-        st.run(prm, prob.dt(), 1 + n, 1, nthreads=threads)
+        st.run(prm, prob.dt(), n, 1, nthreads=threads)
         n += 1
         el = time.perf_counter() - t0
         if el > budget_s or n >= 40:
             break
     return {"value": P * n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{mode} at scale 0.25 (same velocity grids), {P} phase cells, {n} steps, FP64"}
+            "sample": f"{mode} workload as measured ({P} phase cells), {n} steps from the initial state, FP64"}
+
+
+def sub_single(args, mode, threads, acc_steps, oracle_steps, oracle_f=True):
+    """A compact record of one single-problem workload: rate of both forms, per-kernel times,
+    roofline of the flux kernel and the accuracy statement."""
+    import copy
+    a = copy.copy(args)
+    a.steps, a.warmup = min(args.steps, 10), 3     # a compact record: 10 timed steps per form
+    P, res, launches, prob, topo, state = run_single(a, mode, SINGLE[mode][1], 0, 1, None, e2e=False)
+    peak, peak_kind = measured_peaks()
+    kern = res["mixed"].get("kernels", {})
+    rec = {"workload": SINGLE[mode][0], "phase_cells": P, "cells": int(topo["n_cells"]),
+           "value": res["mixed"]["value"], "unit": UNIT, "steps": a.steps,
+           "ms_per_step": res["mixed"]["ms_per_step"],
+           "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]},
+           "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+           "roofline": roofline_of(kern, P, res["ndf"], peak, peak_kind), "gpu_launches": launches}
+    rec["accuracy"] = accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_f=oracle_f)
+    if oracle_steps == 0:
+        rec["accuracy"]["oracle"] = "not run at this size in the default line (the FP64 oracle takes ~40 s per step here)"
+    return rec
 
 
 def main():
@@ -532,19 +656,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-sub", action="store_true", help="headline only: no per-workload sub-records")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the accuracy passes")
     ap.add_argument("--scale", type=float, default=None,
                     help="scale of the base mesh (default: the workload's own; smaller for profiling captures)")
     ap.add_argument("--mode", default="cylinder", choices=["cylinder", "sphere", "sod", "batched", "serve", "adapt", "vsadapt"])
     ap.add_argument("--problems", type=int, default=256, help="batched: number of problems")
     ap.add_argument("--rate", type=float, default=50.0, help="serve: Poisson arrival rate (req/s)")
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
+    ap.add_argument("--max-steps", type=int, default=20000, help="serve: step cap of a request")
     ap.add_argument("--forms", default="mixed,fp64", help="serve: precision forms to run (mixed, fp64)")
     ap.add_argument("--march", default="caidvm", choices=["caidvm", "cip"],
                     help="single-problem modes: time marching (cip: CIP_Marching, meshes without walls)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
-    if args.scale is None:
-        args.scale = SINGLE[args.mode][1] if args.mode in SINGLE else 1.0
+    if args.scale is None and args.mode in SINGLE:
+        args.scale = SINGLE[args.mode][1]
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
@@ -555,12 +682,13 @@ def main():
     threads = os.cpu_count() or 1
 
     if args.impl == "reference":
-        # The reference is Julia and cannot run on this machine; its CPU path is the oracle port.
+        # The reference is Julia and cannot run on this machine; its CPU path is the oracle port,
+        # timed on the headline workload itself (every step a full step of all 61 M phase cells).
         if rank != 0:
             return
         import oracle as O
         from kitgpu import abi, cases, mesh
-        prob = make_problem(scale=0.25)
+        prob = make_problem(scale=1.0)
         topo, state = cases.build(prob)
         P = mesh.phase_cells(topo)
         st = O.OracleState(topo, state)
@@ -574,10 +702,13 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic", "config": {"workload": WORKLOAD + " (bounded CPU sample: scale 0.25)",
-                                                "parallelism": "host threads"},
+                "data": "synthetic (seeded cylinder_buffer_IC state on a generated forest)",
+                "config": {"workload": WORKLOAD, "phase_cells": P, "form": "fp64 (CPU oracle)",
+                           "parallelism": f"host threads ({threads})"},
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                 "sample": f"cylinder at scale 0.25, {P} phase cells per step, FP64 oracle"},
+                                 "sample": f"the full workload ({P} phase cells per step), {args.steps} timed steps "
+                                           f"after {args.warmup}, FP64 oracle; the reference's Julia path is "
+                                           "unavailable on this box"},
                 "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -597,7 +728,8 @@ def main():
         if rank == 0:
             print(json.dumps(line))
         return
-    P, res, launches = run_ours(args, rank, world, dist)
+    P, res, launches, prob, topo, state = run_single(args, args.mode, args.scale, rank, world, dist, e2e=True,
+                                                     march=args.march)
     if rank != 0:
         return
     wname, wscale, wdata = SINGLE[args.mode]
@@ -605,16 +737,8 @@ def main():
     peak, peak_kind = measured_peaks()
     mixed = res["mixed"]
     kern = mixed.get("kernels", {})
-    roof = None
-    if "flux_collide_kernel" in kern:
-        ms, cnt = kern["flux_collide_kernel"]
-        avg_s = ms / cnt / 1e3
-        b_alg = 2 * ndf * 4 * P        # 2 * NDF * sizeof(float) per phase cell (one read, one write of f)
-        ach = b_alg / avg_s / 1e9
-        traffic = ncu_traffic_per_launch() if (args.mode == "cylinder" and args.scale == 1.0) else None
-        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "traffic": traffic, "kernel": "flux_collide_kernel",
-                "peak_kind": peak_kind, "algorithmic_bytes_per_launch": b_alg}
+    traffic = ncu_traffic_per_launch() if (args.mode == "cylinder" and args.scale == 1.0) else None
+    roof = roofline_of(kern, P, ndf, peak, peak_kind, traffic)
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
@@ -634,8 +758,32 @@ def main():
         "gpu_launches": launches,
         "clocks": mixed.get("clocks"),
     }
+    if not args.no_accuracy and world == 1:
+        big = P * ndf > 4e9        # the oracle of a multi-GB-f workload is too slow for this line
+        acc_steps = 10 if big else 100
+        oracle_steps = 0 if big else (100 if P < 2e6 else 2)
+        line["accuracy"] = accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, march=args.march)
     if not args.no_cpu and world == 1:
-        line["cpu_baseline"] = cpu_baseline(os.cpu_count() or 1, mode=args.mode)
+        line["cpu_baseline"] = cpu_baseline(threads, mode=args.mode, built=(prob, topo, state))
+    del topo, state
+    if args.mode == "cylinder" and args.scale == 1.0 and not args.no_sub and world == 1:
+        # one compact record per other workload of the benchmark, so that every one of them
+        # is measured in the default run
+        sub = {}
+        t0 = time.perf_counter()
+        sub["sod"] = sub_single(args, "sod", threads, acc_steps=100, oracle_steps=100)
+        sub["sphere"] = sub_single(args, "sphere", threads, acc_steps=10, oracle_steps=0)
+        b = run_batched(args)
+        sub["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "config", "mixed_over_fp64",
+                                             "accuracy", "gpu_launches")}
+        sub["batched"]["fp64"] = {k: b["forms"]["fp64"][k] for k in ("value", "ms_per_step")}
+        bk = b["forms"]["mixed"].get("kernels", {})
+        sub["batched"]["roofline"] = roofline_of(bk, b["config"]["phase_cells"], 2, peak, peak_kind)
+        sub["batched"]["autotune"] = b["forms"]["mixed"].get("autotune")
+        sv = run_serve(args, requests=12, rate=20.0)
+        sub["serve"] = {"config": sv["config"], "forms": sv["forms"]}
+        sub["wall_s"] = time.perf_counter() - t0
+        line["sub"] = sub
     print(json.dumps(line))
 
 

@@ -85,7 +85,7 @@ typedef struct kg_params {
     double  mu_ref;              /* gas.μᵣ (as the caller computed it)               */
 } kg_params;
 
-/* ---- flattened topology (reference-shaped) ----------- *
+/* ---- flattened topology (reference-shaped arrays) ------------------------ *
  * Arrays are read during kg_upload_topology only and never retained.
  *
  * Velocity grids.  Grid g owns velocity cells [grid_off[g], grid_off[g+1]) in the
@@ -406,7 +406,8 @@ int kg_batch_set_dt(kg_handle *h, int32_t slot, double dt);
  * scratch is a fixed file-scope device array (80 KiB, held by every GPU that loads the
  * library until exit); n_cells above 4,194,304 is rejected with KG_ERR_ARG.  The first
  * call on a device resolves that array's device address (make it before any stream
- * capture).  Calls share the array, so calls that overlap on the GPU race; each call
+ * capture) and keeps it for the life of the process: do not cudaDeviceReset a device
+ * this is used on.  Calls share the array, so calls that overlap on the GPU race; each call
  * writes every scratch row it reads, so no state carries over between calls.
  * Errors: kg_last_error(NULL, ...).                                           */
 int kg_residual_sums_noalloc(const double *prim_new, const double *prim_old, int64_t n_cells,

@@ -32,6 +32,9 @@ constexpr int ROW = 2 * kg::MAXW;
 static __device__ __align__(256) double kg_noalloc_partials[KG_NOALLOC_MAX_BLOCKS * ROW];
 
 // Device address of kg_noalloc_partials per device, resolved once with that device current.
+// The cached address belongs to the device's primary context, which this entry point
+// assumes lives as long as the process: after a cudaDeviceReset the cached address would
+// point into a destroyed context, so a caller must not reset a device it uses this on.
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mu;
 double* g_addr[MAX_DEVICES] = {};
@@ -45,10 +48,14 @@ __global__ void __launch_bounds__(kg::BLOCK) partial_kernel(const double* __rest
     const int64_t c0 = (int64_t)blockIdx.x * KG_NOALLOC_CELLS_PER_BLOCK;
     const int64_t c1 = c0 + KG_NOALLOC_CELLS_PER_BLOCK < n ? c0 + KG_NOALLOC_CELLS_PER_BLOCK : n;
     for (int64_t c = c0 + threadIdx.x; c < c1; c += kg::BLOCK) {
-        for (int q = 0; q < nw; ++q) {
-            const double a = pn[c * nw + q], d = a - po[c * nw + q];
-            v[q] += d * d;
-            v[kg::MAXW + q] += fabs(a);
+        // unrolled over MAXW with a guard, so that v stays in registers
+#pragma unroll
+        for (int q = 0; q < kg::MAXW; ++q) {
+            if (q < nw) {
+                const double a = pn[c * nw + q], d = a - po[c * nw + q];
+                v[q] += d * d;
+                v[kg::MAXW + q] += fabs(a);
+            }
         }
     }
     kg::block_sum<ROW>(v, sred);
@@ -68,7 +75,9 @@ __global__ void __launch_bounds__(kg::BLOCK) final_kernel(const double* __restri
         for (int q = 0; q < ROW; ++q) v[q] += partials[(int64_t)b * ROW + q];
     kg::block_sum<ROW>(v, sred);
     if (threadIdx.x == 0)
-        for (int q = 0; q < nw; ++q) { out[q] = v[q]; out[nw + q] = v[kg::MAXW + q]; }
+#pragma unroll
+        for (int q = 0; q < kg::MAXW; ++q)
+            if (q < nw) { out[q] = v[q]; out[nw + q] = v[kg::MAXW + q]; }
 }
 
 }  // namespace
@@ -90,9 +99,14 @@ extern "C" int kg_residual_sums_noalloc(const double* prim_new, const double* pr
     }
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) {
+    if (e != cudaSuccess) {
         kg::set_global_error(std::string("kg_residual_sums_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
         return KG_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= MAX_DEVICES) {
+        kg::set_global_error("kg_residual_sums_noalloc: device index " + std::to_string(dev) +
+                             " is outside the " + std::to_string(MAX_DEVICES) + " devices this entry point serves");
+        return KG_ERR_ARG;
     }
     double* part = nullptr;
     {

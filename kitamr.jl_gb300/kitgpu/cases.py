@@ -70,7 +70,9 @@ class Problem:
         return self.cfl * min(ds[d] / U[d] for d in range(c.dim))
 
 
-def sod(scale: float = 1.0, max_level: int = 2, nv: int = 28) -> Problem:
+def sod(scale: float = 1.0, max_level: int = 2, nv: int = 28, x_bc: int = M.BC_OUTFLOW) -> Problem:
+    """x_bc: the boundary kind of both x ends (UniformOutflow as in rp_1D.jl:45, or
+    InterpolatedOutflow, CAIDVM.jl:71-94)."""
     tx = max(4, int(round(128 * scale)))
     ty = 4
 
@@ -84,7 +86,7 @@ def sod(scale: float = 1.0, max_level: int = 2, nv: int = 28) -> Problem:
     case = M.Case(
         dim=2, geometry=[0.0, 1.0, 0.0, 0.1], trees_num=[tx, ty], max_level=max_level,
         quadrature=[-5.0, 5.0, -5.0, 5.0], vs_trees_num=[nv, nv],
-        domain_bc=[(M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_PERIOD, None), (M.BC_PERIOD, None)],
+        domain_bc=[(x_bc, None), (x_bc, None), (M.BC_PERIOD, None), (M.BC_PERIOD, None)],
         ic=ic, refine=refine if max_level > 0 else None, gamma=5.0 / 3.0, K=1.0)
     return Problem("sod", case, Gas(Kn=1e-2, K=1.0, omega=0.81, omega_r=0.81), cfl=CFL)
 
@@ -201,9 +203,12 @@ def box3d(n=(6, 4, 4), nv: int = 8, levels: int = 1, Kn: float = 0.05) -> Proble
     return Problem("box3d", case, Gas(Kn=Kn, K=0.0, omega=0.81, omega_r=0.81), cfl=CFL)
 
 
-def sphere(scale: float = 1.0, max_level: int = 2, nv: int = 24, Ma: float = 3.0, Kn: float = 0.05) -> Problem:
+def sphere(scale: float = 1.0, max_level: int = 2, nv: int = 24, Ma: float = 3.0, Kn: float = 0.05,
+           reach: Tuple[float, float] = (1.8, 1.0)) -> Problem:
     """3D Ma 3 / Kn 0.05 flow past a diffuse isothermal sphere of radius 1 on [-6,6]^3,
-    32^3 trees (scaled), 2 levels near the wall, uniform 24^3 velocity grid on [-10,10]^3."""
+    32^3 trees (scaled), 2 levels near the wall, uniform 24^3 velocity grid on [-10,10]^3.
+    ``reach``: distance from the wall within which level 0 / level 1 cells are refined
+    (``sphere_config`` widens it to the ~2e5 cells of the benchmark configuration)."""
     n = max(6, int(round(32 * scale)))
     Uinf = Ma * math.sqrt(5.0 / 6.0)
     R = 1.0
@@ -216,8 +221,8 @@ def sphere(scale: float = 1.0, max_level: int = 2, nv: int = 24, Ma: float = 3.0
 
     def refine(mid, ds, lev):
         r = math.sqrt(mid[0] ** 2 + mid[1] ** 2 + mid[2] ** 2)
-        reach = [1.8, 1.0][min(lev, 1)]
-        return abs(r - R) < reach + 0.5 * math.sqrt(ds[0] ** 2 + ds[1] ** 2 + ds[2] ** 2)
+        rr = reach[min(lev, 1)]
+        return abs(r - R) < rr + 0.5 * math.sqrt(ds[0] ** 2 + ds[1] ** 2 + ds[2] ** 2)
 
     case = M.Case(
         dim=3, geometry=[-6.0, 6.0, -6.0, 6.0, -6.0, 6.0], trees_num=[n, n, n], max_level=max_level,
@@ -226,3 +231,9 @@ def sphere(scale: float = 1.0, max_level: int = 2, nv: int = 24, Ma: float = 3.0
                    (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None), (M.BC_OUTFLOW, None)],
         ic=ic, refine=refine, circle=([0.0, 0.0, 0.0], R, [1.0, 0.0, 0.0, 0.0, 1.0]), K=0.0)
     return Problem("sphere", case, Gas(Kn=Kn, K=0.0, omega=0.81, omega_r=0.81), cfl=CFL)
+
+
+def sphere_config() -> Problem:
+    """The 3D sphere at its benchmark size: 32^3 trees, 2 levels within 3.5 / 1.8 of the wall
+    (about 2.1e5 cells), 24^3 velocity grid: about 2.9e9 phase cells, f 11.7 GB in FP32."""
+    return sphere(scale=1.0, reach=(3.5, 1.8))

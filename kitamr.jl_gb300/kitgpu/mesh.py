@@ -299,25 +299,95 @@ def _box_below_plane(n, lo, hi) -> float:
     return vol * min(max(frac, 0.0), 1.0)
 
 
+def _boxes_below_plane(n, lo, hi) -> np.ndarray:
+    """_box_below_plane over many boxes at once (rows of lo / hi), the same arithmetic in the
+    same order per box."""
+    nb, dim = lo.shape
+    s = hi - lo
+    a = n[None, :] * s
+    b = -(n[None, :] * lo)
+    bsum = np.zeros(nb)
+    for d in range(dim):
+        bsum = bsum + b[:, d]
+        neg = a[:, d] < 0
+        bsum = np.where(neg, bsum - a[:, d], bsum)
+    a = np.abs(a)
+    vol = np.ones(nb)
+    for d in range(dim):
+        vol = vol * s[:, d]
+    out = np.empty(nb)
+    amax = np.max(a, axis=1)
+    act = a > 1e-12 * np.maximum(amax, 1e-300)[:, None]
+    full = np.all(act, axis=1)
+    if np.any(full):
+        # boxes with every coefficient active: the same sum over corners, term by term in
+        # the scalar form's order, for all of them at once
+        af, bf = a[full], bsum[full]
+        tot = np.zeros(af.shape[0])
+        for mask in range(1 << dim):
+            sa = np.zeros(af.shape[0])
+            bits = 0
+            for i in range(dim):
+                if (mask >> i) & 1:
+                    sa = sa + af[:, i]
+                    bits += 1
+            r = bf - sa
+            term = (-1) ** bits * np.power(r, float(dim))
+            tot = np.where(r > 0, tot + term, tot)
+        pr = np.ones(af.shape[0])
+        for i in range(dim):
+            pr = pr * af[:, i]
+        frac = tot / (math.factorial(dim) * pr)
+        out[full] = vol[full] * np.minimum(np.maximum(frac, 0.0), 1.0)
+    for row in np.nonzero(~full)[0]:
+        # the inclusion-exclusion sum is short (at most 2^dim terms): per box, as in the scalar form
+        av = [float(x) for x, m in zip(a[row], act[row]) if m]
+        k = len(av)
+        bb = float(bsum[row])
+        if k == 0:
+            out[row] = vol[row] if bb >= 0 else 0.0
+            continue
+        tot = 0.0
+        for mask in range(1 << k):
+            sa, bits = 0.0, 0
+            for i in range(k):
+                if (mask >> i) & 1:
+                    sa += av[i]
+                    bits += 1
+            r = bb - sa
+            if r > 0:
+                tot += (-1) ** bits * r ** k
+        pr = 1.0
+        for x in av:
+            pr *= x
+        frac = tot / (math.factorial(k) * pr)
+        out[row] = vol[row] * min(max(frac, 0.0), 1.0)
+    return out
+
+
 def cut_cells_3d(normal, g: VGrid, root_ds):
     """3D counterpart of the cut-cell split (Immersed_boundary.jl:250-277): for each velocity
     cell crossed by u.n = 0, its gas (u.n < 0) and solid (u.n > 0) volumes.  The split is
-    host geometry; the volumes come from an exact box / half-space formula."""
+    host geometry; the volumes come from an exact box / half-space formula.  The screening
+    test runs over the whole grid at once; only the crossed cells get the volume formula."""
     if sum(1 for x in normal if abs(x) < 1e-6) > 1:
         return [], [], []
-    index, gas_w, solid_w = [], [], []
-    for i in range(g.nv):
-        ddu = [root_ds[d] / 2 ** int(g.level[i]) for d in range(3)]
-        mid = g.midpoint[i]
-        if abs(sum(mid[d] * normal[d] for d in range(3))) > 0.5 * math.sqrt(sum(x * x for x in ddu)):
-            continue
-        lo = [mid[d] - 0.5 * ddu[d] for d in range(3)]
-        hi = [mid[d] + 0.5 * ddu[d] for d in range(3)]
-        tot = ddu[0] * ddu[1] * ddu[2]
-        gas = _box_below_plane(normal, lo, hi)
-        if 1e-12 * tot < gas < tot * (1 - 1e-12):
-            index.append(i); gas_w.append(gas); solid_w.append(tot - gas)
-    return index, gas_w, solid_w
+    n = np.asarray(normal, dtype=np.float64)
+    lev = np.asarray(g.level, dtype=np.int64)
+    ddu = np.stack([root_ds[d] / 2.0 ** lev for d in range(3)], axis=1)
+    mid = np.asarray(g.midpoint, dtype=np.float64).reshape(-1, 3)
+    proj = mid[:, 0] * n[0] + mid[:, 1] * n[1] + mid[:, 2] * n[2]
+    half_diag = 0.5 * np.sqrt(ddu[:, 0] * ddu[:, 0] + ddu[:, 1] * ddu[:, 1] + ddu[:, 2] * ddu[:, 2])
+    cand = np.nonzero(~(np.abs(proj) > half_diag))[0]
+    if cand.size == 0:
+        return [], [], []
+    lo = mid[cand] - 0.5 * ddu[cand]
+    hi = mid[cand] + 0.5 * ddu[cand]
+    tot = ddu[cand, 0] * ddu[cand, 1] * ddu[cand, 2]
+    gas = _boxes_below_plane(n, lo, hi)
+    keep = (1e-12 * tot < gas) & (gas < tot * (1 - 1e-12))
+    idx = cand[keep]
+    return [int(i) for i in idx], [float(x) for x in gas[keep]], [float(x) for x in (tot - gas)[keep]]
 
 
 def calc_intersect_sphere(f_mid, s_mid, center, radius, solid=True):
@@ -405,11 +475,29 @@ def build_forest(case: Case):
     def h_exact(L, d):
         return (geom[2 * d + 1] - geom[2 * d]) / tn[d] / (1 << L)
 
+    # centre coordinates are exact rationals rounded once; memoised per (level, index) along
+    # each axis, since a coordinate repeats across the leaves of a row
+    _coord: Dict[Tuple[int, int, int], float] = {}
+
+    def coord(L, d, i):
+        key = (L, d, i)
+        v = _coord.get(key)
+        if v is None:
+            v = float(geom[2 * d] + h_exact(L, d) * (i + Fraction(1, 2)))
+            _coord[key] = v
+        return v
+
     def center(L, idx):
-        return np.array([float(geom[2 * d] + h_exact(L, d) * (idx[d] + Fraction(1, 2))) for d in range(dim)])
+        return np.array([coord(L, d, idx[d]) for d in range(dim)])
+
+    _ds: Dict[int, np.ndarray] = {}
 
     def dsv(L):
-        return np.array([float(h_exact(L, d)) for d in range(dim)])
+        v = _ds.get(L)
+        if v is None:
+            v = np.array([float(h_exact(L, d)) for d in range(dim)])
+            _ds[L] = v
+        return v.copy()
 
     leaves = set()
     for idx in np.ndindex(*tn):
@@ -764,11 +852,18 @@ def build_topology(case: Case, dtype_check: bool = True) -> Dict[str, np.ndarray
         cell_quad=np.array(cells, np.int32), n_quads=nleaf,
     )
     # initial state (initialize_ps!, Solver/Initialize.jl:343-380): w from prim, f = Maxwellian
+    # (cells of one grid and one initial state share their block: a freestream is one block)
     K = case.K
+    fcache: Dict = {}
     fblocks = []
     for c in range(ncell):
-        g = grids[cell_grid[c]]
-        fblocks.append(discrete_maxwell(g.midpoint, prims[c], K).reshape(-1, order="F"))
+        key = (int(cell_grid[c]), prims[c].tobytes())
+        blk = fcache.get(key)
+        if blk is None:
+            g = grids[cell_grid[c]]
+            blk = discrete_maxwell(g.midpoint, prims[c], K).reshape(-1, order="F")
+            fcache[key] = blk
+        fblocks.append(blk)
     state = dict(f=np.concatenate(fblocks), w=get_conserved(prims, case.gamma).reshape(-1),
                  prim=prims.reshape(-1).copy())
     return topo, state

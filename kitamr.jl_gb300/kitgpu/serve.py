@@ -73,17 +73,25 @@ def random_request(rng: np.random.Generator, rid: int, arrival: float, small: bo
 
 @dataclass
 class ServeStats:
-    latencies: List[float]
-    solves: int
+    latencies: List[float]          # every finished request, arrival to retirement
+    solves: int                     # requests that converged
     wall: float
     steps_total: int
     phase_updates: int
     refused: int
+    converged_latencies: List[float] = field(default_factory=list)
+    steps_to_converge: List[int] = field(default_factory=list)
 
     def summary(self) -> Dict:
-        lat = np.array(self.latencies) if self.latencies else np.array([np.nan])
-        return {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+        def pct(v, q):
+            return float(np.percentile(np.array(v), q) * 1e3) if v else None
+        return {"p50_ms": pct(self.latencies, 50), "p99_ms": pct(self.latencies, 99),
+                # time to converged steady state, over the requests that converged
+                "p50_converged_ms": pct(self.converged_latencies, 50),
+                "p99_converged_ms": pct(self.converged_latencies, 99),
+                "requests": len(self.latencies), "unconverged": len(self.latencies) - self.solves,
                 "solves": self.solves, "solves_per_s": self.solves / self.wall if self.wall > 0 else 0.0,
+                "steps_to_converge_max": max(self.steps_to_converge) if self.steps_to_converge else None,
                 "wall_s": self.wall, "phase_cell_updates_per_s": self.phase_updates / self.wall if self.wall else 0.0,
                 "admissions_refused": self.refused}
 
@@ -164,7 +172,9 @@ class Server:
                     done.append(r)
         wall = clock() - t0
         lat = [r.finished - r.arrival for r in done]
-        return ServeStats(lat, sum(1 for r in done if r.converged), wall, steps_total, updates, refused)
+        conv = [r for r in done if r.converged]
+        return ServeStats(lat, len(conv), wall, steps_total, updates, refused,
+                          [r.finished - r.arrival for r in conv], [r.steps for r in conv])
 
 
 def poisson_arrivals(rng: np.random.Generator, rate: float, n: int) -> List[float]:

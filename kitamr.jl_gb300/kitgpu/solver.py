@@ -174,15 +174,18 @@ class GpuStep:
         assert fl.size == self.nc
         _check(self.L, self.h, self.L.kg_vs_conserve(self.h, fl.ctypes.data))
 
-    def download_state(self, sdf: bool = False) -> Dict[str, np.ndarray]:
+    def download_state(self, sdf: bool = False, f: bool = True) -> Dict[str, np.ndarray]:
+        """f (unless f=False), w, prim, qf and optionally sdf of every cell."""
         nf = int(self.foff[-1])
-        out = dict(f=np.empty(nf), w=np.empty(self.nc * (self.dim + 2)), prim=np.empty(self.nc * (self.dim + 2)),
+        out = dict(w=np.empty(self.nc * (self.dim + 2)), prim=np.empty(self.nc * (self.dim + 2)),
                    qf=np.empty(self.nc * self.dim))
+        if f:
+            out["f"] = np.empty(nf)
         if sdf:
             out["sdf"] = np.empty(nf * self.dim)
         _check(self.L, self.h, self.L.kg_download_state(
-            self.h, out["f"].ctypes.data, out["w"].ctypes.data, out["prim"].ctypes.data, out["qf"].ctypes.data,
-            out["sdf"].ctypes.data if sdf else None))
+            self.h, out["f"].ctypes.data if f else None, out["w"].ctypes.data, out["prim"].ctypes.data,
+            out["qf"].ctypes.data, out["sdf"].ctypes.data if sdf else None))
         return out
 
     def download_sw(self) -> np.ndarray:

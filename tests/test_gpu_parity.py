@@ -72,6 +72,43 @@ def test_mixed_within_1e5_of_fp64(name, make, nsteps):
     assert not bad, f"{name}: {bad}"
 
 
+# The workloads the benchmark is quoted on, at their own sizes (or half the base mesh):
+#  * the Sod tube as configured: 128x4 trees, 2 levels at the jump, 28^2 velocity grid, outflow
+#    in x, periodic in y, over its full 100 steps;
+#  * the cylinder with its 48^2 velocity roots adapted by 2 levels, at half the base mesh
+#    (15.9 M phase cells);
+#  * the Sod tube with InterpolatedOutflow ends (CAIDVM.jl:71-94), the linear extrapolation
+#    past the domain face.
+from kitgpu import mesh as _mesh  # noqa: E402
+
+CONFIG_CASES = [
+    ("sod_128x4_L2_v28_100_steps", lambda: cases.sod(), 100),
+    ("cylinder_v48_vsL2_half_mesh", lambda: cases.cylinder(scale=0.5, nv=48, vs_levels=2), 2),
+    ("sod_interpolated_outflow", lambda: cases.sod(scale=0.25, nv=16, x_bc=_mesh.BC_INTERP), 20),
+]
+
+
+@pytest.mark.parametrize("name,make,nsteps", CONFIG_CASES, ids=[c[0] for c in CONFIG_CASES])
+def test_config_fp64_matches_oracle(name, make, nsteps):
+    """FP64 within 1e-12 of the oracle on every moment component and on f."""
+    topo, ref, out, rep = run_pair(make(), nsteps, check=10)
+    errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
+    errs["f"] = f_error(topo, ref.f, out["f"])
+    bad = {k: v for k, v in errs.items() if not v <= TOL_FP64}
+    assert not bad, f"{name}: {bad}"
+
+
+@pytest.mark.parametrize("name,make,nsteps", CONFIG_CASES, ids=[c[0] for c in CONFIG_CASES])
+def test_config_mixed_within_1e5_of_oracle(name, make, nsteps):
+    """Mixed form within 1e-5 of the FP64 oracle on ρ, U, T and q (the Sod tube over all of
+    its 100 steps)."""
+    topo, ref, out, rep = run_pair(make(), nsteps, precision=abi.KG_PREC_MIXED, check=10)
+    errs = moment_errors(topo, ref.w, ref.prim, ref.qf, out["w"], out["prim"], out["qf"])
+    keep = {k: v for k, v in errs.items() if k in ("rho", "T") or k.startswith("U") or k.startswith("q")}
+    bad = {k: v for k, v in keep.items() if not v <= TOL_MIXED}
+    assert not bad, f"{name}: {bad}"
+
+
 SW_CASES = [CASES_FP64[1], CASES_FP64[3], CASES_FP64[4]]
 
 

@@ -53,6 +53,38 @@ def test_noalloc_residual_matches_step_report():
     g.close()
 
 
+def _sums_numpy(pn, po):
+    d = pn - po
+    return np.concatenate([np.sum(d * d, axis=0), np.sum(np.abs(pn), axis=0)])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_noalloc_many_blocks_against_numpy(dim):
+    """Sizes that span many scratch rows (3 * 4096 + 17 cells, and about a million), then a
+    small call after the large one: the small call reads only the rows it wrote, so the
+    large call's leftover rows change nothing.  n_cells = 0 gives zeros."""
+    import torch
+    fn = _noalloc(load_library())
+    nw = dim + 2
+    rng = np.random.default_rng(20261203 + dim)
+    for n in (3 * 4096 + 17, 1_000_003, 300, 0):
+        pn = rng.normal(1.0, 0.5, size=(n, nw))
+        po = pn + rng.normal(0.0, 1e-3, size=(n, nw))
+        # (an empty input still passes valid pointers: a one-row buffer nothing reads)
+        dn = torch.tensor(pn if n else np.ones((1, nw)), dtype=torch.float64, device="cuda").contiguous()
+        do = torch.tensor(po if n else np.ones((1, nw)), dtype=torch.float64, device="cuda").contiguous()
+        out = torch.full((2 * nw,), np.nan, dtype=torch.float64, device="cuda")
+        rc = fn(dn.data_ptr(), do.data_ptr(), n, dim, out.data_ptr(), None)
+        assert rc == 0
+        torch.cuda.synchronize()
+        got = out.cpu().numpy()
+        exp = _sums_numpy(pn, po)
+        if n == 0:
+            assert np.all(got == 0.0)
+        else:
+            assert np.allclose(got, exp, rtol=1e-12, atol=0.0), (n, got, exp)
+
+
 def test_noalloc_rejects_oversized_input():
     fn = _noalloc(load_library())
     # refused before any device work: the size check comes first
