@@ -18,6 +18,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
+    static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t cip(const Dev&, int, cudaStream_t);
     static cudaError_t conserve(const Dev&, const int32_t*, int, cudaStream_t);
@@ -161,6 +162,10 @@ struct kg_handle {
     const int32_t* d_indep = nullptr;  // fluid-list entries without a solid / wall incidence
     const int32_t* d_dep = nullptr;    // the others
     int n_indep = 0, n_dep = 0;
+    const int32_t* d_reg = nullptr;    // independent entries of regular cells (regular-cell kernel)
+    const int32_t* d_irr = nullptr;    // independent entries of the other cells
+    const int32_t* d_nonreg = nullptr; // every entry that is not in d_reg
+    int n_reg = 0, n_irr = 0, n_nonreg = 0;
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -410,10 +415,16 @@ int rebuild(kg_handle* h) {
 #define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
         UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
         UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
+        if (!M.vpk.empty()) {
+            const float* vp = nullptr;
+            int r__ = upload_vec(h, M.vpk, &vp);
+            if (r__) return r__;
+            P.vpk = reinterpret_cast<const float4*>(vp);
+        }
         UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
         UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
         UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(slope_items, slope_items); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(regrec, regrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
         UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
         UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
@@ -456,8 +467,10 @@ int rebuild(kg_handle* h) {
     }
 
     {
-        std::vector<int32_t> order(M.fluid_cells.size());
-        for (size_t q = 0; q < order.size(); ++q) order[q] = (int32_t)q;
+        // the cells that are not regular, largest velocity grids first (persistent schedule)
+        std::vector<int32_t> order;
+        for (int q = 0; q < M.n_fluid; ++q)
+            if (!M.fluid_reg[q]) order.push_back(q);
         std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
             return M.dnv[M.fluid_cells[a]] > M.dnv[M.fluid_cells[b]];
         });
@@ -466,16 +479,25 @@ int rebuild(kg_handle* h) {
     }
     {
         // fluid cells whose flux reads no solid cell or wall record (the IB kernels' output)
-        std::vector<int32_t> indep, dep;
+        // and, of those, the regular cells (the regular-cell flux kernel) and the others
+        std::vector<int32_t> indep, dep, reg, irr, nonreg;
         for (int q = 0; q < M.n_fluid; ++q) {
             bool d = false;
             for (int e = M.inc_off[q]; e < M.inc_off[q + 1] && !d; ++e) d = M.inc[e].kind == INC_SOLID;
             (d ? dep : indep).push_back(q);
+            if (!d) (M.fluid_reg[q] ? reg : irr).push_back(q);
+            if (d || !M.fluid_reg[q]) nonreg.push_back(q);
         }
         h->n_indep = (int)indep.size();
         h->n_dep = (int)dep.size();
+        h->n_reg = (int)reg.size();
+        h->n_irr = (int)irr.size();
+        h->n_nonreg = (int)nonreg.size();
         int r = upload_vec(h, indep, &h->d_indep);
         if (!r) r = upload_vec(h, dep, &h->d_dep);
+        if (!r) r = upload_vec(h, reg, &h->d_reg);
+        if (!r) r = upload_vec(h, irr, &h->d_irr);
+        if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
         if (r) return r;
     }
     const int32_t* dl;
@@ -510,14 +532,19 @@ int rebuild(kg_handle* h) {
     return KG_OK;
 }
 
+// The flux of every fluid cell: the regular cells on their own kernel (one CTA per cell), then
+// the others with one CTA per cell (schedule 0) or on persistent CTAs (1: natural order, 2:
+// largest velocity grids first).
 cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
     const Flat& F = h->M;
-    if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux(P, F.n_fluid, F.max_nv, s); });
+    cudaError_t e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+    if (e != cudaSuccess || h->n_nonreg == 0) return e;
+    if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, s); });
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
-    int grid = std::max(1, std::min(F.n_fluid, nsm * std::max(ctas, 1)));
-    const int32_t* order = sched == 2 ? h->d_order : nullptr;
-    return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, F.n_fluid, F.max_nv, grid, h->d_counter, order, s); });
+    int grid = std::max(1, std::min(h->n_nonreg, nsm * std::max(ctas, 1)));
+    const int32_t* order = sched == 2 ? h->d_order : h->d_nonreg;
+    return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, h->n_nonreg, F.max_nv, grid, h->d_counter, order, s); });
 }
 
 // Autotuner: times the flux schedules on the current layout and keeps the fastest.  Every
@@ -639,10 +666,12 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_dep, h->n_dep, F.max_nv, a); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaEventRecord(h->ev_join, a));
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_indep, h->n_indep, F.max_nv, s); });
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_irr, h->n_irr, F.max_nv, s); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
-        *launches += 2;
+        *launches += 1 + (h->n_reg > 0) + (h->n_irr > 0);
         e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
         ++*launches;
@@ -668,7 +697,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         e = launch_flux(h, P, h->sched, h->sched_ctas, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         end("flux_collide_kernel");
-        ++*launches;
+        *launches += (h->n_reg > 0) + (h->n_nonreg > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             begin();
             e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });

@@ -33,6 +33,7 @@ struct Dev {
     const float* ax_hi;                // ax_val as FP32 hi + lo
     const float* ax_lo;
     const uint16_t* vidx;
+    const float4* vpk;                 // 2D: ux, uy, weight, axis indices per velocity cell
     int max_axis;
     // data table
     const int64_t* foff;
@@ -56,6 +57,7 @@ struct Dev {
     const int32_t* fluid_cells;
     const uint8_t* fluid_reg;          // per fluid cell: regular (fast path of the flux kernel)
     const FluxCell* fcrec;             // per fluid cell: its record
+    const RegRec* regrec;              // per fluid cell: the faces of a regular cell
     const SlopeCell* screc;            // per pass-cell entry: its record
     const CritOp* crit_ops;            // per fluid cell and direction (physical-space criterion)
     const int32_t* crit_nbr;

@@ -101,17 +101,17 @@ const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 // (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
 // cost more than filling ~20 MB of records.
 void reset(Flat& F) {
-    static_assert(sizeof(Flat) == 48 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    static_assert(sizeof(Flat) == 50 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
     F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
     F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
     F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
-    F.ax_off.clear(); F.ax_val.clear(); F.ax_hi.clear(); F.ax_lo.clear(); F.vidx.clear();
+    F.ax_off.clear(); F.ax_val.clear(); F.ax_hi.clear(); F.ax_lo.clear(); F.vidx.clear(); F.vpk.clear();
     F.foff.clear(); F.dgrid.clear(); F.dbe.clear(); F.dinvv.clear(); F.dnv.clear(); F.dprob.clear();
     F.dmid.clear(); F.dds.clear();
     F.p_off.clear(); F.p_j0.clear(); F.p_cnt.clear();
     F.pass_off.clear(); F.slope_ops.clear(); F.pass_cells_off.clear(); F.pass_cells.clear();
     F.cell_slope_op.clear(); F.slope_nbr.clear(); F.slope_items.clear(); F.pass_items_off.clear();
-    F.fluid_cells.clear(); F.fcrec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
+    F.fluid_cells.clear(); F.fcrec.clear(); F.regrec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
     F.fluid_reg.clear();
     F.inc_off.clear(); F.inc.clear(); F.bc_prim.clear(); F.bc_hl.clear();
     F.solid_ops.clear(); F.wall_ops.clear(); F.ib_nbr.clear(); F.ib_dx.clear(); F.cut_idx.clear();
@@ -649,7 +649,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             nsn += p.F->slope_nbr.size(); np += p.F->p_j0.size(); npo += p.F->p_off.size();
             nco += p.F->crit_ops.size(); ncn += p.F->crit_nbr.size();
         }
-        M.inc.reserve(ninc); M.fcrec.reserve(nfl); M.fluid_cells.reserve(nfl); M.fluid_reg.reserve(nfl);
+        M.inc.reserve(ninc); M.fcrec.reserve(nfl); M.regrec.reserve(nfl); M.fluid_cells.reserve(nfl); M.fluid_reg.reserve(nfl);
         M.inc_off.reserve(nfl + 1); M.slope_ops.reserve(nso); M.slope_nbr.reserve(nsn);
         M.p_j0.reserve(np); M.p_cnt.reserve(np); M.p_off.reserve(npo + 1);
         M.crit_ops.reserve(nco); M.crit_nbr.reserve(ncn);
@@ -754,6 +754,21 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             fc.ninc = F.inc_off[k + 1] - F.inc_off[k];
             fc.nv = M.dnv[m]; fc.gid = M.dgrid[m]; fc.reg = F.fluid_reg[k];
             M.fcrec.push_back(fc);
+            RegRec rr{};
+            if (fc.reg) {
+                for (int q = 0; q < fc.ninc; ++q) {
+                    const Incidence& a = M.inc[(size_t)fc.inc0 + q];
+                    const int d = a.dir;
+                    const double dm = a.fmid[d] - a.my_mid[d];
+                    const int side = 2 * d + (dm > 0.0 ? 1 : 0);
+                    rr.nfo[side] = a.ofoff;
+                    rr.dxm[side] = dm;
+                    rr.sa[side] = a.sarea;
+                    rr.dxm_f[side] = a.dxm_f[d];
+                    rr.sa_f[side] = a.sarea_f;
+                }
+            }
+            M.regrec.push_back(rr);
         }
         {
             const int32_t cacc = (int32_t)M.crit_nbr.size();
@@ -783,6 +798,18 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         (void)sops;
     }
     M.ax_off.push_back((int32_t)M.ax_val.size());
+    if (D == 2) {
+        M.vpk.assign((size_t)4 * PGtot, 0.0f);
+        for (int64_t i = 0; i < PGtot; ++i) {
+            const uint32_t bits = (uint32_t)M.vidx[(size_t)i] | ((uint32_t)M.vidx[(size_t)PGtot + i] << 16);
+            float b;
+            std::memcpy(&b, &bits, sizeof b);
+            M.vpk[4 * i + 0] = M.vuf[(size_t)i];
+            M.vpk[4 * i + 1] = M.vuf[(size_t)PGtot + i];
+            M.vpk[4 * i + 2] = M.vwf[(size_t)i];
+            M.vpk[4 * i + 3] = b;
+        }
+    }
     // slope passes merged by their index relative to each problem's coarsest level
     M.pass_off.push_back(0);
     M.pass_cells_off.push_back(0);

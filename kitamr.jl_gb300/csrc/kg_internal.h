@@ -95,6 +95,16 @@ struct FluxCell {
     int32_t nv, gid, reg, pad;
 };
 
+// The faces of a regular fluid cell (fluid_reg), by side s = 2 * dir + (face at +ds/2): the
+// neighbour across it (f offset; its sdf is at nfo * dim), the face midpoint minus the cell
+// centre along dir, and the signed area factor of the received flux, in FP64 and rounded to
+// FP32 (built when the problems are merged; zero for cells that are not regular).
+struct RegRec {
+    int64_t nfo[2 * MAXD];
+    double dxm[2 * MAXD], sa[2 * MAXD];
+    float dxm_f[2 * MAXD], sa_f[2 * MAXD];
+};
+
 // ---- immersed boundary ----------------------------------------------------
 struct SolidOp {            // update_solid_cell! for one solid cell
     int32_t cell, list, cnt, pad;
@@ -138,6 +148,9 @@ struct Flat {
     std::vector<double> ax_val;
     std::vector<float> ax_hi, ax_lo;   // ax_val = hi + lo in FP32 pairs (mixed form exponents)
     std::vector<uint16_t> vidx;   // [dim][P_g]
+    std::vector<float> vpk;       // merged 2D layouts: per velocity cell ux, uy, weight (FP32) and
+                                  // the bits of (axis index x) | (axis index y) << 16 -- one
+                                  // 16-byte load of what the regular-cell kernel needs of it
     int max_axis = 0;
     // data table
     std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)
@@ -161,6 +174,7 @@ struct Flat {
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
     std::vector<FluxCell> fcrec;          // merged layout only: per fluid cell
+    std::vector<RegRec> regrec;           // merged layout only: per fluid cell (regular ones filled)
     std::vector<SlopeCell> screc;         // merged layout only: per pass-cell entry
     std::vector<CritOp> crit_ops;         // per fluid cell and direction (fluid-list order)
     std::vector<int32_t> crit_nbr;        // their neighbour lists (data indices)

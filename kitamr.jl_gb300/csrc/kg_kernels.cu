@@ -788,6 +788,146 @@ __host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, i
     return ((fst_global ? (size_t)0 : (size_t)NDF * max_nv) + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
 }
 
+// Indices of the per-CTA constants of the flux kernels (shared array sc, arithmetic precision).
+enum CellConst {
+    C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
+    C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_UNH = C_QA + MAXD, C_UNL = C_UNH + MAXD,
+    C_LCH = C_UNL + MAXD, C_LCL, C_LNH, C_LNL, C_N
+};
+
+// The scalar section of a cell after its first block reduction: red holds the macro flux
+// (red[0 .. D+1]) and the moments of the convected f (red[D+2 ..]).  Two lanes recover the
+// conserved update w + dt/V flux with prim_c and the primitives of the convected f (FP64), the
+// status bits of prim_c are set, the collision constants go to sc, and the factor tables of the
+// two Maxwellians (the second only for CAIDVM marching) are built at Ec.  Ends with the block
+// synchronised; sscal holds prim_c (row 0) and the convected f's primitives (row 1).
+template <int D, int NDF, typename A, int NT>
+__device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot, const ProbParams& PP, double dt,
+                                               double invV, const double (&red)[2 * (D + 2)], double* sscal, A* sc,
+                                               A* Ec, int gid) {
+    const double Kgas = PP.K;
+    const int MA = P.max_axis;
+    {
+        // Two lanes recover the two sets of primitives in one FP64 instruction stream (on
+        // GB300 an FP64 warp instruction costs the same for one lane or 32): lane 0 the
+        // conserved update w + dt/V·flux and prim_c, lane 1 the primitives of the convected f
+        // (Euler: both lanes the same, so prim_n = prim_c)
+        if (threadIdx.x < 2) {
+            const int ln = threadIdx.x;
+            double* w = P.w + (int64_t)cell * MAXW;
+            const double dtV = dt * invV;
+            const bool lane_mom = P.marching != KG_MARCH_EULER ? ln == 1 : P.flux == KG_FLUX_DVM;
+            double wv[MAXW], pv[MAXW];
+#pragma unroll
+            for (int q = 0; q < D + 2; ++q) wv[q] = lane_mom ? red[D + 2 + q] : fma(red[q], dtV, w[q]);
+            get_prim_r<D>(wv, PP.gamma, pv);
+#pragma unroll
+            for (int q = 0; q < D + 2; ++q) sscal[ln * MAXW + q] = pv[q];
+            if (ln == 0) {
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) w[q] = wv[q];
+            }
+        }
+        if (threadIdx.x < 32) {
+            __syncwarp();
+            const int lane = threadIdx.x;
+            // hi/lo pairs (one lane each, one instruction stream): U_c (lanes 0..D-1),
+            // U_n (8..), lambda_c (16), lambda_n (17)
+            int src = -1, dh = 0, dl = 0;
+            if (lane < D) { src = 1 + lane; dh = C_UH + lane; dl = C_UL + lane; }
+            else if (lane >= 8 && lane < 8 + D) { src = MAXW + 1 + lane - 8; dh = C_UNH + lane - 8; dl = C_UNL + lane - 8; }
+            else if (lane == 16) { src = D + 1; dh = C_LCH; dl = C_LCL; }
+            else if (lane == 17) { src = MAXW + D + 1; dh = C_LNH; dl = C_LNL; }
+            if (src >= 0) {
+                const double x = sscal[src];
+                const A h = (A)x;
+                sc[dh] = h;
+                sc[dl] = (A)(x - (double)h);
+            }
+            // status of prim_c: one lane per component
+            int bad = 0;
+            if (lane < D + 2) {
+                const double x = sscal[lane];
+                if (!isfinite(x)) bad |= ST_NONFINITE;
+                if ((lane == 0 || lane == D + 1) && !(x > 0.0)) bad |= ST_NEGATIVE;
+            }
+            bad = __reduce_or_sync(0xffffffffu, bad);
+            if (lane == 0) {
+                if (bad) atomicOr(&P.status[slot], bad);
+                const double* pc = sscal;
+                const double* pn = sscal + MAXW;
+                const double lc = pc[D + 1], ln = pn[D + 1];
+                if constexpr (sizeof(A) == 8) {
+                    // get_τ (Gas/Model.jl:14) and the constants of discrete_maxwell / shakhov_part
+                    const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
+                    sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
+                    sc[C_PREN] = pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5));
+                    sc[C_BFC] = Kgas / (2.0 * lc);
+                    sc[C_BFN] = Kgas / (2.0 * ln);
+                    sc[C_R1] = tau / (tau + dt);
+                    sc[C_R2] = dt / (tau + dt);
+                    sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
+                    sc[C_LC] = lc;
+                } else {
+                    // mixed form: the same constants in FP32 (they scale FP32 per-velocity values)
+                    const float rc = (float)pc[0], rn = (float)pn[0];
+                    const float lcf = (float)sc[C_LCH], lnf = (float)sc[C_LNH];
+                    const float dtf = PP.dtf;
+                    const float tau = PP.mu2f * powf(lcf, PP.omf) / rc;
+                    constexpr float IPI = (float)(1.0 / PI);
+                    sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
+                    sc[C_PREN] = rn * (D == 2 ? lnf * IPI : powf(lnf * IPI, 1.5f));
+                    sc[C_BFC] = PP.Kf / (2.f * lcf);
+                    sc[C_BFN] = PP.Kf / (2.f * lnf);
+                    sc[C_R1] = tau / (tau + dtf);
+                    sc[C_R2] = dtf / (tau + dtf);
+                    sc[C_SK] = PP.shkf * lcf * lcf / rc;
+                    sc[C_LC] = lcf;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    // factor tables of the two Maxwellians (discrete_maxwell, 2D2F.jl:1-21 / 3D1F.jl:1-23)
+    const bool need_n = P.marching == KG_MARCH_CAIDVM;
+    A* En = Ec + (size_t)D * MA;
+    if constexpr (sizeof(A) == 8) {
+        gauss_table<D, NT>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
+        if (need_n) gauss_table<D, NT>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
+    } else {
+        gauss_table<D, NT>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
+        if (need_n)
+            gauss_table<D, NT>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
+    }
+    __syncthreads();
+}
+
+// prim_c, the residual terms of residual_check! (Solver/Finalize.jl:5-11) and qf of a cell
+// after its collision, one lane per component.
+template <int D>
+__device__ __forceinline__ void cell_outputs(const Dev& P, int cell, int fcx, int64_t step, int check_interval,
+                                             const double* sscal, const double* qv) {
+    if (threadIdx.x < MAXW) {
+        const int q = threadIdx.x;
+        double* pr = P.prim + (int64_t)cell * MAXW;
+        double* res = P.cell_res + (int64_t)fcx * 2 * MAXW;
+        const bool chk = (step % check_interval) == 0;
+        if (q < D + 2) {
+            const double pcq = sscal[q];
+            const double dl = pcq - pr[q];
+            res[q] = chk ? dl * dl : 0.0;
+            res[MAXW + q] = chk ? fabs(pcq) : 0.0;
+            pr[q] = pcq;
+        } else {
+            res[q] = 0.0;
+            res[MAXW + q] = 0.0;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+            if (q == d) P.qf[(int64_t)cell * MAXD + d] = 0.5 * qv[d];
+    }
+}
+
 // the faces of a regular cell (fluid_reg), by direction and side (2*dir + (face at +ds/2))
 template <typename A, typename T> struct RegFace {
     const T* of;    // the neighbour's f and sdf blocks
@@ -798,8 +938,10 @@ template <typename A, typename T> struct RegFace {
 
 // flux + collision of fluid cell number fcx (one CTA; every thread of the block takes part).
 // FG: the convected f is staged in the cell's output block instead of shared memory (a
-// compile-time choice, so that the shared-memory variant keeps shared-memory instructions)
-template <int D, int NDF, typename T, bool FG, int NT>
+// compile-time choice, so that the shared-memory variant keeps shared-memory instructions).
+// REG: the cell is regular (fluid_reg): its faces come from its RegRec, with no incidence
+// list, and the regular branch of the gather runs.
+template <int D, int NDF, typename T, bool FG, int NT, bool REG>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -810,10 +952,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     __shared__ A sbpre[MAX_INC], sbk[MAX_INC];  // ρ (λ/π)^{D/2} and K/(2λ) of that Maxwellian
     __shared__ double sred[2 * (D + 2) * (NT / 32)];
     __shared__ double sscal[4 * MAXW];
-    // per-CTA scalars in the arithmetic precision, computed once by thread 0
-    enum { C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
-           C_UH, C_UL = C_UH + MAXD, C_QA = C_UL + MAXD, C_UNH = C_QA + MAXD, C_UNL = C_UNH + MAXD,
-           C_LCH = C_UNL + MAXD, C_LCL, C_LNH, C_LNL, C_N };
+    // per-CTA scalars in the arithmetic precision (CellConst)
     __shared__ A sc[C_N];
     // one record of the cell, then its incidences: two dependent loads before the barrier
     const FluxCell FC = P.fcrec[fcx];
@@ -829,8 +968,8 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const double Kgas = PP.K;
     const int64_t step = P.prob_step[slot];
     const int check_interval = PP.check;
-    const int i0 = FC.inc0, ninc = FC.ninc;
-    const bool reg = FC.reg != 0;
+    const int i0 = FC.inc0, ninc = REG ? 0 : FC.ninc;
+    const bool reg = REG || FC.reg != 0;
     for (int e = threadIdx.x; e < ninc; e += NT) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
@@ -870,6 +1009,19 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             RegFace<A, T> rf;
             rf.of = ia.of; rf.os = ia.os; rf.dxm = dm; rf.sarea = ia.sarea;
             srf[2 * d + (dm > (A)0 ? 1 : 0)] = rf;
+        }
+    }
+    if constexpr (REG) {
+        // the faces of a regular cell from its RegRec, by side 2 * dir + (face at +ds/2)
+        if (threadIdx.x < 2 * D) {
+            const int q = threadIdx.x;
+            const RegRec& RR = P.regrec[fcx];
+            RegFace<A, T> rf;
+            rf.of = (const T*)P.f_in + RR.nfo[q];
+            rf.os = (const T*)P.sdf + RR.nfo[q] * D;
+            if constexpr (sizeof(A) == 4) { rf.dxm = RR.dxm_f[q]; rf.sarea = RR.sa_f[q]; }
+            else { rf.dxm = (A)RR.dxm[q]; rf.sarea = (A)RR.sa[q]; }
+            srf[q] = rf;
         }
     }
     const double invV = FC.invV;
@@ -980,7 +1132,6 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     // ---- 1. fluxes gathered over the incidences; convected f into shared memory ----
     KSum<A> wacc[D + 2], wfc[D + 2];
     for (int i = threadIdx.x; i < nv; i += NT) {
-        const int li = P.vlev[g.goff + i];
         A u[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) u[d] = VU[(int64_t)d * PG + g.goff + i];
@@ -1075,6 +1226,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
                 for (int k = 0; k < NDF; ++k) { acc[k] += sa * mic[k]; accM[k] += sa * mic[k]; }
             } else {
                 // incoming from a cell on a different velocity grid: mapped through the pairing
+                const int li = P.vlev[g.goff + i];
                 const int64_t po = P.p_off[ia.pair] + i;
                 const int j0 = P.p_j0[po], jc = P.p_cnt[po];
                 A mic[NDF];
@@ -1161,98 +1313,10 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             for (int q = 0; q < D + 2; ++q) { both[q] = wacc[q]; both[D + 2 + q] = wfc[q]; }
             block_sum_ks<2 * (D + 2), NT>(both, red, sred);
         }
-        // Two lanes recover the two sets of primitives in one FP64 instruction stream (on
-        // GB300 an FP64 warp instruction costs the same for one lane or 32): lane 0 the
-        // conserved update w + dt/V·flux and prim_c, lane 1 the primitives of the convected f
-        // (Euler: both lanes the same, so prim_n = prim_c)
-        if (threadIdx.x < 2) {
-            const int ln = threadIdx.x;
-            double* w = P.w + (int64_t)cell * MAXW;
-            const double dtV = dt * invV;
-            const bool lane_mom = P.marching != KG_MARCH_EULER ? ln == 1 : P.flux == KG_FLUX_DVM;
-            double wv[MAXW], pv[MAXW];
-#pragma unroll
-            for (int q = 0; q < D + 2; ++q) wv[q] = lane_mom ? red[D + 2 + q] : fma(red[q], dtV, w[q]);
-            get_prim_r<D>(wv, PP.gamma, pv);
-#pragma unroll
-            for (int q = 0; q < D + 2; ++q) sscal[ln * MAXW + q] = pv[q];
-            if (ln == 0) {
-#pragma unroll
-                for (int q = 0; q < D + 2; ++q) w[q] = wv[q];
-            }
-        }
-        if (threadIdx.x < 32) {
-            __syncwarp();
-            const int lane = threadIdx.x;
-            // hi/lo pairs (one lane each, one instruction stream): U_c (lanes 0..D-1),
-            // U_n (8..), lambda_c (16), lambda_n (17)
-            int src = -1, dh = 0, dl = 0;
-            if (lane < D) { src = 1 + lane; dh = C_UH + lane; dl = C_UL + lane; }
-            else if (lane >= 8 && lane < 8 + D) { src = MAXW + 1 + lane - 8; dh = C_UNH + lane - 8; dl = C_UNL + lane - 8; }
-            else if (lane == 16) { src = D + 1; dh = C_LCH; dl = C_LCL; }
-            else if (lane == 17) { src = MAXW + D + 1; dh = C_LNH; dl = C_LNL; }
-            if (src >= 0) {
-                const double x = sscal[src];
-                const A h = (A)x;
-                sc[dh] = h;
-                sc[dl] = (A)(x - (double)h);
-            }
-            // status of prim_c: one lane per component
-            int bad = 0;
-            if (lane < D + 2) {
-                const double x = sscal[lane];
-                if (!isfinite(x)) bad |= ST_NONFINITE;
-                if ((lane == 0 || lane == D + 1) && !(x > 0.0)) bad |= ST_NEGATIVE;
-            }
-            bad = __reduce_or_sync(0xffffffffu, bad);
-            if (lane == 0) {
-                if (bad) atomicOr(&P.status[slot], bad);
-                const double* pc = sscal;
-                const double* pn = sscal + MAXW;
-                const double lc = pc[D + 1], ln = pn[D + 1];
-                if constexpr (sizeof(A) == 8) {
-                    // get_τ (Gas/Model.jl:14) and the constants of discrete_maxwell / shakhov_part
-                    const double tau = PP.mu_ref * 2.0 * pow(lc, 1.0 - PP.omega) / pc[0];
-                    sc[C_PREC] = pc[0] * (D == 2 ? lc / PI : pow(lc / PI, 1.5));
-                    sc[C_PREN] = pn[0] * (D == 2 ? ln / PI : pow(ln / PI, 1.5));
-                    sc[C_BFC] = Kgas / (2.0 * lc);
-                    sc[C_BFN] = Kgas / (2.0 * ln);
-                    sc[C_R1] = tau / (tau + dt);
-                    sc[C_R2] = dt / (tau + dt);
-                    sc[C_SK] = 0.8 * (1.0 - PP.Pr) * lc * lc / pc[0];
-                    sc[C_LC] = lc;
-                } else {
-                    // mixed form: the same constants in FP32 (they scale FP32 per-velocity values)
-                    const float rc = (float)pc[0], rn = (float)pn[0];
-                    const float lcf = (float)sc[C_LCH], lnf = (float)sc[C_LNH];
-                    const float dtf = PP.dtf;
-                    const float tau = PP.mu2f * powf(lcf, PP.omf) / rc;
-                    constexpr float IPI = (float)(1.0 / PI);
-                    sc[C_PREC] = rc * (D == 2 ? lcf * IPI : powf(lcf * IPI, 1.5f));
-                    sc[C_PREN] = rn * (D == 2 ? lnf * IPI : powf(lnf * IPI, 1.5f));
-                    sc[C_BFC] = PP.Kf / (2.f * lcf);
-                    sc[C_BFN] = PP.Kf / (2.f * lnf);
-                    sc[C_R1] = tau / (tau + dtf);
-                    sc[C_R2] = dtf / (tau + dtf);
-                    sc[C_SK] = PP.shkf * lcf * lcf / rc;
-                    sc[C_LC] = lcf;
-                }
-            }
-        }
-        __syncthreads();
+        cell_constants<D, NDF, A, NT>(P, cell, slot, PP, dt, invV, red, sscal, sc, Ec, gid);
     }
-    // factor tables of the two Maxwellians (discrete_maxwell, 2D2F.jl:1-21 / 3D1F.jl:1-23)
     const bool need_n = P.marching == KG_MARCH_CAIDVM;
     A* En = Ec + (size_t)D * MA;
-    if constexpr (sizeof(A) == 8) {
-        gauss_table<D, NT>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
-        if (need_n) gauss_table<D, NT>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
-    } else {
-        gauss_table<D, NT>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
-        if (need_n)
-            gauss_table<D, NT>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
-    }
-    __syncthreads();
     const A prec = sc[C_PREC], pren = sc[C_PREN];
     const A bfc = sc[C_BFC], bfn = sc[C_BFN];
     // peculiar velocity c = u - U with U split into two floats (hi + lo), so that c keeps
@@ -1362,26 +1426,201 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         }
     }
     // ---- 5. per-cell outputs and residual terms ------------------------------------
-    // one lane per component
-    if (threadIdx.x < MAXW) {
-        const int q = threadIdx.x;
-        double* pr = P.prim + (int64_t)cell * MAXW;
-        double* res = P.cell_res + (int64_t)fcx * 2 * MAXW;
-        const bool chk = (step % check_interval) == 0;
-        if (q < D + 2) {
-            const double pcq = sscal[q];
-            const double dl = pcq - pr[q];
-            res[q] = chk ? dl * dl : 0.0;
-            res[MAXW + q] = chk ? fabs(pcq) : 0.0;
-            pr[q] = pcq;
-        } else {
-            res[q] = 0.0;
-            res[MAXW + q] = 0.0;
-        }
-#pragma unroll
-        for (int d = 0; d < D; ++d)
-            if (q == d) P.qf[(int64_t)cell * MAXD + d] = 0.5 * qv[d];
+    cell_outputs<D>(P, cell, fcx, step, check_interval, sscal, qv);
+}
+
+// ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
+// Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
+// thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
+// velocity cell through the reconstruction, the fluxes, the correction and the relaxation, and
+// the pair (macro flux, moments of the convected f) through the moment sums, so a velocity
+// cell issues about half the FP32 instructions of the scalar form.  The per-thread moment
+// sums are plain FP32 (a thread adds at most a few tens of terms; the block reduction that
+// follows is float-float).
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 abs2(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+
+// positivity_preserving_reconstruct (Flux/CAIDVM.jl:127-142) of the pair f with slopes s0, s1
+// (directions 0 and 1) and cell sizes ds0, ds1: the limiter factor per lane
+__device__ __forceinline__ float2 pp_theta2(float2 f, float2 s0, float2 s1, float ds0, float ds1) {
+    const float2 sabs = fma2(bc2(ds1), abs2(s1), mul2(bc2(ds0), abs2(s0)));
+    const float2 den = fma2(bc2(0.5f), sabs, bc2((float)EPS_REF));
+    const float2 num = add2(f, bc2(-(float)JL_EPS));
+    return make_float2(fminf(fabsf(__fdividef(num.x, den.x)), 1.f), fminf(fabsf(__fdividef(num.y, den.y)), 1.f));
+}
+
+template <int NT>
+__device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx) {
+    constexpr int D = 2;
+    extern __shared__ __align__(16) unsigned char sh_raw[];
+    __shared__ double sred[2 * (D + 2) * (NT / 32)];
+    __shared__ double sscal[4 * MAXW];
+    __shared__ float sc[C_N];
+    __shared__ int64_t nfo[4];
+    const FluxCell FC = P.fcrec[fcx];
+    const int nv = FC.nv;
+    if (threadIdx.x == 32) {
+        prefetch_l2((const float*)P.f_in + FC.foff, sizeof(float) * (size_t)2 * nv);
+        prefetch_l2((const float*)P.sdf + FC.foff * D, sizeof(float) * (size_t)D * 2 * nv);
     }
+    const int cell = FC.cell, slot = FC.slot;
+    const ProbParams& PP = P.probs[slot];
+    const double dt = PP.dt;
+    const int64_t step = P.prob_step[slot];
+    if (threadIdx.x == 0) {
+        sc[C_SDT] = (float)(dt * FC.invV);
+        sc[C_ADT] = (float)dt;
+        sc[C_DS0] = (float)FC.ds[0];
+        sc[C_DS0 + 1] = (float)FC.ds[1];
+    }
+    // the four faces (side 2 * dir + (face at +ds/2)): neighbour f offset (shared memory),
+    // dxm and area factor (registers)
+    const RegRec& RR = P.regrec[fcx];
+    if (threadIdx.x < 4) nfo[threadIdx.x] = RR.nfo[threadIdx.x];
+    float rdm[4], rsa[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) { rdm[q] = RR.dxm_f[q]; rsa[q] = RR.sa_f[q]; }
+    __syncthreads();
+    const float s_dt = sc[C_SDT], adt = sc[C_ADT], ds0 = sc[C_DS0], ds1 = sc[C_DS0 + 1];
+    const float* fbase = (const float*)P.f_in;
+    const float* sbase = (const float*)P.sdf;
+    const float* fc = fbase + FC.foff;
+    const float* scl = sbase + FC.foff * D;
+    const float4* vp = P.vpk + FC.goff;
+    float2* fst = reinterpret_cast<float2*>(sh_raw);               // convected (h, b) per velocity
+    float* Ec = reinterpret_cast<float*>(sh_raw) + (size_t)2 * nv;  // factor tables (flux_smem)
+    const bool caidvm = P.flux == KG_FLUX_CAIDVM;
+    const bool march_caidvm = P.marching == KG_MARCH_CAIDVM;
+
+    // ---- 1. the fluxes through the four faces and the convected f ----------------------
+    // accumulators of the pairs (macro flux, moments of the convected f): ρ, ρU_x, ρU_y, ρE
+    float2 m0 = bc2(0.f), m1 = bc2(0.f), m2 = bc2(0.f), mE = bc2(0.f);
+    for (int i = threadIdx.x; i < nv; i += NT) {
+        const float4 V = vp[i];
+        const float u0 = V.x, u1 = V.y, wi = V.z;
+        const float2 f2 = make_float2(fc[i], fc[nv + i]);
+        const float2 s0 = make_float2(scl[i], scl[nv + i]);
+        const float2 s1 = make_float2(scl[2 * nv + i], scl[3 * nv + i]);
+        const float2 th = pp_theta2(f2, s0, s1, ds0, ds1);
+        float2 acc = bc2(0.f);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const float ud = d == 0 ? u0 : u1;
+            const bool pos = ud > 0.f;
+            // outgoing through the face the velocity points at: the own reconstruction
+            const float dmo = pos ? rdm[2 * d + 1] : rdm[2 * d];
+            const float sao = pos ? rsa[2 * d + 1] : rsa[2 * d];
+            const float dx0 = (d == 0 ? dmo : 0.f) - u0 * adt;
+            const float dx1 = (d == 1 ? dmo : 0.f) - u1 * adt;
+            const float2 sdx = fma2(bc2(dx1), s1, mul2(bc2(dx0), s0));
+            const float2 mo = mul2(fma2(th, sdx, f2), bc2(ud));
+            acc = fma2(bc2(sao), mo, acc);
+            // incoming through the opposite face: the upwind neighbour's reconstruction
+            const float dmi = pos ? rdm[2 * d] : rdm[2 * d + 1];
+            const float sai = pos ? rsa[2 * d] : rsa[2 * d + 1];
+            const int64_t no = nfo[2 * d + (pos ? 0 : 1)];
+            const float* of = fbase + no;
+            const float* os = sbase + no * D;
+            const float2 g2 = make_float2(of[i], of[nv + i]);
+            const float2 t0 = make_float2(os[i], os[nv + i]);
+            const float2 t1 = make_float2(os[2 * nv + i], os[3 * nv + i]);
+            const float ndx0 = (d == 0 ? -dmi : 0.f) - u0 * adt;
+            const float ndx1 = (d == 1 ? -dmi : 0.f) - u1 * adt;
+            const float2 nsdx = fma2(bc2(ndx1), t1, mul2(bc2(ndx0), t0));
+            const float2 thn = pp_theta2(g2, t0, t1, ds0, ds1);
+            const float2 mi = mul2(fma2(thn, nsdx, g2), bc2(ud));
+            acc = fma2(bc2(sai), mi, acc);
+        }
+        const float2 fs = fma2(bc2(s_dt), acc, f2);
+        fst[i] = fs;
+        // macro flux (CAIDVM) and the moments of the convected f (CAIDVM marching) or of f
+        // (Euler), as the pairs (flux, f) in one set of packed sums
+        const float2 mf = march_caidvm ? fs : f2;
+        const float2 H = make_float2(caidvm ? acc.x : 0.f, mf.x);
+        const float2 B = make_float2(caidvm ? acc.y : 0.f, mf.y);
+        float u2 = u0 * u0;
+        u2 += u1 * u1;
+        const float2 a0 = mul2(bc2(wi), H);
+        m0 = add2(m0, a0);
+        m1 = fma2(bc2(u0), a0, m1);
+        m2 = fma2(bc2(u1), a0, m2);
+        mE = fma2(bc2(0.5f * wi), fma2(bc2(u2), H, B), mE);
+    }
+    double qv[D];
+    {
+        double red[2 * (D + 2)];
+        float hi[2 * (D + 2)] = {m0.x, m1.x, m2.x, mE.x, m0.y, m1.y, m2.y, mE.y};
+        float lo[2 * (D + 2)] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        block_sum_ff<2 * (D + 2), NT>(hi, lo, red, sred);
+        cell_constants<D, 2, float, NT>(P, cell, slot, PP, dt, FC.invV, red, sscal, sc, Ec, FC.gid);
+    }
+    const int MA = P.max_axis;
+    const float* En = Ec + (size_t)D * MA;
+    const float prec = sc[C_PREC], pren = sc[C_PREN], bfc = sc[C_BFC], bfn = sc[C_BFN];
+    const float Uh0 = sc[C_UH], Uh1 = sc[C_UH + 1], Ul0 = sc[C_UL], Ul1 = sc[C_UL + 1];
+    // ---- 3. conservation correction f += M(prim_c) - M(prim) (CAIDVM marching) and q -------
+    {
+        float2 q2 = bc2(0.f);
+        for (int i = threadIdx.x; i < nv; i += NT) {
+            const float4 V = vp[i];
+            const uint32_t bits = __float_as_uint(V.w);
+            const int ix = (int)(bits & 0xffffu), iy = (int)(bits >> 16);
+            float2 fv;
+            if (march_caidvm) {
+                float mc = prec;
+                mc *= Ec[ix];
+                mc *= Ec[MA + iy];
+                float mn = pren;
+                mn *= En[ix];
+                mn *= En[MA + iy];
+                const float2 fs = fst[i];
+                fv = make_float2(fs.x + (mc - mn), fs.y + (mc * bfc - mn * bfn));
+                fst[i] = fv;
+            } else {
+                fv = make_float2(fc[i], fc[nv + i]);   // Euler: q of f before convection
+            }
+            const float c0 = (V.x - Uh0) - Ul0, c1 = (V.y - Uh1) - Ul1;
+            float c2 = c0 * c0;
+            c2 += c1 * c1;
+            const float hb = c2 * fv.x + fv.y;
+            q2 = fma2(mul2(bc2(V.z), make_float2(c0, c1)), bc2(hb), q2);
+        }
+        float hi[D] = {q2.x, q2.y}, lo[D] = {0.f, 0.f};
+        block_sum_ff<D, NT>(hi, lo, qv, sred);
+        if (threadIdx.x == 0)
+            for (int d = 0; d < D; ++d) sc[C_QA + d] = (float)(0.5 * qv[d]);
+        __syncthreads();
+    }
+    // ---- 4. Shakhov g+ (shakhov_part_2D2F) and the implicit relaxation --------------------
+    {
+        const float r1 = sc[C_R1], r2 = sc[C_R2], sk = sc[C_SK], lc = sc[C_LC];
+        const float Kk = (float)PP.K;
+        const float qa0 = sc[C_QA], qa1 = sc[C_QA + 1];
+        float* fo = (float*)P.f_out + FC.foff;
+        for (int i = threadIdx.x; i < nv; i += NT) {
+            const float4 V = vp[i];
+            const uint32_t bits = __float_as_uint(V.w);
+            const int ix = (int)(bits & 0xffffu), iy = (int)(bits >> 16);
+            float mc = prec;
+            mc *= Ec[ix];
+            mc *= Ec[MA + iy];
+            const float c0 = (V.x - Uh0) - Ul0, c1 = (V.y - Uh1) - Ul1;
+            float c2 = c0 * c0;
+            c2 += c1 * c1;
+            float cq = c0 * qa0;
+            cq += c1 * qa1;
+            const float mb = mc * bfc;
+            const float pol = 2.f * lc * c2 + Kk;
+            const float2 gp = make_float2(mc + sk * cq * (pol - 5.f) * mc, mb + sk * cq * (pol - 3.f) * mb);
+            const float2 fn = fma2(bc2(r2), gp, mul2(fst[i], bc2(r1)));
+            fo[i] = fn.x;
+            fo[nv + i] = fn.y;
+        }
+    }
+    cell_outputs<D>(P, cell, fcx, step, PP.check, sscal, qv);
 }
 
 // Flux + collision of the fluid cells.  Two schedules share this one function, so the
@@ -1403,10 +1642,22 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
             __syncthreads();
         }
         if (it >= n) break;
-        flux_collide_cell<D, NDF, T, FG, NT>(P, order ? order[it] : it);
+        flux_collide_cell<D, NDF, T, FG, NT, false>(P, order ? order[it] : it);
         if (!counter) break;
         __syncthreads();
     }
+}
+
+// Flux + collision of the listed regular fluid cells, one CTA each (the generic cell's regular
+// branch; the 2D mixed form under CAIDVM or Euler marching takes flux_packed_kernel instead).
+template <int D, int NDF, typename T, bool FG, int NT>
+__global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) flux_regular_kernel(Dev P,
+                                                                                             const int32_t* list) {
+    flux_collide_cell<D, NDF, T, FG, NT, true>(P, list[blockIdx.x]);
+}
+template <int NT>
+__global__ void __launch_bounds__(NT, 4 * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
+    flux_regular_packed<NT>(P, list[blockIdx.x]);
 }
 
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
@@ -2348,6 +2599,25 @@ struct Launch {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, list, n);
+        return cudaGetLastError();
+    }
+    // the regular-cell kernel, one CTA per listed fluid-list entry (every one regular)
+    static cudaError_t flux_reg_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        using A = typename Arith<T>::type;
+        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
+        using RegFn = void (*)(Dev, const int32_t*);
+        RegFn fn = P.fst_global ? flux_regular_kernel<D, NDF, T, true, BLOCK>
+                                : (P.flux_nt == 128 ? flux_regular_kernel<D, NDF, T, false, 128>
+                                                    : flux_regular_kernel<D, NDF, T, false, BLOCK>);
+        if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
+            // the packed-FP32 kernel (its convected f always in shared memory)
+            if (!P.fst_global && P.marching != KG_MARCH_CIP)
+                fn = P.flux_nt == 128 ? flux_packed_kernel<128> : flux_packed_kernel<BLOCK>;
+        }
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        fn<<<n, flux_threads(P), smem, s>>>(P, list);
         return cudaGetLastError();
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch

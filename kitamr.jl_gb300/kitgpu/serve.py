@@ -37,6 +37,7 @@ class Request:
     residual: float = math.inf
     converged: bool = False
     result: Optional[Dict] = None
+    Ma: float = 0.0
 
 
 def residual_of(rep: abi.KgStepReport, n_quads: int, nw: int) -> np.ndarray:
@@ -68,7 +69,7 @@ def random_request(rng: np.random.Generator, rid: int, arrival: float, small: bo
     else:
         p = cases.cylinder(scale=n / 64.0, max_level=1 if small else 2, nv=m, vs_levels=0, Ma=Ma, Kn=Kn)
         p.case.quadrature = [-L, L, -L, L]
-    return Request(rid, p, arrival)
+    return Request(rid, p, arrival, Ma=Ma)
 
 
 @dataclass
@@ -81,6 +82,7 @@ class ServeStats:
     refused: int
     converged_latencies: List[float] = field(default_factory=list)
     steps_to_converge: List[int] = field(default_factory=list)
+    unconverged_detail: List[Dict] = field(default_factory=list)
 
     def summary(self) -> Dict:
         def pct(v, q):
@@ -93,7 +95,7 @@ class ServeStats:
                 "solves": self.solves, "solves_per_s": self.solves / self.wall if self.wall > 0 else 0.0,
                 "steps_to_converge_max": max(self.steps_to_converge) if self.steps_to_converge else None,
                 "wall_s": self.wall, "phase_cell_updates_per_s": self.phase_updates / self.wall if self.wall else 0.0,
-                "admissions_refused": self.refused}
+                "admissions_refused": self.refused, "unconverged_requests": self.unconverged_detail}
 
 
 class Server:
@@ -173,8 +175,10 @@ class Server:
         wall = clock() - t0
         lat = [r.finished - r.arrival for r in done]
         conv = [r for r in done if r.converged]
+        unconv = [dict(kind=r.problem.name, Ma=r.Ma, Kn=r.problem.gas.Kn, cells=int(r.topo["n_cells"]),
+                       steps=r.steps, residual=r.residual) for r in done if not r.converged]
         return ServeStats(lat, len(conv), wall, steps_total, updates, refused,
-                          [r.finished - r.arrival for r in conv], [r.steps for r in conv])
+                          [r.finished - r.arrival for r in conv], [r.steps for r in conv], unconv)
 
 
 def poisson_arrivals(rng: np.random.Generator, rate: float, n: int) -> List[float]:
