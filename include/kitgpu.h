@@ -323,6 +323,24 @@ int kg_download_restart(kg_handle *h, const int32_t *quad_index, int32_t n_quads
 int kg_upload_restart(kg_handle *h, const int32_t *quad_index, int32_t n_quads, const double *vs_df,
                       const double *ws);
 
+/* ---- save_result rows from the device state (IO/Output.jl:198-255) ----------------------
+ * As save_result first runs update_slope! and update_solid_cell!, the slopes are recomputed
+ * from the current f and the solid cells updated (state changes the reference makes too).
+ *   ps_prim   n_quads x (dim+2) row-major: PS_Solution.prim (IO/Types.jl:56-68) of every
+ *             quadrant, row quad_index[c] for cell c; NaN for cells with bound_enc < 0 and for
+ *             quadrants without a cell (InsideSolidData)
+ *   ps_qf     n_quads x dim, the same for PS_Solution.qf
+ *   wall_rows per SolidNeighbor record (topology order) its Boundary_PS_Solution of
+ *             save_boundary_result! (Boundary/Immersed_boundary.jl:12-61): prim (dim+2), qf (dim)
+ *             and the pressure tensor p (2D: p11 p12 p22; 3D: p11 p12 p13 p22 p23 p33) of the
+ *             wall distribution rebuilt at the aux point -- 9 doubles a row in 2D, 14 in 3D.  As
+ *             in the reference the record's wall-direction slope is refreshed and its
+ *             distribution left as it was.
+ * quad_index may be NULL (n_quads must then equal n_cells); any output may be NULL.  The
+ * VS_Solution rows are kg_download_state's f; the JLD2 / VTK writers stay with the caller.   */
+int kg_download_solution(kg_handle *h, const int32_t *quad_index, int32_t n_quads, double *ps_prim,
+                         double *ps_qf, double *wall_rows);
+
 /* Advance `nsteps` steps with time step dt; `step` is status.step before the
  * first of them (drives the residual cadence).  One call = nsteps x
  * (slope -> flux -> iterate).                                               */

@@ -1,4 +1,5 @@
 // kg_api.cu -- the C-ABI of libkitgpu.so (include/kitgpu.h).
+#include <limits>
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <chrono>
@@ -15,6 +16,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t slope(const Dev&, int, int, cudaStream_t);
     static cudaError_t solid(const Dev&, int, cudaStream_t);
     static cudaError_t wall(const Dev&, int, int, cudaStream_t);
+    static cudaError_t wall_rows(const Dev&, int, double*, cudaStream_t);
     static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
@@ -2028,3 +2030,71 @@ int kg_batch_set_dt(kg_handle* h, int32_t slot, double dt) {
 }
 
 }  // extern "C"
+
+// save_result's rows (IO/Output.jl:198-255): as save_result first runs update_slope! and
+// update_solid_cell!, the slopes are recomputed from the current f and the solid cells updated
+// (the state changes the reference makes too); save_boundary_result! then rebuilds each
+// SolidNeighbor's wall distribution (refreshing its wall-direction slope, as the reference's
+// boundary_slope! view does) without keeping it: the records' f blocks are restored after
+// their rows are taken.
+int kg_download_solution(kg_handle* h, const int32_t* quad_index, int32_t n_quads, double* ps_prim, double* ps_qf,
+                         double* wall_rows) {
+    if (!h) return KG_ERR_ARG;
+    if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle: save_result rows are per single-problem handle");
+    if (!h->have_state) return fail(h, KG_ERR_STATE, "no state on the device");
+    cudaSetDevice(h->device);
+    int rc = rebuild(h);
+    if (rc) return rc;
+    Problem& pb = h->probs[0];
+    const Flat& L = pb.F;
+    if ((rc = check_quads(h, L, quad_index, n_quads))) return rc;
+    const int D = h->prm.dim, NW = D + 2, NC = L.n_cells, NWALL = L.n_walls;
+    const int WR = 2 * D + 2 + D * (D + 1) / 2;
+    const Flat& M = h->M;
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fA : h->fB;
+    P.f_out = h->parity == 0 ? h->fB : h->fA;
+    cudaStream_t s = h->stream;
+    cudaError_t e = enqueue_slopes(h, P, s);
+    if (e == cudaSuccess && !M.solid_ops.empty())
+        e = dispatch(h, [&](auto Lc) { return decltype(Lc)::solid(P, (int)M.solid_ops.size(), s); });
+    if (e != cudaSuccess) return cuda_fail(h, e, "save_result: slopes and solid cells");
+    if (wall_rows && NWALL > 0) {
+        const size_t ss = storage_size(h);
+        const int64_t w0 = M.foff[pb.dbase + NC], w1 = M.foff[pb.dbase + NC + NWALL];
+        const size_t wb = (size_t)(w1 - w0) * ss;
+        char* tmp = nullptr;
+        e = cudaMalloc((void**)&tmp, 2 * wb + sizeof(double) * (size_t)NWALL * WR);
+        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc save_result rows");
+        char* fa = (char*)P.f_in + (size_t)w0 * ss;
+        char* fb = (char*)P.f_out + (size_t)w0 * ss;
+        double* drows = (double*)(tmp + 2 * wb);
+        e = cudaMemcpyAsync(tmp, fa, wb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(tmp + wb, fb, wb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = dispatch(h, [&](auto Lc) { return decltype(Lc)::wall(P, (int)M.wall_ops.size(), M.max_nv, s); });
+        if (e == cudaSuccess) e = dispatch(h, [&](auto Lc) { return decltype(Lc)::wall_rows(P, (int)M.wall_ops.size(), drows, s); });
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fa, tmp, wb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(fb, tmp + wb, wb, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(wall_rows, drows, sizeof(double) * (size_t)NWALL * WR, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(h, e, "save_result: wall rows");
+    }
+    if (ps_prim || ps_qf) {
+        std::vector<double> pp((size_t)NC * MAXW), qq((size_t)NC * MAXD);
+        KG_CUDA(h, cudaMemcpyAsync(pp.data(), h->prim + pb.dbase * MAXW, sizeof(double) * pp.size(), cudaMemcpyDeviceToHost, s));
+        KG_CUDA(h, cudaMemcpyAsync(qq.data(), h->qf + pb.dbase * MAXD, sizeof(double) * qq.size(), cudaMemcpyDeviceToHost, s));
+        KG_CUDA(h, cudaStreamSynchronize(s));
+        const double nan = std::numeric_limits<double>::quiet_NaN();
+        if (ps_prim) std::fill(ps_prim, ps_prim + (size_t)n_quads * NW, nan);
+        if (ps_qf) std::fill(ps_qf, ps_qf + (size_t)n_quads * D, nan);
+        for (int c = 0; c < NC; ++c) {
+            if (L.dbe[c] < 0) continue;   // PS_Solution of a solid cell: NaN (IO/Types.jl:56-63)
+            const int64_t q = quad_index ? quad_index[c] : c;
+            if (ps_prim) for (int e2 = 0; e2 < NW; ++e2) ps_prim[q * NW + e2] = pp[(size_t)c * MAXW + e2];
+            if (ps_qf) for (int d = 0; d < D; ++d) ps_qf[q * D + d] = qq[(size_t)c * MAXD + d];
+        }
+    }
+    return KG_OK;
+}

@@ -2552,6 +2552,68 @@ __global__ void __launch_bounds__(BLOCK) conserve_kernel(Dev P, const int32_t* l
     }
 }
 
+// save_boundary_result! (Boundary/Immersed_boundary.jl:12-61) from the wall distribution the
+// wall kernel just rebuilt in each SolidNeighbor record's f block (the donor's velocity grid):
+// aux_w = calc_w0, aux_prim = get_prim(aux_w), aux_qf = calc_qf(aux_prim) and the pressure
+// tensor Σ w u_a u_b h (pressure_2D / pressure_3D, lib/KitCore/2D.jl:31-37, 3D.jl:37-46), all
+// in FP64.  One CTA per record; out row: prim (D+2), qf (D), p (D (D+1) / 2).
+template <int D, int NDF, typename T>
+__global__ void __launch_bounds__(BLOCK) wall_rows_kernel(Dev P, double* out) {
+    constexpr int NP = D * (D + 1) / 2;
+    constexpr int N1 = D + 2 + NP;
+    constexpr int W = D + 2 + D + NP;
+    __shared__ double sred[N1 * (BLOCK / 32)];
+    __shared__ double sprim[MAXW];
+    const WallOp op = P.wall_ops[blockIdx.x];
+    const VGridView g = grid_view(P, op.donor);
+    const int nv = g.nv;
+    const T* wf = (const T*)P.f_in + P.foff[op.data];
+    double v[N1];
+#pragma unroll
+    for (int q = 0; q < N1; ++q) v[q] = 0.0;
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const double wt = P.vw[g.goff + i];
+        const double h = (double)wf[i];
+        const double b = NDF == 2 ? (double)wf[(NDF - 1) * nv + i] : 0.0;
+        double u[D], u2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { u[d] = g.u(i, d); u2 += u[d] * u[d]; }
+        v[0] += wt * h;
+#pragma unroll
+        for (int d = 0; d < D; ++d) v[1 + d] += wt * u[d] * h;
+        v[D + 1] += NDF == 2 ? 0.5 * wt * (u2 * h + b) : 0.5 * wt * u2 * h;
+        int e = D + 2;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int c = a; c < D; ++c) v[e++] += u[a] * u[c] * h * wt;
+    }
+    block_sum<N1>(v, sred);
+    if (threadIdx.x == 0) get_prim<D>(v, P.probs[P.dprob[op.donor]].gamma, sprim);
+    __syncthreads();
+    double q[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) q[d] = 0.0;
+    for (int i = threadIdx.x; i < nv; i += BLOCK) {
+        const double wt = P.vw[g.goff + i];
+        const double h = (double)wf[i];
+        const double b = NDF == 2 ? (double)wf[(NDF - 1) * nv + i] : 0.0;
+        double c[D], c2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { c[d] = g.u(i, d) - sprim[1 + d]; c2 += c[d] * c[d]; }
+        const double hb = NDF == 2 ? c2 * h + b : c2 * h;
+#pragma unroll
+        for (int d = 0; d < D; ++d) q[d] += 0.5 * wt * c[d] * hb;
+    }
+    block_sum<D>(q, sred);
+    if (threadIdx.x == 0) {
+        double* o = out + (int64_t)blockIdx.x * W;
+        for (int e = 0; e < D + 2; ++e) o[e] = sprim[e];
+        for (int d = 0; d < D; ++d) o[D + 2 + d] = q[d];
+        for (int e = 0; e < NP; ++e) o[2 * D + 2 + e] = v[D + 2 + e];
+    }
+}
+
 template <int D, int NDF, typename T>
 struct Launch {
     // the slope work items [item_base, item_base + n) of one pass
@@ -2564,6 +2626,11 @@ struct Launch {
     static cudaError_t solid(const Dev& P, int n, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
         solid_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P);
+        return cudaGetLastError();
+    }
+    static cudaError_t wall_rows(const Dev& P, int n, double* out, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        wall_rows_kernel<D, NDF, T><<<n, BLOCK, 0, s>>>(P, out);
         return cudaGetLastError();
     }
     static cudaError_t wall(const Dev& P, int n, int max_nv, cudaStream_t s) {

@@ -59,6 +59,7 @@ def load_library(path: Optional[str] = None):
     L.kg_vs_flags.argtypes = [vp, vp, vp, vp, vp]
     L.kg_batch_vs_flags.argtypes = [vp, i32, vp, vp, vp, vp]
     L.kg_upload_restart.argtypes = [vp, vp, i32, vp, vp]
+    L.kg_download_solution.argtypes = [vp, vp, i32, vp, vp, vp]
     L.kg_batch_download_restart.argtypes = [vp, i32, vp, i32, vp, vp]
     L.kg_autotune_result.argtypes = [vp, C.POINTER(i32), C.POINTER(i32), C.POINTER(dbl), i32]
     L.kg_serve.argtypes = [vp, i32, vp, vp, vp, dbl, i64, i32, vp, vp, vp, vp, vp]
@@ -76,6 +77,7 @@ EXPORTS = [
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
     "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
+    "kg_download_solution",
     "kg_vs_flags", "kg_batch_vs_flags", "kg_serve", "kg_vs_conserve", "kg_batch_vs_conserve",
 ]
 
@@ -234,6 +236,22 @@ class GpuStep:
         _check(self.L, self.h, self.L.kg_download_restart(self.h, None if qi is None else qi.ctypes.data, nq,
                                                             vs_df.ctypes.data, ws.ctypes.data))
         return vs_df.reshape(ndf, -1).T, ws.reshape(self.dim + 2, nq).T
+
+    def download_solution(self, quad_index: Optional[np.ndarray] = None, n_quads: Optional[int] = None):
+        """save_result's rows (kg_download_solution): PS_Solution prim (n_quads, dim+2) and qf
+        (n_quads, dim) with NaN rows for solid cells and quadrants without a cell, and per
+        SolidNeighbor record prim, qf and the pressure tensor (n_walls, 2 dim + 2 + dim (dim+1)/2)."""
+        nq = self.nc if n_quads is None else int(n_quads)
+        qi = None if quad_index is None else np.ascontiguousarray(quad_index, dtype=np.int32)
+        d = self.dim
+        wr = 2 * d + 2 + d * (d + 1) // 2
+        nwall = int(self.topo["n_walls"])
+        prim = np.empty(nq * (d + 2))
+        qf = np.empty(nq * d)
+        walls = np.empty(max(nwall, 1) * wr)
+        _check(self.L, self.h, self.L.kg_download_solution(self.h, None if qi is None else qi.ctypes.data, nq,
+                                                             prim.ctypes.data, qf.ctypes.data, walls.ctypes.data))
+        return {"prim": prim.reshape(nq, d + 2), "qf": qf.reshape(nq, d), "walls": walls[:nwall * wr].reshape(nwall, wr)}
 
     def upload_restart(self, vs_df: np.ndarray, ws: np.ndarray, quad_index: Optional[np.ndarray] = None):
         """restart(): f from vs_df, w from ws, prim = get_prim(w)."""

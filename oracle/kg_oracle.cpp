@@ -1306,6 +1306,59 @@ int kgo_slope(const kg_params* prm, const kg_topology* t, const double* f, doubl
     return KG_OK;
 }
 
+// save_result (IO/Output.jl:198-255) on the state as it stands: update_slope! and
+// update_solid_cell! change the state (slopes, solid cells' df, w, prim), then per
+// SolidNeighbor save_boundary_result! (Boundary/Immersed_boundary.jl:12-61) rebuilds the wall
+// distribution at the aux point -- its wall-direction slope is written through the ssdf view,
+// its df is a local -- and reports prim, qf (calc_w0, get_prim, calc_qf) and the pressure
+// tensor (pressure_2D / pressure_3D, lib/KitCore/2D.jl:31-37, 3D.jl:37-46).
+// rows: per wall record prim (dim+2), qf (dim), p (dim (dim+1) / 2).
+int kgo_solution(const kg_params* prm, const kg_topology* t, double* f, double* sdf, double* w, double* prim,
+                 double* wall_f, double* wall_sdf, double* rows, int32_t nthreads) {
+    Model m;
+    int rc = setup(m, prm, t);
+    if (rc) return rc;
+    m.f = f; m.sdf = sdf; m.w = w; m.prim = prim;
+    std::vector<double> qdummy((size_t)std::max(1, t->n_cells * t->dim), 0.0);
+    m.qf = qdummy.data();
+    m.nthreads = nthreads < 1 ? 1 : nthreads;
+    m.wall_f.assign(wall_f, wall_f + m.wfoff[t->n_walls]);
+    m.wall_sdf.assign(wall_sdf, wall_sdf + m.wsoff[t->n_walls]);
+    try {
+        slope(m);
+        update_solid_cells(m);
+        const std::vector<double> kept = m.wall_f;
+        update_walls(m);
+        const int D = m.dim, NDF = m.ndf, NP = D * (D + 1) / 2, WR = 2 * D + 2 + NP;
+        for (int wi = 0; wi < t->n_walls; ++wi) {
+            Data cd{1, t->wall_donor[wi]}, wd{2, wi};
+            const Grid& g = m.grid_of(cd);
+            const double* df = m.df(wd);
+            double wv[5], pv[5], q[3];
+            calc_w0(m, g, df, wv);
+            get_prim(m, wv, pv);
+            heat_flux(m, g, df, pv, q);
+            double* o = rows + (size_t)wi * WR;
+            for (int e = 0; e < D + 2; ++e) o[e] = pv[e];
+            for (int d = 0; d < D; ++d) o[D + 2 + d] = q[d];
+            int e = 2 * D + 2;
+            for (int a = 0; a < D; ++a)
+                for (int b = a; b < D; ++b) {
+                    double sum = 0.0;
+                    for (int i = 0; i < g.nv; ++i) sum += g.u(i, a) * g.u(i, b) * df[i] * g.weight[i];
+                    o[e++] = sum;
+                }
+            (void)NDF;
+        }
+        m.wall_f = kept;
+    } catch (...) {
+        return KG_ERR_TOPOLOGY;
+    }
+    std::copy(m.wall_f.begin(), m.wall_f.end(), wall_f);
+    std::copy(m.wall_sdf.begin(), m.wall_sdf.end(), wall_sdf);
+    return KG_OK;
+}
+
 // ---- physical-space adaptation: the state moves of ps_replace! (Physical_space/AMR.jl:633-703)
 // vs_merge! (AMR.jl:343-366): the level merge walk adding the cells of grid n onto grid p --
 // one-to-one on equal levels, finer cells over 2^(dim*Δl), a coarser cell into each cell it

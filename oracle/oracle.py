@@ -45,6 +45,7 @@ def lib():
         L.kgo_criterion.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 3 + \
             [C.c_double, C.POINTER(C.c_double)]
         L.kgo_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.kgo_solution.argtypes = [C.c_void_p, C.c_void_p] + [C.POINTER(C.c_double)] * 7 + [C.c_int32]
         L.kgo_iprojection.argtypes = [C.c_int, C.c_int, C.c_int] + [C.POINTER(C.c_double)] * 5
         _lib = L
     return _lib
@@ -167,6 +168,30 @@ class OracleState:
         if rc != 0:
             raise RuntimeError(f"oracle vs_flags failed: {rc}")
         return flags[:nv_total], eta[:nv_total], vr
+
+    def solution(self, params, quad_index=None, n_quads=None, nthreads: int = 1):
+        """save_result's rows on this state (changing it as save_result does: fresh slopes,
+        updated solid cells, refreshed wall-direction slopes of the SolidNeighbors):
+        PS_Solution prim / qf per quadrant (NaN rows for solid cells and quadrants without a
+        cell) and per SolidNeighbor prim, qf and the pressure tensor."""
+        nc, dim = self.topo["n_cells"], self.topo["dim"]
+        nwall = int(self.topo["n_walls"])
+        wr = 2 * dim + 2 + dim * (dim + 1) // 2
+        rows = np.zeros(max(nwall, 1) * wr)
+        rc = lib().kgo_solution(C.byref(params), C.cast(self.tref.ptr, C.c_void_p), abi.dptr(self.f),
+                                abi.dptr(self.sdf), abi.dptr(self.w), abi.dptr(self.prim), abi.dptr(self.wall_f),
+                                abi.dptr(self.wall_sdf), abi.dptr(rows), nthreads)
+        if rc != 0:
+            raise RuntimeError(f"oracle solution failed: {rc}")
+        nq = nc if n_quads is None else int(n_quads)
+        qi = np.arange(nc) if quad_index is None else np.asarray(quad_index)
+        prim = np.full((nq, dim + 2), np.nan)
+        qf = np.full((nq, dim), np.nan)
+        be = np.asarray(self.topo["cell_bound_enc"])
+        fl = be >= 0
+        prim[qi[fl]] = self.prim.reshape(nc, dim + 2)[fl]
+        qf[qi[fl]] = self.qf[:nc * dim].reshape(nc, dim)[fl]
+        return {"prim": prim, "qf": qf, "walls": rows[:nwall * wr].reshape(nwall, wr)}
 
     def moments(self, params):
         nc, nw = self.topo["n_cells"], self.topo["dim"] + 2

@@ -390,3 +390,31 @@ def test_vs_rebuild_refine_then_coarsen_returns_the_grid_and_f():
     t2 = mesh.with_cell_vgrids(t1, coarse)
     s2 = s1.adapt(prm, t2, mesh.vs_sources(t2))
     assert np.allclose(s2.f, st.f, rtol=4e-16, atol=0)
+
+
+def test_oracle_solution_rows_are_consistent():
+    """save_result rows of the oracle (kgo_solution): the PS rows are the state's prim / qf with
+    NaN for solid cells and inside-solid quadrants, and for every SolidNeighbor of a 3D sphere
+    the trace of the pressure tensor equals 2 ρE of the same distribution (3D1F: ρE = ½ Σ w |u|² f),
+    recovered from the reported prim."""
+    from kitgpu import abi, cases
+    import oracle as O
+    p = cases.sphere(scale=0.25, nv=8)
+    topo, state = cases.build(p)
+    prm = abi.make_params(p, st_check_interval=1)
+    st = O.OracleState(topo, state).run(prm, p.dt(), 0, 1, nthreads=4)
+    qi, nq = topo["cell_quad"], int(topo["n_quads"])
+    out = st.solution(prm, quad_index=qi, n_quads=nq, nthreads=4)
+    be = np.asarray(topo["cell_bound_enc"])
+    assert np.all(np.isnan(out["prim"][qi[be < 0]]))
+    mask = np.ones(nq, bool)
+    mask[qi] = False
+    assert np.all(np.isnan(out["prim"][mask]))
+    assert np.allclose(out["prim"][qi[be >= 0]], st.prim.reshape(-1, 5)[be >= 0], rtol=0, atol=0)
+    walls = out["walls"]
+    assert walls.shape == (topo["n_walls"], 14)
+    rho, U, lam = walls[:, 0], walls[:, 1:4], walls[:, 4]
+    # 3D monatomic (K = 0): rho E = rho |U|^2 / 2 + 3 rho / (4 lam) with lam = rho / (2 p)
+    rhoE = 0.5 * rho * np.sum(U * U, axis=1) + 0.75 * rho / lam
+    trace = walls[:, 8] + walls[:, 11] + walls[:, 13]
+    assert np.allclose(trace, 2.0 * rhoE, rtol=1e-12)
