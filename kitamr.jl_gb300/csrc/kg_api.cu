@@ -161,13 +161,9 @@ struct kg_handle {
     // read none of their output (fork / join through the two events)
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-    const int32_t* d_indep = nullptr;  // fluid-list entries without a solid / wall incidence
-    const int32_t* d_dep = nullptr;    // the others
-    int n_indep = 0, n_dep = 0;
-    const int32_t* d_reg = nullptr;    // independent entries of regular cells (regular-cell kernel)
-    const int32_t* d_irr = nullptr;    // independent entries of the other cells
-    const int32_t* d_nonreg = nullptr; // every entry that is not in d_reg
-    int n_reg = 0, n_irr = 0, n_nonreg = 0;
+    const int32_t* d_reg = nullptr;    // fluid-list entries of regular cells (regular-cell kernel)
+    const int32_t* d_nonreg = nullptr; // every other entry
+    int n_reg = 0, n_nonreg = 0;
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -480,25 +476,13 @@ int rebuild(kg_handle* h) {
         if (r) return r;
     }
     {
-        // fluid cells whose flux reads no solid cell or wall record (the IB kernels' output)
-        // and, of those, the regular cells (the regular-cell flux kernel) and the others
-        std::vector<int32_t> indep, dep, reg, irr, nonreg;
-        for (int q = 0; q < M.n_fluid; ++q) {
-            bool d = false;
-            for (int e = M.inc_off[q]; e < M.inc_off[q + 1] && !d; ++e) d = M.inc[e].kind == INC_SOLID;
-            (d ? dep : indep).push_back(q);
-            if (!d) (M.fluid_reg[q] ? reg : irr).push_back(q);
-            if (d || !M.fluid_reg[q]) nonreg.push_back(q);
-        }
-        h->n_indep = (int)indep.size();
-        h->n_dep = (int)dep.size();
+        // the regular fluid cells (the regular-cell flux kernel; a regular cell never reads a
+        // solid cell or wall record) and the others
+        std::vector<int32_t> reg, nonreg;
+        for (int q = 0; q < M.n_fluid; ++q) (M.fluid_reg[q] ? reg : nonreg).push_back(q);
         h->n_reg = (int)reg.size();
-        h->n_irr = (int)irr.size();
         h->n_nonreg = (int)nonreg.size();
-        int r = upload_vec(h, indep, &h->d_indep);
-        if (!r) r = upload_vec(h, dep, &h->d_dep);
-        if (!r) r = upload_vec(h, reg, &h->d_reg);
-        if (!r) r = upload_vec(h, irr, &h->d_irr);
+        int r = upload_vec(h, reg, &h->d_reg);
         if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
         if (r) return r;
     }
@@ -647,11 +631,11 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         end("slope_kernel");
         ++*launches;
     }
-    const bool ib = !F.solid_ops.empty() || !F.wall_ops.empty();
-    if (!timed && ib && h->sched == 0 && h->n_dep > 0 && h->n_indep > 0 && h->prm.marching != KG_MARCH_CIP) {
-        // the IB kernels and then the flux of the cells that read their output on the second
-        // stream (higher priority: its CTAs take SM slots first as they free up), beside the
-        // flux of the cells that read none of it; the step ends on one tail
+    if (!timed && h->sched == 0 && h->n_reg > 0 && h->n_nonreg > 0) {
+        // two streams after the slopes: the regular cells' kernel on the handle's stream; the
+        // IB kernels and then the flux of every other cell (those that read the IB kernels'
+        // output among them) on the second, higher-priority stream, whose CTAs take SM slots
+        // first as they free up; the step ends on one tail
         cudaStream_t a = h->aux;
         KG_CUDA(h, cudaEventRecord(h->ev_fork, s));
         KG_CUDA(h, cudaStreamWaitEvent(a, h->ev_fork, 0));
@@ -665,15 +649,18 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
             if (e != cudaSuccess) return cuda_fail(h, e, "wall_kernel");
             ++*launches;
         }
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_dep, h->n_dep, F.max_nv, a); });
+        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, a); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaEventRecord(h->ev_join, a));
         e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_irr, h->n_irr, F.max_nv, s); });
-        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
-        *launches += 1 + (h->n_reg > 0) + (h->n_irr > 0);
+        *launches += 2;
+        if (h->prm.marching == KG_MARCH_CIP) {
+            e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "cip_kernel");
+            ++*launches;
+        }
         e = launch_residual(P, h->d_live, (int)h->live.size(), h->res_out, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "residual_kernel");
         ++*launches;

@@ -133,13 +133,6 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
                            !t.wall_normal || !t.wall_bc || !t.wall_cut_off)))
         { err = "null topology array"; return KG_ERR_ARG; }
     const int D = t.dim, NDF = t.ndf, NC = t.n_cells, NWL = t.n_walls;
-    if (prm.marching == KG_MARCH_CIP) {
-        // iterate!(CIP_Marching) calls positivity_preserving_ib! on cells next to a wall
-        // (Boundary/Positivity.jl:1-44), which this library does not provide
-        bool ib = NWL > 0;
-        for (int i = 0; i < NC && !ib; ++i) ib = t.cell_bound_enc[i] != 0;
-        if (ib) { err = "CIP marching on a mesh with immersed-boundary cells is not supported"; return KG_ERR_ARG; }
-    }
     F.dim = D; F.ndf = NDF; F.n_cells = NC; F.n_walls = NWL; F.n_data = NC + NWL;
     Ctx c{&t, D, NDF, &F, {}, &err, {}, t.n_grids};
     if (t.n_grids <= 1024) c.dense.assign((size_t)t.n_grids * t.n_grids, -3);
@@ -492,6 +485,10 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         a.pair = pairing(c, t.cell_grid[here], F.dgrid[od]);
         if (a.pair == -2) return KG_ERR_TOPOLOGY;
         if (solid && od >= NC && F.dgrid[od] != t.cell_grid[here]) { err = "wall grid differs from donor grid"; return KG_ERR_TOPOLOGY; }
+        if (solid && od >= NC) {
+            a.wallrec = 1;
+            a.pert = a.ot_mid[dir] - t.wall_aux_point[(size_t)(od - NC) * D + dir];
+        }
         incs[fill[here]++] = a;
         if (!solid && od < NC) {
             // the there side receives the same flux with the opposite sign
@@ -738,6 +735,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             }
             a.orient_f = (float)a.orient;
             a.sarea_f = (float)a.sarea;
+            a.pert_f = (float)a.pert;
             a.pair = rp(a.pair);
             a.bc += bcacc;
             M.inc.push_back(a);

@@ -67,7 +67,7 @@ enum IncKind : int8_t { INC_INNER = 0, INC_DOMAIN = 1, INC_SOLID = 2 };
 // solid PsData); the reference reconstructs the here side without the positivity
 // limiter and (CAIDVM) takes the there side unreconstructed.
 
-struct Incidence {          // 192 bytes
+struct Incidence {          // 208 bytes
     double fmid[MAXD];      // face (sub-face) midpoint
     double my_mid[MAXD];    // centre used for this cell's reconstruction
     double ot_mid[MAXD];    // centre used for the other side's reconstruction
@@ -82,6 +82,12 @@ struct Incidence {          // 192 bytes
     int64_t ofoff;          // f offset of the other side (-1 for a domain face)
     int32_t onv, ogo;       // its velocity count and grid offset
     float dxm_f[MAXD], dxo_f[MAXD], ods_f[MAXD], orient_f, sarea_f;   // FP32 roundings
+    // a face to a SolidNeighbor record: the reconstruction perturbance's lever arm
+    // x_solid[dir] - x_aux[dir] (update_solid_neighbor!, Immersed_boundary.jl:477), which
+    // positivity_preserving_ib! reads under CIP marching
+    double pert;
+    float pert_f;
+    int32_t wallrec;        // 1 for such a face
 };
 
 // What the flux kernel needs of a fluid cell before its first barrier, in one record

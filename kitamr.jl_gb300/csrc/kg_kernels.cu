@@ -788,6 +788,74 @@ __host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, i
     return ((fst_global ? (size_t)0 : (size_t)NDF * max_nv) + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
 }
 
+// Julia's min of two floats (NaN if either is NaN)
+__device__ __forceinline__ double jl_min(double a, double b) { return (a != a || b != b) ? (a + b) : (a < b ? a : b); }
+
+// positivity_preserving_ib! (Boundary/Positivity.jl:13-27): the micro flux a SolidNeighbor's
+// reconstruction perturbance sends into the donor through incidence ia at velocity i (which
+// enters from the wall): (ndf + ndx . sdf) u_dir area, with ndf = ssdf (x_solid - x_aux)[dir]
+// (pert), ndx = face midpoint - u dt - x_solid and sdf the record's slopes (zero but for the
+// wall direction, ssdf).
+template <int D, int NDF, typename T, typename A, typename IA>
+__device__ __forceinline__ void pp_ib_micro(const IA& ia, A pert, int i, const A* u, A adt, A* out) {
+    const int dir = ia.dir;
+    const A ud = D == 2 ? (dir == 0 ? u[0] : u[D - 1]) : (dir == 0 ? u[0] : (dir == 1 ? u[1] : u[D - 1]));
+    const int nv = ia.onv;
+#pragma unroll
+    for (int k = 0; k < NDF; ++k) {
+        A dot = 0, ss = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const A sd = (A)ia.os[(d * NDF + k) * nv + i];
+            dot += (ia.dxo[d] - u[d] * adt) * sd;
+            if (d == dir) ss = sd;
+        }
+        out[k] = (ss * pert + dot) * ud * ia.sarea;
+    }
+}
+
+// The two passes of positivity_preserving_ib! over a donor cell's velocities (kept out of
+// line: only donor cells under CIP marching run them).  fst == nullptr: the moments of the
+// SolidNeighbors' perturbance micro fluxes into wev (a block reduction); otherwise
+// fst += scale * micro (scale = dt / V * theta) at every velocity entering from a wall.
+template <int D, int NDF, typename T, int NT>
+__device__ __noinline__ void pp_ib_pass(const Incidence* sinc, const IncA<typename Arith<T>::type, T>* sia, int ninc,
+                                        int nv, const typename Arith<T>::type* vu, int64_t PG,
+                                        const typename Arith<T>::type* vw, typename Arith<T>::type adt,
+                                        typename Arith<T>::type scale, typename Arith<T>::type* fst, double* wev,
+                                        double* sred) {
+    using A = typename Arith<T>::type;
+    KSum<A> wpp[D + 2];
+    for (int i = threadIdx.x; i < nv; i += NT) {
+        A u[D], uu = 0;
+#pragma unroll
+        for (int d = 0; d < D; ++d) { u[d] = vu[(int64_t)d * PG + i]; uu += u[d] * u[d]; }
+        const A wv = vw[i];
+        for (int e = 0; e < ninc; ++e) {
+            if (!sinc[e].wallrec) continue;
+            const IncA<A, T>& ia = sia[e];
+            const int dir = ia.dir;
+            const A ud = D == 2 ? (dir == 0 ? u[0] : u[D - 1]) : (dir == 0 ? u[0] : (dir == 1 ? u[1] : u[D - 1]));
+            if (!(ia.orient * ud > (A)0)) continue;
+            A mp[NDF];
+            const A pert = sizeof(A) == 4 ? (A)sinc[e].pert_f : (A)sinc[e].pert;
+            pp_ib_micro<D, NDF, T, A>(ia, pert, i, u, adt, mp);
+            if (fst) {
+#pragma unroll
+                for (int k = 0; k < NDF; ++k) fst[(int64_t)k * nv + i] += scale * mp[k];
+            } else {
+                const A b0 = wv * mp[0];
+                wpp[0].add(b0);
+#pragma unroll
+                for (int d = 0; d < D; ++d) wpp[1 + d].add(u[d] * b0);
+                if (NDF == 2) wpp[D + 1].add((A)0.5 * wv * (uu * mp[0] + mp[NDF - 1]));
+                else wpp[D + 1].add((A)0.5 * uu * b0);
+            }
+        }
+    }
+    if (!fst) block_sum_ks<D + 2, NT>(wpp, *reinterpret_cast<double(*)[D + 2]>(wev), sred);
+}
+
 // Indices of the per-CTA constants of the flux kernels (shared array sc, arithmetic precision).
 enum CellConst {
     C_SDT = 0, C_ADT, C_DS0, C_PREC = C_DS0 + MAXD, C_PREN, C_BFC, C_BFN, C_R1, C_R2, C_SK, C_LC,
@@ -801,10 +869,13 @@ enum CellConst {
 // status bits of prim_c are set, the collision constants go to sc, and the factor tables of the
 // two Maxwellians (the second only for CAIDVM marching) are built at Ec.  Ends with the block
 // synchronised; sscal holds prim_c (row 0) and the convected f's primitives (row 1).
+// we (CIP marching, a donor cell): the moments of the SolidNeighbors' reconstruction
+// perturbance, which positivity_preserving_ib! (Boundary/Positivity.jl:1-43) adds to the
+// updated w with its limiter factor theta (left in sscal[2 * MAXW]); nullptr otherwise.
 template <int D, int NDF, typename A, int NT>
 __device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot, const ProbParams& PP, double dt,
                                                double invV, const double (&red)[2 * (D + 2)], double* sscal, A* sc,
-                                               A* Ec, int gid) {
+                                               A* Ec, int gid, const double* we = nullptr) {
     const double Kgas = PP.K;
     const int MA = P.max_axis;
     {
@@ -820,6 +891,29 @@ __device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot,
             double wv[MAXW], pv[MAXW];
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) wv[q] = lane_mom ? red[D + 2 + q] : fma(red[q], dtV, w[q]);
+            if (we && ln == 0) {
+                // positivity_preserving_ib!: theta = min(theta_rho, theta_e), margin 1e-3
+                double wev[MAXW];
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) wev[q] = we[q] * dtV;
+                const double delta = 1e-3;
+                const double th_rho = wev[0] > 0.0 ? 1.0 : jl_min(1.0, (1.0 - delta) * wv[0] / (fabs(wev[0]) + JL_EPS));
+                double rub2 = 0.0, rue2 = 0.0, rbe = 0.0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) {
+                    rub2 += wv[1 + d] * wv[1 + d];
+                    rue2 += wev[1 + d] * wev[1 + d];
+                    rbe += wv[1 + d] * wev[1 + d];
+                }
+                const double eb = wv[D + 1] - rub2 / (2.0 * wv[0]);
+                const double ee = wev[D + 1] - rbe / wv[0];
+                const double gam = rue2 / (2.0 * wv[0]);
+                const double th_e = jl_min(1.0, 2.0 * (1.0 - delta) * eb / (sqrt(ee * ee + 4.0 * gam * (1.0 - delta) * eb) - ee + JL_EPS));
+                const double th = jl_min(th_rho, th_e);
+#pragma unroll
+                for (int q = 0; q < D + 2; ++q) wv[q] += th * wev[q];
+                sscal[2 * MAXW] = th;
+            }
             get_prim_r<D>(wv, PP.gamma, pv);
 #pragma unroll
             for (int q = 0; q < D + 2; ++q) sscal[ln * MAXW + q] = pv[q];
@@ -941,7 +1035,7 @@ template <typename A, typename T> struct RegFace {
 // compile-time choice, so that the shared-memory variant keeps shared-memory instructions).
 // REG: the cell is regular (fluid_reg): its faces come from its RegRec, with no incidence
 // list, and the regular branch of the gather runs.
-template <int D, int NDF, typename T, bool FG, int NT, bool REG>
+template <int D, int NDF, typename T, bool FG, int NT, bool REG, bool PPIB = false>
 __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     using A = typename Arith<T>::type;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -1131,6 +1225,12 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 
     // ---- 1. fluxes gathered over the incidences; convected f into shared memory ----
     KSum<A> wacc[D + 2], wfc[D + 2];
+    // CIP marching, a donor cell: positivity_preserving_ib! (one uniform flag per CTA)
+    // (PPIB: the kernel variant of CIP-marching layouts with walls, so that no other layout
+    // carries this code)
+    bool pp_ib = false;
+    if constexpr (PPIB)
+        for (int e = 0; e < ninc; ++e) pp_ib |= sinc[e].wallrec != 0;
     for (int i = threadIdx.x; i < nv; i += NT) {
         A u[D];
 #pragma unroll
@@ -1313,8 +1413,15 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
             for (int q = 0; q < D + 2; ++q) { both[q] = wacc[q]; both[D + 2 + q] = wfc[q]; }
             block_sum_ks<2 * (D + 2), NT>(both, red, sred);
         }
-        cell_constants<D, NDF, A, NT>(P, cell, slot, PP, dt, invV, red, sscal, sc, Ec, gid);
+        double wev[D + 2];
+        if constexpr (PPIB)
+            if (pp_ib) pp_ib_pass<D, NDF, T, NT>(sinc, sia, ninc, nv, VU + g.goff, PG, VW, adt, (A)0, nullptr, wev, sred);
+        cell_constants<D, NDF, A, NT>(P, cell, slot, PP, dt, invV, red, sscal, sc, Ec, gid, (PPIB && pp_ib) ? wev : nullptr);
     }
+    // the limited perturbance joins the convected f: f += dt/V theta micro (the velocity-space
+    // flux of iterate!(CIP_Marching), I-projection.jl:176)
+    if constexpr (PPIB)
+        if (pp_ib) pp_ib_pass<D, NDF, T, NT>(sinc, sia, ninc, nv, VU + g.goff, PG, VW, adt, s_dt * (A)sscal[2 * MAXW], fst, nullptr, sred);
     const bool need_n = P.marching == KG_MARCH_CAIDVM;
     A* En = Ec + (size_t)D * MA;
     const A prec = sc[C_PREC], pren = sc[C_PREN];
@@ -1430,6 +1537,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 }
 
 // ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
+constexpr int PACKED_VPT = 2;   // velocity cells per thread and gather pass
 // Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
 // thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
 // velocity cell through the reconstruction, the fluxes, the correction and the relaxation, and
@@ -1452,7 +1560,7 @@ __device__ __forceinline__ float2 pp_theta2(float2 f, float2 s0, float2 s1, floa
     return make_float2(fminf(fabsf(__fdividef(num.x, den.x)), 1.f), fminf(fabsf(__fdividef(num.y, den.y)), 1.f));
 }
 
-template <int NT>
+template <int NT, int VPT>
 __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx) {
     constexpr int D = 2;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -1498,14 +1606,26 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     // ---- 1. the fluxes through the four faces and the convected f ----------------------
     // accumulators of the pairs (macro flux, moments of the convected f): ρ, ρU_x, ρU_y, ρE
     float2 m0 = bc2(0.f), m1 = bc2(0.f), m2 = bc2(0.f), mE = bc2(0.f);
-    for (int i = threadIdx.x; i < nv; i += NT) {
-        const float4 V = vp[i];
-        const float u0 = V.x, u1 = V.y, wi = V.z;
-        const float2 f2 = make_float2(fc[i], fc[nv + i]);
+    // the flux sum acc and f of velocity i (loads first, so that VPT velocities' loads are in
+    // flight together)
+    auto gather = [&](int i, const float4& V, float2& f2, float2& acc) {
+        const float u0 = V.x, u1 = V.y;
+        f2 = make_float2(fc[i], fc[nv + i]);
         const float2 s0 = make_float2(scl[i], scl[nv + i]);
         const float2 s1 = make_float2(scl[2 * nv + i], scl[3 * nv + i]);
+        float2 g2[D], t0[D], t1[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const bool pos = (d == 0 ? u0 : u1) > 0.f;
+            const int64_t no = nfo[2 * d + (pos ? 0 : 1)];
+            const float* of = fbase + no;
+            const float* os = sbase + no * D;
+            g2[d] = make_float2(of[i], of[nv + i]);
+            t0[d] = make_float2(os[i], os[nv + i]);
+            t1[d] = make_float2(os[2 * nv + i], os[3 * nv + i]);
+        }
         const float2 th = pp_theta2(f2, s0, s1, ds0, ds1);
-        float2 acc = bc2(0.f);
+        acc = bc2(0.f);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             const float ud = d == 0 ? u0 : u1;
@@ -1521,23 +1641,20 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             // incoming through the opposite face: the upwind neighbour's reconstruction
             const float dmi = pos ? rdm[2 * d] : rdm[2 * d + 1];
             const float sai = pos ? rsa[2 * d] : rsa[2 * d + 1];
-            const int64_t no = nfo[2 * d + (pos ? 0 : 1)];
-            const float* of = fbase + no;
-            const float* os = sbase + no * D;
-            const float2 g2 = make_float2(of[i], of[nv + i]);
-            const float2 t0 = make_float2(os[i], os[nv + i]);
-            const float2 t1 = make_float2(os[2 * nv + i], os[3 * nv + i]);
             const float ndx0 = (d == 0 ? -dmi : 0.f) - u0 * adt;
             const float ndx1 = (d == 1 ? -dmi : 0.f) - u1 * adt;
-            const float2 nsdx = fma2(bc2(ndx1), t1, mul2(bc2(ndx0), t0));
-            const float2 thn = pp_theta2(g2, t0, t1, ds0, ds1);
-            const float2 mi = mul2(fma2(thn, nsdx, g2), bc2(ud));
+            const float2 nsdx = fma2(bc2(ndx1), t1[d], mul2(bc2(ndx0), t0[d]));
+            const float2 thn = pp_theta2(g2[d], t0[d], t1[d], ds0, ds1);
+            const float2 mi = mul2(fma2(thn, nsdx, g2[d]), bc2(ud));
             acc = fma2(bc2(sai), mi, acc);
         }
+    };
+    // the convected f, and the macro flux (CAIDVM) with the moments of the convected f (CAIDVM
+    // marching) or of f (Euler) as the pairs (flux, f) in one set of packed sums
+    auto finish = [&](int i, const float4& V, const float2& f2, const float2& acc) {
+        const float u0 = V.x, u1 = V.y, wi = V.z;
         const float2 fs = fma2(bc2(s_dt), acc, f2);
         fst[i] = fs;
-        // macro flux (CAIDVM) and the moments of the convected f (CAIDVM marching) or of f
-        // (Euler), as the pairs (flux, f) in one set of packed sums
         const float2 mf = march_caidvm ? fs : f2;
         const float2 H = make_float2(caidvm ? acc.x : 0.f, mf.x);
         const float2 B = make_float2(caidvm ? acc.y : 0.f, mf.y);
@@ -1548,6 +1665,22 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         m1 = fma2(bc2(u0), a0, m1);
         m2 = fma2(bc2(u1), a0, m2);
         mE = fma2(bc2(0.5f * wi), fma2(bc2(u2), H, B), mE);
+    };
+    for (int i0 = threadIdx.x; i0 < nv; i0 += VPT * NT) {
+        int iv[VPT];
+        float4 V[VPT];
+        float2 f2[VPT], acc[VPT];
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+            iv[v] = i0 + v * NT;
+            if (iv[v] >= nv) iv[v] = i0;    // a valid index for the loads; not finished
+            V[v] = vp[iv[v]];
+        }
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) gather(iv[v], V[v], f2[v], acc[v]);
+#pragma unroll
+        for (int v = 0; v < VPT; ++v)
+            if (v == 0 || i0 + v * NT < nv) finish(iv[v], V[v], f2[v], acc[v]);
     }
     double qv[D];
     {
@@ -1629,7 +1762,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
 //  * persistent: `gridDim.x` resident CTAs take cells from the work counter (in `order`,
 //    when given), so a batch of uneven problems keeps every SM busy to the end of the
 //    sub-step.  The counter must be zero at launch.
-template <int D, int NDF, typename T, bool FG, int NT>
+template <int D, int NDF, typename T, bool FG, int NT, bool PPIB = false>
 __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) flux_collide_kernel(Dev P, int* counter,
                                                                                              const int32_t* order, int n) {
     __shared__ int item;
@@ -1642,7 +1775,7 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
             __syncthreads();
         }
         if (it >= n) break;
-        flux_collide_cell<D, NDF, T, FG, NT, false>(P, order ? order[it] : it);
+        flux_collide_cell<D, NDF, T, FG, NT, false, PPIB>(P, order ? order[it] : it);
         if (!counter) break;
         __syncthreads();
     }
@@ -1655,9 +1788,11 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
                                                                                              const int32_t* list) {
     flux_collide_cell<D, NDF, T, FG, NT, true>(P, list[blockIdx.x]);
 }
-template <int NT>
-__global__ void __launch_bounds__(NT, 4 * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
-    flux_regular_packed<NT>(P, list[blockIdx.x]);
+// VPT velocity cells per thread and pass of the gather (their loads in flight together);
+// more registers, so fewer resident CTAs
+template <int NT, int VPT>
+__global__ void __launch_bounds__(NT, (VPT == 1 ? 4 : 3) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
+    flux_regular_packed<NT, VPT>(P, list[blockIdx.x]);
 }
 
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
@@ -2644,10 +2779,15 @@ struct Launch {
     // the flux kernel of the layout's staging choice
     using FluxFn = void (*)(Dev, int*, const int32_t*, int);
     static FluxFn flux_fn(const Dev& P) {
+        // CIP marching on a layout with walls: the variant with positivity_preserving_ib!
+        if (P.marching == KG_MARCH_CIP && P.n_walls > 0)
+            return P.fst_global ? flux_collide_kernel<D, NDF, T, true, BLOCK, true> : flux_collide_kernel<D, NDF, T, false, BLOCK, true>;
         if (P.fst_global) return flux_collide_kernel<D, NDF, T, true, BLOCK>;
         return P.flux_nt == 128 ? flux_collide_kernel<D, NDF, T, false, 128> : flux_collide_kernel<D, NDF, T, false, BLOCK>;
     }
-    static int flux_threads(const Dev& P) { return P.fst_global ? BLOCK : (P.flux_nt == 128 ? 128 : BLOCK); }
+    static int flux_threads(const Dev& P) {
+        return (P.fst_global || (P.marching == KG_MARCH_CIP && P.n_walls > 0)) ? BLOCK : (P.flux_nt == 128 ? 128 : BLOCK);
+    }
     static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
@@ -2680,7 +2820,7 @@ struct Launch {
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             // the packed-FP32 kernel (its convected f always in shared memory)
             if (!P.fst_global && P.marching != KG_MARCH_CIP)
-                fn = P.flux_nt == 128 ? flux_packed_kernel<128> : flux_packed_kernel<BLOCK>;
+                fn = P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT> : flux_packed_kernel<BLOCK, PACKED_VPT>;
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;

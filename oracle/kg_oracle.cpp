@@ -1081,6 +1081,77 @@ void conserved_iprojection(int D, int NDF, const double* mid, const double* wt, 
 // ------------------------------------------------------------- iterate --------
 // iterate!(CAIDVM_Marching) (Theory/Iterate.jl:96-130), iterate!(Euler) (:131-162) and
 // iterate!(CIP_Marching) (Theory/I-projection.jl:161-193)
+// positivity_preserving_ib! (Boundary/Positivity.jl:1-43) of donor cell c (CIP marching,
+// after the macroscopic update): per SolidNeighbor, in face order, the velocities entering
+// from the wall (rot u_dir > 0) carry the reconstruction perturbance of update_solid_neighbor!
+// -- the record's flux ssdf (x_solid - x_aux) along dir, reconstructed with the record's sdf
+// (zero but for its wall-direction slope) from the solid centre to the face -- times u_dir and
+// the signed face area.  Their moments, scaled by dt / volume, enter w with the largest
+// factor theta <= 1 that keeps the density and the internal energy positive (margin 1e-3),
+// and theta times the micro fluxes join the cell's velocity-space flux.
+void positivity_ib(Model& m, int c, double volume) {
+    const kg_topology* t = m.t;
+    const int D = m.dim, NDF = m.ndf, NW = m.nw();
+    Data cd{1, c};
+    const Grid& g = m.grid_of(cd);
+    const int nv = g.nv;
+    std::vector<int> walls;
+    for (int w = 0; w < t->n_walls; ++w)
+        if (t->wall_donor[w] == c) walls.push_back(w);
+    std::sort(walls.begin(), walls.end(), [&](int a, int b) { return t->wall_faceid[a] < t->wall_faceid[b]; });
+    if (walls.empty()) return;
+    const double* cm = t->cell_midpoint + (size_t)c * D;
+    const double* ds = t->cell_ds + (size_t)c * D;
+    std::vector<double> micros(walls.size() * (size_t)nv * NDF, 0.0);
+    double we[5] = {0, 0, 0, 0, 0};
+    for (size_t j = 0; j < walls.size(); ++j) {
+        const int w = walls[j];
+        const int k = t->wall_faceid[w], dir = k / 2;
+        const double rot = (k % 2 == 0) ? 1.0 : -1.0;
+        double fmid[3] = {0.0, 0.0, 0.0};
+        for (int d = 0; d < D; ++d) fmid[d] = cm[d];
+        fmid[dir] -= 0.5 * rot * ds[dir];
+        const double* sm = t->cell_midpoint + (size_t)t->wall_solid[w] * D;
+        const double* aux = t->wall_aux_point + (size_t)w * D;
+        double area = rot;
+        for (int d = 0; d < D; ++d)
+            if (d != dir) area *= ds[d];
+        Data wd{2, w};
+        double* wsdf = m.sdfp(wd);
+        double* mic = micros.data() + j * (size_t)nv * NDF;
+        for (int i = 0; i < nv; ++i) {
+            const double vn = g.u(i, dir);
+            if (!(rot * vn > 0.0)) continue;
+            for (int kk = 0; kk < NDF; ++kk) {
+                const double ndf = Model::S(wsdf, nv, NDF, i, kk, dir) * (sm[dir] - aux[dir]);
+                double dot = 0.0;
+                for (int d = 0; d < D; ++d) dot += (fmid[d] - g.u(i, d) * m.dt - sm[d]) * Model::S(wsdf, nv, NDF, i, kk, d);
+                mic[(size_t)kk * nv + i] = (ndf + dot) * vn * area;
+            }
+        }
+        double wm[5];
+        calc_w0(m, g, mic, wm);
+        for (int e = 0; e < NW; ++e) we[e] += wm[e];
+    }
+    for (int e = 0; e < NW; ++e) we[e] *= m.dt / volume;
+    double* wb = m.w + (size_t)c * NW;
+    const double delta = 1e-3;
+    const double th_rho = we[0] > 0.0 ? 1.0 : std::min(1.0, (1.0 - delta) * wb[0] / (std::fabs(we[0]) + JL_EPS));
+    double rub2 = 0.0, rue2 = 0.0, rbe = 0.0;
+    for (int d = 0; d < D; ++d) { rub2 += wb[1 + d] * wb[1 + d]; rue2 += we[1 + d] * we[1 + d]; rbe += wb[1 + d] * we[1 + d]; }
+    const double eb = wb[D + 1] - rub2 / (2.0 * wb[0]);
+    const double ee = we[D + 1] - rbe / wb[0];
+    const double gam = rue2 / (2.0 * wb[0]);
+    const double th_e = std::min(1.0, 2.0 * (1.0 - delta) * eb / (std::sqrt(ee * ee + 4.0 * gam * (1.0 - delta) * eb) - ee + JL_EPS));
+    const double th = std::min(th_rho, th_e);
+    for (int e = 0; e < NW; ++e) wb[e] += th * we[e];
+    double* vf = m.vsflux.data() + m.foff[c];
+    for (size_t j = 0; j < walls.size(); ++j) {
+        const double* mic = micros.data() + j * (size_t)nv * NDF;
+        for (size_t a = 0; a < (size_t)nv * NDF; ++a) vf[a] += th * mic[a];
+    }
+}
+
 void iterate(Model& m, int64_t step, double* sum_res, double* sum_avg) {
     const kg_topology* t = m.t;
     int D = m.dim, NDF = m.ndf, NW = m.nw();
@@ -1131,8 +1202,10 @@ void iterate(Model& m, int64_t step, double* sum_res, double* sum_avg) {
                 }
             }
         } else if (m.prm.marching == KG_MARCH_CIP) {
-            // w update, convection, q of the convected f, I-projection of f onto w, relaxation
+            // w update, the positivity-preserving wall flux of a donor, convection, q of the
+            // convected f, I-projection of f onto w, relaxation
             for (int e = 0; e < NW; ++e) w[e] += wf[e] * dt / area;
+            if (t->cell_bound_enc[c] != 0) positivity_ib(m, c, area);
             get_prim(m, w, prim_c);
             double s = dt / area;
             for (size_t a = 0; a < (size_t)nv * NDF; ++a) fp[a] += s * vf[a];

@@ -21,6 +21,10 @@ CASES = [
     ("sod_levels", lambda: cases.sod(scale=0.125, nv=16), 6),
     ("collision_two_grids", lambda: cases.collision(), 6),
     ("box3d_levels", lambda: cases.box3d(n=(6, 4, 4), nv=8, levels=1), 4),
+    # immersed-boundary walls: positivity_preserving_ib! (Boundary/Positivity.jl:1-43) on the
+    # donor cells
+    ("cylinder_ib_positivity", lambda: cases.cylinder(scale=0.25, nv=16, vs_levels=1), 4),
+    ("sphere3d_ib_positivity", lambda: cases.sphere(scale=0.25, nv=8), 3),
 ]
 
 

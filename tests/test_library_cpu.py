@@ -66,17 +66,13 @@ def test_rejects_dvm_maxwell_domain(lib):
     assert "undefined" in str(e.value)
 
 
-def test_rejects_cip_marching_with_immersed_boundaries(lib):
-    # iterate!(CIP_Marching) calls positivity_preserving_ib! next to walls, which the library
-    # does not provide; meshes without walls are accepted
+def test_accepts_cip_marching_with_immersed_boundaries(lib):
+    # iterate!(CIP_Marching) calls positivity_preserving_ib! next to walls (built: the flux
+    # kernel's CIP variant for layouts with walls); such meshes lay out like any other
     p = cases.cylinder(scale=0.25, nv=8, vs_levels=0)
     topo, _ = cases.build(p)
-    with pytest.raises(S.KitGpuError) as e:
-        S.topology_footprint(abi.make_params(p, marching=abi.KG_MARCH_CIP), topo)
-    assert "immersed-boundary" in str(e.value)
-    q = cases.sod(scale=0.125, nv=8)
-    tq, _ = cases.build(q)
-    assert S.topology_footprint(abi.make_params(q, marching=abi.KG_MARCH_CIP), tq) > 0
+    assert topo["n_walls"] > 0
+    assert S.topology_footprint(abi.make_params(p, marching=abi.KG_MARCH_CIP), topo) > 0
 
 
 def test_create_fails_loudly_without_device(lib):
