@@ -17,7 +17,6 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t solid(const Dev&, int, cudaStream_t);
     static cudaError_t wall(const Dev&, int, int, cudaStream_t);
     static cudaError_t wall_rows(const Dev&, int, double*, cudaStream_t);
-    static cudaError_t flux(const Dev&, int, int, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t);

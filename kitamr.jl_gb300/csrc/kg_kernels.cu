@@ -1063,7 +1063,8 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
     const int64_t step = P.prob_step[slot];
     const int check_interval = PP.check;
     const int i0 = FC.inc0, ninc = REG ? 0 : FC.ninc;
-    const bool reg = REG || FC.reg != 0;
+    // regular cells run the regular-cell kernels only (every schedule routes them there)
+    constexpr bool reg = REG;
     for (int e = threadIdx.x; e < ninc; e += NT) {
         const Incidence I = P.inc[i0 + e];
         sinc[e] = I;
@@ -1537,7 +1538,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 }
 
 // ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
-constexpr int PACKED_VPT = 2;   // velocity cells per thread and gather pass
+constexpr int PACKED_VPT = 1;   // velocity cells per thread and gather pass
 // Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
 // thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
 // velocity cell through the reconstruction, the fluxes, the correction and the relaxation, and
@@ -2788,15 +2789,6 @@ struct Launch {
     static int flux_threads(const Dev& P) {
         return (P.fst_global || (P.marching == KG_MARCH_CIP && P.n_walls > 0)) ? BLOCK : (P.flux_nt == 128 ? 128 : BLOCK);
     }
-    static cudaError_t flux(const Dev& P, int n, int max_nv, cudaStream_t s) {
-        using A = typename Arith<T>::type;
-        size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
-        const FluxFn fn = flux_fn(P);
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, nullptr, n);
-        return cudaGetLastError();
-    }
     // one CTA per listed fluid-list entry
     static cudaError_t flux_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
@@ -2814,6 +2806,9 @@ struct Launch {
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
         using RegFn = void (*)(Dev, const int32_t*);
+        // (the CTA size of the layout; the generic kernel's CIP variant for layouts with walls
+        // runs 256 threads, which does not concern regular cells)
+        const int nt = P.fst_global ? BLOCK : (P.flux_nt == 128 ? 128 : BLOCK);
         RegFn fn = P.fst_global ? flux_regular_kernel<D, NDF, T, true, BLOCK>
                                 : (P.flux_nt == 128 ? flux_regular_kernel<D, NDF, T, false, 128>
                                                     : flux_regular_kernel<D, NDF, T, false, BLOCK>);
@@ -2824,7 +2819,7 @@ struct Launch {
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        fn<<<n, flux_threads(P), smem, s>>>(P, list);
+        fn<<<n, nt, smem, s>>>(P, list);
         return cudaGetLastError();
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
