@@ -293,10 +293,11 @@ def accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_
             out[f"{form}_vs_oracle"] = dict(summary(e), steps=oracle_steps)
         del ref
     out["tolerance"] = {"mixed": 1e-5, "fp64_vs_oracle": 1e-12}
-    out["mixed_form"] = ("FP32 f / sdf and per-velocity arithmetic, compensated FP32 moment sums reduced to FP64, "
-                         "FP64 conserved update and primitive recovery; the Maxwellian exponent formed in float-float "
-                         "(~44 bits) and tau / Shakhov / relaxation constants in FP32 from the FP64 primitives (a "
-                         "departure from an all-FP64 exponent, held to the same 1e-5)")
+    out["mixed_form"] = ("FP32 f / sdf and per-velocity arithmetic (packed FP32x2 in the 2D regular-cell kernel), "
+                         "per-thread FP32 moment sums (compensated in the generic kernel) reduced in float-float to "
+                         "FP64, FP64 conserved update and primitive recovery; the Maxwellian exponent formed in "
+                         "float-float (~44 bits) and tau / Shakhov / relaxation constants in FP32 from the FP64 "
+                         "primitives (a departure from an all-FP64 exponent, held to the same 1e-5)")
     return out
 
 

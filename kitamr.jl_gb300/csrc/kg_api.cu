@@ -457,9 +457,11 @@ int rebuild(kg_handle* h) {
         const int occ_glob = (int)dispatch(h, [&](auto L) { return (cudaError_t)decltype(L)::flux_occupancy(P, M.max_nv); });
         P.fst_global = occ_glob > occ_smem ? 1 : 0;
         // small velocity grids: the per-cell fixed work (setup, reductions, the scalar chain)
-        // outweighs the per-velocity work, and 128-thread CTAs keep twice the cells in flight
+        // outweighs the per-velocity work, and 128-thread CTAs keep twice the cells in flight;
+        // 2D layouts take 128 threads at every grid size (the packed regular-cell kernel issues
+        // half the instructions per velocity cell, so the per-cell fixed work weighs more)
         const double mean_nv = (double)M.phase_cells / (double)M.n_fluid;
-        P.flux_nt = (!P.fst_global && mean_nv < 1024.0) ? 128 : BLOCK;
+        P.flux_nt = (!P.fst_global && (mean_nv < 1024.0 || M.dim == 2)) ? 128 : BLOCK;
         P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
     }
 
@@ -2047,7 +2049,7 @@ int kg_download_solution(kg_handle* h, const int32_t* quad_index, int32_t n_quad
     if (e != cudaSuccess) return cuda_fail(h, e, "save_result: slopes and solid cells");
     if (wall_rows && NWALL > 0) {
         const size_t ss = storage_size(h);
-        const int64_t w0 = M.foff[pb.dbase + NC], w1 = M.foff[pb.dbase + NC + NWALL];
+        const int64_t w0 = pb.fbase + L.foff[NC], w1 = pb.fbase + L.foff[NC + NWALL];
         const size_t wb = (size_t)(w1 - w0) * ss;
         char* tmp = nullptr;
         e = cudaMalloc((void**)&tmp, 2 * wb + sizeof(double) * (size_t)NWALL * WR);

@@ -1538,7 +1538,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 }
 
 // ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
-constexpr int PACKED_VPT = 1;   // velocity cells per thread and gather pass
+constexpr int PACKED_VPT = 2;   // velocity cells per thread and gather pass
 // Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
 // thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
 // velocity cell through the reconstruction, the fluxes, the correction and the relaxation, and

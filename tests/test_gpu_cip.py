@@ -24,7 +24,9 @@ CASES = [
     # immersed-boundary walls: positivity_preserving_ib! (Boundary/Positivity.jl:1-43) on the
     # donor cells
     ("cylinder_ib_positivity", lambda: cases.cylinder(scale=0.25, nv=16, vs_levels=1), 4),
-    ("sphere3d_ib_positivity", lambda: cases.sphere(scale=0.25, nv=8), 3),
+    # (16^3: on coarser velocity grids the I-projection of this Ma 3 flow diverges, in the
+    # oracle as on the device)
+    ("sphere3d_ib_positivity", lambda: cases.sphere(scale=0.25, nv=16), 3),
 ]
 
 
