@@ -20,6 +20,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t);
+    static cudaError_t flux_r2_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t cip(const Dev&, int, cudaStream_t);
     static cudaError_t conserve(const Dev&, const int32_t*, int, cudaStream_t);
@@ -162,7 +163,8 @@ struct kg_handle {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     const int32_t* d_reg = nullptr;    // fluid-list entries of regular cells (regular-cell kernel)
     const int32_t* d_nonreg = nullptr; // every other entry
-    int n_reg = 0, n_nonreg = 0;
+    const int32_t* d_r2 = nullptr;     // regular cells whose slopes the packed kernel computes
+    int n_reg = 0, n_nonreg = 0, n_r2 = 0;
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -184,6 +186,12 @@ struct kg_handle {
     int64_t pool_bytes = 0;
     // merged topology (rebuilt when membership changes)
     bool dirty = true;
+    // the fused slopes of the packed regular-cell kernel: off for a layout whose convected f
+    // cannot stay in shared memory (the packed kernel is not used there)
+    bool fuse_off = false;
+    // the sdf of the lazy pass cells is the last step's only after enqueue_lazy_slopes ran on
+    // the f that step read (set by every step of a layout with lazy items)
+    bool sdf_partial = false;
     int64_t version = 0;
     std::vector<void*> topo_allocs;
     int64_t topo_bytes = 0;
@@ -388,7 +396,8 @@ int rebuild(kg_handle* h) {
         h->live.push_back(s);
     }
     std::vector<int32_t> ranges;
-    merge(parts, (int32_t)h->dcap, h->M, ranges);
+    const bool fuse = !h->fuse_off && h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED && h->prm.marching != KG_MARCH_CIP;
+    merge(parts, (int32_t)h->dcap, h->M, ranges, fuse);
     Flat& M = h->M;
     if (!parts.empty()) {
         if (M.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
@@ -421,7 +430,7 @@ int rebuild(kg_handle* h) {
         UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
         UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
         UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(slope_items, slope_items); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(regrec, regrec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(regrec, regrec); UP(r2rec, r2rec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
         UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
         UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
@@ -442,7 +451,16 @@ int rebuild(kg_handle* h) {
     { int r = upload_all(); if (r) return r; }
     P.max_axis = M.max_axis;
     P.max_bcm = M.max_bcm;
-    P.slope_split = (int64_t)M.slope_items.size() / 2 != (int64_t)M.pass_cells.size();
+    {
+        // explicit work items when a pass cell is split into chunks or the items are not the
+        // pass cells in order (lazy items moved to the end); a chunk is SLOPE_CHUNK velocity
+        // cells, or the whole cell
+        bool by_size = false, in_order = (int64_t)M.slope_items.size() / 2 == (int64_t)M.pass_cells.size();
+        for (int32_t m : M.pass_cells) by_size |= M.dnv[m] > 2 * SLOPE_CHUNK;
+        for (size_t i = 0; in_order && i < M.slope_items.size() / 2; ++i) in_order = M.slope_items[2 * i] == (int32_t)i;
+        P.slope_split = by_size || !in_order;
+        P.slope_chunk = by_size ? SLOPE_CHUNK : (1 << 30);
+    }
     if (M.n_fluid > 0) {
         // stage the flux kernel's convected f in global memory when shared memory would cost
         // resident CTAs (or not fit at all)
@@ -479,12 +497,19 @@ int rebuild(kg_handle* h) {
     {
         // the regular fluid cells (the regular-cell flux kernel; a regular cell never reads a
         // solid cell or wall record) and the others
-        std::vector<int32_t> reg, nonreg;
-        for (int q = 0; q < M.n_fluid; ++q) (M.fluid_reg[q] ? reg : nonreg).push_back(q);
+        // (the regular cells whose slopes the packed kernel computes form a list of their own)
+        std::vector<int32_t> reg, nonreg, r2;
+        for (int q = 0; q < M.n_fluid; ++q) {
+            if (!M.fluid_reg[q]) nonreg.push_back(q);
+            else if (M.fluid_r2[q]) r2.push_back(q);
+            else reg.push_back(q);
+        }
         h->n_reg = (int)reg.size();
         h->n_nonreg = (int)nonreg.size();
+        h->n_r2 = (int)r2.size();
         int r = upload_vec(h, reg, &h->d_reg);
         if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
+        if (!r) r = upload_vec(h, r2, &h->d_r2);
         if (r) return r;
     }
     const int32_t* dl;
@@ -525,6 +550,7 @@ int rebuild(kg_handle* h) {
 cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
     const Flat& F = h->M;
     cudaError_t e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+    if (e == cudaSuccess) e = dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
     if (e != cudaSuccess || h->n_nonreg == 0) return e;
     if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, s); });
     int nsm = 0;
@@ -586,9 +612,10 @@ int autotune_flux(kg_handle* h) {
 
 // One step of every live problem on the handle's stream (graph-capturable).
 // The level passes of slope! on the current f (the first phase of a step).
+int n_slope_passes(const Flat& F) { return std::max(0, (int)F.pass_items_off.size() - 2); }
 cudaError_t enqueue_slopes(kg_handle* h, const Dev& P, cudaStream_t s) {
     const Flat& F = h->M;
-    const int npass = (int)F.pass_items_off.size() - 1;
+    const int npass = n_slope_passes(F);
     for (int p = 0; p < npass; ++p) {
         const int base = F.pass_items_off[p], n = F.pass_items_off[p + 1] - base;
         if (n <= 0) continue;
@@ -596,6 +623,37 @@ cudaError_t enqueue_slopes(kg_handle* h, const Dev& P, cudaStream_t s) {
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;
+}
+// The lazy items: the slopes of the cells whose flux kernel computes them and whose slopes no
+// other cell reads in a step (every slope of the regular form, so one launch in any order).
+cudaError_t enqueue_lazy_slopes(kg_handle* h, const Dev& P, cudaStream_t s) {
+    const Flat& F = h->M;
+    if (F.pass_items_off.size() < 2) return cudaSuccess;
+    const int base = F.pass_items_off[F.pass_items_off.size() - 2], n = F.pass_items_off.back() - base;
+    if (n <= 0) return cudaSuccess;
+    return dispatch(h, [&](auto L) { return decltype(L)::slope(P, base, n, s); });
+}
+// slope! on the current f for every pass cell (the sync points that recompute the slopes:
+// the criterion, an adaptation, save_result's rows)
+cudaError_t enqueue_slopes_full(kg_handle* h, const Dev& P, cudaStream_t s) {
+    cudaError_t e = enqueue_slopes(h, P, s);
+    if (e == cudaSuccess) e = enqueue_lazy_slopes(h, P, s);
+    if (e == cudaSuccess) h->sdf_partial = false;
+    return e;
+}
+// Before a sync point reads the slopes the last step used: the lazy cells' slopes from the f
+// that step read (the other f buffer, whose fluid cells the step did not write).
+bool has_lazy_slopes(const kg_handle* h) {
+    const Flat& F = h->M;
+    return F.pass_items_off.size() >= 2 && F.pass_items_off.back() > F.pass_items_off[F.pass_items_off.size() - 2];
+}
+int complete_last_slopes(kg_handle* h) {
+    if (!h->sdf_partial) return KG_OK;
+    Dev P = h->dev;
+    P.f_in = h->parity == 0 ? h->fB : h->fA;
+    KG_CUDA(h, enqueue_lazy_slopes(h, P, h->stream));
+    h->sdf_partial = false;
+    return KG_OK;
 }
 
 int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
@@ -622,7 +680,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         cudaEventDestroy(e0); cudaEventDestroy(e1);
     };
     cudaError_t e;
-    int npass = (int)F.pass_items_off.size() - 1;
+    int npass = n_slope_passes(F);
     for (int p = 0; p < npass; ++p) {
         int base = F.pass_items_off[p], n = F.pass_items_off[p + 1] - base;
         if (n <= 0) continue;
@@ -632,11 +690,14 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         end("slope_kernel");
         ++*launches;
     }
-    if (!timed && h->sched == 0 && h->n_reg > 0 && h->n_nonreg > 0) {
-        // two streams after the slopes: the regular cells' kernel on the handle's stream; the
-        // IB kernels and then the flux of every other cell (those that read the IB kernels'
-        // output among them) on the second, higher-priority stream, whose CTAs take SM slots
-        // first as they free up; the step ends on one tail
+    const int n_main = h->n_r2 > 0 ? h->n_r2 : h->n_reg;
+    const int n_aux = h->n_nonreg + (h->n_r2 > 0 ? h->n_reg : 0);
+    if (!timed && h->sched == 0 && n_main > 0 && n_aux > 0) {
+        // two streams after the slopes: the regular cells whose slopes the flux kernel computes
+        // (or, without those, the other regular cells) on the handle's stream; the IB kernels
+        // and then the flux of every other cell (those that read the IB kernels' output among
+        // them) on the second, higher-priority stream, whose CTAs take SM slots first as they
+        // free up; the step ends on one tail
         cudaStream_t a = h->aux;
         KG_CUDA(h, cudaEventRecord(h->ev_fork, s));
         KG_CUDA(h, cudaStreamWaitEvent(a, h->ev_fork, 0));
@@ -652,11 +713,17 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         }
         e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, a); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
-        KG_CUDA(h, cudaEventRecord(h->ev_join, a));
-        e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+        if (h->n_r2 > 0) {
+            e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, a); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+            e = dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
+        } else {
+            e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+        }
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        KG_CUDA(h, cudaEventRecord(h->ev_join, a));
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
-        *launches += 2;
+        *launches += (h->n_nonreg > 0) + (h->n_reg > 0) + (h->n_r2 > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
             if (e != cudaSuccess) return cuda_fail(h, e, "cip_kernel");
@@ -687,7 +754,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         e = launch_flux(h, P, h->sched, h->sched_ctas, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         end("flux_collide_kernel");
-        *launches += (h->n_reg > 0) + (h->n_nonreg > 0);
+        *launches += (h->n_reg > 0) + (h->n_nonreg > 0) + (h->n_r2 > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             begin();
             e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
@@ -707,6 +774,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
 int run_steps(kg_handle* h, int32_t nsteps, double* device_ms, int64_t* launches_out) {
     int rc = rebuild(h);
     if (rc) return rc;
+    if (nsteps > 0 && has_lazy_slopes(h)) h->sdf_partial = true;   // the steps leave the lazy cells' sdf
     if (h->autotune && h->tuned_version != h->version) {
         rc = autotune_flux(h);
         if (rc) return rc;
@@ -789,6 +857,7 @@ int serve(kg_handle* h, int32_t n, const double* const* f_in, const double* cons
     if (!pb.live) { pb.live = true; h->dirty = true; }
     int rc = rebuild(h);
     if (rc) return rc;
+    if (nsteps > 0 && has_lazy_slopes(h)) h->sdf_partial = true;   // the steps leave the lazy cells' sdf
     if (h->autotune && h->tuned_version != h->version && (rc = autotune_flux(h))) return rc;
     if (pb.pp.dt != dt && (rc = set_prob_dt(h, 0, dt))) return rc;
     const Flat& L = pb.F;
@@ -998,12 +1067,18 @@ int upload_problem_state(kg_handle* h, int slot, const double* f, const double* 
 
 // Places a flattened problem into the pools (the merged topology is rebuilt before the
 // next step) and uploads its state.
+int complete_last_slopes(kg_handle* h);
 int place_problem(kg_handle* h, int slot, Flat&& F, const kg_params& prm, const double* f, const double* w,
                   const double* prim, double dt, int64_t step) {
     Problem& pb = h->probs[slot];
     const int64_t nf = F.foff.back();
     const int64_t nd = F.n_data;
     int64_t fb, db;
+    {
+        // the last step's slopes of the lazy cells of the live problems, before the layout changes
+        const int rc0 = complete_last_slopes(h);
+        if (rc0) return rc0;
+    }
     if (!h->fslab.alloc(nf, &fb)) return fail(h, KG_ERR_BUDGET, "f pool exhausted (admission refused by footprint)");
     if (!h->dslab.alloc(nd, &db)) { h->fslab.release(fb, nf); return fail(h, KG_ERR_BUDGET, "cell pool exhausted"); }
     pb.F = std::move(F);
@@ -1033,6 +1108,7 @@ int download_problem(kg_handle* h, int slot, double* f, double* w, double* prim,
         }
     }
     if (sdf) {
+        { const int rc2 = complete_last_slopes(h); if (rc2) return rc2; }
         const char* ssrc = (const char*)h->sdf + pb.fbase * D * ss;
         if (h->prm.precision == KG_PREC_FP64) {
             KG_CUDA(h, cudaMemcpyAsync(sdf, ssrc, sizeof(double) * nfc * D, cudaMemcpyDeviceToHost, h->stream));
@@ -1089,7 +1165,12 @@ int sync_point_rows(kg_handle* h, int slot, double* sw_host, double thr, double*
     // ps_adaptive_mesh_refinement! (Physical_space/AMR.jl:1108-1116) runs slope! on the current
     // f before update_criterion!; the next step recomputes the same slopes, so the state a step
     // sees is unchanged (in a batch the pass covers every live problem)
-    if (e == cudaSuccess && loh_host) e = enqueue_slopes(h, P, h->stream);
+    if (e == cudaSuccess && loh_host) e = enqueue_slopes_full(h, P, h->stream);
+    if (e == cudaSuccess && !loh_host) {
+        // sw of the slopes the last step used
+        const int rc2 = complete_last_slopes(h);
+        if (rc2) { cudaFree(d); return rc2; }
+    }
     if (e == cudaSuccess)
         e = dispatch(h, [&](auto L) { return decltype(L)::macro_slope(P, fb, n, (int)pb.dbase, dsw, h->stream); });
     if (e == cudaSuccess && loh_host)
@@ -1267,7 +1348,7 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
         Dev P = h->dev;
         P.f_in = h->parity == 0 ? h->fA : h->fB;
         P.f_out = h->parity == 0 ? h->fB : h->fA;
-        KG_CUDA(h, enqueue_slopes(h, P, h->stream));
+        KG_CUDA(h, enqueue_slopes_full(h, P, h->stream));
     }
     KG_CUDA(h, cudaStreamSynchronize(h->stream));
     clk.mark("adapt:slopes");
@@ -1522,6 +1603,9 @@ int vs_conserve(kg_handle* h, int slot, const uint8_t* cell_flags) {
 }
 
 int vs_flags(kg_handle* h, int slot, const kg_vs_config* cfg, uint8_t* flags, double* eta, double* vr_out) {
+    // the flags read the slopes the last step used
+    { int rc0 = rebuild(h); if (rc0) return rc0; }
+    { int rc0 = complete_last_slopes(h); if (rc0) return rc0; }
     const int D = h->prm.dim, NDF = h->prm.ndf;
     if (cfg->maxlevel < 0 || cfg->maxlevel > 12) return fail(h, KG_ERR_ARG, "maxlevel out of range");
     if (cfg->mode != KG_VS_LOHNER && cfg->mode != KG_VS_CONTRIBUTION) return fail(h, KG_ERR_ARG, "bad mode");
@@ -1697,6 +1781,7 @@ int kg_upload_topology(kg_handle* h, const kg_topology* topo) {
     pb.pp = params_of(h->prm, 0.0);
     pb.live = false;   // becomes live with its state
     h->have_state = false;
+    h->sdf_partial = false;
     h->dirty = true;
     return KG_OK;
 }
@@ -1715,6 +1800,7 @@ int kg_upload_state(kg_handle* h, const double* f, const double* w, const double
     int rc = upload_problem_state(h, 0, f, w, prim, 0);
     if (rc) return rc;
     h->have_state = true;
+    h->sdf_partial = false;   // a fresh state's slopes are zero
     return KG_OK;
 }
 
@@ -1780,6 +1866,7 @@ int kg_upload_restart(kg_handle* h, const int32_t* quad_index, int32_t n_quads, 
     int rc = upload_restart(h, 0, quad_index, n_quads, vs_df, ws, 0);
     if (rc) { if (!was_live) pb.live = false; return rc; }
     h->have_state = true;
+    h->sdf_partial = false;   // restart() builds its PsData with zero slopes
     return KG_OK;
 }
 
@@ -1876,6 +1963,18 @@ int kg_autotune(kg_handle* h, int enable) {
     return KG_OK;
 }
 
+int kg_fuse_slopes(kg_handle* h, int enable) {
+    if (!h) return KG_ERR_ARG;
+    if (h->fuse_off == (enable == 0)) return KG_OK;
+    cudaSetDevice(h->device);
+    // the last step's slopes complete under the current layout before it changes
+    int rc = complete_last_slopes(h);
+    if (rc) return rc;
+    h->fuse_off = enable == 0;
+    h->dirty = true;
+    return KG_OK;
+}
+
 int kg_autotune_result(const kg_handle* h, int32_t* schedule, int32_t* ctas_per_sm, double* trial_ms, int32_t cap) {
     if (!h) return KG_ERR_ARG;
     if (schedule) *schedule = h->sched;
@@ -1927,6 +2026,12 @@ int kg_batch_admit(kg_handle* h, const kg_params* params, const kg_topology* top
 }
 
 int kg_batch_release(kg_handle* h, int32_t slot) {
+    if (h && h->is_batch) {
+        // the last step's slopes of the lazy cells, while the layout still holds this problem
+        cudaSetDevice(h->device);
+        const int rc0 = complete_last_slopes(h);
+        if (rc0) return rc0;
+    }
     if (!h || !h->is_batch || slot < 0 || slot >= MAX_SLOTS || !h->probs[slot].live) return fail(h, KG_ERR_ARG, "bad slot");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
@@ -2043,7 +2148,7 @@ int kg_download_solution(kg_handle* h, const int32_t* quad_index, int32_t n_quad
     P.f_in = h->parity == 0 ? h->fA : h->fB;
     P.f_out = h->parity == 0 ? h->fB : h->fA;
     cudaStream_t s = h->stream;
-    cudaError_t e = enqueue_slopes(h, P, s);
+    cudaError_t e = enqueue_slopes_full(h, P, s);
     if (e == cudaSuccess && !M.solid_ops.empty())
         e = dispatch(h, [&](auto Lc) { return decltype(Lc)::solid(P, (int)M.solid_ops.size(), s); });
     if (e != cudaSuccess) return cuda_fail(h, e, "save_result: slopes and solid cells");

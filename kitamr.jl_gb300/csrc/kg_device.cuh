@@ -51,6 +51,7 @@ struct Dev {
     const int32_t* pass_cells;
     const int32_t* slope_items;        // (pass-cell entry, velocity chunk) per slope CTA
     int slope_split;                   // 0: one item per pass cell, item == pass-cell entry
+    int slope_chunk;                   // velocity cells per work item (SLOPE_CHUNK or a whole cell)
     const int32_t* cell_slope_op;
     const NbrRef* slope_nbr;
     // flux
@@ -58,6 +59,7 @@ struct Dev {
     const uint8_t* fluid_reg;          // per fluid cell: regular (fast path of the flux kernel)
     const FluxCell* fcrec;             // per fluid cell: its record
     const RegRec* regrec;              // per fluid cell: the faces of a regular cell
+    const R2Rec* r2rec;                // per fluid cell: R2 cells' neighbours of neighbours
     const SlopeCell* screc;            // per pass-cell entry: its record
     const CritOp* crit_ops;            // per fluid cell and direction (physical-space criterion)
     const int32_t* crit_nbr;

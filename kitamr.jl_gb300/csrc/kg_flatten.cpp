@@ -101,7 +101,7 @@ const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 // (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
 // cost more than filling ~20 MB of records.
 void reset(Flat& F) {
-    static_assert(sizeof(Flat) == 50 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    static_assert(sizeof(Flat) == 52 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
     F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
     F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
     F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
@@ -111,7 +111,7 @@ void reset(Flat& F) {
     F.p_off.clear(); F.p_j0.clear(); F.p_cnt.clear();
     F.pass_off.clear(); F.slope_ops.clear(); F.pass_cells_off.clear(); F.pass_cells.clear();
     F.cell_slope_op.clear(); F.slope_nbr.clear(); F.slope_items.clear(); F.pass_items_off.clear();
-    F.fluid_cells.clear(); F.fcrec.clear(); F.regrec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
+    F.fluid_cells.clear(); F.fcrec.clear(); F.regrec.clear(); F.fluid_r2.clear(); F.r2rec.clear(); F.screc.clear(); F.crit_ops.clear(); F.crit_nbr.clear();
     F.fluid_reg.clear();
     F.inc_off.clear(); F.inc.clear(); F.bc_prim.clear(); F.bc_hl.clear();
     F.solid_ops.clear(); F.wall_ops.clear(); F.ib_nbr.clear(); F.ib_dx.clear(); F.cut_idx.clear();
@@ -621,7 +621,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
     return KG_OK;
 }
 
-void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges) {
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges, bool fuse) {
     reset(M);
     if (parts.empty()) return;
     const int D = parts[0].F->dim;
@@ -764,6 +764,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
                     rr.sa[side] = a.sarea;
                     rr.dxm_f[side] = a.dxm_f[d];
                     rr.sa_f[side] = a.sarea_f;
+                    rr.nd[side] = a.other;
                 }
             }
             M.regrec.push_back(rr);
@@ -851,19 +852,76 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         c.regular = reg ? 1 : 0;
         M.screc[k] = c;
     }
+    // Slopes in the flux kernel (fuse: 2D layouts of the packed regular-cell kernel).  A
+    // regular cell whose own slopes and whose four neighbours' slopes are of the regular form
+    // (slope-regular, and the neighbours flux-regular: fluid cells on the same grid whose f
+    // nothing writes during a step) gets an R2Rec; one whose four neighbours all have one reads
+    // no sdf and no other cell reads its sdf in a step, so its slopes leave the passes (lazy
+    // items, computed only where a sync point reads the slopes).
+    M.fluid_r2.assign((size_t)M.n_fluid, 0);
+    M.r2rec.assign((size_t)M.n_fluid, R2Rec{});
+    if (fuse && D == 2) {
+        std::vector<int32_t> dsc((size_t)dcap, -1), dfl((size_t)dcap, -1);
+        for (size_t k = 0; k < M.pass_cells.size(); ++k) dsc[M.pass_cells[k]] = (int32_t)k;
+        for (int q = 0; q < M.n_fluid; ++q) dfl[M.fluid_cells[q]] = q;
+        auto slope_reg = [&](int32_t m) { return m >= 0 && m < dcap && dsc[m] >= 0 && M.screc[dsc[m]].regular; };
+        for (int q = 0; q < M.n_fluid; ++q) {
+            const int32_t m = M.fluid_cells[q];
+            if (!M.fluid_reg[q] || !slope_reg(m)) continue;
+            const RegRec& rr = M.regrec[q];
+            const SlopeCell& me = M.screc[dsc[m]];
+            bool ok = true;
+            for (int sd = 0; sd < 4 && ok; ++sd) {
+                const int32_t n = rr.nd[sd];
+                ok = n >= 0 && n < dcap && dfl[n] >= 0 && M.fluid_reg[dfl[n]] && slope_reg(n) && me.nfoff[sd] == rr.nfo[sd];
+            }
+            if (!ok) continue;
+            R2Rec r{};
+            for (int t = 0; t < 4; ++t) r.sinv[t] = me.inv_f[t];
+            for (int sd = 0; sd < 4; ++sd) {
+                const SlopeCell& nb = M.screc[dsc[rr.nd[sd]]];
+                for (int t = 0; t < 4; ++t) { r.nn[sd][t] = nb.nfoff[t]; r.ninv[sd][t] = nb.inv_f[t]; }
+            }
+            M.r2rec[q] = r;
+            M.fluid_r2[q] = 1;
+        }
+        for (int q = 0; q < M.n_fluid; ++q) {
+            if (!M.fluid_r2[q]) continue;
+            bool interior = true;
+            for (int sd = 0; sd < 4 && interior; ++sd) interior = M.fluid_r2[dfl[M.regrec[q].nd[sd]]] != 0;
+            if (interior) M.fluid_r2[q] = 2;
+        }
+    }
     // work items of the slope passes: when some grid exceeds two chunks, a pass cell per
     // SLOPE_CHUNK velocity cells (large 3D grids: fewer cells than resident CTAs per level);
-    // otherwise one item per pass cell, in order, and the kernel indexes directly
+    // otherwise one item per pass cell (the kernel indexes the pass cells directly when every
+    // pass cell has its item in order, i.e. without lazy items)
     bool split = false;
     for (int32_t m : M.pass_cells) split |= M.dnv[m] > 2 * SLOPE_CHUNK;
+    std::vector<uint8_t> lazy(M.pass_cells.size(), 0);
+    if (fuse && D == 2) {
+        std::vector<int32_t> dfl((size_t)dcap, -1);
+        for (int q = 0; q < M.n_fluid; ++q) dfl[M.fluid_cells[q]] = q;
+        for (size_t k = 0; k < M.pass_cells.size(); ++k) {
+            const int32_t q = dfl[M.pass_cells[k]];
+            lazy[k] = q >= 0 && M.fluid_r2[q] == 2;
+        }
+    }
     M.pass_items_off.push_back(0);
     for (size_t ps = 0; ps + 1 < M.pass_cells_off.size(); ++ps) {
         for (int32_t k = M.pass_cells_off[ps]; k < M.pass_cells_off[ps + 1]; ++k) {
+            if (lazy[k]) continue;
             const int nch = split ? (M.dnv[M.pass_cells[k]] + SLOPE_CHUNK - 1) / SLOPE_CHUNK : 1;
             for (int c = 0; c < nch; ++c) { M.slope_items.push_back(k); M.slope_items.push_back(c); }
         }
         M.pass_items_off.push_back((int32_t)(M.slope_items.size() / 2));
     }
+    for (size_t k = 0; k < M.pass_cells.size(); ++k) {
+        if (!lazy[k]) continue;
+        const int nch = split ? (M.dnv[M.pass_cells[k]] + SLOPE_CHUNK - 1) / SLOPE_CHUNK : 1;
+        for (int c = 0; c < nch; ++c) { M.slope_items.push_back((int32_t)k); M.slope_items.push_back(c); }
+    }
+    M.pass_items_off.push_back((int32_t)(M.slope_items.size() / 2));
     if (M.p_j0.empty()) { M.p_j0.push_back(0); M.p_cnt.push_back(0); }
 }
 

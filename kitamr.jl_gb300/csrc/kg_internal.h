@@ -109,6 +109,18 @@ struct RegRec {
     int64_t nfo[2 * MAXD];
     double dxm[2 * MAXD], sa[2 * MAXD];
     float dxm_f[2 * MAXD], sa_f[2 * MAXD];
+    int32_t nd[2 * MAXD];   // the neighbours' data indices
+};
+
+// A regular 2D cell whose four neighbours are regular too, in the slope sense as well: the
+// flux kernel computes its own slopes and its neighbours' from f (the regular slope formula,
+// the same bits as slope_kernel), so neither reads nor needs sdf.  Per side s of the cell
+// (2 * dir + (face at +ds/2)): that neighbour's own four neighbours (f offsets, by its sides)
+// and its slope factors; the cell's own slope factors.
+struct R2Rec {
+    int64_t nn[4][4];
+    float ninv[4][4];
+    float sinv[4];
 };
 
 // ---- immersed boundary ----------------------------------------------------
@@ -175,12 +187,18 @@ struct Flat {
     std::vector<int32_t> pass_cells;
     std::vector<int32_t> cell_slope_op;   // per pass-cell entry: first op index (dim ops each)
     std::vector<int32_t> slope_items;     // merged layout: (pass-cell entry, velocity chunk) pairs
-    std::vector<int32_t> pass_items_off;  // merged layout: per pass its items (one CTA each)
+    std::vector<int32_t> pass_items_off;  // merged layout: per pass its items (one CTA each), then
+                                          // one entry more: the end of the lazy items (the slopes a
+                                          // step does not need, computed only at sync points)
     std::vector<NbrRef> slope_nbr;
     // flux incidences, per fluid cell
     std::vector<int32_t> fluid_cells;     // fluid cell ids (bound_enc >= 0), flux/collide order
     std::vector<FluxCell> fcrec;          // merged layout only: per fluid cell
     std::vector<RegRec> regrec;           // merged layout only: per fluid cell (regular ones filled)
+    std::vector<uint8_t> fluid_r2;        // merged layout only: per fluid cell, 1 = slopes computed in
+                                          // the flux kernel (R2Rec), 2 = besides, no other cell reads its
+                                          // slopes in a step (they leave the slope passes: lazy items)
+    std::vector<R2Rec> r2rec;             // merged layout only: per fluid cell (fluid_r2 > 0 filled)
     std::vector<SlopeCell> screc;         // merged layout only: per pass-cell entry
     std::vector<CritOp> crit_ops;         // per fluid cell and direction (fluid-list order)
     std::vector<int32_t> crit_nbr;        // their neighbour lists (data indices)
@@ -257,7 +275,8 @@ struct Part {
 };
 // Concatenates the parts into one gather form whose data indices are pool positions
 // (dcap slots); fills the fluid range of every part into `ranges` (begin, end pairs).
-void merge(const std::vector<Part>& parts, int32_t dcap, Flat& out, std::vector<int32_t>& ranges);
+// fuse: 2D layouts of the packed regular-cell kernel, which computes the slopes of its R2 cells
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& out, std::vector<int32_t>& ranges, bool fuse);
 int64_t device_bytes(const Flat& f, int precision);
 
 }  // namespace kg

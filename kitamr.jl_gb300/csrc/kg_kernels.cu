@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
     int pc = item_base + blockIdx.x, v0 = 0;
     if (P.slope_split) {
         pc = P.slope_items[2 * pc];
-        v0 = P.slope_items[2 * (item_base + blockIdx.x) + 1] * SLOPE_CHUNK;
+        v0 = P.slope_items[2 * (item_base + blockIdx.x) + 1] * P.slope_chunk;
     }
     const SlopeCell& SC = P.screc[pc];
     if (SC.regular) {
@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
         // resolved.  Several velocity cells per thread and pass: all their loads are issued
         // before any store, so each thread keeps that many sets of loads in flight.
         const int nv = SC.nv;
-        const int v1 = P.slope_split ? min(nv, v0 + SLOPE_CHUNK) : nv;
+        const int v1 = P.slope_split ? (int)min((int64_t)nv, (int64_t)v0 + P.slope_chunk) : nv;
         const T* fcell = (const T*)P.f_in + SC.foff;
         T* scell = (T*)P.sdf + SC.foff * D;
         if (threadIdx.x < NDF) prefetch_l2(fcell + (int64_t)threadIdx.x * nv + v0, sizeof(T) * (size_t)(v1 - v0));
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
         snb[e] = c;
     }
     __syncthreads();
-    const int v1 = P.slope_split ? min(nv, v0 + SLOPE_CHUNK) : nv;
+    const int v1 = P.slope_split ? (int)min((int64_t)nv, (int64_t)v0 + P.slope_chunk) : nv;
     for (int i = v0 + threadIdx.x; i < v1; i += NT) {
         const int li = P.vlev[g.goff + i];
         A fc[NDF];
@@ -1539,6 +1539,7 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 
 // ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
 constexpr int PACKED_VPT = 2;   // velocity cells per thread and gather pass
+constexpr int R2_VPT = 1;       // the same for the kernel that computes the slopes (more loads a cell)
 // Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
 // thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
 // velocity cell through the reconstruction, the fluxes, the correction and the relaxation, and
@@ -1561,7 +1562,13 @@ __device__ __forceinline__ float2 pp_theta2(float2 f, float2 s0, float2 s1, floa
     return make_float2(fminf(fabsf(__fdividef(num.x, den.x)), 1.f), fminf(fabsf(__fdividef(num.y, den.y)), 1.f));
 }
 
-template <int NT, int VPT>
+// minmod of each lane, and the regular slope (f - f_n) inv of a pair (slope_kernel's arithmetic:
+// the same bits)
+__device__ __forceinline__ float2 minmod2(float2 a, float2 b) { return make_float2(minmod(a.x, b.x), minmod(a.y, b.y)); }
+__device__ __forceinline__ float2 dslope2(float2 f, float2 fn, float inv) { return mul2(fma2(fn, bc2(-1.f), f), bc2(inv)); }
+
+// R2: the cell's slopes and its upwind neighbours' are computed here from f (R2Rec), so no sdf is read
+template <int NT, int VPT, bool R2>
 __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx) {
     constexpr int D = 2;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -1589,6 +1596,17 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     // dxm and area factor (registers)
     const RegRec& RR = P.regrec[fcx];
     if (threadIdx.x < 4) nfo[threadIdx.x] = RR.nfo[threadIdx.x];
+    // R2: the neighbours' neighbours and slope factors, and the cell's own slope factors
+    __shared__ int64_t snn[R2 ? 16 : 1];
+    __shared__ float sninv[R2 ? 16 : 1], ssinv[R2 ? 4 : 1];
+    if constexpr (R2) {
+        const R2Rec& Q = P.r2rec[fcx];
+        if (threadIdx.x < 16) {
+            snn[threadIdx.x] = Q.nn[threadIdx.x / 4][threadIdx.x % 4];
+            sninv[threadIdx.x] = Q.ninv[threadIdx.x / 4][threadIdx.x % 4];
+        }
+        if (threadIdx.x < 4) ssinv[threadIdx.x] = Q.sinv[threadIdx.x];
+    }
     float rdm[4], rsa[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) { rdm[q] = RR.dxm_f[q]; rsa[q] = RR.sa_f[q]; }
@@ -1612,18 +1630,59 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     auto gather = [&](int i, const float4& V, float2& f2, float2& acc) {
         const float u0 = V.x, u1 = V.y;
         f2 = make_float2(fc[i], fc[nv + i]);
-        const float2 s0 = make_float2(scl[i], scl[nv + i]);
-        const float2 s1 = make_float2(scl[2 * nv + i], scl[3 * nv + i]);
-        float2 g2[D], t0[D], t1[D];
+        float2 s0, s1, g2[D], t0[D], t1[D];
+        if constexpr (R2) {
+            // f of the four neighbours and, per direction, of the upwind neighbour's other
+            // neighbours (along the direction the far one, across it both); the slopes follow
+            float2 fn[4];
 #pragma unroll
-        for (int d = 0; d < D; ++d) {
-            const bool pos = (d == 0 ? u0 : u1) > 0.f;
-            const int64_t no = nfo[2 * d + (pos ? 0 : 1)];
-            const float* of = fbase + no;
-            const float* os = sbase + no * D;
-            g2[d] = make_float2(of[i], of[nv + i]);
-            t0[d] = make_float2(os[i], os[nv + i]);
-            t1[d] = make_float2(os[2 * nv + i], os[3 * nv + i]);
+            for (int q = 0; q < 4; ++q) {
+                const float* o = fbase + nfo[q];
+                fn[q] = make_float2(o[i], o[nv + i]);
+            }
+            float2 ffar[D], fxa[D], fxb[D];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const bool pos = (d == 0 ? u0 : u1) > 0.f;
+                const int su = 2 * d + (pos ? 0 : 1);
+                const int e = 1 - d;   // the direction across
+                const float* oa = fbase + snn[4 * su + su];
+                const float* ob = fbase + snn[4 * su + 2 * e];
+                const float* oc = fbase + snn[4 * su + 2 * e + 1];
+                ffar[d] = make_float2(oa[i], oa[nv + i]);
+                fxa[d] = make_float2(ob[i], ob[nv + i]);
+                fxb[d] = make_float2(oc[i], oc[nv + i]);
+            }
+            s0 = minmod2(dslope2(f2, fn[0], ssinv[0]), dslope2(f2, fn[1], ssinv[1]));
+            s1 = minmod2(dslope2(f2, fn[2], ssinv[2]), dslope2(f2, fn[3], ssinv[3]));
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const bool pos = (d == 0 ? u0 : u1) > 0.f;
+                const int su = 2 * d + (pos ? 0 : 1);
+                const int e = 1 - d;
+                const float2 gn = fn[su];
+                g2[d] = gn;
+                // along d: the neighbour's far side is side su, the cell itself the other
+                const float2 fa = (su & 1) ? f2 : ffar[d];
+                const float2 fb = (su & 1) ? ffar[d] : f2;
+                const float2 sd = minmod2(dslope2(gn, fa, sninv[4 * su + 2 * d]), dslope2(gn, fb, sninv[4 * su + 2 * d + 1]));
+                const float2 se = minmod2(dslope2(gn, fxa[d], sninv[4 * su + 2 * e]), dslope2(gn, fxb[d], sninv[4 * su + 2 * e + 1]));
+                t0[d] = d == 0 ? sd : se;
+                t1[d] = d == 0 ? se : sd;
+            }
+        } else {
+            s0 = make_float2(scl[i], scl[nv + i]);
+            s1 = make_float2(scl[2 * nv + i], scl[3 * nv + i]);
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+                const bool pos = (d == 0 ? u0 : u1) > 0.f;
+                const int64_t no = nfo[2 * d + (pos ? 0 : 1)];
+                const float* of = fbase + no;
+                const float* os = sbase + no * D;
+                g2[d] = make_float2(of[i], of[nv + i]);
+                t0[d] = make_float2(os[i], os[nv + i]);
+                t1[d] = make_float2(os[2 * nv + i], os[3 * nv + i]);
+            }
         }
         const float2 th = pp_theta2(f2, s0, s1, ds0, ds1);
         acc = bc2(0.f);
@@ -1791,9 +1850,9 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
 }
 // VPT velocity cells per thread and pass of the gather (their loads in flight together);
 // more registers, so fewer resident CTAs
-template <int NT, int VPT>
-__global__ void __launch_bounds__(NT, (VPT == 1 ? 4 : 3) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
-    flux_regular_packed<NT, VPT>(P, list[blockIdx.x]);
+template <int NT, int VPT, bool R2>
+__global__ void __launch_bounds__(NT, (VPT == 1 && !R2 ? 4 : 3) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
+    flux_regular_packed<NT, VPT, R2>(P, list[blockIdx.x]);
 }
 
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
@@ -2815,12 +2874,28 @@ struct Launch {
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             // the packed-FP32 kernel (its convected f always in shared memory)
             if (!P.fst_global && P.marching != KG_MARCH_CIP)
-                fn = P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT> : flux_packed_kernel<BLOCK, PACKED_VPT>;
+                fn = P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT, false> : flux_packed_kernel<BLOCK, PACKED_VPT, false>;
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         fn<<<n, nt, smem, s>>>(P, list);
         return cudaGetLastError();
+    }
+    // the packed kernel of the R2 cells (slopes from f), one CTA per listed entry
+    static cudaError_t flux_r2_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
+            using A = typename Arith<T>::type;
+            size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, 0);
+            const int nt = P.flux_nt == 128 ? 128 : BLOCK;
+            using RegFn = void (*)(Dev, const int32_t*);
+            RegFn fn = nt == 128 ? flux_packed_kernel<128, R2_VPT, true> : flux_packed_kernel<BLOCK, R2_VPT, true>;
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            fn<<<n, nt, smem, s>>>(P, list);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;   // R2 lists exist only for the 2D mixed form
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
     static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,

@@ -49,6 +49,7 @@ def load_library(path: Optional[str] = None):
     L.kg_batch_info.argtypes = [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i64)]
     L.kg_batch_set_dt.argtypes = [vp, i32, dbl]
     L.kg_autotune.argtypes = [vp, C.c_int]
+    L.kg_fuse_slopes.argtypes = [vp, C.c_int]
     L.kg_download_sw.argtypes = [vp, vp]
     L.kg_batch_download_sw.argtypes = [vp, i32, vp]
     L.kg_criterion.argtypes = [vp, dbl, vp]
@@ -74,7 +75,7 @@ EXPORTS = [
     "kg_step", "kg_profile_enable", "kg_profile_read", "kg_memory_footprint",
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
-    "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result",
+    "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result", "kg_fuse_slopes",
     "kg_download_sw", "kg_batch_download_sw", "kg_criterion", "kg_batch_criterion",
     "kg_adapt", "kg_batch_adapt", "kg_download_restart", "kg_upload_restart", "kg_batch_download_restart",
     "kg_download_solution",
@@ -267,6 +268,9 @@ class GpuStep:
     def autotune(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
 
+    def fuse_slopes(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_fuse_slopes(self.h, int(enable)))
+
     def autotune_result(self):
         return _autotune_result(self.L, self.h)
 
@@ -415,6 +419,9 @@ class GpuBatch:
 
     def autotune(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
+
+    def fuse_slopes(self, enable: bool = True):
+        _check(self.L, self.h, self.L.kg_fuse_slopes(self.h, int(enable)))
 
     def autotune_result(self):
         return _autotune_result(self.L, self.h)
