@@ -183,7 +183,7 @@ def run_single(args, mode, scale, rank, world, dist, e2e=True, march="caidvm"):
         mcode = {"caidvm": abi.KG_MARCH_CAIDVM, "cip": abi.KG_MARCH_CIP}[march]
         prm = abi.make_params(prob, precision=prec, st_check_interval=100, marching=mcode)
         g = GpuStep(prm, topo, device=dev)
-        g.fuse_slopes(getattr(args, "fuse", "on") == "on")
+        g.fuse_slopes(getattr(args, "fuse", "off") == "on")
         g.upload_state(state["f"], state["w"], state["prim"])
         # the timed call replays a CUDA graph of `steps` steps (captured by the last warm-up
         # call, outside the timed region): the same kernels, without per-launch host overhead
@@ -668,7 +668,7 @@ def main():
     ap.add_argument("--requests", type=int, default=64, help="serve: number of requests")
     ap.add_argument("--max-steps", type=int, default=20000, help="serve: step cap of a request")
     ap.add_argument("--forms", default="mixed,fp64", help="serve: precision forms to run (mixed, fp64)")
-    ap.add_argument("--fuse", default="on", choices=["on", "off"],
+    ap.add_argument("--fuse", default="off", choices=["on", "off"],
                     help="slopes of regular cells in the flux kernel (kg_fuse_slopes; the same results)")
     ap.add_argument("--march", default="caidvm", choices=["caidvm", "cip"],
                     help="single-problem modes: time marching (cip: CIP_Marching, meshes without walls)")

@@ -388,14 +388,15 @@ int kg_use_graph(kg_handle *h, int enable);
 int kg_autotune(kg_handle *h, int enable);
 int kg_autotune_result(const kg_handle *h, int32_t *schedule, int32_t *ctas_per_sm, double *trial_ms, int32_t cap);
 
-/* Slopes in the flux kernel (2D mixed form, CAIDVM or Euler marching; default on).  A regular
+/* Slopes in the flux kernel (2D mixed form, CAIDVM or Euler marching; default off).  A regular
  * cell whose four neighbours are regular has its slopes and its upwind neighbours' slopes
  * computed in the flux kernel from f (the slope passes' arithmetic, the same bits), so it reads
  * no sdf; when its neighbours are such cells too, no cell reads its slopes in a step and they
  * leave the slope passes (sdf of such cells is filled in only where a call reads the slopes:
  * kg_download_state's sdf, kg_download_sw, kg_vs_flags, or a call that recomputes them).
  * Off: every slope goes through the slope passes and sdf.  Results do not depend on the
- * setting; it exists for validation and timing.                                       */
+ * setting.  On moves less DRAM traffic per step but, on GB300, takes longer (the flux kernel
+ * issues more instructions and waits on longer chains of loads).                        */
 int kg_fuse_slopes(kg_handle *h, int enable);
 
 /* ---- batches --------------------------------------------------------------

@@ -186,9 +186,10 @@ struct kg_handle {
     int64_t pool_bytes = 0;
     // merged topology (rebuilt when membership changes)
     bool dirty = true;
-    // the fused slopes of the packed regular-cell kernel: off for a layout whose convected f
-    // cannot stay in shared memory (the packed kernel is not used there)
-    bool fuse_off = false;
+    // the slopes of R2 cells in the packed regular-cell kernel (kg_fuse_slopes; off by default:
+    // it moves less DRAM traffic but takes longer on GB300, the flux kernel being issue- and
+    // latency-bound rather than bandwidth-bound)
+    bool fuse_off = true;
     // the sdf of the lazy pass cells is the last step's only after enqueue_lazy_slopes ran on
     // the f that step read (set by every step of a layout with lazy items)
     bool sdf_partial = false;
