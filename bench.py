@@ -125,10 +125,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic_per_launch():
-    """dram bytes per flux_collide launch from the committed ncu summary (scaled to the
-    full workload there), or None."""
-    p = os.path.join(ROOT, "profiles", "flux_collide_kernel_cylinder.txt")
+def ncu_traffic_per_launch(kernel):
+    """dram bytes per launch of `kernel` on the full cylinder, from the committed ncu summary
+    (profiles/<kernel>_cylinder.txt), or None."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_cylinder.txt")
     if not os.path.exists(p):
         return None
     m = re.search(r"traffic_bytes_per_full_launch:\s*([0-9.eE+]+)", open(p).read())
@@ -302,18 +302,42 @@ def accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_
     return out
 
 
+FLUX_KERNELS = ("flux_packed_kernel", "flux_packed_kernel_r2", "flux_regular_kernel", "flux_collide_kernel")
+
+
 def roofline_of(kern, P, ndf, peak, peak_kind, traffic=None):
-    """Roofline of the flux kernel from its per-launch CUDA-event time: 2 * NDF * 4 B per phase
-    cell (one read, one write of f in FP32) over that time, against the measured HBM peak."""
-    if "flux_collide_kernel" not in kern:
+    """Roofline of the dominant flux kernel (the flux kernel with the largest device time) from
+    its per-launch CUDA-event time: 2 * NDF * 4 B per phase cell it processed (one read and one
+    write of f in FP32) over that time, against the measured HBM peak.  `flux_kernels` gives
+    the same per flux kernel, `flux_step` for all flux kernels of a step together (the
+    profiling pass launches them one after another)."""
+    fk = {k: v for k, v in kern.items() if k in FLUX_KERNELS and v[1] > 0}
+    if not fk:
         return None
-    ms, cnt = kern["flux_collide_kernel"]
+    if all(len(v) < 3 or v[2] == 0 for v in fk.values()):
+        # no per-kernel phase cells: all flux kernels over the problem's phase cells
+        ms = sum(v[0] for v in fk.values())
+        cnt = max(v[1] for v in fk.values())
+        fk = {"flux_collide_kernel": (ms, cnt, P * cnt)}
+    name = max(fk, key=lambda k: fk[k][0])
+    ms, cnt, units = fk[name][:3]
     avg_s = ms / cnt / 1e3
-    b_alg = 2 * ndf * 4 * P
+    b_alg = 2 * ndf * 4 * units / cnt
     ach = b_alg / avg_s / 1e9
+    per = {}
+    for k, v in fk.items():
+        lb = 2 * ndf * 4 * v[2] / v[1]
+        per[k] = {"launch_ms": v[0] / v[1], "phase_cells": int(v[2] // v[1]),
+                  "achieved": lb / (v[0] / v[1] / 1e3) / 1e9, "frac": lb / (v[0] / v[1] / 1e3) / 1e9 / peak}
+    steps = cnt
+    step_ms = sum(v[0] for v in fk.values()) / steps
+    step_b = 2 * ndf * 4 * sum(v[2] for v in fk.values()) / steps
     return {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-            "traffic": traffic, "kernel": "flux_collide_kernel", "peak_kind": peak_kind,
-            "algorithmic_bytes_per_launch": b_alg, "launch_ms": avg_s * 1e3}
+            "traffic": traffic, "kernel": name, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_launch": b_alg, "launch_ms": avg_s * 1e3, "flux_kernels": per,
+            "flux_step": {"ms": step_ms, "algorithmic_bytes": step_b,
+                          "achieved": step_b / (step_ms / 1e3) / 1e9,
+                          "frac": step_b / (step_ms / 1e3) / 1e9 / peak}}
 
 
 def batch_shapes():
@@ -643,7 +667,7 @@ def sub_single(args, mode, threads, acc_steps, oracle_steps, oracle_f=True):
            "value": res["mixed"]["value"], "unit": UNIT, "steps": a.steps,
            "ms_per_step": res["mixed"]["ms_per_step"],
            "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]},
-           "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+           "kernels_ms": {k: {"total_ms": v[0], "launches": v[1], "phase_cells": v[2]} for k, v in kern.items()},
            "roofline": roofline_of(kern, P, res["ndf"], peak, peak_kind), "gpu_launches": launches}
     rec["accuracy"] = accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_f=oracle_f)
     if oracle_steps == 0:
@@ -741,8 +765,9 @@ def main():
     peak, peak_kind = measured_peaks()
     mixed = res["mixed"]
     kern = mixed.get("kernels", {})
-    traffic = ncu_traffic_per_launch() if (args.mode == "cylinder" and args.scale == 1.0) else None
-    roof = roofline_of(kern, P, ndf, peak, peak_kind, traffic)
+    roof = roofline_of(kern, P, ndf, peak, peak_kind)
+    if roof and args.mode == "cylinder" and args.scale == 1.0:
+        roof["traffic"] = ncu_traffic_per_launch(roof["kernel"])
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
@@ -756,7 +781,7 @@ def main():
                    "parallelism": f"replicas{world}", "cuda_graph": True, "marching": args.march},
         "forms": {"mixed": {"value": mixed["value"], "ms_per_step": mixed["ms_per_step"]},
                   "fp64": {"value": res["fp64"]["value"], "ms_per_step": res["fp64"]["ms_per_step"]}},
-        "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+        "kernels_ms": {k: {"total_ms": v[0], "launches": v[1], "phase_cells": v[2]} for k, v in kern.items()},
         "roofline": roof,
         "e2e": mixed.get("e2e"),
         "gpu_launches": launches,

@@ -362,10 +362,13 @@ int kg_serve(kg_handle *h, int32_t n_requests, const double *const *f_in, const 
              kg_step_report *reports);
 
 /* Optional per-kernel device timing (CUDA events on the handle's stream).
- * kg_profile_read fills up to `cap` entries; names are static strings.       */
+ * kg_profile_read fills up to `cap` entries; names are static strings.
+ * kg_profile_units: per entry (same order) the phase cells its launches
+ * processed, summed over the launches (the flux kernels; 0 for the others). */
 int kg_profile_enable(kg_handle *h, int enable);
 int kg_profile_read(kg_handle *h, const char **names, double *total_ms, int64_t *launches,
                     int32_t cap, int32_t *count);
+int kg_profile_units(kg_handle *h, int64_t *units, int32_t cap, int32_t *count);
 
 /* Device bytes held by the handle, and the bytes a topology would need.     */
 int kg_memory_footprint(const kg_handle *h, int64_t *bytes);

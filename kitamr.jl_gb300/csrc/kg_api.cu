@@ -165,6 +165,7 @@ struct kg_handle {
     const int32_t* d_nonreg = nullptr; // every other entry
     const int32_t* d_r2 = nullptr;     // regular cells whose slopes the packed kernel computes
     int n_reg = 0, n_nonreg = 0, n_r2 = 0;
+    int64_t ph_reg = 0, ph_nonreg = 0, ph_r2 = 0;   // their phase cells (profile units)
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -211,6 +212,7 @@ struct kg_handle {
     std::vector<std::string> pnames;
     std::vector<double> pms;
     std::vector<int64_t> pcount;
+    std::vector<int64_t> punits;   // phase cells the entry's launches processed (flux kernels)
     std::vector<const char*> pname_ptrs;
     // flux schedule (autotuned): 0 one CTA per cell, 1 persistent in cell order,
     // 2 persistent with the largest velocity grids first
@@ -350,6 +352,7 @@ int prof_slot(kg_handle* h, const char* name) {
     h->pnames.push_back(name);
     h->pms.push_back(0.0);
     h->pcount.push_back(0);
+    h->punits.push_back(0);
     return (int)h->pnames.size() - 1;
 }
 
@@ -508,6 +511,14 @@ int rebuild(kg_handle* h) {
         h->n_reg = (int)reg.size();
         h->n_nonreg = (int)nonreg.size();
         h->n_r2 = (int)r2.size();
+        auto phase = [&](const std::vector<int32_t>& l) {
+            int64_t n = 0;
+            for (int32_t q : l) n += M.dnv[M.fluid_cells[q]];
+            return n;
+        };
+        h->ph_reg = phase(reg);
+        h->ph_nonreg = phase(nonreg);
+        h->ph_r2 = phase(r2);
         int r = upload_vec(h, reg, &h->d_reg);
         if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
         if (!r) r = upload_vec(h, r2, &h->d_r2);
@@ -548,17 +559,25 @@ int rebuild(kg_handle* h) {
 // The flux of every fluid cell: the regular cells on their own kernel (one CTA per cell), then
 // the others with one CTA per cell (schedule 0) or on persistent CTAs (1: natural order, 2:
 // largest velocity grids first).
-cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
+// The flux of the fluid cells by list: 0 the regular cells, 1 the R2 cells, 2 the others
+// (under the schedule `sched`).
+cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, int ctas, cudaStream_t s) {
     const Flat& F = h->M;
-    cudaError_t e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
-    if (e == cudaSuccess) e = dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
-    if (e != cudaSuccess || h->n_nonreg == 0) return e;
+    if (part == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+    if (part == 1) return dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
+    if (h->n_nonreg == 0) return cudaSuccess;
     if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, s); });
     int nsm = 0;
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
     int grid = std::max(1, std::min(h->n_nonreg, nsm * std::max(ctas, 1)));
     const int32_t* order = sched == 2 ? h->d_order : h->d_nonreg;
     return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, h->n_nonreg, F.max_nv, grid, h->d_counter, order, s); });
+}
+
+cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
+    cudaError_t e = cudaSuccess;
+    for (int part = 0; part < 3 && e == cudaSuccess; ++part) e = launch_flux_part(h, P, part, sched, ctas, s);
+    return e;
 }
 
 // Autotuner: times the flux schedules on the current layout and keeps the fastest.  Every
@@ -669,7 +688,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         cudaEventCreate(&e0); cudaEventCreate(&e1);
         cudaEventRecord(e0, s);
     };
-    auto end = [&](const char* name) {
+    auto end = [&](const char* name, int64_t units = 0) {
         if (!timed) return;
         cudaEventRecord(e1, s);
         cudaEventSynchronize(e1);
@@ -678,6 +697,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         int k = prof_slot(h, name);
         h->pms[k] += ms;
         h->pcount[k] += 1;
+        h->punits[k] += units;
         cudaEventDestroy(e0); cudaEventDestroy(e1);
     };
     cudaError_t e;
@@ -751,10 +771,21 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         ++*launches;
     }
     if (F.n_fluid > 0) {
-        begin();
-        e = launch_flux(h, P, h->sched, h->sched_ctas, s);
-        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
-        end("flux_collide_kernel");
+        // one timed span per flux kernel: the regular cells' kernel (the packed FP32 kernel in
+        // the 2D mixed form outside CIP marching), the R2 cells' and the other cells'
+        const bool packed = h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED && !P.fst_global &&
+                            h->prm.marching != KG_MARCH_CIP;
+        const char* names[3] = {packed ? "flux_packed_kernel" : "flux_regular_kernel", "flux_packed_kernel_r2",
+                                "flux_collide_kernel"};
+        const int counts[3] = {h->n_reg, h->n_r2, h->n_nonreg};
+        const int64_t units[3] = {h->ph_reg, h->ph_r2, h->ph_nonreg};
+        for (int part = 0; part < 3; ++part) {
+            if (counts[part] == 0) continue;
+            begin();
+            e = launch_flux_part(h, P, part, h->sched, h->sched_ctas, s);
+            if (e != cudaSuccess) return cuda_fail(h, e, names[part]);
+            end(names[part], units[part]);
+        }
         *launches += (h->n_reg > 0) + (h->n_nonreg > 0) + (h->n_r2 > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             begin();
@@ -1920,7 +1951,7 @@ int kg_serve(kg_handle* h, int32_t n_requests, const double* const* f_in, const 
 int kg_profile_enable(kg_handle* h, int enable) {
     if (!h) return KG_ERR_ARG;
     h->prof = enable != 0;
-    if (h->prof) { h->pnames.clear(); h->pms.clear(); h->pcount.clear(); }
+    if (h->prof) { h->pnames.clear(); h->pms.clear(); h->pcount.clear(); h->punits.clear(); }
     return KG_OK;
 }
 
@@ -1935,6 +1966,14 @@ int kg_profile_read(kg_handle* h, const char** names, double* total_ms, int64_t*
         if (launches) launches[i] = h->pcount[i];
     }
     *count = (int32_t)h->pnames.size();
+    return KG_OK;
+}
+
+int kg_profile_units(kg_handle* h, int64_t* units, int32_t cap, int32_t* count) {
+    if (!h || !count) return KG_ERR_ARG;
+    const int n = (int)std::min<size_t>(h->punits.size(), (size_t)std::max(cap, 0));
+    for (int i = 0; i < n && units; ++i) units[i] = h->punits[i];
+    *count = (int32_t)h->punits.size();
     return KG_OK;
 }
 

@@ -37,6 +37,7 @@ def load_library(path: Optional[str] = None):
     L.kg_step.argtypes = [vp, dbl, i64, i32, vp]
     L.kg_profile_enable.argtypes = [vp, C.c_int]
     L.kg_profile_read.argtypes = [vp, C.POINTER(C.c_char_p), C.POINTER(dbl), C.POINTER(i64), i32, C.POINTER(i32)]
+    L.kg_profile_units.argtypes = [vp, C.POINTER(i64), i32, C.POINTER(i32)]
     L.kg_memory_footprint.argtypes = [vp, C.POINTER(i64)]
     L.kg_topology_footprint.argtypes = [vp, vp, C.POINTER(i64)]
     L.kg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
@@ -70,9 +71,22 @@ def load_library(path: Optional[str] = None):
     return L
 
 
+def _profile_read(L, h):
+    cap = 32
+    names = (C.c_char_p * cap)()
+    ms = (C.c_double * cap)()
+    cnt = (C.c_int64 * cap)()
+    units = (C.c_int64 * cap)()
+    n = C.c_int32()
+    _check(L, h, L.kg_profile_read(h, names, ms, cnt, cap, C.byref(n)))
+    m = C.c_int32()
+    _check(L, h, L.kg_profile_units(h, units, cap, C.byref(m)))
+    return {names[i].decode(): (ms[i], cnt[i], units[i]) for i in range(min(n.value, cap))}
+
+
 EXPORTS = [
     "kg_create", "kg_destroy", "kg_upload_topology", "kg_upload_state", "kg_download_state",
-    "kg_step", "kg_profile_enable", "kg_profile_read", "kg_memory_footprint",
+    "kg_step", "kg_profile_enable", "kg_profile_read", "kg_profile_units", "kg_memory_footprint",
     "kg_topology_footprint", "kg_last_error", "kg_use_graph",
     "kg_batch_create", "kg_batch_admit", "kg_batch_release", "kg_batch_step", "kg_batch_download",
     "kg_batch_info", "kg_batch_set_dt", "kg_autotune", "kg_autotune_result", "kg_fuse_slopes",
@@ -275,13 +289,8 @@ class GpuStep:
         return _autotune_result(self.L, self.h)
 
     def profile_read(self):
-        cap = 16
-        names = (C.c_char_p * cap)()
-        ms = (C.c_double * cap)()
-        cnt = (C.c_int64 * cap)()
-        n = C.c_int32()
-        _check(self.L, self.h, self.L.kg_profile_read(self.h, names, ms, cnt, cap, C.byref(n)))
-        return {names[i].decode(): (ms[i], cnt[i]) for i in range(min(n.value, cap))}
+        """name -> (total ms, launches, phase cells processed) of the profiled launches."""
+        return _profile_read(self.L, self.h)
 
     def use_graph(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_use_graph(self.h, int(enable)))
@@ -409,13 +418,8 @@ class GpuBatch:
         _check(self.L, self.h, self.L.kg_profile_enable(self.h, int(enable)))
 
     def profile_read(self):
-        cap = 16
-        names = (C.c_char_p * cap)()
-        ms = (C.c_double * cap)()
-        cnt = (C.c_int64 * cap)()
-        n = C.c_int32()
-        _check(self.L, self.h, self.L.kg_profile_read(self.h, names, ms, cnt, cap, C.byref(n)))
-        return {names[i].decode(): (ms[i], cnt[i]) for i in range(min(n.value, cap))}
+        """name -> (total ms, launches, phase cells processed) of the profiled launches."""
+        return _profile_read(self.L, self.h)
 
     def autotune(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_autotune(self.h, int(enable)))
