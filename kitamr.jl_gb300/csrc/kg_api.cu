@@ -425,12 +425,6 @@ int rebuild(kg_handle* h) {
 #define UP(field, vec) do { int r__ = upload_vec(h, M.vec, &P.field); if (r__) return r__; } while (0)
         UP(g_off, g_off); UP(vlev, vlev); UP(vw, vw); UP(vu, vu);
         UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
-        if (!M.vpk.empty()) {
-            const float* vp = nullptr;
-            int r__ = upload_vec(h, M.vpk, &vp);
-            if (r__) return r__;
-            P.vpk = reinterpret_cast<const float4*>(vp);
-        }
         UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
         UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
         UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(slope_items, slope_items); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
@@ -676,29 +670,49 @@ int complete_last_slopes(kg_handle* h) {
     return KG_OK;
 }
 
+// Timed launches of a profiled step, added to the profile table when the step's work is done.
+struct ProfSpans {
+    kg_handle* h;
+    struct Span { const char* name; int64_t units; cudaEvent_t a, b; };
+    std::vector<Span> v;
+    ~ProfSpans() {
+        if (v.empty()) return;
+        cudaEventSynchronize(v.back().b);
+        for (const Span& x : v) {
+            float ms = 0.f;
+            if (cudaEventElapsedTime(&ms, x.a, x.b) == cudaSuccess) {
+                const int k = prof_slot(h, x.name);
+                h->pms[k] += ms;
+                h->pcount[k] += 1;
+                h->punits[k] += x.units;
+            }
+            cudaEventDestroy(x.a);
+            cudaEventDestroy(x.b);
+        }
+    }
+};
+
 int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
     Flat& F = h->M;
     Dev P = h->dev;
     P.f_in = h->parity == 0 ? h->fA : h->fB;
     P.f_out = h->parity == 0 ? h->fB : h->fA;
     cudaStream_t s = h->stream;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    // profiling: an event pair around each launch, read once the step's last launch is done
+    // (the kernels run back to back as in an unprofiled step; no host wait between them)
+    ProfSpans spans{h};
+    cudaEvent_t e0 = nullptr;
     auto begin = [&]() {
         if (!timed) return;
-        cudaEventCreate(&e0); cudaEventCreate(&e1);
+        cudaEventCreate(&e0);
         cudaEventRecord(e0, s);
     };
     auto end = [&](const char* name, int64_t units = 0) {
         if (!timed) return;
+        cudaEvent_t e1 = nullptr;
+        cudaEventCreate(&e1);
         cudaEventRecord(e1, s);
-        cudaEventSynchronize(e1);
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        int k = prof_slot(h, name);
-        h->pms[k] += ms;
-        h->pcount[k] += 1;
-        h->punits[k] += units;
-        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        spans.v.push_back({name, units, e0, e1});
     };
     cudaError_t e;
     int npass = n_slope_passes(F);

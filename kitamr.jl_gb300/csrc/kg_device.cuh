@@ -33,7 +33,6 @@ struct Dev {
     const float* ax_hi;                // ax_val as FP32 hi + lo
     const float* ax_lo;
     const uint16_t* vidx;
-    const float4* vpk;                 // 2D: ux, uy, weight, axis indices per velocity cell
     int max_axis;
     // data table
     const int64_t* foff;

@@ -101,11 +101,11 @@ const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 // (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
 // cost more than filling ~20 MB of records.
 void reset(Flat& F) {
-    static_assert(sizeof(Flat) == 52 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    static_assert(sizeof(Flat) == 51 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
     F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
     F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
     F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
-    F.ax_off.clear(); F.ax_val.clear(); F.ax_hi.clear(); F.ax_lo.clear(); F.vidx.clear(); F.vpk.clear();
+    F.ax_off.clear(); F.ax_val.clear(); F.ax_hi.clear(); F.ax_lo.clear(); F.vidx.clear();
     F.foff.clear(); F.dgrid.clear(); F.dbe.clear(); F.dinvv.clear(); F.dnv.clear(); F.dprob.clear();
     F.dmid.clear(); F.dds.clear();
     F.p_off.clear(); F.p_j0.clear(); F.p_cnt.clear();
@@ -457,6 +457,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         int here = t.face_here[fi];
         if (here < 0 || here >= NC || t.cell_bound_enc[here] < 0) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
         double rot = t.face_rot[fi], area = t.face_area[fi];
+        if (rot != 1.0 && rot != -1.0) { err = "face_rot must be +1 or -1"; return KG_ERR_TOPOLOGY; }
         for (int d = 0; d < D; ++d) { a.fmid[d] = t.face_midpoint[(size_t)fi * D + d]; a.my_mid[d] = t.cell_midpoint[(size_t)here * D + d]; }
         a.dir = (int8_t)dir;
         if (t.face_kind[fi] == KG_FACE_DOMAIN) {
@@ -797,18 +798,6 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         (void)sops;
     }
     M.ax_off.push_back((int32_t)M.ax_val.size());
-    if (D == 2) {
-        M.vpk.assign((size_t)4 * PGtot, 0.0f);
-        for (int64_t i = 0; i < PGtot; ++i) {
-            const uint32_t bits = (uint32_t)M.vidx[(size_t)i] | ((uint32_t)M.vidx[(size_t)PGtot + i] << 16);
-            float b;
-            std::memcpy(&b, &bits, sizeof b);
-            M.vpk[4 * i + 0] = M.vuf[(size_t)i];
-            M.vpk[4 * i + 1] = M.vuf[(size_t)PGtot + i];
-            M.vpk[4 * i + 2] = M.vwf[(size_t)i];
-            M.vpk[4 * i + 3] = b;
-        }
-    }
     // slope passes merged by their index relative to each problem's coarsest level
     M.pass_off.push_back(0);
     M.pass_cells_off.push_back(0);

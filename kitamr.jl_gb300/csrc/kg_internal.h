@@ -166,9 +166,6 @@ struct Flat {
     std::vector<double> ax_val;
     std::vector<float> ax_hi, ax_lo;   // ax_val = hi + lo in FP32 pairs (mixed form exponents)
     std::vector<uint16_t> vidx;   // [dim][P_g]
-    std::vector<float> vpk;       // merged 2D layouts: per velocity cell ux, uy, weight (FP32) and
-                                  // the bits of (axis index x) | (axis index y) << 16 -- one
-                                  // 16-byte load of what the regular-cell kernel needs of it
     int max_axis = 0;
     // data table
     std::vector<int64_t> foff;    // n_data + 1, element offsets (ndf * nv blocks)

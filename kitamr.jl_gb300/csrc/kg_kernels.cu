@@ -757,14 +757,16 @@ __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const double*
 }
 // Mixed form: FP32 tables whose exponents are formed in float-float arithmetic from the
 // FP32 hi + lo pairs of x, U and lam, so no FP64 instruction runs per entry.
-template <int D, int NT = BLOCK>
+// (entry a of axis d at E[(d * max_axis + a) * TS]: TS = 4 for the packed kernel's interleaved
+// table of (M_c, M_n, u) factors)
+template <int D, int NT = BLOCK, int TS = 1>
 __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const float* Uh, const float* Ul, float lh,
                                             float ll, float* E) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
         for (int a = threadIdx.x; a < na; a += NT)
-            E[d * P.max_axis + a] = exp_gauss_ff(P.ax_hi[a0 + a], P.ax_lo[a0 + a], Uh[d], Ul[d], lh, ll);
+            E[(d * P.max_axis + a) * TS] = exp_gauss_ff(P.ax_hi[a0 + a], P.ax_lo[a0 + a], Uh[d], Ul[d], lh, ll);
     }
 }
 
@@ -783,6 +785,12 @@ __device__ __forceinline__ void get_prim_r(const double* w, double gamma, double
 // dynamic shared memory of the flux kernel: convected f (unless it is staged in the cell's
 // output block), then the factor tables (two collision Maxwellians, or one per
 // Maxwellian-state domain face earlier in the step)
+// the packed kernel's dynamic shared memory: the convected (h, b) pairs, then (16-byte
+// aligned) the interleaved axis table of D * max_axis float4
+__host__ __device__ __forceinline__ size_t packed_table_off(int nv) { return ((size_t)8 * nv + 15) / 16 * 16; }
+__host__ __device__ __forceinline__ size_t packed_smem(int max_nv, int max_axis) {
+    return packed_table_off(max_nv) + (size_t)16 * 2 * max_axis;
+}
 template <int D, int NDF, typename A>
 __host__ __device__ __forceinline__ size_t flux_smem(int max_nv, int max_axis, int max_bcm, int fst_global) {
     return ((fst_global ? (size_t)0 : (size_t)NDF * max_nv) + (size_t)(max_bcm > 2 ? max_bcm : 2) * D * max_axis) * sizeof(A);
@@ -872,7 +880,9 @@ enum CellConst {
 // we (CIP marching, a donor cell): the moments of the SolidNeighbors' reconstruction
 // perturbance, which positivity_preserving_ib! (Boundary/Positivity.jl:1-43) adds to the
 // updated w with its limiter factor theta (left in sscal[2 * MAXW]); nullptr otherwise.
-template <int D, int NDF, typename A, int NT>
+// Ec: the factor tables of the two Maxwellians, M_c at Ec[(d * max_axis + a) * TS] and M_n
+// after them (TS = 1) or interleaved with them at + 1 (TS = 4, the packed kernel's table)
+template <int D, int NDF, typename A, int NT, int TS = 1>
 __device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot, const ProbParams& PP, double dt,
                                                double invV, const double (&red)[2 * (D + 2)], double* sscal, A* sc,
                                                A* Ec, int gid, const double* we = nullptr) {
@@ -983,15 +993,16 @@ __device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot,
         __syncthreads();
     }
     // factor tables of the two Maxwellians (discrete_maxwell, 2D2F.jl:1-21 / 3D1F.jl:1-23)
+    static_assert(TS == 1 || sizeof(A) == 4, "interleaved tables are FP32");
     const bool need_n = P.marching == KG_MARCH_CAIDVM;
-    A* En = Ec + (size_t)D * MA;
+    A* En = TS == 1 ? Ec + (size_t)D * MA : Ec + 1;
     if constexpr (sizeof(A) == 8) {
         gauss_table<D, NT>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
         if (need_n) gauss_table<D, NT>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
     } else {
-        gauss_table<D, NT>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
+        gauss_table<D, NT, TS>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
         if (need_n)
-            gauss_table<D, NT>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
+            gauss_table<D, NT, TS>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
     }
     __syncthreads();
 }
@@ -1610,15 +1621,31 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     float rdm[4], rsa[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) { rdm[q] = RR.dxm_f[q]; rsa[q] = RR.sa_f[q]; }
+    // per axis entry a of the grid: (M_c factor, M_n factor, u_d, -) in one 16-byte record, so
+    // a velocity's metadata is its two axis indices and its weight (8 bytes) and one shared
+    // load per axis (the u_d here are the FP32 velocities of the grid, bit for bit)
+    float2* fst = reinterpret_cast<float2*>(sh_raw);               // convected (h, b) per velocity
+    float4* T4 = reinterpret_cast<float4*>(sh_raw + packed_table_off(nv));
+    const int MA = P.max_axis;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        const int a0 = P.ax_off[FC.gid * MAXD + d], na = P.ax_off[FC.gid * MAXD + d + 1] - a0;
+        for (int a = threadIdx.x; a < na; a += NT) T4[d * MA + a].z = P.ax_hi[a0 + a];
+    }
     __syncthreads();
     const float s_dt = sc[C_SDT], adt = sc[C_ADT], ds0 = sc[C_DS0], ds1 = sc[C_DS0 + 1];
     const float* fbase = (const float*)P.f_in;
     const float* sbase = (const float*)P.sdf;
     const float* fc = fbase + FC.foff;
     const float* scl = sbase + FC.foff * D;
-    const float4* vp = P.vpk + FC.goff;
-    float2* fst = reinterpret_cast<float2*>(sh_raw);               // convected (h, b) per velocity
-    float* Ec = reinterpret_cast<float*>(sh_raw) + (size_t)2 * nv;  // factor tables (flux_smem)
+    const uint16_t* vxa = P.vidx + FC.goff;           // axis indices of the velocities
+    const uint16_t* vxb = P.vidx + P.PG + FC.goff;
+    const float* vwt = P.vwf + FC.goff;               // weights
+    // (u_x, u_y, weight, -) of velocity i
+    auto vel = [&](int i) {
+        const int ix = vxa[i], iy = vxb[i];
+        return make_float4(T4[ix].z, T4[MA + iy].z, vwt[i], 0.f);
+    };
     const bool caidvm = P.flux == KG_FLUX_CAIDVM;
     const bool march_caidvm = P.marching == KG_MARCH_CAIDVM;
 
@@ -1734,7 +1761,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         for (int v = 0; v < VPT; ++v) {
             iv[v] = i0 + v * NT;
             if (iv[v] >= nv) iv[v] = i0;    // a valid index for the loads; not finished
-            V[v] = vp[iv[v]];
+            V[v] = vel(iv[v]);
         }
 #pragma unroll
         for (int v = 0; v < VPT; ++v) gather(iv[v], V[v], f2[v], acc[v]);
@@ -1748,38 +1775,36 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         float hi[2 * (D + 2)] = {m0.x, m1.x, m2.x, mE.x, m0.y, m1.y, m2.y, mE.y};
         float lo[2 * (D + 2)] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         block_sum_ff<2 * (D + 2), NT>(hi, lo, red, sred);
-        cell_constants<D, 2, float, NT>(P, cell, slot, PP, dt, FC.invV, red, sscal, sc, Ec, FC.gid);
+        cell_constants<D, 2, float, NT, 4>(P, cell, slot, PP, dt, FC.invV, red, sscal, sc, &T4[0].x, FC.gid);
     }
-    const int MA = P.max_axis;
-    const float* En = Ec + (size_t)D * MA;
     const float prec = sc[C_PREC], pren = sc[C_PREN], bfc = sc[C_BFC], bfn = sc[C_BFN];
     const float Uh0 = sc[C_UH], Uh1 = sc[C_UH + 1], Ul0 = sc[C_UL], Ul1 = sc[C_UL + 1];
     // ---- 3. conservation correction f += M(prim_c) - M(prim) (CAIDVM marching) and q -------
     {
         float2 q2 = bc2(0.f);
+#pragma unroll 4
         for (int i = threadIdx.x; i < nv; i += NT) {
-            const float4 V = vp[i];
-            const uint32_t bits = __float_as_uint(V.w);
-            const int ix = (int)(bits & 0xffffu), iy = (int)(bits >> 16);
+            const int ix = vxa[i], iy = vxb[i];
+            const float4 ta = T4[ix], tb = T4[MA + iy];
             float2 fv;
             if (march_caidvm) {
                 float mc = prec;
-                mc *= Ec[ix];
-                mc *= Ec[MA + iy];
+                mc *= ta.x;
+                mc *= tb.x;
                 float mn = pren;
-                mn *= En[ix];
-                mn *= En[MA + iy];
+                mn *= ta.y;
+                mn *= tb.y;
                 const float2 fs = fst[i];
                 fv = make_float2(fs.x + (mc - mn), fs.y + (mc * bfc - mn * bfn));
                 fst[i] = fv;
             } else {
                 fv = make_float2(fc[i], fc[nv + i]);   // Euler: q of f before convection
             }
-            const float c0 = (V.x - Uh0) - Ul0, c1 = (V.y - Uh1) - Ul1;
+            const float c0 = (ta.z - Uh0) - Ul0, c1 = (tb.z - Uh1) - Ul1;
             float c2 = c0 * c0;
             c2 += c1 * c1;
             const float hb = c2 * fv.x + fv.y;
-            q2 = fma2(mul2(bc2(V.z), make_float2(c0, c1)), bc2(hb), q2);
+            q2 = fma2(mul2(bc2(vwt[i]), make_float2(c0, c1)), bc2(hb), q2);
         }
         float hi[D] = {q2.x, q2.y}, lo[D] = {0.f, 0.f};
         block_sum_ff<D, NT>(hi, lo, qv, sred);
@@ -1793,14 +1818,14 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         const float Kk = (float)PP.K;
         const float qa0 = sc[C_QA], qa1 = sc[C_QA + 1];
         float* fo = (float*)P.f_out + FC.foff;
+#pragma unroll 4
         for (int i = threadIdx.x; i < nv; i += NT) {
-            const float4 V = vp[i];
-            const uint32_t bits = __float_as_uint(V.w);
-            const int ix = (int)(bits & 0xffffu), iy = (int)(bits >> 16);
+            const int ix = vxa[i], iy = vxb[i];
+            const float4 ta = T4[ix], tb = T4[MA + iy];
             float mc = prec;
-            mc *= Ec[ix];
-            mc *= Ec[MA + iy];
-            const float c0 = (V.x - Uh0) - Ul0, c1 = (V.y - Uh1) - Ul1;
+            mc *= ta.x;
+            mc *= tb.x;
+            const float c0 = (ta.z - Uh0) - Ul0, c1 = (tb.z - Uh1) - Ul1;
             float c2 = c0 * c0;
             c2 += c1 * c1;
             float cq = c0 * qa0;
@@ -2873,8 +2898,10 @@ struct Launch {
                                                     : flux_regular_kernel<D, NDF, T, false, BLOCK>);
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             // the packed-FP32 kernel (its convected f always in shared memory)
-            if (!P.fst_global && P.marching != KG_MARCH_CIP)
+            if (!P.fst_global && P.marching != KG_MARCH_CIP) {
                 fn = P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT, false> : flux_packed_kernel<BLOCK, PACKED_VPT, false>;
+                smem = packed_smem(max_nv, P.max_axis);
+            }
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -2886,7 +2913,7 @@ struct Launch {
         if (n <= 0) return cudaSuccess;
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             using A = typename Arith<T>::type;
-            size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, 0);
+            const size_t smem = packed_smem(max_nv, P.max_axis);
             const int nt = P.flux_nt == 128 ? 128 : BLOCK;
             using RegFn = void (*)(Dev, const int32_t*);
             RegFn fn = nt == 128 ? flux_packed_kernel<128, R2_VPT, true> : flux_packed_kernel<BLOCK, R2_VPT, true>;
