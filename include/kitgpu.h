@@ -402,6 +402,22 @@ int kg_autotune_result(const kg_handle *h, int32_t *schedule, int32_t *ctas_per_
  * issues more instructions and waits on longer chains of loads).                        */
 int kg_fuse_slopes(kg_handle *h, int enable);
 
+/* Builder of the gather form of a single-problem handle: after kg_upload_topology and kg_adapt
+ * (amr_recover!'s rebuild of faces and neighbours, Solver/AMR.jl:54-70, from
+ * initialize_faces!, Solver/Initialize.jl:5-158) the slope operations and their neighbour
+ * lists, the slope-pass order, the criterion rows, the face incidences and the per-cell flux
+ * and slope records are built on the device (enable = 1, the default) or on the host (0).
+ * Both give the same arrays byte for byte (kg_layout_read); batch handles build on the host. */
+int kg_device_flatten(kg_handle *h, int enable);
+
+/* Test support: copies the named array of the gather form the next step reads ("slope_ops",
+ * "slope_nbr", "cell_slope_op", "pass_cells", "screc", "crit_ops", "crit_nbr", "inc_off",
+ * "inc", "bc_prim", "bc_hl", "fluid_cells", "fluid_reg", "fcrec", "regrec", "r2rec",
+ * "slope_items", "reg_list", "nonreg_list", "r2_list", "p_off", "p_j0", "p_cnt", "ib_nbr",
+ * "wall_ops", "solid_ops") into out, up to cap bytes; *bytes receives the array's size.
+ * No counterpart in the reference (it exposes its Julia objects instead).               */
+int kg_layout_read(kg_handle *h, const char *name, void *out, int64_t cap, int64_t *bytes);
+
 /* ---- batches --------------------------------------------------------------
  * Many independent problems (uneven cell and velocity counts, their own gas constants,
  * Δt and step counters) advanced together: every sub-step is one launch over all of

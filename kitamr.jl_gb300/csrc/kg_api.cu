@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -10,6 +11,7 @@
 #include <string>
 #include <vector>
 #include "kg_device.cuh"
+#include "kg_devflat.h"
 
 namespace kg {
 template <int D, int NDF, typename T> struct Launch {
@@ -146,6 +148,7 @@ struct RangeAlloc {
 struct Problem {
     bool live = false;
     Flat F;
+    DevLayout dl;                  // F.devlay: the step arrays built on the device
     int64_t fbase = 0, fsize = 0;
     int64_t dbase = 0, dsize = 0;
     ProbParams pp{};
@@ -200,6 +203,8 @@ struct kg_handle {
     // the read-only topology arrays of a layout in one allocation
     char* arena = nullptr;
     size_t arena_cap = 0, arena_used = 0;
+    char* upin = nullptr;          // pinned staging of the arena's upload
+    size_t upin_cap = 0;
     bool arena_measure = false;    // first pass: only sum the sizes
     Flat M;
     Flat spare;                    // a previous problem's arrays, reused by the next flattening
@@ -235,6 +240,23 @@ struct kg_handle {
     int g_nsteps = -1, g_parity = -1;
     int64_t g_version = -1;
     int64_t last_launches = 0;
+    // single-problem handles build the gather form after a topology upload or an adaptation on
+    // the device (kg_devflat.cu); kg_device_flatten(h, 0) selects the host builder
+    bool devflat = true;
+    DevScratch dscratch;
+    // a single handle's previous pools, kept after an adaptation moved the state out of them:
+    // the next adaptation that fits takes them instead of allocating (and freeing) pools
+    struct PoolSet {
+        std::vector<void*> allocs;
+        void *fA = nullptr, *fB = nullptr, *sdf = nullptr;
+        double *w = nullptr, *prim = nullptr, *qf = nullptr, *staging = nullptr;
+        ProbParams* d_probs = nullptr;
+        int64_t* d_step = nullptr;
+        int* d_status = nullptr;
+        double* res_out = nullptr;
+        int* d_counter = nullptr;
+        int64_t fcap = 0, dcap = 0, bytes = 0;
+    } spare_pools;
 };
 
 namespace {
@@ -254,27 +276,60 @@ int cuda_fail(kg_handle* h, cudaError_t e, const char* what) {
 
 size_t storage_size(const kg_handle* h) { return h->prm.precision == KG_PREC_FP64 ? sizeof(double) : sizeof(float); }
 
+// The read-only arrays of a layout go into one device arena in two passes: the first only sums
+// their sizes; the second copies each into a pinned staging block at its arena offset, and the
+// block goes to the device in one copy (upload_arena).
 template <typename V>
 int upload_vec(kg_handle* h, const std::vector<V>& v, const V** out) {
     size_t n = std::max<size_t>(v.size(), 1) * sizeof(V);
     const size_t n256 = (n + 255) / 256 * 256;
     if (h->arena_measure) { h->arena_used += n256; *out = nullptr; return KG_OK; }
-    void* p = nullptr;
-    if (h->arena && h->arena_used + n256 <= h->arena_cap) {
-        p = h->arena + h->arena_used;
-        h->arena_used += n256;
-    } else {
-        cudaError_t e = cudaMalloc(&p, n);
-        if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-        h->topo_allocs.push_back(p);
-        h->topo_bytes += (int64_t)n;
+    if (!h->arena || h->arena_used + n256 > h->arena_cap || h->upin_cap < h->arena_cap)
+        return fail(h, KG_ERR_ARG, "topology arena sized wrongly");
+    if (!v.empty()) std::memcpy(h->upin + h->arena_used, v.data(), v.size() * sizeof(V));
+    *out = (const V*)(h->arena + h->arena_used);
+    h->arena_used += n256;
+    return KG_OK;
+}
+// n bytes of the arena that a kernel fills (no upload)
+int arena_reserve(kg_handle* h, size_t n, void** out) {
+    const size_t n256 = (std::max<size_t>(n, 1) + 255) / 256 * 256;
+    if (h->arena_measure) { h->arena_used += n256; *out = nullptr; return KG_OK; }
+    if (!h->arena || h->arena_used + n256 > h->arena_cap) return fail(h, KG_ERR_ARG, "topology arena sized wrongly");
+    *out = h->arena + h->arena_used;
+    h->arena_used += n256;
+    return KG_OK;
+}
+// after the measuring pass: an arena (and pinned staging) of at least arena_used bytes, kept
+// from the last layout when large enough
+int size_arena(kg_handle* h) {
+    const size_t need = std::max<size_t>(h->arena_used, 256);
+    if (h->arena_cap < need) {
+        if (h->arena) cudaFree(h->arena);
+        h->arena = nullptr;
+        h->topo_bytes -= (int64_t)h->arena_cap;
+        h->arena_cap = 0;
+        const size_t cap = need + need / 8;
+        void* a = nullptr;
+        if (cudaMalloc(&a, cap) != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc topology");
+        h->arena = (char*)a;
+        h->arena_cap = cap;
+        h->topo_bytes += (int64_t)cap;
     }
-    if (!v.empty()) {
-        // on the handle's stream: a non-blocking stream is not ordered after the legacy one
-        cudaError_t e = cudaMemcpyAsync(p, v.data(), v.size() * sizeof(V), cudaMemcpyHostToDevice, h->stream);
-        if (e != cudaSuccess) return cuda_fail(h, e, "cudaMemcpyAsync topology");
+    if (h->upin_cap < h->arena_cap) {
+        if (h->upin) cudaFreeHost(h->upin);
+        h->upin = nullptr;
+        h->upin_cap = 0;
+        void* p = nullptr;
+        if (cudaMallocHost(&p, h->arena_cap) != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMallocHost topology staging");
+        h->upin = (char*)p;
+        h->upin_cap = h->arena_cap;
     }
-    *out = (const V*)p;
+    h->arena_used = 0;
+    return KG_OK;
+}
+int upload_arena(kg_handle* h) {
+    KG_CUDA(h, cudaMemcpyAsync(h->arena, h->upin, h->arena_used, cudaMemcpyHostToDevice, h->stream));
     return KG_OK;
 }
 int pool_alloc(kg_handle* h, size_t n, void** out) {
@@ -291,19 +346,26 @@ int pool_alloc(kg_handle* h, size_t n, void** out) {
     return KG_OK;
 }
 
-void free_topology(kg_handle* h) {
+// keep_arena: the next layout reuses the arena (and its staging) when large enough
+void free_topology(kg_handle* h, bool keep_arena = false) {
     if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
     h->g_nsteps = -1;
     for (void* p : h->topo_allocs) cudaFree(p);
     h->topo_allocs.clear();
-    h->topo_bytes = 0;
+    h->arena_used = 0;
+    if (keep_arena) return;
     if (h->arena) cudaFree(h->arena);
+    if (h->upin) cudaFreeHost(h->upin);
     h->arena = nullptr;
-    h->arena_cap = h->arena_used = 0;
+    h->upin = nullptr;
+    h->arena_cap = h->upin_cap = 0;
+    h->topo_bytes = 0;
 }
 
-void free_pools(kg_handle* h) {
-    free_topology(h);
+// keep_arena: new pools follow at once (make_pools, adopt_pools), so the topology arena and its
+// staging stay for the next layout
+void free_pools(kg_handle* h, bool keep_arena = false) {
+    free_topology(h, keep_arena);
     for (void* p : h->pool_allocs) cudaFree(p);
     h->pool_allocs.clear();
     h->pool_bytes = 0;
@@ -317,7 +379,7 @@ void free_pools(kg_handle* h) {
 
 // Pools for fcap f elements and dcap data slots.
 int make_pools(kg_handle* h, int64_t fcap, int64_t dcap) {
-    free_pools(h);
+    free_pools(h, true);
     const int D = h->prm.dim;
     size_t ss = storage_size(h);
     void* p;
@@ -344,6 +406,45 @@ int make_pools(kg_handle* h, int64_t fcap, int64_t dcap) {
     // state upload lands in the pools
     KG_CUDA(h, cudaStreamSynchronize(h->stream));
     return KG_OK;
+}
+
+// the handle's current pools as a set, and a set adopted as the current pools (no allocation,
+// no fill: an adaptation writes every data item of the new mesh before a step reads it)
+kg_handle::PoolSet take_pools(kg_handle* h) {
+    kg_handle::PoolSet ps;
+    ps.allocs.swap(h->pool_allocs);
+    ps.fA = h->fA; ps.fB = h->fB; ps.sdf = h->sdf;
+    ps.w = h->w; ps.prim = h->prim; ps.qf = h->qf; ps.staging = h->staging;
+    ps.d_probs = h->d_probs; ps.d_step = h->d_step; ps.d_status = h->d_status; ps.res_out = h->res_out;
+    ps.d_counter = h->d_counter;
+    ps.fcap = h->fcap; ps.dcap = h->dcap; ps.bytes = h->pool_bytes;
+    h->fA = h->fB = h->sdf = nullptr;
+    h->w = h->prim = h->qf = h->staging = nullptr;
+    h->pool_bytes = 0;
+    return ps;
+}
+int adopt_pools(kg_handle* h, kg_handle::PoolSet& ps) {
+    free_pools(h, true);
+    h->pool_allocs.swap(ps.allocs);
+    h->fA = ps.fA; h->fB = ps.fB; h->sdf = ps.sdf;
+    h->w = ps.w; h->prim = ps.prim; h->qf = ps.qf; h->staging = ps.staging;
+    h->d_probs = ps.d_probs; h->d_step = ps.d_step; h->d_status = ps.d_status; h->res_out = ps.res_out;
+    h->d_counter = ps.d_counter;
+    h->pool_bytes = ps.bytes;
+    h->fcap = ps.fcap; h->dcap = ps.dcap;
+    ps = kg_handle::PoolSet();
+    h->fslab.reset(h->fcap);
+    h->dslab.reset(h->dcap);
+    h->probs.assign(MAX_SLOTS, Problem());
+    h->parity = 0;
+    h->dirty = true;
+    KG_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int) * MAX_SLOTS, h->stream));
+    KG_CUDA(h, cudaMemsetAsync(h->d_step, 0, sizeof(int64_t) * MAX_SLOTS, h->stream));
+    return KG_OK;
+}
+void release_pools(kg_handle::PoolSet& ps) {
+    for (void* p : ps.allocs) cudaFree(p);
+    ps = kg_handle::PoolSet();
 }
 
 int prof_slot(kg_handle* h, const char* name) {
@@ -386,11 +487,90 @@ int set_prob_dt(kg_handle* h, int slot, double dt) {
     return KG_OK;
 }
 
+// Host wall time of the phases of a call, into the profile table when profiling is on.
+struct PhaseClock {
+    kg_handle* h;
+    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+    void mark(const char* name) {
+        if (!h->prof) return;
+        const auto n = std::chrono::steady_clock::now();
+        const int k = prof_slot(h, name);
+        h->pms[k] += std::chrono::duration<double, std::milli>(n - t).count();
+        h->pcount[k] += 1;
+        t = n;
+    }
+};
+
+// Bits of x (21 used) spread to every dim-th bit: one coordinate of a Morton key.
+uint64_t morton_spread(uint64_t x, int dim) {
+    uint64_t r = 0;
+    for (int b = 0; b < 21; ++b) r |= ((x >> b) & 1ull) << (dim * b);
+    return r;
+}
+
+// Launch order of a list of fluid-list entries: per problem, along a Morton curve through the
+// cells' midpoints, so that the cells a wave of CTAs advances together are neighbours in space
+// and read one another's f and sdf while those are still in L2.  Every cell writes only its
+// own data, so the order changes no result.
+void sfc_order(const Flat& M, std::vector<int32_t>& list) {
+    if (list.size() < 2) return;
+    const int D = M.dim;
+    struct Box { int slot; double lo[MAXD], h[MAXD]; };
+    std::vector<Box> box;   // per problem slot met (a few; searched from the last one found)
+    size_t last = 0;
+    auto find = [&](int slot) -> Box& {
+        if (last < box.size() && box[last].slot == slot) return box[last];
+        for (last = 0; last < box.size(); ++last)
+            if (box[last].slot == slot) return box[last];
+        Box b;
+        b.slot = slot;
+        for (int d = 0; d < MAXD; ++d) { b.lo[d] = 1e300; b.h[d] = 1e300; }
+        box.push_back(b);
+        last = box.size() - 1;
+        return box[last];
+    };
+    for (int32_t q : list) {
+        const int32_t m = M.fluid_cells[q];
+        Box& b = find(M.dprob[m]);
+        for (int d = 0; d < D; ++d) {
+            const double mid = M.dmid[(size_t)m * MAXD + d], ds = M.dds[(size_t)m * MAXD + d];
+            b.lo[d] = std::min(b.lo[d], mid - 0.5 * ds);
+            b.h[d] = std::min(b.h[d], ds);
+        }
+    }
+    struct Key { int slot; uint64_t key; int32_t q; };
+    std::vector<Key> keys;
+    keys.reserve(list.size());
+    for (int32_t q : list) {
+        const int32_t m = M.fluid_cells[q];
+        const Box& b = find(M.dprob[m]);
+        uint64_t k = 0;
+        for (int d = 0; d < D; ++d) {
+            const double x = std::floor((M.dmid[(size_t)m * MAXD + d] - b.lo[d]) / b.h[d]);
+            const uint64_t ix = (uint64_t)std::min(std::max(x, 0.0), 2097151.0);
+            k |= morton_spread(ix, D) << d;
+        }
+        keys.push_back(Key{M.dprob[m], k, q});
+    }
+    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
+        return a.slot != b.slot ? a.slot < b.slot : (a.key != b.key ? a.key < b.key : a.q < b.q);
+    });
+    for (size_t i = 0; i < list.size(); ++i) list[i] = keys[i].q;
+}
+
+// The gather form of a single handle's problem: on the device (kg_devflat.cu) unless the
+// host builder was selected; a batch handle's problems are always flattened on the host.
+int build_layout(kg_handle* h, const kg_topology& topo, int slot, Flat& F, DevLayout& dl, std::string& err) {
+    if (h->is_batch || !h->devflat) return flatten(h->prm, topo, F, err);
+    return device_flatten(h->prm, topo, slot, h->stream, F, dl, h->dscratch, err);
+}
+
 // Rebuilds the merged gather form of the live problems and uploads it.
 int rebuild(kg_handle* h) {
     if (!h->dirty) return KG_OK;
+    PhaseClock clk{h};
     cudaStreamSynchronize(h->stream);
-    free_topology(h);
+    free_topology(h, true);
     std::vector<Part> parts;
     h->live.clear();
     for (int s = 0; s < (int)h->probs.size(); ++s) {
@@ -401,8 +581,18 @@ int rebuild(kg_handle* h) {
     }
     std::vector<int32_t> ranges;
     const bool fuse = !h->fuse_off && h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED && h->prm.marching != KG_MARCH_CIP;
-    merge(parts, (int32_t)h->dcap, h->M, ranges, fuse);
+    // a single problem whose step arrays were built on the device: merge the host-side arrays,
+    // then its R2 records on the device and the slope work items
+    DevLayout* DL = (parts.size() == 1 && parts[0].F->devlay) ? &h->probs[parts[0].slot].dl : nullptr;
+    merge(parts, (int32_t)h->dcap, h->M, ranges, fuse, DL != nullptr);
     Flat& M = h->M;
+    if (DL) {
+        std::string err;
+        const int rc = device_r2(M, *DL, fuse, h->stream, M.fluid_r2, err);
+        if (rc) return fail(h, rc, err);
+        slope_items(M, (int32_t)h->dcap, fuse);
+    }
+    clk.mark("rebuild:merge");
     if (!parts.empty()) {
         if (M.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
         int dev_smem = 0;
@@ -416,6 +606,33 @@ int rebuild(kg_handle* h) {
         const size_t smax = std::max(sflux, swall);
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
     }
+    // the launch lists of the flux kernels: the cells that are not regular, largest velocity
+    // grids first (persistent schedule); the regular fluid cells (the regular-cell kernel; a
+    // regular cell never reads a solid cell or wall record), those whose slopes the packed
+    // kernel computes, and the others; each in space-filling-curve order
+    std::vector<int32_t> order, reg, nonreg, r2, all((size_t)M.n_fluid);
+    for (int q = 0; q < M.n_fluid; ++q) all[q] = q;
+    sfc_order(M, all);
+    for (int32_t q : all) {
+        if (!M.fluid_reg[q]) { nonreg.push_back(q); order.push_back(q); }
+        else if (M.fluid_r2[q]) r2.push_back(q);
+        else reg.push_back(q);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        return M.dnv[M.fluid_cells[x]] > M.dnv[M.fluid_cells[y]];
+    });
+    h->n_reg = (int)reg.size();
+    h->n_nonreg = (int)nonreg.size();
+    h->n_r2 = (int)r2.size();
+    auto phase = [&](const std::vector<int32_t>& l) {
+        int64_t n = 0;
+        for (int32_t q : l) n += M.dnv[M.fluid_cells[q]];
+        return n;
+    };
+    h->ph_reg = phase(reg);
+    h->ph_nonreg = phase(nonreg);
+    h->ph_r2 = phase(r2);
+    clk.mark("rebuild:lists");
     Dev& P = h->dev;
     P = Dev{};
     P.dim = h->prm.dim; P.ndf = h->prm.ndf; P.n_cells = M.n_cells; P.n_walls = M.n_walls;
@@ -427,26 +644,40 @@ int rebuild(kg_handle* h) {
         UP(vuf, vuf); UP(vwf, vwf); UP(ax_off, ax_off); UP(ax_val, ax_val); UP(ax_hi, ax_hi); UP(ax_lo, ax_lo); UP(vidx, vidx);
         UP(foff, foff); UP(dgrid, dgrid); UP(dbe, dbe); UP(dmid, dmid); UP(dds, dds); UP(dinvv, dinvv); UP(dnv, dnv); UP(dprob, dprob);
         UP(p_off, p_off); UP(p_j0, p_j0); UP(p_cnt, p_cnt);
-        UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(slope_items, slope_items); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
-        UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(regrec, regrec); UP(r2rec, r2rec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+        UP(slope_items, slope_items);
+        if (!DL) {
+            UP(slope_ops, slope_ops); UP(pass_cells, pass_cells); UP(cell_slope_op, cell_slope_op); UP(slope_nbr, slope_nbr);
+            UP(fluid_cells, fluid_cells); UP(fluid_reg, fluid_reg); UP(fcrec, fcrec); UP(regrec, regrec); UP(r2rec, r2rec); UP(screc, screc); UP(crit_ops, crit_ops); UP(crit_nbr, crit_nbr); UP(inc_off, inc_off); UP(inc, inc); UP(bc_prim, bc_prim); UP(bc_hl, bc_hl);
+        }
         UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
         UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
-        return KG_OK;
+        int r = upload_vec(h, order, &h->d_order);
+        if (!r) r = upload_vec(h, reg, &h->d_reg);
+        if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
+        if (!r) r = upload_vec(h, r2, &h->d_r2);
+        const int32_t* dlive = nullptr;
+        if (!r) r = upload_vec(h, h->live, &dlive);
+        h->d_live = const_cast<int32_t*>(dlive);
+        void* cr = nullptr;
+        if (!r) r = arena_reserve(h, sizeof(double) * std::max<int64_t>(M.n_fluid, 1) * 2 * MAXW, &cr);
+        P.cell_res = (double*)cr;
+        return r;
     };
     h->arena_measure = true;
     h->arena_used = 0;
     upload_all();
     h->arena_measure = false;
-    {
-        void* a = nullptr;
-        if (cudaMalloc(&a, h->arena_used) != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc topology");
-        h->arena = (char*)a;
-        h->arena_cap = h->arena_used;
-        h->topo_bytes += (int64_t)h->arena_cap;
-        h->arena_used = 0;
-    }
+    { int r = size_arena(h); if (r) return r; }
     { int r = upload_all(); if (r) return r; }
+    { int r = upload_arena(h); if (r) return r; }
+    clk.mark("rebuild:upload");
+    if (DL) {
+        P.slope_ops = DL->slope_ops; P.pass_cells = DL->pass_cells; P.cell_slope_op = DL->cell_slope_op;
+        P.slope_nbr = DL->slope_nbr; P.fluid_cells = DL->fluid_cells; P.fluid_reg = DL->fluid_reg; P.fcrec = DL->fcrec;
+        P.regrec = DL->regrec; P.r2rec = DL->r2rec; P.screc = DL->screc; P.crit_ops = DL->crit_ops; P.crit_nbr = DL->crit_nbr;
+        P.inc_off = DL->inc_off; P.inc = DL->inc; P.bc_prim = DL->bc_prim; P.bc_hl = DL->bc_hl;
+    }
     P.max_axis = M.max_axis;
     P.max_bcm = M.max_bcm;
     {
@@ -481,53 +712,6 @@ int rebuild(kg_handle* h) {
         P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
     }
 
-    {
-        // the cells that are not regular, largest velocity grids first (persistent schedule)
-        std::vector<int32_t> order;
-        for (int q = 0; q < M.n_fluid; ++q)
-            if (!M.fluid_reg[q]) order.push_back(q);
-        std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
-            return M.dnv[M.fluid_cells[a]] > M.dnv[M.fluid_cells[b]];
-        });
-        int r = upload_vec(h, order, &h->d_order);
-        if (r) return r;
-    }
-    {
-        // the regular fluid cells (the regular-cell flux kernel; a regular cell never reads a
-        // solid cell or wall record) and the others
-        // (the regular cells whose slopes the packed kernel computes form a list of their own)
-        std::vector<int32_t> reg, nonreg, r2;
-        for (int q = 0; q < M.n_fluid; ++q) {
-            if (!M.fluid_reg[q]) nonreg.push_back(q);
-            else if (M.fluid_r2[q]) r2.push_back(q);
-            else reg.push_back(q);
-        }
-        h->n_reg = (int)reg.size();
-        h->n_nonreg = (int)nonreg.size();
-        h->n_r2 = (int)r2.size();
-        auto phase = [&](const std::vector<int32_t>& l) {
-            int64_t n = 0;
-            for (int32_t q : l) n += M.dnv[M.fluid_cells[q]];
-            return n;
-        };
-        h->ph_reg = phase(reg);
-        h->ph_nonreg = phase(nonreg);
-        h->ph_r2 = phase(r2);
-        int r = upload_vec(h, reg, &h->d_reg);
-        if (!r) r = upload_vec(h, nonreg, &h->d_nonreg);
-        if (!r) r = upload_vec(h, r2, &h->d_r2);
-        if (r) return r;
-    }
-    const int32_t* dl;
-    { int r = upload_vec(h, h->live, &dl); if (r) return r; }
-    h->d_live = const_cast<int32_t*>(dl);
-    void* cr = nullptr;
-    size_t crn = sizeof(double) * std::max<int64_t>(M.n_fluid, 1) * 2 * MAXW;
-    cudaError_t e = cudaMalloc(&cr, crn);
-    if (e != cudaSuccess) return fail(h, KG_ERR_NOMEM, "cudaMalloc residual scratch");
-    h->topo_allocs.push_back(cr);
-    h->topo_bytes += (int64_t)crn;
-    P.cell_res = (double*)cr;
     // per-slot parameters with the fluid ranges of this layout
     std::vector<ProbParams> table(MAX_SLOTS);
     for (size_t q = 0; q < parts.size(); ++q) {
@@ -547,6 +731,7 @@ int rebuild(kg_handle* h) {
     P.flux = h->prm.flux; P.marching = h->prm.marching;
     h->dirty = false;
     h->version += 1;
+    clk.mark("rebuild:params");
     return KG_OK;
 }
 
@@ -1367,24 +1552,13 @@ int build_adapt_plan(kg_handle* h, const Flat& Fo, int64_t fbo, int64_t dbo, con
 // ones are filled.  Batch: the new slabs are placed beside the previous ones in the shared
 // pools, then the previous ones are released.
 // With profiling on, host wall time of the phases of an adaptation (ms, into the profile table).
-struct PhaseClock {
-    kg_handle* h;
-    std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
-    void mark(const char* name) {
-        if (!h->prof) return;
-        const auto n = std::chrono::steady_clock::now();
-        const int k = prof_slot(h, name);
-        h->pms[k] += std::chrono::duration<double, std::milli>(n - t).count();
-        h->pcount[k] += 1;
-        t = n;
-    }
-};
 
 int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adapt_src* src) {
     PhaseClock clk{h};
     Flat Fn = std::move(h->spare);
+    DevLayout dln;
     std::string err;
-    int rc = flatten(h->prm, *topo, Fn, err);
+    int rc = build_layout(h, *topo, slot, Fn, dln, err);
     clk.mark("adapt:flatten");
     if (rc) return fail(h, rc, err);
     if (Fn.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
@@ -1408,16 +1582,21 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     const void* of = h->parity == 0 ? h->fA : h->fB;
     const void* osdf = h->sdf;
     const double *ow = h->w, *oprim = h->prim, *oqf = h->qf;
-    std::vector<void*> old_pools;
+    kg_handle::PoolSet prev;
     const int64_t nf = Fn.foff.back(), nd = Fn.n_data;
     if (!h->is_batch) {
-        // hand the previous pools over to this call, then size new ones for the new mesh
-        old_pools.swap(h->pool_allocs);
-        h->pool_bytes = 0;
-        h->fA = h->fB = h->sdf = nullptr;
-        h->w = h->prim = h->qf = h->staging = nullptr;
-        rc = make_pools(h, nf, nd);   // clears the slot table
-        if (rc) { for (void* p : old_pools) cudaFree(p); return rc; }
+        // hand the previous pools over to this call, then take the spare pools of an earlier
+        // adaptation when they hold the new mesh, or new ones with room for a mesh an eighth
+        // larger (both clear the slot table)
+        prev = take_pools(h);
+        kg_handle::PoolSet& sp = h->spare_pools;
+        if (!sp.allocs.empty() && sp.fcap >= nf && sp.dcap >= nd) {
+            rc = adopt_pools(h, sp);
+        } else {
+            release_pools(sp);
+            rc = make_pools(h, nf + nf / 8, nd + nd / 8);
+        }
+        if (rc) { release_pools(prev); return rc; }
         Problem& pn = h->probs[slot];
         h->fslab.alloc(nf, &pn.fbase);
         h->dslab.alloc(nd, &pn.dbase);
@@ -1433,6 +1612,7 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     }
     Problem& pb = h->probs[slot];
     pb.F = std::move(Fn);
+    pb.dl = dln;
     pb.fsize = nf; pb.dsize = nd;
     pb.pp = old.pp;
     pb.live = true;
@@ -1478,7 +1658,9 @@ int adapt_problem(kg_handle* h, int slot, const kg_topology* topo, const kg_adap
     if (tab) cudaFree(tab);
     h->spare = std::move(old.F);
     if (!h->is_batch) {
-        for (void* p : old_pools) cudaFree(p);
+        // the previous pools become the spare set of the next adaptation
+        if (rc == KG_OK) h->spare_pools = std::move(prev);
+        else release_pools(prev);
         clk.mark("adapt:release");
         if (rc) { free_pools(h); return rc; }
         h->have_state = true;
@@ -1783,6 +1965,8 @@ int kg_destroy(kg_handle* h) {
     cudaStreamSynchronize(h->stream);
     cudaStreamSynchronize(h->aux);
     free_pools(h);
+    release_pools(h->spare_pools);
+    h->dscratch.release();
     if (h->d_tri) cudaFree(h->d_tri);
     if (h->sv_buf) cudaFree(h->sv_buf);
     if (h->s_in) { cudaStreamSynchronize(h->s_in); cudaStreamDestroy(h->s_in); }
@@ -1812,15 +1996,18 @@ int kg_upload_topology(kg_handle* h, const kg_topology* topo) {
     if (h->is_batch) return fail(h, KG_ERR_STATE, "a batch handle admits problems with kg_batch_admit");
     cudaSetDevice(h->device);
     cudaStreamSynchronize(h->stream);
+    release_pools(h->spare_pools);
     Flat F = std::move(h->spare);
+    DevLayout dl;
     std::string err;
-    int rc = flatten(h->prm, *topo, F, err);
+    int rc = build_layout(h, *topo, 0, F, dl, err);
     if (rc) { free_pools(h); return fail(h, rc, err); }
     if (!h->probs.empty()) h->spare = std::move(h->probs[0].F);
     if (F.max_inc > MAX_INC) { free_pools(h); return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported (" + std::to_string(F.max_inc) + ")"); }
     if ((rc = make_pools(h, F.foff.back(), F.n_data))) return rc;
     Problem& pb = h->probs[0];
     pb.F = std::move(F);
+    pb.dl = dl;
     pb.fbase = 0; pb.fsize = pb.F.foff.back(); pb.dbase = 0; pb.dsize = pb.F.n_data;
     h->fslab.alloc(pb.fsize, &pb.fbase);
     h->dslab.alloc(pb.dsize, &pb.dbase);
@@ -2014,6 +2201,61 @@ int kg_autotune(kg_handle* h, int enable) {
     h->autotune = enable != 0;
     h->tuned_version = -1;
     if (!h->autotune) { h->sched = 0; h->sched_ctas = 0; }
+    return KG_OK;
+}
+
+int kg_device_flatten(kg_handle* h, int enable) {
+    if (!h) return KG_ERR_ARG;
+    h->devflat = enable != 0;
+    return KG_OK;
+}
+
+int kg_layout_read(kg_handle* h, const char* name, void* out, int64_t cap, int64_t* bytes) {
+    if (!h || !name || !bytes) return fail(h, KG_ERR_ARG, "null argument");
+    cudaSetDevice(h->device);
+    int rc = rebuild(h);
+    if (rc) return rc;
+    const Flat& M = h->M;
+    const bool dl = h->live.size() == 1 && h->probs[h->live[0]].F.devlay;
+    const DevLayout* L = dl ? &h->probs[h->live[0]].dl : nullptr;
+    const Dev& P = h->dev;
+    const void* ptr = nullptr;
+    int64_t n = -1;
+#define LAY(nm, field, count) if (!std::strcmp(name, nm)) { ptr = P.field; n = (int64_t)(count) * (int64_t)sizeof(*P.field); }
+    LAY("slope_ops", slope_ops, L ? L->n_slope_ops : (int64_t)M.slope_ops.size());
+    LAY("slope_nbr", slope_nbr, L ? L->n_slope_nbr : (int64_t)M.slope_nbr.size());
+    LAY("cell_slope_op", cell_slope_op, L ? L->n_pass : (int64_t)M.cell_slope_op.size());
+    LAY("pass_cells", pass_cells, L ? L->n_pass : (int64_t)M.pass_cells.size());
+    LAY("screc", screc, L ? L->n_pass : (int64_t)M.screc.size());
+    LAY("crit_ops", crit_ops, L ? L->n_crit_ops : (int64_t)M.crit_ops.size());
+    LAY("crit_nbr", crit_nbr, L ? L->n_crit_nbr : (int64_t)M.crit_nbr.size());
+    LAY("inc_off", inc_off, L ? L->n_fluid + 1 : (int64_t)M.inc_off.size());
+    LAY("inc", inc, L ? L->n_inc : (int64_t)M.inc.size());
+    LAY("bc_prim", bc_prim, L ? L->n_bc * MAXW : (int64_t)M.bc_prim.size());
+    LAY("bc_hl", bc_hl, L ? L->n_bc * 2 * MAXW : (int64_t)M.bc_hl.size());
+    LAY("fluid_cells", fluid_cells, L ? L->n_fluid : (int64_t)M.fluid_cells.size());
+    LAY("fluid_reg", fluid_reg, L ? L->n_fluid : (int64_t)M.fluid_reg.size());
+    LAY("fcrec", fcrec, L ? L->n_fluid : (int64_t)M.fcrec.size());
+    LAY("regrec", regrec, L ? L->n_fluid : (int64_t)M.regrec.size());
+    LAY("r2rec", r2rec, L ? L->n_fluid : (int64_t)M.r2rec.size());
+    LAY("slope_items", slope_items, M.slope_items.size());
+    LAY("p_off", p_off, M.p_off.size());
+    LAY("p_j0", p_j0, M.p_j0.size());
+    LAY("p_cnt", p_cnt, M.p_cnt.size());
+    LAY("ib_nbr", ib_nbr, M.ib_nbr.size());
+    LAY("wall_ops", wall_ops, M.wall_ops.size());
+    LAY("solid_ops", solid_ops, M.solid_ops.size());
+#undef LAY
+    if (!std::strcmp(name, "reg_list")) { ptr = h->d_reg; n = (int64_t)h->n_reg * 4; }
+    if (!std::strcmp(name, "nonreg_list")) { ptr = h->d_nonreg; n = (int64_t)h->n_nonreg * 4; }
+    if (!std::strcmp(name, "r2_list")) { ptr = h->d_r2; n = (int64_t)h->n_r2 * 4; }
+    if (n < 0) return fail(h, KG_ERR_ARG, std::string("unknown layout array ") + name);
+    *bytes = n;
+    if (out && n > 0) {
+        if (cap < n) return fail(h, KG_ERR_ARG, "output buffer too small");
+        KG_CUDA(h, cudaMemcpyAsync(out, ptr, (size_t)n, cudaMemcpyDeviceToHost, h->stream));
+        KG_CUDA(h, cudaStreamSynchronize(h->stream));
+    }
     return KG_OK;
 }
 

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <set>
 #include <unordered_map>
 #include <utility>
 #include "kg_internal.h"
@@ -19,10 +20,8 @@ struct Ctx {
     const kg_topology* t;
     int D, NDF;
     Flat* F;
-    std::map<std::pair<int, int>, int> pairs;  // (my grid, other grid) -> id
+    PairIds* pid;
     std::string* err;
-    std::vector<int32_t> dense;                 // the same for up to 1024 grids: G x G, -3 unknown
-    int G = 0;
 };
 
 int grid_nv(const kg_topology& t, int g) { return (int)(t.grid_off[g + 1] - t.grid_off[g]); }
@@ -71,37 +70,93 @@ int data_of(const Ctx& c, int32_t r) {
     return c.t->n_cells + (-1 - r);
 }
 
+// the pairing id of (my grid ga <- its grid gb): -1 for the same grid (identity), -2 when the
+// canonical table has no such pair (a reference the pair scan did not see: a malformed list)
 int pairing(Ctx& c, int ga, int gb) {
     if (ga == gb) return -1;
-    int32_t* slot = c.dense.empty() ? nullptr : &c.dense[(size_t)ga * c.G + gb];
-    if (slot && *slot != -3) return *slot;
-    auto key = std::make_pair(ga, gb);
-    auto it = c.pairs.find(key);
-    if (it != c.pairs.end()) { if (slot) *slot = it->second; return it->second; }
-    const kg_topology& t = *c.t;
-    Flat& F = *c.F;
-    std::vector<int32_t> runs;
-    if (!level_runs(t.vs_level + t.grid_off[ga], grid_nv(t, ga), t.vs_level + t.grid_off[gb], grid_nv(t, gb), c.D, runs)) {
-        *c.err = "velocity grids do not tile the same root lattice";
-        return -2;
-    }
-    int id = (int)F.p_off.size() - 1;
-    for (size_t q = 0; q < runs.size(); q += 2) { F.p_j0.push_back(runs[q]); F.p_cnt.push_back(runs[q + 1]); }
-    F.p_off.push_back((int64_t)F.p_j0.size());
-    c.pairs[key] = id;
-    if (slot) *slot = id;
+    const int id = c.pid->find(ga, gb);
+    if (id < 0) { *c.err = "velocity pairing missing for a referenced grid pair"; return -2; }
     return id;
 }
 
 const double* dmid(const Ctx& c, int d) { return &c.F->dmid[(size_t)d * MAXD]; }
 
+
+// data index of a neighbour reference without a context
+int data_ref(const kg_topology& t, int32_t r) {
+    if (r == KG_NBR_NONE || r == KG_NBR_INSIDE) return -1;
+    if (r >= 0) return r < t.n_cells ? r : -1;
+    const int w = -1 - r;
+    return w < t.n_walls ? t.n_cells + w : -1;
+}
+
 }  // namespace
+
+int PairIds::find(int ga, int gb) const {
+    if (!dense.empty()) return dense[(size_t)ga * G + gb];
+    auto it = ids.find(std::make_pair(ga, gb));
+    return it == ids.end() ? -1 : it->second;
+}
+
+// The velocity pairings of a topology in one canonical order: every (my grid, its grid) pair,
+// in both directions, that a neighbour reference, an inner face or a wall record relates,
+// numbered by ascending (my grid, its grid).  The host and the device builders of the gather
+// form look pairings up here, so both give every reference the same id.
+int build_pairs(const kg_topology& t, Flat& F, PairIds& pid, std::string& err) {
+    const int G = t.n_grids, NC = t.n_cells, NF = 2 * t.dim;
+    pid.G = G;
+    std::vector<uint8_t> mark;
+    std::set<std::pair<int, int>> sp;
+    if (G <= 1024) mark.assign((size_t)G * G, 0);
+    auto add = [&](int ga, int gb) {
+        if (ga == gb) return;
+        if (!mark.empty()) { mark[(size_t)ga * G + gb] = 1; mark[(size_t)gb * G + ga] = 1; }
+        else { sp.insert(std::make_pair(ga, gb)); sp.insert(std::make_pair(gb, ga)); }
+    };
+    for (int i = 0; i < NC; ++i) {
+        const int gi = t.cell_grid[i];
+        for (int32_t r = t.nbr_off[i * NF]; r < t.nbr_off[(i + 1) * NF]; ++r) {
+            const int dn = data_ref(t, t.nbr_ref[r]);
+            if (dn >= 0) add(gi, F.dgrid[dn]);
+        }
+    }
+    for (int fi = 0; fi < t.n_faces; ++fi) {
+        if (t.face_kind[fi] == KG_FACE_DOMAIN) continue;
+        const int here = t.face_here[fi], od = data_ref(t, t.face_there[fi]);
+        if (here >= 0 && here < NC && od >= 0) add(t.cell_grid[here], F.dgrid[od]);
+    }
+    for (int w = 0; w < t.n_walls; ++w) add(t.cell_grid[t.wall_donor[w]], t.cell_grid[t.wall_solid[w]]);
+    std::vector<std::pair<int, int>> order;
+    if (!mark.empty()) {
+        for (int a = 0; a < G; ++a)
+            for (int b = 0; b < G; ++b)
+                if (mark[(size_t)a * G + b]) order.push_back(std::make_pair(a, b));
+        pid.dense.assign((size_t)G * G, -1);
+    } else {
+        order.assign(sp.begin(), sp.end());
+    }
+    F.p_off.assign(1, 0);
+    std::vector<int32_t> runs;
+    for (size_t q = 0; q < order.size(); ++q) {
+        const int ga = order[q].first, gb = order[q].second;
+        if (!level_runs(t.vs_level + t.grid_off[ga], grid_nv(t, ga), t.vs_level + t.grid_off[gb], grid_nv(t, gb), t.dim, runs)) {
+            err = "velocity grids do not tile the same root lattice";
+            return KG_ERR_TOPOLOGY;
+        }
+        for (size_t r = 0; r < runs.size(); r += 2) { F.p_j0.push_back(runs[r]); F.p_cnt.push_back(runs[r + 1]); }
+        F.p_off.push_back((int64_t)F.p_j0.size());
+        if (!pid.dense.empty()) pid.dense[(size_t)ga * G + gb] = (int32_t)q;
+        else pid.ids[order[q]] = (int)q;
+    }
+    return KG_OK;
+}
 
 // Empties a gather form but keeps the capacity of its arrays: rebuilding one of a similar size
 // (the next adaptation, the next merge) then touches no fresh pages, whose first-touch faults
 // cost more than filling ~20 MB of records.
 void reset(Flat& F) {
-    static_assert(sizeof(Flat) == 51 * sizeof(std::vector<int32_t>) + 56, "a Flat member was added or removed: reset it here");
+    static_assert(sizeof(Flat) == 51 * sizeof(std::vector<int32_t>) + 64, "a Flat member was added or removed: reset it here");
+    F.devlay = false;
     F.dim = 2; F.ndf = 2; F.n_cells = 0; F.n_walls = 0; F.n_data = 0; F.n_fluid = 0; F.phase_cells = 0;
     F.max_nv = 0; F.max_axis = 0; F.max_inc = 0; F.max_bcm = 0;
     F.g_off.clear(); F.vlev.clear(); F.vw.clear(); F.vu.clear(); F.vuf.clear(); F.vwf.clear();
@@ -118,8 +173,9 @@ void reset(Flat& F) {
     F.cut_gw.clear(); F.cut_sw.clear(); F.cvcw.clear();
 }
 
-int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& err) {
+int flatten_head(const kg_params& prm, const kg_topology& t, Flat& F, PairIds& pid, std::string& err) {
     reset(F);
+    pid.clear();
     if (t.dim != 2 && t.dim != 3) { err = "dim must be 2 or 3"; return KG_ERR_ARG; }
     if (t.ndf != (t.dim == 2 ? 2 : 1)) { err = "ndf must be 2 in 2D and 1 in 3D"; return KG_ERR_ARG; }
     if (prm.dim != t.dim || prm.ndf != t.ndf) { err = "params and topology disagree on dim/ndf"; return KG_ERR_ARG; }
@@ -134,9 +190,6 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         { err = "null topology array"; return KG_ERR_ARG; }
     const int D = t.dim, NDF = t.ndf, NC = t.n_cells, NWL = t.n_walls;
     F.dim = D; F.ndf = NDF; F.n_cells = NC; F.n_walls = NWL; F.n_data = NC + NWL;
-    Ctx c{&t, D, NDF, &F, {}, &err, {}, t.n_grids};
-    if (t.n_grids <= 1024) c.dense.assign((size_t)t.n_grids * t.n_grids, -3);
-    F.p_off.push_back(0);
 
     // ---- velocity grids ------------------------------------------------------
     int64_t PG = t.grid_off[t.n_grids];
@@ -233,12 +286,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         int32_t v = t.nbr_ref[r];
         if (v >= NC || (v < 0 && v != KG_NBR_NONE && v != KG_NBR_INSIDE && (-1 - v) >= NWL)) { err = "nbr_ref out of range"; return KG_ERR_TOPOLOGY; }
     }
-    auto st = [&](int cell, int k) { return (int)t.nbr_state[cell * NF + k]; };
-    auto lst = [&](int cell, int k) { return t.nbr_ref + t.nbr_off[cell * NF + k]; };
-    auto cnt = [&](int cell, int k) { return (int)(t.nbr_off[cell * NF + k + 1] - t.nbr_off[cell * NF + k]); };
-    auto be_of = [&](int data) { return F.dbe[data]; };
-
-    // ---- slope ops (slope!, Flux/Slope.jl:458-1070) ------------------------------------
+    // fluid cells: count, phase cells, levels
     int Lmin = INT32_MAX, Lmax = 0;
     for (int i = 0; i < NC; ++i) {
         if (t.cell_bound_enc[i] < 0) continue;
@@ -248,6 +296,136 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         Lmax = std::max(Lmax, t.cell_level[i]);
     }
     if (F.n_fluid == 0) { err = "no fluid cells"; return KG_ERR_TOPOLOGY; }
+    pid.lmin = Lmin;
+    pid.lmax = Lmax;
+    return build_pairs(t, F, pid, err);
+}
+
+// The checks of the face list that the host builder makes while it places the incidences, in
+// its order and with its messages (the device builder runs them here first).
+int flatten_checks(const kg_params& prm, const kg_topology& t, const Flat& F, std::string& err) {
+    const int D = t.dim, NC = t.n_cells;
+    for (int fi = 0; fi < t.n_faces; ++fi) {
+        const int here = t.face_here[fi];
+        if (here < 0 || here >= NC) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
+    }
+    for (int fi = 0; fi < t.n_faces; ++fi) {
+        const int dir = t.face_dir[fi];
+        if (dir < 0 || dir >= D) { err = "face_dir out of range"; return KG_ERR_TOPOLOGY; }
+        const int here = t.face_here[fi];
+        if (t.cell_bound_enc[here] < 0) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
+        const double rot = t.face_rot[fi];
+        if (rot != 1.0 && rot != -1.0) { err = "face_rot must be +1 or -1"; return KG_ERR_TOPOLOGY; }
+        if (t.face_kind[fi] == KG_FACE_DOMAIN) {
+            const int bk = t.face_bc_kind[fi];
+            if (bk < KG_BC_MAXWELL || bk > KG_BC_INTERP) { err = "unknown domain boundary kind"; return KG_ERR_TOPOLOGY; }
+            if (bk == KG_BC_MAXWELL && prm.flux == KG_FLUX_DVM) { err = "DVM Maxwellian domain flux is undefined in the reference (DVM.jl:3,12)"; return KG_ERR_TOPOLOGY; }
+            if (bk == KG_BC_INTERP && D != 2) { err = "InterpolatedOutflow is 2D only in the reference"; return KG_ERR_TOPOLOGY; }
+            continue;
+        }
+        const int od = data_ref(t, t.face_there[fi]);
+        if (od < 0) { err = "inner face without a there side"; return KG_ERR_TOPOLOGY; }
+        if (F.dbe[od] < 0 && od >= NC && F.dgrid[od] != t.cell_grid[here]) { err = "wall grid differs from donor grid"; return KG_ERR_TOPOLOGY; }
+    }
+    return KG_OK;
+}
+
+// The immersed-boundary records (update_solid_cell!, Boundary/Immersed_boundary.jl:122-146;
+// update_solid_neighbor!, :367-500): the solid cells' extrapolation sources and the wall
+// records' image sources, cut cells and weights.
+int flatten_ib(const kg_topology& t, Flat& F, const PairIds& pid, std::string& err) {
+    const int D = t.dim, NC = t.n_cells, NWL = t.n_walls, NF = 2 * D;
+    Ctx c{&t, D, t.ndf, &F, const_cast<PairIds*>(&pid), &err};
+    auto lst = [&](int cell, int k) { return t.nbr_ref + t.nbr_off[cell * NF + k]; };
+    // ---- immersed boundary (Boundary/Immersed_boundary.jl:122-146,367-500) -----------------
+    auto fluid_sources = [&](int cell, const double* target, std::vector<int>& srcs) {
+        for (int k = 0; k < NF; ++k) {
+            int32_t r = lst(cell, k)[0];
+            if (r >= 0 && t.cell_bound_enc[r] >= 0) srcs.push_back(r);
+        }
+        (void)target;
+    };
+    auto push_sources = [&](int tgt_grid, const std::vector<int>& srcs, const double* target) -> int {
+        for (int s : srcs) {
+            int p = pairing(c, tgt_grid, t.cell_grid[s]);
+            if (p == -2) return KG_ERR_TOPOLOGY;
+            F.ib_nbr.push_back(NbrRef{s, p});
+            for (int d = 0; d < MAXD; ++d) F.ib_dx.push_back(d < D ? target[d] - t.cell_midpoint[(size_t)s * D + d] : 0.0);
+        }
+        return KG_OK;
+    };
+    for (int i = 0; i < NC; ++i) {
+        if (t.cell_bound_enc[i] >= 0) continue;
+        std::vector<int> srcs;
+        const double* tm = t.cell_midpoint + (size_t)i * D;
+        fluid_sources(i, tm, srcs);
+        SolidOp so{};
+        so.cell = i; so.list = (int32_t)F.ib_nbr.size(); so.cnt = (int32_t)srcs.size();
+        if (srcs.empty()) { err = "solid cell without fluid neighbours"; return KG_ERR_TOPOLOGY; }
+        int rc = push_sources(t.cell_grid[i], srcs, tm);
+        if (rc) return rc;
+        F.solid_ops.push_back(so);
+    }
+    for (int w = 0; w < NWL; ++w) {
+        WallOp wo{};
+        int dn = t.wall_donor[w], sc = t.wall_solid[w];
+        int k = t.wall_faceid[w];
+        if (k < 0 || k >= NF) { err = "wall faceid out of range"; return KG_ERR_TOPOLOGY; }
+        wo.donor = dn; wo.solid = sc; wo.data = NC + w; wo.dir = k / 2;
+        for (int d = 0; d < D; ++d) {
+            wo.aux[d] = t.wall_aux_point[(size_t)w * D + d];
+            wo.normal[d] = t.wall_normal[(size_t)w * D + d];
+            wo.ib_point[d] = wo.aux[d] + t.cell_midpoint[(size_t)dn * D + d] - t.cell_midpoint[(size_t)sc * D + d];
+        }
+        for (int e = 0; e < D + 2; ++e) wo.bc[e] = t.wall_bc[(size_t)w * (D + 2) + e];
+        int dir = wo.dir;
+        wo.dxf = wo.ib_point[dir] - t.cell_midpoint[(size_t)dn * D + dir];
+        wo.dxs = t.cell_midpoint[(size_t)dn * D + dir] - t.cell_midpoint[(size_t)sc * D + dir];
+        wo.dxL = wo.aux[dir] - wo.ib_point[dir];
+        std::vector<int> srcs;
+        fluid_sources(dn, wo.ib_point, srcs);
+        srcs.push_back(dn);  // image_df appends the donor itself (Immersed_boundary.jl:373)
+        wo.list = (int32_t)F.ib_nbr.size(); wo.cnt = (int32_t)srcs.size();
+        int rc = push_sources(t.cell_grid[dn], srcs, wo.ib_point);
+        if (rc) return rc;
+        wo.spair = pairing(c, t.cell_grid[dn], t.cell_grid[sc]);
+        if (wo.spair == -2) return KG_ERR_TOPOLOGY;
+        int c0 = t.wall_cut_off[w], c1 = t.wall_cut_off[w + 1];
+        if (c1 < c0) { err = "wall_cut_off must be non-decreasing"; return KG_ERR_TOPOLOGY; }
+        wo.cut_off = (int32_t)F.cut_idx.size(); wo.cut_cnt = c1 - c0;
+        int nv = grid_nv(t, t.cell_grid[dn]);
+        wo.cvcw_off = (int64_t)F.cvcw.size();
+        const double* wt = t.vs_weight + t.grid_off[t.cell_grid[dn]];
+        size_t base = F.cvcw.size();
+        F.cvcw.insert(F.cvcw.end(), wt, wt + nv);
+        for (int a = c0; a < c1; ++a) {
+            int idx = t.wall_cut_index[a];
+            if (idx < 0 || idx >= nv) { err = "wall_cut_index out of range"; return KG_ERR_TOPOLOGY; }
+            F.cut_idx.push_back(idx); F.cut_gw.push_back(t.wall_cut_gas_w[a]); F.cut_sw.push_back(t.wall_cut_solid_w[a]);
+            F.cvcw[base + idx] = 0.0;
+        }
+        // the donor's neighbour entry for this face must be this wall record
+        if (lst(dn, k)[0] != KG_WALL(w)) { err = "donor neighbour entry does not reference its wall record"; return KG_ERR_TOPOLOGY; }
+        F.wall_ops.push_back(wo);
+    }
+    return KG_OK;
+}
+
+int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& err) {
+    PairIds pid;
+    int rc0 = flatten_head(prm, t, F, pid, err);
+    if (rc0) return rc0;
+    const int D = t.dim, NDF = t.ndf, NC = t.n_cells, NWL = t.n_walls;
+    (void)NWL;
+    Ctx c{&t, D, NDF, &F, &pid, &err};
+    const int NF = 2 * D;
+    auto st = [&](int cell, int k) { return (int)t.nbr_state[cell * NF + k]; };
+    auto lst = [&](int cell, int k) { return t.nbr_ref + t.nbr_off[cell * NF + k]; };
+    auto cnt = [&](int cell, int k) { return (int)(t.nbr_off[cell * NF + k + 1] - t.nbr_off[cell * NF + k]); };
+    auto be_of = [&](int data) { return F.dbe[data]; };
+
+    // ---- slope ops (slope!, Flux/Slope.jl:458-1070) ------------------------------------
+    const int Lmin = pid.lmin, Lmax = pid.lmax;
     const int half = 1 << (D - 1);
     auto add_list = [&](int cell, int k, int& off, int& n) -> int {
         off = (int)F.slope_nbr.size();
@@ -329,7 +507,6 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         op.kind = SLOPE_SKIP;
         return KG_OK;
     };
-    if (Lmin == INT32_MAX) Lmin = 0;
     F.pass_off.push_back(0);
     F.pass_cells_off.push_back(0);
     for (int L = Lmin; L <= Lmax; ++L) {
@@ -442,7 +619,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         if (here < 0 || here >= NC) { err = "face here side must be a fluid cell"; return KG_ERR_TOPOLOGY; }
         nper[here + 1] += 1;
         if (t.face_kind[fi] != KG_FACE_DOMAIN) {
-            const int od = data_of(c, t.face_there[fi]);
+            const int od = data_ref(t, t.face_there[fi]);
             if (od >= 0 && od < NC && F.dbe[od] >= 0) nper[od + 1] += 1;
         }
     }
@@ -477,7 +654,7 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
             incs[fill[here]++] = a;
             continue;
         }
-        int od = data_of(c, t.face_there[fi]);
+        int od = data_ref(t, t.face_there[fi]);
         if (od < 0) { err = "inner face without a there side"; return KG_ERR_TOPOLOGY; }
         bool solid = F.dbe[od] < 0;
         a.kind = solid ? INC_SOLID : INC_INNER;
@@ -547,82 +724,15 @@ int flatten(const kg_params& prm, const kg_topology& t, Flat& F, std::string& er
         F.inc_off.push_back(nper[i + 1]);
     }
 
-    // ---- immersed boundary (Boundary/Immersed_boundary.jl:122-146,367-500) -----------------
-    auto fluid_sources = [&](int cell, const double* target, std::vector<int>& srcs) {
-        for (int k = 0; k < NF; ++k) {
-            int32_t r = lst(cell, k)[0];
-            if (r >= 0 && t.cell_bound_enc[r] >= 0) srcs.push_back(r);
-        }
-        (void)target;
-    };
-    auto push_sources = [&](int tgt_grid, const std::vector<int>& srcs, const double* target) -> int {
-        for (int s : srcs) {
-            int p = pairing(c, tgt_grid, t.cell_grid[s]);
-            if (p == -2) return KG_ERR_TOPOLOGY;
-            F.ib_nbr.push_back(NbrRef{s, p});
-            for (int d = 0; d < MAXD; ++d) F.ib_dx.push_back(d < D ? target[d] - t.cell_midpoint[(size_t)s * D + d] : 0.0);
-        }
-        return KG_OK;
-    };
-    for (int i = 0; i < NC; ++i) {
-        if (t.cell_bound_enc[i] >= 0) continue;
-        std::vector<int> srcs;
-        const double* tm = t.cell_midpoint + (size_t)i * D;
-        fluid_sources(i, tm, srcs);
-        SolidOp so{};
-        so.cell = i; so.list = (int32_t)F.ib_nbr.size(); so.cnt = (int32_t)srcs.size();
-        if (srcs.empty()) { err = "solid cell without fluid neighbours"; return KG_ERR_TOPOLOGY; }
-        int rc = push_sources(t.cell_grid[i], srcs, tm);
+    {
+        const int rc = flatten_ib(t, F, pid, err);
         if (rc) return rc;
-        F.solid_ops.push_back(so);
-    }
-    for (int w = 0; w < NWL; ++w) {
-        WallOp wo{};
-        int dn = t.wall_donor[w], sc = t.wall_solid[w];
-        int k = t.wall_faceid[w];
-        if (k < 0 || k >= NF) { err = "wall faceid out of range"; return KG_ERR_TOPOLOGY; }
-        wo.donor = dn; wo.solid = sc; wo.data = NC + w; wo.dir = k / 2;
-        for (int d = 0; d < D; ++d) {
-            wo.aux[d] = t.wall_aux_point[(size_t)w * D + d];
-            wo.normal[d] = t.wall_normal[(size_t)w * D + d];
-            wo.ib_point[d] = wo.aux[d] + t.cell_midpoint[(size_t)dn * D + d] - t.cell_midpoint[(size_t)sc * D + d];
-        }
-        for (int e = 0; e < D + 2; ++e) wo.bc[e] = t.wall_bc[(size_t)w * (D + 2) + e];
-        int dir = wo.dir;
-        wo.dxf = wo.ib_point[dir] - t.cell_midpoint[(size_t)dn * D + dir];
-        wo.dxs = t.cell_midpoint[(size_t)dn * D + dir] - t.cell_midpoint[(size_t)sc * D + dir];
-        wo.dxL = wo.aux[dir] - wo.ib_point[dir];
-        std::vector<int> srcs;
-        fluid_sources(dn, wo.ib_point, srcs);
-        srcs.push_back(dn);  // image_df appends the donor itself (Immersed_boundary.jl:373)
-        wo.list = (int32_t)F.ib_nbr.size(); wo.cnt = (int32_t)srcs.size();
-        int rc = push_sources(t.cell_grid[dn], srcs, wo.ib_point);
-        if (rc) return rc;
-        wo.spair = pairing(c, t.cell_grid[dn], t.cell_grid[sc]);
-        if (wo.spair == -2) return KG_ERR_TOPOLOGY;
-        int c0 = t.wall_cut_off[w], c1 = t.wall_cut_off[w + 1];
-        if (c1 < c0) { err = "wall_cut_off must be non-decreasing"; return KG_ERR_TOPOLOGY; }
-        wo.cut_off = (int32_t)F.cut_idx.size(); wo.cut_cnt = c1 - c0;
-        int nv = grid_nv(t, t.cell_grid[dn]);
-        wo.cvcw_off = (int64_t)F.cvcw.size();
-        const double* wt = t.vs_weight + t.grid_off[t.cell_grid[dn]];
-        size_t base = F.cvcw.size();
-        F.cvcw.insert(F.cvcw.end(), wt, wt + nv);
-        for (int a = c0; a < c1; ++a) {
-            int idx = t.wall_cut_index[a];
-            if (idx < 0 || idx >= nv) { err = "wall_cut_index out of range"; return KG_ERR_TOPOLOGY; }
-            F.cut_idx.push_back(idx); F.cut_gw.push_back(t.wall_cut_gas_w[a]); F.cut_sw.push_back(t.wall_cut_solid_w[a]);
-            F.cvcw[base + idx] = 0.0;
-        }
-        // the donor's neighbour entry for this face must be this wall record
-        if (lst(dn, k)[0] != KG_WALL(w)) { err = "donor neighbour entry does not reference its wall record"; return KG_ERR_TOPOLOGY; }
-        F.wall_ops.push_back(wo);
     }
     if (F.p_j0.empty()) { F.p_j0.push_back(0); F.p_cnt.push_back(0); }
     return KG_OK;
 }
 
-void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges, bool fuse) {
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<int32_t>& ranges, bool fuse, bool light) {
     reset(M);
     if (parts.empty()) return;
     const int D = parts[0].F->dim;
@@ -712,13 +822,14 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             M.p_cnt.insert(M.p_cnt.end(), F.p_cnt.begin(), F.p_cnt.begin() + F.p_off.back());
         }
         auto rp = [&](int32_t pr) { return pr >= 0 ? pr + pairacc : pr; };
+        int32_t fb = (int32_t)M.fluid_cells.size();
+        for (int c : F.fluid_cells) M.fluid_cells.push_back(c + p.dbase);
+        M.fluid_reg.insert(M.fluid_reg.end(), F.fluid_reg.begin(), F.fluid_reg.end());
+        if (!light) {
         // slope ops and neighbour lists
         for (SlopeOp op : F.slope_ops) { op.cell += p.dbase; op.listA += snb; op.listB += snb; M.slope_ops.push_back(op); }
         for (NbrRef r : F.slope_nbr) { r.data += p.dbase; r.pair = rp(r.pair); M.slope_nbr.push_back(r); }
         // flux incidences
-        int32_t fb = (int32_t)M.fluid_cells.size();
-        for (int c : F.fluid_cells) M.fluid_cells.push_back(c + p.dbase);
-        M.fluid_reg.insert(M.fluid_reg.end(), F.fluid_reg.begin(), F.fluid_reg.end());
         for (size_t q = 1; q < F.inc_off.size(); ++q) M.inc_off.push_back(incacc + F.inc_off[q]);
         for (Incidence a : F.inc) {
             if (a.other >= 0) {
@@ -777,6 +888,7 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
         }
         M.bc_prim.insert(M.bc_prim.end(), F.bc_prim.begin(), F.bc_prim.end());
         M.bc_hl.insert(M.bc_hl.end(), F.bc_hl.begin(), F.bc_hl.end());
+        }   // !light
         ranges.push_back(fb);
         ranges.push_back((int32_t)M.fluid_cells.size());
         M.n_fluid += F.n_fluid;
@@ -812,12 +924,13 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             if (ps + 1 >= F.pass_cells_off.size()) continue;
             for (int32_t k = F.pass_cells_off[ps]; k < F.pass_cells_off[ps + 1]; ++k) {
                 M.pass_cells.push_back(F.pass_cells[k] + parts[q].dbase);
-                M.cell_slope_op.push_back(F.cell_slope_op[k] + sops_base[q]);
+                if (!light) M.cell_slope_op.push_back(F.cell_slope_op[k] + sops_base[q]);
             }
         }
         M.pass_off.push_back((int32_t)M.slope_ops.size());
         M.pass_cells_off.push_back((int32_t)M.pass_cells.size());
     }
+    if (light) return;
     M.screc.resize(M.pass_cells.size());
     for (size_t k = 0; k < M.pass_cells.size(); ++k) {
         const int32_t m = M.pass_cells[k];
@@ -881,6 +994,13 @@ void merge(const std::vector<Part>& parts, int32_t dcap, Flat& M, std::vector<in
             if (interior) M.fluid_r2[q] = 2;
         }
     }
+    slope_items(M, dcap, fuse);
+}
+
+void slope_items(Flat& M, int32_t dcap, bool fuse) {
+    const int D = M.dim;
+    M.slope_items.clear();
+    M.pass_items_off.clear();
     // work items of the slope passes: when some grid exceeds two chunks, a pass cell per
     // SLOPE_CHUNK velocity cells (large 3D grids: fewer cells than resident CTAs per level);
     // otherwise one item per pass cell (the kernel indexes the pass cells directly when every

@@ -9,7 +9,9 @@
 // deterministic.
 #pragma once
 #include <cstdint>
+#include <map>
 #include <string>
+#include <utility>
 #include <vector>
 #include "../../include/kitgpu.h"
 
@@ -82,6 +84,7 @@ struct Incidence {          // 208 bytes
     int64_t ofoff;          // f offset of the other side (-1 for a domain face)
     int32_t onv, ogo;       // its velocity count and grid offset
     float dxm_f[MAXD], dxo_f[MAXD], ods_f[MAXD], orient_f, sarea_f;   // FP32 roundings
+    float pad_f;            // zero (keeps the record free of implicit padding)
     // a face to a SolidNeighbor record: the reconstruction perturbance's lever arm
     // x_solid[dir] - x_aux[dir] (update_solid_neighbor!, Immersed_boundary.jl:477), which
     // positivity_preserving_ib! reads under CIP marching
@@ -215,6 +218,9 @@ struct Flat {
     std::vector<double> cvcw;
     int max_inc = 0;
     int max_bcm = 0;                      // most Maxwellian-state domain faces (wall, inflow) of a cell
+    // the arrays a step reads beyond these (slope ops and lists, criterion rows, incidences,
+    // per-cell records) were built on the device (kg_devflat.cu) and live there only
+    bool devlay = false;
 };
 
 // One cell of an adapted mesh and the cells of the previous mesh its state comes from
@@ -259,6 +265,28 @@ bool level_runs(const int8_t* la, int na, const int8_t* lb, int nb, int D, std::
 // Empties a gather form, keeping the capacity of its arrays for the next build.
 void reset(Flat& F);
 
+// The canonical velocity pairings of one topology (build_pairs): every (my grid, its grid)
+// pair that a neighbour reference, an inner face or a wall record relates, numbered by
+// ascending (my grid, its grid); and the coarsest and finest fluid-cell levels.
+struct PairIds {
+    int G = 0;
+    std::vector<int32_t> dense;              // G x G ids (-1: none) when G <= 1024
+    std::map<std::pair<int, int>, int> ids;  // otherwise
+    int lmin = 0, lmax = 0;
+    void clear() { G = 0; dense.clear(); ids.clear(); lmin = lmax = 0; }
+    int find(int ga, int gb) const;
+};
+int build_pairs(const kg_topology& t, Flat& F, PairIds& pid, std::string& err);
+
+// The part of the gather form both builders share: argument and topology checks, the velocity
+// grids and their axis tables, the data table, the fluid-cell count and levels, and the
+// pairing tables (F.p_*).
+int flatten_head(const kg_params& prm, const kg_topology& t, Flat& F, PairIds& pid, std::string& err);
+// The face-list checks the host builder makes while placing incidences (same order, messages).
+int flatten_checks(const kg_params& prm, const kg_topology& t, const Flat& F, std::string& err);
+// The immersed-boundary records (solid_ops, wall_ops, ib_nbr, ib_dx, cut_*, cvcw).
+int flatten_ib(const kg_topology& t, Flat& F, const PairIds& pid, std::string& err);
+
 // Builds the gather form; returns KG_OK or an error code with a message.
 int flatten(const kg_params& prm, const kg_topology& t, Flat& out, std::string& err);
 
@@ -273,7 +301,12 @@ struct Part {
 // Concatenates the parts into one gather form whose data indices are pool positions
 // (dcap slots); fills the fluid range of every part into `ranges` (begin, end pairs).
 // fuse: 2D layouts of the packed regular-cell kernel, which computes the slopes of its R2 cells
-void merge(const std::vector<Part>& parts, int32_t dcap, Flat& out, std::vector<int32_t>& ranges, bool fuse);
+// light: the parts' step arrays were built on the device (Flat::devlay); only the host-side
+// arrays are merged, and the slope work items are left to slope_items()
+void merge(const std::vector<Part>& parts, int32_t dcap, Flat& out, std::vector<int32_t>& ranges, bool fuse,
+           bool light = false);
+// The work items of the slope passes of a merged layout, from its pass cells and fluid_r2.
+void slope_items(Flat& M, int32_t dcap, bool fuse);
 int64_t device_bytes(const Flat& f, int precision);
 
 }  // namespace kg

@@ -1549,7 +1549,13 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
 }
 
 // ---- packed-FP32 regular-cell kernel (2D, two distributions, mixed form) ---------------
-constexpr int PACKED_VPT = 2;   // velocity cells per thread and gather pass
+#ifndef KG_PACKED_VPT
+#define KG_PACKED_VPT 2
+#endif
+#ifndef KG_PACKED_MINB
+#define KG_PACKED_MINB 3
+#endif
+constexpr int PACKED_VPT = KG_PACKED_VPT;   // velocity cells per thread and gather pass
 constexpr int R2_VPT = 1;       // the same for the kernel that computes the slopes (more loads a cell)
 // Blackwell's FP32x2 instructions (__ffma2_rn / __fmul2_rn / __fadd2_rn: two FP32 lanes per
 // thread instruction, each rounded as the scalar instruction) carry the pair (h, b) of every
@@ -1876,7 +1882,7 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
 // VPT velocity cells per thread and pass of the gather (their loads in flight together);
 // more registers, so fewer resident CTAs
 template <int NT, int VPT, bool R2>
-__global__ void __launch_bounds__(NT, (VPT == 1 && !R2 ? 4 : 3) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
+__global__ void __launch_bounds__(NT, (R2 ? 3 : (VPT == 1 ? 4 : KG_PACKED_MINB)) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
     flux_regular_packed<NT, VPT, R2>(P, list[blockIdx.x]);
 }
 

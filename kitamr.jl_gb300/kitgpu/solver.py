@@ -42,6 +42,8 @@ def load_library(path: Optional[str] = None):
     L.kg_topology_footprint.argtypes = [vp, vp, C.POINTER(i64)]
     L.kg_last_error.argtypes = [vp, C.c_char_p, C.c_size_t]
     L.kg_use_graph.argtypes = [vp, C.c_int]
+    L.kg_device_flatten.argtypes = [vp, C.c_int]
+    L.kg_layout_read.argtypes = [vp, C.c_char_p, vp, i64, C.POINTER(i64)]
     L.kg_batch_create.argtypes = [vp, C.c_int, i64, C.POINTER(vp)]
     L.kg_batch_admit.argtypes = [vp, vp, vp, vp, vp, vp, dbl, i64, C.POINTER(i32)]
     L.kg_batch_release.argtypes = [vp, i32]
@@ -128,13 +130,15 @@ def topology_footprint(params: abi.KgParams, topo: Dict) -> int:
 class GpuStep:
     """One libkitgpu handle holding one topology and its state on one device."""
 
-    def __init__(self, params: abi.KgParams, topo: Dict, device: int = 0):
+    def __init__(self, params: abi.KgParams, topo: Dict, device: int = 0, device_flatten: bool = True):
         self.L = load_library()
         self.params = params
         self.topo = topo
         h = C.c_void_p()
         _check(self.L, None, self.L.kg_create(C.byref(params), device, C.byref(h)))
         self.h = h
+        # the gather form of the topology built on the device (default) or on the host
+        _check(self.L, self.h, self.L.kg_device_flatten(self.h, int(device_flatten)))
         self._tref = abi.TopologyRef(topo)
         _check(self.L, self.h, self.L.kg_upload_topology(self.h, C.cast(self._tref.ptr, C.c_void_p)))
         from .mesh import f_offsets
@@ -284,6 +288,18 @@ class GpuStep:
 
     def fuse_slopes(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_fuse_slopes(self.h, int(enable)))
+
+    def device_flatten(self, enable: bool = True):
+        """Builder of the gather form for later topology changes: device (True) or host."""
+        _check(self.L, self.h, self.L.kg_device_flatten(self.h, int(enable)))
+
+    def layout_read(self, name: str) -> bytes:
+        """The named array of the gather form the next step reads, as raw bytes."""
+        n = C.c_int64()
+        _check(self.L, self.h, self.L.kg_layout_read(self.h, name.encode(), None, 0, C.byref(n)))
+        buf = (C.c_char * max(n.value, 1))()
+        _check(self.L, self.h, self.L.kg_layout_read(self.h, name.encode(), buf, n.value, C.byref(n)))
+        return bytes(buf[: n.value])
 
     def autotune_result(self):
         return _autotune_result(self.L, self.h)
