@@ -575,7 +575,7 @@ def run_adapt(args):
         adapt.append((t2 - t1) * 1e3)
         g.step(dt, step, 1)
         step += 1
-    phases = {k: v[0] / max(v[1], 1) for k, v in g.profile_read().items() if k.startswith(("adapt:", "rebuild:"))}
+    phases = {k: v[0] / max(v[1], 1) for k, v in g.profile_read().items() if k.startswith(("adapt:", "rebuild:", "flatten:"))}
     g.close()
     # flattening alone (host), the part of kg_adapt that is not device work
     from kitgpu.solver import load_library

@@ -371,7 +371,13 @@ void free_pools(kg_handle* h, bool keep_arena = false) {
     h->pool_bytes = 0;
     h->fA = h->fB = h->sdf = nullptr;
     h->w = h->prim = h->qf = h->staging = nullptr;
-    h->probs.clear();
+    if (keep_arena && h->probs.size() == (size_t)MAX_SLOTS) {
+        // the slot table stays: only the slots in use are emptied
+        for (Problem& pb : h->probs)
+            if (pb.live || pb.fsize || pb.dsize || pb.F.n_data) pb = Problem();
+    } else {
+        h->probs.clear();
+    }
     h->live.clear();
     h->dirty = true;
     h->have_state = false;
@@ -399,7 +405,7 @@ int make_pools(kg_handle* h, int64_t fcap, int64_t dcap) {
     h->fcap = fcap; h->dcap = dcap;
     h->fslab.reset(fcap);
     h->dslab.reset(dcap);
-    h->probs.assign(MAX_SLOTS, Problem());
+    if (h->probs.size() != (size_t)MAX_SLOTS) h->probs.assign(MAX_SLOTS, Problem());
     h->parity = 0;
     h->dirty = true;
     // the zero fill of a pool of hundreds of GB runs for tens of ms; finish it before any
@@ -435,7 +441,7 @@ int adopt_pools(kg_handle* h, kg_handle::PoolSet& ps) {
     ps = kg_handle::PoolSet();
     h->fslab.reset(h->fcap);
     h->dslab.reset(h->dcap);
-    h->probs.assign(MAX_SLOTS, Problem());
+    if (h->probs.size() != (size_t)MAX_SLOTS) h->probs.assign(MAX_SLOTS, Problem());
     h->parity = 0;
     h->dirty = true;
     KG_CUDA(h, cudaMemsetAsync(h->d_status, 0, sizeof(int) * MAX_SLOTS, h->stream));
@@ -501,68 +507,21 @@ struct PhaseClock {
     }
 };
 
-// Bits of x (21 used) spread to every dim-th bit: one coordinate of a Morton key.
-uint64_t morton_spread(uint64_t x, int dim) {
-    uint64_t r = 0;
-    for (int b = 0; b < 21; ++b) r |= ((x >> b) & 1ull) << (dim * b);
-    return r;
-}
-
-// Launch order of a list of fluid-list entries: per problem, along a Morton curve through the
-// cells' midpoints, so that the cells a wave of CTAs advances together are neighbours in space
-// and read one another's f and sdf while those are still in L2.  Every cell writes only its
-// own data, so the order changes no result.
-void sfc_order(const Flat& M, std::vector<int32_t>& list) {
-    if (list.size() < 2) return;
-    const int D = M.dim;
-    struct Box { int slot; double lo[MAXD], h[MAXD]; };
-    std::vector<Box> box;   // per problem slot met (a few; searched from the last one found)
-    size_t last = 0;
-    auto find = [&](int slot) -> Box& {
-        if (last < box.size() && box[last].slot == slot) return box[last];
-        for (last = 0; last < box.size(); ++last)
-            if (box[last].slot == slot) return box[last];
-        Box b;
-        b.slot = slot;
-        for (int d = 0; d < MAXD; ++d) { b.lo[d] = 1e300; b.h[d] = 1e300; }
-        box.push_back(b);
-        last = box.size() - 1;
-        return box[last];
-    };
-    for (int32_t q : list) {
-        const int32_t m = M.fluid_cells[q];
-        Box& b = find(M.dprob[m]);
-        for (int d = 0; d < D; ++d) {
-            const double mid = M.dmid[(size_t)m * MAXD + d], ds = M.dds[(size_t)m * MAXD + d];
-            b.lo[d] = std::min(b.lo[d], mid - 0.5 * ds);
-            b.h[d] = std::min(b.h[d], ds);
-        }
-    }
-    struct Key { int slot; uint64_t key; int32_t q; };
-    std::vector<Key> keys;
-    keys.reserve(list.size());
-    for (int32_t q : list) {
-        const int32_t m = M.fluid_cells[q];
-        const Box& b = find(M.dprob[m]);
-        uint64_t k = 0;
-        for (int d = 0; d < D; ++d) {
-            const double x = std::floor((M.dmid[(size_t)m * MAXD + d] - b.lo[d]) / b.h[d]);
-            const uint64_t ix = (uint64_t)std::min(std::max(x, 0.0), 2097151.0);
-            k |= morton_spread(ix, D) << d;
-        }
-        keys.push_back(Key{M.dprob[m], k, q});
-    }
-    std::sort(keys.begin(), keys.end(), [](const Key& a, const Key& b) {
-        return a.slot != b.slot ? a.slot < b.slot : (a.key != b.key ? a.key < b.key : a.q < b.q);
-    });
-    for (size_t i = 0; i < list.size(); ++i) list[i] = keys[i].q;
-}
-
 // The gather form of a single handle's problem: on the device (kg_devflat.cu) unless the
 // host builder was selected; a batch handle's problems are always flattened on the host.
 int build_layout(kg_handle* h, const kg_topology& topo, int slot, Flat& F, DevLayout& dl, std::string& err) {
     if (h->is_batch || !h->devflat) return flatten(h->prm, topo, F, err);
-    return device_flatten(h->prm, topo, slot, h->stream, F, dl, h->dscratch, err);
+    double t[4] = {0, 0, 0, 0};
+    const int rc = device_flatten(h->prm, topo, slot, h->stream, F, dl, h->dscratch, err, t);
+    if (h->prof) {
+        const char* names[4] = {"flatten:host", "flatten:upload", "flatten:count", "flatten:build"};
+        for (int k = 0; k < 4; ++k) {
+            const int e = prof_slot(h, names[k]);
+            h->pms[e] += t[k];
+            h->pcount[e] += 1;
+        }
+    }
+    return rc;
 }
 
 // Rebuilds the merged gather form of the live problems and uploads it.
@@ -609,11 +568,9 @@ int rebuild(kg_handle* h) {
     // the launch lists of the flux kernels: the cells that are not regular, largest velocity
     // grids first (persistent schedule); the regular fluid cells (the regular-cell kernel; a
     // regular cell never reads a solid cell or wall record), those whose slopes the packed
-    // kernel computes, and the others; each in space-filling-curve order
-    std::vector<int32_t> order, reg, nonreg, r2, all((size_t)M.n_fluid);
-    for (int q = 0; q < M.n_fluid; ++q) all[q] = q;
-    sfc_order(M, all);
-    for (int32_t q : all) {
+    // kernel computes, and the others
+    std::vector<int32_t> order, reg, nonreg, r2;
+    for (int q = 0; q < M.n_fluid; ++q) {
         if (!M.fluid_reg[q]) { nonreg.push_back(q); order.push_back(q); }
         else if (M.fluid_r2[q]) r2.push_back(q);
         else reg.push_back(q);

@@ -12,6 +12,7 @@
 // compiled without FMA contraction so every double expression rounds as the host's does.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include "kg_device.cuh"
 #include "kg_devflat.h"
@@ -643,7 +644,13 @@ static cudaError_t grow(DevScratch& S, size_t dev_bytes, size_t pin_bytes) {
 #define DF_CUDA(x) do { cudaError_t e__ = (x); if (e__ != cudaSuccess) { err = std::string("device layout: ") + cudaGetErrorString(e__); return KG_ERR_CUDA; } } while (0)
 
 int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStream_t s, Flat& F, DevLayout& L,
-                   DevScratch& S, std::string& err) {
+                   DevScratch& S, std::string& err, double* t_ms) {
+    auto t0 = std::chrono::steady_clock::now();
+    auto lap = [&](int k) {
+        const auto n = std::chrono::steady_clock::now();
+        if (t_ms) t_ms[k] += std::chrono::duration<double, std::milli>(n - t0).count();
+        t0 = n;
+    };
     PairIds pid;
     int rc = flatten_head(prm, t, F, pid, err);
     if (rc) return rc;
@@ -674,6 +681,7 @@ int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStr
     }
     const int npc = nfl;
     const int64_t nref = t.nbr_off[NC * NF];
+    lap(0);
     // ---- one pinned block with the topology arrays and the host tables, one copy -----------
     struct Seg { const void* src; size_t n; size_t off; };
     std::vector<Seg> segs;
@@ -727,6 +735,7 @@ int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStr
     char* dv = (char*)S.dev;
     DF_CUDA(cudaMemcpyAsync(dv, pin, in_bytes, cudaMemcpyHostToDevice, s));
     DF_CUDA(cudaMemsetAsync(dv + in_bytes, 0, dev_bytes - in_bytes, s));
+    lap(1);
     DT T;
     T.D = D; T.NC = NC; T.NWL = t.n_walls; T.NFACE = NFACE; T.G = G; T.half = 1 << (D - 1); T.lmin = pid.lmin;
     T.be = (const int32_t*)(dv + o_be); T.lev = (const int32_t*)(dv + o_lev); T.grid = (const int32_t*)(dv + o_grid);
@@ -778,6 +787,7 @@ int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStr
     DF_CUDA(cudaMemcpyAsync(&tots[4], flags, 8, cudaMemcpyDeviceToHost, s));
     DF_CUDA(cudaStreamSynchronize(s));
     if (tots[4]) { err = df_message(tots[4]); return KG_ERR_TOPOLOGY; }
+    lap(2);
     const int nsn = tots[0], ncn = tots[1], ninc = tots[2], nbc = tots[3];
     // ---- the layout's arrays ---------------------------------------------------------------
     size_t lb = bytes_of<SlopeOp>((size_t)npc * D) + bytes_of<NbrRef>(nsn) + 3 * bytes_of<int32_t>(npc) +
@@ -880,6 +890,7 @@ int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStr
     F.max_inc = hm[0];
     F.max_bcm = hm[1];
     F.devlay = true;
+    lap(3);
     if (F.p_j0.empty()) { F.p_j0.push_back(0); F.p_cnt.push_back(0); }
     return KG_OK;
 }

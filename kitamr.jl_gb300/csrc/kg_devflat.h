@@ -47,8 +47,11 @@ struct DevScratch {
 // Builds the gather form of topology t for problem slot `slot` on stream s: the host part
 // (flatten_head, flatten_checks, flatten_ib) into F, the rest into L; F.devlay is set.
 // Returns KG_OK or an error code with the host builder's message.
+// t_ms (optional, 4 entries): host wall time of the host part (checks, grids, data table,
+// pairings, wall records), of packing and uploading the arrays, of the counting kernels and of
+// the rest (fills, slope-pass order, records)
 int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStream_t s, Flat& F, DevLayout& L,
-                   DevScratch& S, std::string& err);
+                   DevScratch& S, std::string& err, double* t_ms = nullptr);
 
 // The R2 records and flags of a device-built layout (slopes in the flux kernel; zeros unless
 // fuse and 2D); the flags also into r2 (host).
