@@ -51,8 +51,8 @@ extern "C" {
 #define KG_MARCH_CIP        2   /* iterate!(::Type{CIP_Marching}) I-projection.jl:161:
                                    convection, then the conservative I-projection of f
                                    onto w (a Newton solve per cell) before relaxation;
-                                   meshes without immersed-boundary cells
-                                   (positivity_preserving_ib! is not provided)       */
+                                   next to immersed-boundary walls with
+                                   positivity_preserving_ib! (Boundary/Positivity.jl)  */
 #define KG_PREC_FP64        0   /* f, sdf, fluxes in FP64 (plain form)               */
 #define KG_PREC_MIXED       1   /* f, sdf, micro fluxes in FP32; moments compensated;
                                    w, prim, exponents, wall density in FP64          */
@@ -402,12 +402,14 @@ int kg_autotune_result(const kg_handle *h, int32_t *schedule, int32_t *ctas_per_
  * issues more instructions and waits on longer chains of loads).                        */
 int kg_fuse_slopes(kg_handle *h, int enable);
 
-/* Builder of the gather form of a single-problem handle: after kg_upload_topology and kg_adapt
+/* Builder of the gather form: after kg_upload_topology, kg_batch_admit and kg_adapt
  * (amr_recover!'s rebuild of faces and neighbours, Solver/AMR.jl:54-70, from
  * initialize_faces!, Solver/Initialize.jl:5-158) the slope operations and their neighbour
  * lists, the slope-pass order, the criterion rows, the face incidences and the per-cell flux
  * and slope records are built on the device (enable = 1, the default) or on the host (0).
- * Both give the same arrays byte for byte (kg_layout_read); batch handles build on the host. */
+ * Both give the same arrays byte for byte (kg_layout_read).  A batch handle merges its
+ * problems' device-built arrays on the device; its builder can change only while it holds no
+ * problem (KG_ERR_STATE otherwise).                                                     */
 int kg_device_flatten(kg_handle *h, int enable);
 
 /* Test support: copies the named array of the gather form the next step reads ("slope_ops",

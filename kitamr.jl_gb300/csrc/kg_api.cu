@@ -244,6 +244,8 @@ struct kg_handle {
     // the device (kg_devflat.cu); kg_device_flatten(h, 0) selects the host builder
     bool devflat = true;
     DevScratch dscratch;
+    DevLayout mdl;                 // the merged device-built layout of a batch
+    DevLayout* cur_dl = nullptr;   // the device-built arrays of the current layout, if any
     // a single handle's previous pools, kept after an adaptation moved the state out of them:
     // the next adaptation that fits takes them instead of allocating (and freeing) pools
     struct PoolSet {
@@ -507,10 +509,10 @@ struct PhaseClock {
     }
 };
 
-// The gather form of a single handle's problem: on the device (kg_devflat.cu) unless the
-// host builder was selected; a batch handle's problems are always flattened on the host.
+// The gather form of a problem: on the device (kg_devflat.cu) unless the host builder was
+// selected.
 int build_layout(kg_handle* h, const kg_topology& topo, int slot, Flat& F, DevLayout& dl, std::string& err) {
-    if (h->is_batch || !h->devflat) return flatten(h->prm, topo, F, err);
+    if (!h->devflat) return flatten(h->prm, topo, F, err);
     double t[4] = {0, 0, 0, 0};
     const int rc = device_flatten(h->prm, topo, slot, h->stream, F, dl, h->dscratch, err, t);
     if (h->prof) {
@@ -540,18 +542,58 @@ int rebuild(kg_handle* h) {
     }
     std::vector<int32_t> ranges;
     const bool fuse = !h->fuse_off && h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED && h->prm.marching != KG_MARCH_CIP;
-    // a single problem whose step arrays were built on the device: merge the host-side arrays,
-    // then its R2 records on the device and the slope work items
-    DevLayout* DL = (parts.size() == 1 && parts[0].F->devlay) ? &h->probs[parts[0].slot].dl : nullptr;
+    // problems whose step arrays were built on the device: the host-side arrays are merged here;
+    // a single problem at data and f base 0 keeps its own device arrays, several are merged on
+    // the device (device_merge); then the R2 records on the device and the slope work items
+    bool all_dev = !parts.empty();
+    for (const Part& p : parts) all_dev = all_dev && p.F->devlay;
+    DevLayout* DL = nullptr;
+    if (all_dev)
+        DL = (parts.size() == 1 && parts[0].dbase == 0 && parts[0].fbase == 0) ? &h->probs[parts[0].slot].dl : &h->mdl;
     merge(parts, (int32_t)h->dcap, h->M, ranges, fuse, DL != nullptr);
     Flat& M = h->M;
+    h->cur_dl = DL;
+    if (DL == &h->mdl) {
+        // each part's offsets as merge() accumulates them, and the merged start of its passes
+        size_t npass = 0;
+        for (const Part& p : parts) npass = std::max(npass, p.F->pass_cells_off.size() - 1);
+        std::vector<MergeIn> mi(parts.size());
+        int32_t run = 0;
+        for (size_t ps = 0; ps < npass; ++ps)
+            for (size_t q = 0; q < parts.size(); ++q) {
+                const Flat& F = *parts[q].F;
+                if (ps + 1 >= F.pass_cells_off.size()) continue;
+                mi[q].pass_base.push_back(run);
+                run += F.pass_cells_off[ps + 1] - F.pass_cells_off[ps];
+            }
+        int32_t snb = 0, sops = 0, cacc = 0, incacc = 0, bcacc = 0, pairacc = 0, Gacc = 0;
+        int64_t PGacc = 0;
+        for (size_t q = 0; q < parts.size(); ++q) {
+            const Flat& F = *parts[q].F;
+            const DevLayout& L = h->probs[parts[q].slot].dl;
+            MergeIn& m = mi[q];
+            m.L = &L;
+            m.fbase = parts[q].fbase; m.dbase = parts[q].dbase;
+            m.snb = snb; m.sops = sops; m.cacc = cacc; m.incacc = incacc; m.bcacc = bcacc; m.pairacc = pairacc;
+            m.Gacc = Gacc; m.PGacc = PGacc;
+            m.pass_off = F.pass_cells_off;
+            snb += (int32_t)L.n_slope_nbr; sops += (int32_t)L.n_slope_ops; cacc += (int32_t)L.n_crit_nbr;
+            incacc += (int32_t)L.n_inc; bcacc += (int32_t)L.n_bc; pairacc += (int32_t)F.p_off.size() - 1;
+            Gacc += (int32_t)F.g_off.size() - 1; PGacc += (int64_t)F.vw.size();
+        }
+        std::string err;
+        const int rc = device_merge(mi, h->dcap, (int64_t)M.pass_cells.size(), M.foff.data(), M.dnv.data(), M.dim,
+                                    h->stream, h->mdl, h->dscratch, err);
+        if (rc) return fail(h, rc, err);
+    }
+    clk.mark("rebuild:merge");
     if (DL) {
         std::string err;
         const int rc = device_r2(M, *DL, fuse, h->stream, M.fluid_r2, err);
         if (rc) return fail(h, rc, err);
         slope_items(M, (int32_t)h->dcap, fuse);
     }
-    clk.mark("rebuild:merge");
+    clk.mark("rebuild:r2");
     if (!parts.empty()) {
         if (M.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
         int dev_smem = 0;
@@ -1923,6 +1965,8 @@ int kg_destroy(kg_handle* h) {
     cudaStreamSynchronize(h->aux);
     free_pools(h);
     release_pools(h->spare_pools);
+    h->mdl.release();
+    h->cur_dl = nullptr;
     h->dscratch.release();
     if (h->d_tri) cudaFree(h->d_tri);
     if (h->sv_buf) cudaFree(h->sv_buf);
@@ -2163,6 +2207,9 @@ int kg_autotune(kg_handle* h, int enable) {
 
 int kg_device_flatten(kg_handle* h, int enable) {
     if (!h) return KG_ERR_ARG;
+    if (h->is_batch && h->devflat != (enable != 0))
+        for (const Problem& pb : h->probs)
+            if (pb.live) return fail(h, KG_ERR_STATE, "a batch's problems share one layout builder: set it before the first admission");
     h->devflat = enable != 0;
     return KG_OK;
 }
@@ -2173,8 +2220,7 @@ int kg_layout_read(kg_handle* h, const char* name, void* out, int64_t cap, int64
     int rc = rebuild(h);
     if (rc) return rc;
     const Flat& M = h->M;
-    const bool dl = h->live.size() == 1 && h->probs[h->live[0]].F.devlay;
-    const DevLayout* L = dl ? &h->probs[h->live[0]].dl : nullptr;
+    const DevLayout* L = h->cur_dl;
     const Dev& P = h->dev;
     const void* ptr = nullptr;
     int64_t n = -1;
@@ -2263,17 +2309,19 @@ int kg_batch_admit(kg_handle* h, const kg_params* params, const kg_topology* top
         return fail(h, KG_ERR_ARG, "a batch holds problems of one dim / precision / flux / marching");
     if (!(dt > 0.0)) return fail(h, KG_ERR_ARG, "dt must be > 0");
     cudaSetDevice(h->device);
-    Flat F;
-    std::string err;
-    int rc = flatten(*params, *topo, F, err);
-    if (rc) return fail(h, rc, err);
-    if (F.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
     int s = -1;
     for (int i = 0; i < MAX_SLOTS; ++i) if (!h->probs[i].live) { s = i; break; }
     if (s < 0) return fail(h, KG_ERR_BUDGET, "all problem slots are in use");
     cudaStreamSynchronize(h->stream);
+    Flat F;
+    DevLayout dl;
+    std::string err;
+    int rc = h->devflat ? device_flatten(*params, *topo, s, h->stream, F, dl, h->dscratch, err) : flatten(*params, *topo, F, err);
+    if (rc) return fail(h, rc, err);
+    if (F.max_inc > MAX_INC) return fail(h, KG_ERR_TOPOLOGY, "a cell has more face incidences than supported");
     rc = place_problem(h, s, std::move(F), *params, f, w, prim, dt, step);
     if (rc) return rc;
+    h->probs[s].dl = dl;
     *slot = s;
     return KG_OK;
 }

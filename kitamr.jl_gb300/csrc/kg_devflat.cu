@@ -917,3 +917,194 @@ int device_r2(const Flat& M, DevLayout& L, bool fuse, cudaStream_t s, std::vecto
 }
 
 }  // namespace kg
+
+// ---- merging device-built layouts (a batch of problems) ------------------------------------
+namespace kg {
+namespace {
+
+__global__ void k_m_slope_ops(const SlopeOp* in, int64_t n, SlopeOp* out, int32_t dbase, int32_t snb) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    SlopeOp op = in[i];
+    op.cell += dbase;
+    op.listA += snb;
+    op.listB += snb;
+    out[i] = op;
+}
+__global__ void k_m_nbr(const NbrRef* in, int64_t n, NbrRef* out, int32_t dbase, int32_t pairacc) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    NbrRef r = in[i];
+    r.data += dbase;
+    r.pair = r.pair >= 0 ? r.pair + pairacc : r.pair;
+    out[i] = r;
+}
+__global__ void k_m_crit(const CritOp* in, int64_t n, CritOp* out, int32_t cacc) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    CritOp op = in[i];
+    op.listA += cacc;
+    op.listB += cacc;
+    out[i] = op;
+}
+__global__ void k_m_crit_nbr(const int32_t* in, int64_t n, int32_t* out, int32_t dbase) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) out[i] = in[i] >= 0 ? in[i] + dbase : -1;
+}
+__global__ void k_m_inc(const Incidence* in, int64_t n, Incidence* out, int32_t dbase, int64_t fbase, int64_t PGacc,
+                        int32_t pairacc, int32_t bcacc) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Incidence a = in[i];
+    if (a.other >= 0) {
+        a.other += dbase;
+        a.ofoff += fbase;
+        a.ogo += (int32_t)PGacc;
+    }
+    a.pair = a.pair >= 0 ? a.pair + pairacc : a.pair;
+    a.bc += bcacc;
+    out[i] = a;
+}
+// per fluid-list entry: the cell, the regular flag, the incidence range end, the flux record and
+// the regular cell's faces, at their merged positions
+__global__ void k_m_fluid(const int32_t* cells, const uint8_t* reg, const int32_t* inc_off, const FluxCell* fc,
+                          const RegRec* rr, int n, int32_t* cells_o, uint8_t* reg_o, int32_t* inc_off_o, FluxCell* fc_o,
+                          RegRec* rr_o, int32_t dbase, int64_t fbase, int64_t PGacc, int32_t incacc, int32_t Gacc, int D) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    cells_o[q] = cells[q] + dbase;
+    reg_o[q] = reg[q];
+    inc_off_o[q + 1] = inc_off[q + 1] + incacc;
+    FluxCell c = fc[q];
+    c.foff += fbase;
+    c.goff += PGacc;
+    c.cell += dbase;
+    c.inc0 += incacc;
+    c.gid += Gacc;
+    fc_o[q] = c;
+    RegRec r = rr[q];
+    if (reg[q]) {
+        for (int s = 0; s < 2 * D; ++s) { r.nfo[s] += fbase; r.nd[s] += dbase; }
+    }
+    rr_o[q] = r;
+}
+// one part's pass-cell entries into the merged pass order: entry k of pass p goes to
+// base[p] + k - off[p]
+__global__ void k_m_pass(const int32_t* pc, const int32_t* cop, int npc, const int32_t* off, const int32_t* base,
+                         int npass, int32_t* pc_o, int32_t* cop_o, int32_t dbase, int32_t sops) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= npc) return;
+    int p = 0;
+    while (p + 1 < npass && off[p + 1] <= k) ++p;
+    const int m = base[p] + k - off[p];
+    pc_o[m] = pc[k] + dbase;
+    cop_o[m] = cop[k] + sops;
+}
+
+}  // namespace
+
+int device_merge(const std::vector<MergeIn>& parts, int64_t n_data, int64_t npc_total, const int64_t* foff,
+                 const int32_t* dnv, int D, cudaStream_t s, DevLayout& M, DevScratch& S, std::string& err) {
+    int64_t nso = 0, nsn = 0, ncop = 0, ncn = 0, nfl = 0, ninc = 0, nbc = 0;
+    size_t tab = 0;
+    for (const MergeIn& p : parts) {
+        const DevLayout& L = *p.L;
+        nso += L.n_slope_ops; nsn += L.n_slope_nbr; ncop += L.n_crit_ops; ncn += L.n_crit_nbr;
+        nfl += L.n_fluid; ninc += L.n_inc; nbc += L.n_bc;
+        tab += 2 * p.pass_off.size();
+    }
+    size_t lb = bytes_of<SlopeOp>(nso) + bytes_of<NbrRef>(nsn) + 3 * bytes_of<int32_t>(npc_total) +
+                bytes_of<SlopeCell>(npc_total) + bytes_of<CritOp>(ncop) + bytes_of<int32_t>(ncn) +
+                bytes_of<int32_t>(nfl + 1) + bytes_of<Incidence>(ninc) + bytes_of<double>(nbc * MAXW) +
+                bytes_of<float>(nbc * 2 * MAXW) + 2 * bytes_of<uint8_t>(nfl) + bytes_of<FluxCell>(nfl) +
+                bytes_of<RegRec>(nfl) + bytes_of<R2Rec>(nfl) + 2 * bytes_of<int32_t>(n_data) + bytes_of<int32_t>(nfl) +
+                bytes_of<int64_t>(n_data + 1) + bytes_of<int32_t>(n_data);
+    M.release();
+    {
+        void* a = nullptr;
+        DF_CUDA(cudaMalloc(&a, lb));
+        M.arena = std::shared_ptr<void>(a, [](void* p) { cudaFree(p); });
+    }
+    M.bytes = lb;
+    Bump b{(char*)M.arena.get(), 0, lb};
+    M.slope_ops = b.take<SlopeOp>(nso);
+    M.slope_nbr = b.take<NbrRef>(nsn);
+    M.cell_slope_op = b.take<int32_t>(npc_total);
+    M.pass_cells = b.take<int32_t>(npc_total);
+    b.take<int32_t>(npc_total);
+    M.screc = b.take<SlopeCell>(npc_total);
+    M.crit_ops = b.take<CritOp>(ncop);
+    M.crit_nbr = b.take<int32_t>(ncn);
+    M.inc_off = b.take<int32_t>(nfl + 1);
+    M.inc = b.take<Incidence>(ninc);
+    M.bc_prim = b.take<double>(nbc * MAXW);
+    M.bc_hl = b.take<float>(nbc * 2 * MAXW);
+    M.fluid_reg = b.take<uint8_t>(nfl);
+    M.fluid_r2 = b.take<uint8_t>(nfl);
+    M.fcrec = b.take<FluxCell>(nfl);
+    M.regrec = b.take<RegRec>(nfl);
+    M.r2rec = b.take<R2Rec>(nfl);
+    M.fluid_cells = b.take<int32_t>(nfl);
+    M.dsc = b.take<int32_t>(n_data);
+    M.dfl = b.take<int32_t>(n_data);
+    int64_t* d_foff = b.take<int64_t>(n_data + 1);
+    int32_t* d_dnv = b.take<int32_t>(n_data);
+    M.n_slope_ops = nso; M.n_slope_nbr = nsn; M.n_pass = npc_total; M.n_crit_ops = ncop; M.n_crit_nbr = ncn;
+    M.n_fluid = nfl; M.n_inc = ninc; M.n_bc = nbc; M.n_data = n_data;
+    DF_CUDA(cudaMemsetAsync(M.arena.get(), 0, lb, s));
+    DF_CUDA(cudaMemcpyAsync(d_foff, foff, sizeof(int64_t) * (n_data + 1), cudaMemcpyHostToDevice, s));
+    DF_CUDA(cudaMemcpyAsync(d_dnv, dnv, sizeof(int32_t) * n_data, cudaMemcpyHostToDevice, s));
+    // the per-part pass tables (local pass offsets, merged bases) through the pinned scratch
+    DF_CUDA(grow(S, std::max<size_t>(4 * tab, 256), std::max<size_t>(4 * tab, 256)));
+    int32_t* pin = (int32_t*)S.pin;
+    {
+        size_t at = 0;
+        for (const MergeIn& p : parts) {
+            for (size_t i = 0; i < p.pass_off.size(); ++i) pin[at + i] = p.pass_off[i];
+            for (size_t i = 0; i < p.pass_base.size(); ++i) pin[at + p.pass_off.size() + i] = p.pass_base[i];
+            at += 2 * p.pass_off.size();
+        }
+        if (tab) DF_CUDA(cudaMemcpyAsync(S.dev, pin, 4 * tab, cudaMemcpyHostToDevice, s));
+    }
+    int64_t so = 0, sn = 0, co = 0, cn = 0, fl = 0, ic = 0, bc = 0;
+    size_t at = 0;
+    for (const MergeIn& p : parts) {
+        const DevLayout& L = *p.L;
+        if (L.n_slope_ops) k_m_slope_ops<<<grid_of((int)L.n_slope_ops), 256, 0, s>>>(L.slope_ops, L.n_slope_ops, M.slope_ops + so, p.dbase, p.snb);
+        if (L.n_slope_nbr) k_m_nbr<<<grid_of((int)L.n_slope_nbr), 256, 0, s>>>(L.slope_nbr, L.n_slope_nbr, M.slope_nbr + sn, p.dbase, p.pairacc);
+        if (L.n_crit_ops) k_m_crit<<<grid_of((int)L.n_crit_ops), 256, 0, s>>>(L.crit_ops, L.n_crit_ops, M.crit_ops + co, p.cacc);
+        if (L.n_crit_nbr) k_m_crit_nbr<<<grid_of((int)L.n_crit_nbr), 256, 0, s>>>(L.crit_nbr, L.n_crit_nbr, M.crit_nbr + cn, p.dbase);
+        if (L.n_inc) k_m_inc<<<grid_of((int)L.n_inc), 256, 0, s>>>(L.inc, L.n_inc, M.inc + ic, p.dbase, p.fbase, p.PGacc, p.pairacc, p.bcacc);
+        if (L.n_fluid)
+            k_m_fluid<<<grid_of((int)L.n_fluid), 128, 0, s>>>(L.fluid_cells, L.fluid_reg, L.inc_off, L.fcrec, L.regrec, (int)L.n_fluid,
+                                                             M.fluid_cells + fl, M.fluid_reg + fl, M.inc_off + fl, M.fcrec + fl,
+                                                             M.regrec + fl, p.dbase, p.fbase, p.PGacc, p.incacc, p.Gacc, D);
+        if (L.n_bc) {
+            DF_CUDA(cudaMemcpyAsync(M.bc_prim + bc * MAXW, L.bc_prim, sizeof(double) * L.n_bc * MAXW, cudaMemcpyDeviceToDevice, s));
+            DF_CUDA(cudaMemcpyAsync(M.bc_hl + bc * 2 * MAXW, L.bc_hl, sizeof(float) * L.n_bc * 2 * MAXW, cudaMemcpyDeviceToDevice, s));
+        }
+        if (L.n_pass) {
+            const int32_t* off = (const int32_t*)S.dev + at;
+            const int32_t* base = off + p.pass_off.size();
+            k_m_pass<<<grid_of((int)L.n_pass), 256, 0, s>>>(L.pass_cells, L.cell_slope_op, (int)L.n_pass, off, base,
+                                                          (int)p.pass_base.size(), M.pass_cells, M.cell_slope_op, p.dbase, p.sops);
+        }
+        at += 2 * p.pass_off.size();
+        so += L.n_slope_ops; sn += L.n_slope_nbr; co += L.n_crit_ops; cn += L.n_crit_nbr;
+        fl += L.n_fluid; ic += L.n_inc; bc += L.n_bc;
+    }
+    // the slope records from the merged arrays
+    DT T;
+    std::memset(&T, 0, sizeof(DT));
+    T.D = D;
+    T.foff = d_foff;
+    T.dnv = d_dnv;
+    if (npc_total)
+        k_screc<<<grid_of((int)npc_total, 128), 128, 0, s>>>(T, M.pass_cells, (int)npc_total, M.cell_slope_op, M.slope_ops,
+                                                            M.slope_nbr, M.screc);
+    DF_CUDA(cudaGetLastError());
+    DF_CUDA(cudaStreamSynchronize(s));   // the pinned tables are read by the copy above
+    return KG_OK;
+}
+
+}  // namespace kg

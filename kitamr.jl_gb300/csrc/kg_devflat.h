@@ -53,6 +53,24 @@ struct DevScratch {
 int device_flatten(const kg_params& prm, const kg_topology& t, int slot, cudaStream_t s, Flat& F, DevLayout& L,
                    DevScratch& S, std::string& err, double* t_ms = nullptr);
 
+// One device-built problem of a batch and its offsets in the merged layout (the host merge's
+// accumulators: data and f base, slope-neighbour, slope-op, criterion-neighbour, incidence,
+// boundary-record, pairing, grid and velocity-cell counts before it), with its local pass
+// offsets and the merged start of each of its passes.
+struct MergeIn {
+    const DevLayout* L = nullptr;
+    int64_t fbase = 0, PGacc = 0;
+    int32_t dbase = 0, snb = 0, sops = 0, cacc = 0, incacc = 0, bcacc = 0, pairacc = 0, Gacc = 0;
+    std::vector<int32_t> pass_off;
+    std::vector<int32_t> pass_base;
+};
+
+// The merged gather form of device-built problems in M, equal to the host merge of their
+// host-built forms; foff, dnv: the merged data table (host arrays, n_data entries and one more
+// for foff); npc_total: the merged pass-cell entries.
+int device_merge(const std::vector<MergeIn>& parts, int64_t n_data, int64_t npc_total, const int64_t* foff,
+                 const int32_t* dnv, int D, cudaStream_t s, DevLayout& M, DevScratch& S, std::string& err);
+
 // The R2 records and flags of a device-built layout (slopes in the flux kernel; zeros unless
 // fuse and 2D); the flags also into r2 (host).
 int device_r2(const Flat& M, DevLayout& L, bool fuse, cudaStream_t s, std::vector<uint8_t>& r2, std::string& err);

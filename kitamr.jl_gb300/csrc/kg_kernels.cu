@@ -759,14 +759,18 @@ __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const double*
 // FP32 hi + lo pairs of x, U and lam, so no FP64 instruction runs per entry.
 // (entry a of axis d at E[(d * max_axis + a) * TS]: TS = 4 for the packed kernel's interleaved
 // table of (M_c, M_n, u) factors)
-template <int D, int NT = BLOCK, int TS = 1>
+// CW (TS = 4, the collision Maxwellian's table): the peculiar velocity c_d = (u_d - U_hi) - U_lo
+// of each axis entry goes to the record's fourth float, so the per-velocity passes read it
+template <int D, int NT = BLOCK, int TS = 1, bool CW = false>
 __device__ __forceinline__ void gauss_table(const Dev& P, int gid, const float* Uh, const float* Ul, float lh,
                                             float ll, float* E) {
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         const int a0 = P.ax_off[gid * MAXD + d], na = P.ax_off[gid * MAXD + d + 1] - a0;
-        for (int a = threadIdx.x; a < na; a += NT)
+        for (int a = threadIdx.x; a < na; a += NT) {
             E[(d * P.max_axis + a) * TS] = exp_gauss_ff(P.ax_hi[a0 + a], P.ax_lo[a0 + a], Uh[d], Ul[d], lh, ll);
+            if constexpr (CW) E[(d * P.max_axis + a) * TS + 3] = (P.ax_hi[a0 + a] - Uh[d]) - Ul[d];
+        }
     }
 }
 
@@ -1000,7 +1004,7 @@ __device__ __forceinline__ void cell_constants(const Dev& P, int cell, int slot,
         gauss_table<D, NT>(P, gid, &sscal[1], sscal[D + 1], (double*)Ec);
         if (need_n) gauss_table<D, NT>(P, gid, &sscal[MAXW + 1], sscal[MAXW + D + 1], (double*)En);
     } else {
-        gauss_table<D, NT, TS>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
+        gauss_table<D, NT, TS, TS == 4>(P, gid, (const float*)&sc[C_UH], (const float*)&sc[C_UL], (float)sc[C_LCH], (float)sc[C_LCL], (float*)Ec);
         if (need_n)
             gauss_table<D, NT, TS>(P, gid, (const float*)&sc[C_UNH], (const float*)&sc[C_UNL], (float)sc[C_LNH], (float)sc[C_LNL], (float*)En);
     }
@@ -1627,7 +1631,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     float rdm[4], rsa[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) { rdm[q] = RR.dxm_f[q]; rsa[q] = RR.sa_f[q]; }
-    // per axis entry a of the grid: (M_c factor, M_n factor, u_d, -) in one 16-byte record, so
+    // per axis entry a of the grid: (M_c factor, M_n factor, u_d, c_d) in one 16-byte record, so
     // a velocity's metadata is its two axis indices and its weight (8 bytes) and one shared
     // load per axis (the u_d here are the FP32 velocities of the grid, bit for bit)
     float2* fst = reinterpret_cast<float2*>(sh_raw);               // convected (h, b) per velocity
@@ -1784,7 +1788,6 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         cell_constants<D, 2, float, NT, 4>(P, cell, slot, PP, dt, FC.invV, red, sscal, sc, &T4[0].x, FC.gid);
     }
     const float prec = sc[C_PREC], pren = sc[C_PREN], bfc = sc[C_BFC], bfn = sc[C_BFN];
-    const float Uh0 = sc[C_UH], Uh1 = sc[C_UH + 1], Ul0 = sc[C_UL], Ul1 = sc[C_UL + 1];
     // ---- 3. conservation correction f += M(prim_c) - M(prim) (CAIDVM marching) and q -------
     {
         float2 q2 = bc2(0.f);
@@ -1806,7 +1809,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             } else {
                 fv = make_float2(fc[i], fc[nv + i]);   // Euler: q of f before convection
             }
-            const float c0 = (ta.z - Uh0) - Ul0, c1 = (tb.z - Uh1) - Ul1;
+            const float c0 = ta.w, c1 = tb.w;   // (u_d - U_hi) - U_lo from the table
             float c2 = c0 * c0;
             c2 += c1 * c1;
             const float hb = c2 * fv.x + fv.y;
@@ -1831,7 +1834,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             float mc = prec;
             mc *= ta.x;
             mc *= tb.x;
-            const float c0 = (ta.z - Uh0) - Ul0, c1 = (tb.z - Uh1) - Ul1;
+            const float c0 = ta.w, c1 = tb.w;   // (u_d - U_hi) - U_lo from the table
             float c2 = c0 * c0;
             c2 += c1 * c1;
             float cq = c0 * qa0;

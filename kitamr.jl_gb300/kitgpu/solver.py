@@ -323,12 +323,14 @@ MAX_SLOTS = 4096
 class GpuBatch:
     """A batch handle: independent problems advanced together on one device."""
 
-    def __init__(self, params: abi.KgParams, pool_bytes: int, device: int = 0):
+    def __init__(self, params: abi.KgParams, pool_bytes: int, device: int = 0, device_flatten: bool = True):
         self.L = load_library()
         self.params = params
         h = C.c_void_p()
         _check(self.L, None, self.L.kg_batch_create(C.byref(params), device, int(pool_bytes), C.byref(h)))
         self.h = h
+        # the gather form of admitted / adapted problems built on the device (default) or host
+        _check(self.L, self.h, self.L.kg_device_flatten(self.h, int(device_flatten)))
         self.meta = {}            # slot -> (topo, foff)
         self._reports = (abi.KgStepReport * MAX_SLOTS)()
 
@@ -442,6 +444,10 @@ class GpuBatch:
 
     def fuse_slopes(self, enable: bool = True):
         _check(self.L, self.h, self.L.kg_fuse_slopes(self.h, int(enable)))
+
+    def layout_read(self, name: str) -> bytes:
+        """The named array of the merged gather form the next step reads, as raw bytes."""
+        return GpuStep.layout_read(self, name)
 
     def autotune_result(self):
         return _autotune_result(self.L, self.h)

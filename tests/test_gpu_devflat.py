@@ -131,3 +131,34 @@ def test_device_layout_after_adaptation(name, make_old, make_new):
     _same_state(a, b, name + " adapted")
     a.close()
     b.close()
+
+
+def test_device_layout_equals_host_in_a_batch():
+    """Problems admitted to a batch handle: each built on the device and the layouts merged on
+    the device equal the host builder's merge, across a release and an admission."""
+    from kitgpu.solver import GpuBatch
+    probs = [cases.sod(scale=0.125, nv=16), cases.cavity(n=8, nv=12, levels=1, Kn=0.01),
+             cases.cylinder(scale=0.125, nv=16, vs_levels=1), cases.collision(center=0.5)]
+    built = [cases.build(p) for p in probs]
+    prec = abi.KG_PREC_MIXED
+    handles = [GpuBatch(abi.make_params(probs[0], precision=prec), 512 << 20, device_flatten=dev) for dev in (True, False)]
+    slots = [[], []]
+    for b, sl in zip(handles, slots):
+        for p, (t, s) in zip(probs[:3], built[:3]):
+            sl.append(b.admit(abi.make_params(p, precision=prec, st_check_interval=2), t, s["f"], s["w"], s["prim"], p.dt()))
+    _same_layout(handles[0], handles[1], "batch of three")
+    for b in handles:
+        b.step(2)
+    for b, sl in zip(handles, slots):
+        b.release(sl[0])
+        p3, (t3, s3) = probs[3], built[3]
+        b.admit(abi.make_params(p3, precision=prec, st_check_interval=2), t3, s3["f"], s3["w"], s3["prim"], p3.dt())
+    _same_layout(handles[0], handles[1], "batch after a release and an admission")
+    for b in handles:
+        b.step(2)
+    for k in slots[0][1:]:
+        x, y = handles[0].download(k), handles[1].download(k)
+        for key in ("f", "w", "prim", "qf"):
+            assert np.array_equal(x[key], y[key]), key
+    for b in handles:
+        b.close()
