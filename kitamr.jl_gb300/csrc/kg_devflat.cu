@@ -1076,7 +1076,7 @@ int device_merge(const std::vector<MergeIn>& parts, int64_t n_data, int64_t npc_
         if (L.n_crit_nbr) k_m_crit_nbr<<<grid_of((int)L.n_crit_nbr), 256, 0, s>>>(L.crit_nbr, L.n_crit_nbr, M.crit_nbr + cn, p.dbase);
         if (L.n_inc) k_m_inc<<<grid_of((int)L.n_inc), 256, 0, s>>>(L.inc, L.n_inc, M.inc + ic, p.dbase, p.fbase, p.PGacc, p.pairacc, p.bcacc);
         if (L.n_fluid)
-            k_m_fluid<<<grid_of((int)L.n_fluid), 128, 0, s>>>(L.fluid_cells, L.fluid_reg, L.inc_off, L.fcrec, L.regrec, (int)L.n_fluid,
+            k_m_fluid<<<grid_of((int)L.n_fluid, 128), 128, 0, s>>>(L.fluid_cells, L.fluid_reg, L.inc_off, L.fcrec, L.regrec, (int)L.n_fluid,
                                                              M.fluid_cells + fl, M.fluid_reg + fl, M.inc_off + fl, M.fcrec + fl,
                                                              M.regrec + fl, p.dbase, p.fbase, p.PGacc, p.incacc, p.Gacc, D);
         if (L.n_bc) {

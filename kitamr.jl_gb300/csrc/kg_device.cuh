@@ -147,27 +147,46 @@ __device__ __forceinline__ void two_sum_acc(float& h, float& l, float h2, float 
     l = l + l2 + err;
     h = sum;
 }
+// The warp stage transposes as it sums: with the N elements padded to P = 2^K, each exchange
+// at offset 16, 8, ... hands the partner the half of the elements it keeps and adds the half it
+// receives, so after K exchanges every lane holds one element (e = lane >> (5 - K)) summed over
+// 2^K lanes, and plain butterflies at the remaining offsets finish it: 2 (P - 1) + 2 (5 - K)
+// shuffles and P - 1 + 5 - K float-float additions instead of 10 N and 5 N.
+template <int N> struct Pow2 { static constexpr int K = N <= 1 ? 0 : N <= 2 ? 1 : N <= 4 ? 2 : N <= 8 ? 3 : N <= 16 ? 4 : 5; };
 template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], double (&out)[N], double* sred) {
     // sred: shared scratch of at least N * (NT/32) doubles; NT: threads of the block
     constexpr int NWARP = NT / 32;
     static_assert(NWARP == 4 || NWARP == 8, "the warp-0 stage maps NWARP lanes per element");
+    static_assert(N <= 32, "at most 32 elements");
     constexpr int GROUPS = 32 / NWARP;            // elements per round of warp 0
+    constexpr int K = Pow2<N>::K, P = 1 << K;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float h[P], l[P];
 #pragma unroll
-    for (int e = 0; e < N; ++e) {
-        float h = hi[e], l = lo[e];
+    for (int e = 0; e < P; ++e) { h[e] = e < N ? hi[e] : 0.f; l[e] = e < N ? lo[e] : 0.f; }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            two_sum_acc(h, l, __shfl_xor_sync(0xffffffffu, h, o), __shfl_xor_sync(0xffffffffu, l, o));
-        hi[e] = h;
-        lo[e] = l;
+    for (int s = 0; s < K; ++s) {
+        const int o = 16 >> s, c = P >> s, half = c >> 1;
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int j = 0; j < half; ++j) {
+            const float mh = up ? h[j + half] : h[j], ml = up ? l[j + half] : l[j];
+            const float sh = up ? h[j] : h[j + half], sl = up ? l[j] : l[j + half];
+            float rh = mh, rl = ml;
+            two_sum_acc(rh, rl, __shfl_xor_sync(0xffffffffu, sh, o), __shfl_xor_sync(0xffffffffu, sl, o));
+            h[j] = rh;
+            l[j] = rl;
+        }
     }
+#pragma unroll
+    for (int o = 16 >> K; o > 0; o >>= 1)
+        two_sum_acc(h[0], l[0], __shfl_xor_sync(0xffffffffu, h[0], o), __shfl_xor_sync(0xffffffffu, l[0], o));
     float2* sf = reinterpret_cast<float2*>(sred);   // [N][NWARP] partials
     __syncthreads();
-    if (lane == 0) {
-#pragma unroll
-        for (int e = 0; e < N; ++e) sf[e * NWARP + wid] = make_float2(hi[e], lo[e]);
+    {
+        const int e = lane >> (5 - K);
+        if ((lane & ((1 << (5 - K)) - 1)) == 0 && e < N) sf[e * NWARP + wid] = make_float2(h[0], l[0]);
     }
     __syncthreads();
     if (wid == 0) {
