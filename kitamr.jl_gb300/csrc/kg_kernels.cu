@@ -1588,8 +1588,16 @@ __device__ __forceinline__ float2 pp_theta2(float2 f, float2 s0, float2 s1, floa
 __device__ __forceinline__ float2 minmod2(float2 a, float2 b) { return make_float2(minmod(a.x, b.x), minmod(a.y, b.y)); }
 __device__ __forceinline__ float2 dslope2(float2 f, float2 fn, float inv) { return mul2(fma2(fn, bc2(-1.f), f), bc2(inv)); }
 
-// R2: the cell's slopes and its upwind neighbours' are computed here from f (R2Rec), so no sdf is read
-template <int NT, int VPT, bool R2>
+// R2: the cell's slopes and its upwind neighbours' are computed here from f (R2Rec), so no sdf is read.
+// INNER: a cell whose faces are all inner faces to fluid cells on its own velocity grid, at most
+// two sub-faces a side (hanging faces, neighbours of other sizes: packed_inner_ok); per velocity
+// and direction the sub-faces of the side it leaves through take its own reconstruction, those
+// of the side it enters through the neighbour's.
+struct PSub {                 // one sub-face of a side (INNER): the incidence's FP32 geometry
+    float dxm0, dxm1, dxo0, dxo1, ods0, ods1, sa, pad;
+    int64_t ofoff;
+};
+template <int NT, int VPT, bool R2, bool INNER = false>
 __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx) {
     constexpr int D = 2;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -1597,6 +1605,8 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     __shared__ double sscal[4 * MAXW];
     __shared__ float sc[C_N];
     __shared__ int64_t nfo[4];
+    __shared__ PSub psub[INNER ? 4 : 1][INNER ? 2 : 1];
+    __shared__ int pcnt[INNER ? 4 : 1];
     const FluxCell FC = P.fcrec[fcx];
     const int nv = FC.nv;
     if (threadIdx.x == 32) {
@@ -1616,7 +1626,24 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     // the four faces (side 2 * dir + (face at +ds/2)): neighbour f offset (shared memory),
     // dxm and area factor (registers)
     const RegRec& RR = P.regrec[fcx];
-    if (threadIdx.x < 4) nfo[threadIdx.x] = RR.nfo[threadIdx.x];
+    if (!INNER && threadIdx.x < 4) nfo[threadIdx.x] = RR.nfo[threadIdx.x];
+    if constexpr (INNER) {
+        // the sub-faces by side (the incidences of such a cell: at most 2 a side, checked)
+        if (threadIdx.x == 0) {
+            int cnt[4] = {0, 0, 0, 0};
+            for (int e = 0; e < FC.ninc; ++e) {
+                const Incidence& a = P.inc[FC.inc0 + e];
+                const int d = a.dir;
+                const int sd = 2 * d + (a.dxm_f[d] > 0.f ? 1 : 0);
+                const int k = cnt[sd] < 2 ? cnt[sd]++ : 1;
+                PSub q;
+                q.dxm0 = a.dxm_f[0]; q.dxm1 = a.dxm_f[1]; q.dxo0 = a.dxo_f[0]; q.dxo1 = a.dxo_f[1];
+                q.ods0 = a.ods_f[0]; q.ods1 = a.ods_f[1]; q.sa = a.sarea_f; q.pad = 0.f; q.ofoff = a.ofoff;
+                psub[sd][k] = q;
+            }
+            for (int sd = 0; sd < 4; ++sd) pcnt[sd] = cnt[sd];
+        }
+    }
     // R2: the neighbours' neighbours and slope factors, and the cell's own slope factors
     __shared__ int64_t snn[R2 ? 16 : 1];
     __shared__ float sninv[R2 ? 16 : 1], ssinv[R2 ? 4 : 1];
@@ -1630,7 +1657,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     }
     float rdm[4], rsa[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) { rdm[q] = RR.dxm_f[q]; rsa[q] = RR.sa_f[q]; }
+    for (int q = 0; q < 4; ++q) { rdm[q] = INNER ? 0.f : RR.dxm_f[q]; rsa[q] = INNER ? 0.f : RR.sa_f[q]; }
     // per axis entry a of the grid: (M_c factor, M_n factor, u_d, c_d) in one 16-byte record, so
     // a velocity's metadata is its two axis indices and its weight (8 bytes) and one shared
     // load per axis (the u_d here are the FP32 velocities of the grid, bit for bit)
@@ -1746,6 +1773,61 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             acc = fma2(bc2(sai), mi, acc);
         }
     };
+    // INNER: the flux sum of velocity i through the sub-faces of the four sides (the loads of
+    // the two sides it enters through first)
+    auto gather_inner = [&](int i, const float4& V, float2& f2, float2& acc) {
+        const float u0 = V.x, u1 = V.y;
+        f2 = make_float2(fc[i], fc[nv + i]);
+        const float2 s0 = make_float2(scl[i], scl[nv + i]);
+        const float2 s1 = make_float2(scl[2 * nv + i], scl[3 * nv + i]);
+        float2 g2[D][2], t0[D][2], t1[D][2];
+        int so[D], si[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const bool pos = (d == 0 ? u0 : u1) > 0.f;
+            so[d] = 2 * d + (pos ? 1 : 0);
+            si[d] = 2 * d + (pos ? 0 : 1);
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                // a side with one sub-face reads that one twice (in flight together; unused)
+                const int64_t no = psub[si[d]][k < pcnt[si[d]] ? k : 0].ofoff;
+                const float* of = fbase + no;
+                const float* os = sbase + no * D;
+                g2[d][k] = make_float2(of[i], of[nv + i]);
+                t0[d][k] = make_float2(os[i], os[nv + i]);
+                t1[d][k] = make_float2(os[2 * nv + i], os[3 * nv + i]);
+            }
+        }
+        const float2 th = pp_theta2(f2, s0, s1, ds0, ds1);
+        acc = bc2(0.f);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            const float ud = d == 0 ? u0 : u1;
+            // outgoing through the side the velocity points at: the own reconstruction
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k >= pcnt[so[d]]) break;
+                const PSub& q = psub[so[d]][k];
+                const float dx0 = q.dxm0 - u0 * adt;
+                const float dx1 = q.dxm1 - u1 * adt;
+                const float2 sdx = fma2(bc2(dx1), s1, mul2(bc2(dx0), s0));
+                const float2 mo = mul2(fma2(th, sdx, f2), bc2(ud));
+                acc = fma2(bc2(q.sa), mo, acc);
+            }
+            // incoming through the opposite side: the neighbours' reconstructions
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+                if (k >= pcnt[si[d]]) break;
+                const PSub& q = psub[si[d]][k];
+                const float ndx0 = q.dxo0 - u0 * adt;
+                const float ndx1 = q.dxo1 - u1 * adt;
+                const float2 nsdx = fma2(bc2(ndx1), t1[d][k], mul2(bc2(ndx0), t0[d][k]));
+                const float2 thn = pp_theta2(g2[d][k], t0[d][k], t1[d][k], q.ods0, q.ods1);
+                const float2 mi = mul2(fma2(thn, nsdx, g2[d][k]), bc2(ud));
+                acc = fma2(bc2(q.sa), mi, acc);
+            }
+        }
+    };
     // the convected f, and the macro flux (CAIDVM) with the moments of the convected f (CAIDVM
     // marching) or of f (Euler) as the pairs (flux, f) in one set of packed sums
     auto finish = [&](int i, const float4& V, const float2& f2, const float2& acc) {
@@ -1774,7 +1856,10 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             V[v] = vel(iv[v]);
         }
 #pragma unroll
-        for (int v = 0; v < VPT; ++v) gather(iv[v], V[v], f2[v], acc[v]);
+        for (int v = 0; v < VPT; ++v) {
+            if constexpr (INNER) gather_inner(iv[v], V[v], f2[v], acc[v]);
+            else gather(iv[v], V[v], f2[v], acc[v]);
+        }
 #pragma unroll
         for (int v = 0; v < VPT; ++v)
             if (v == 0 || i0 + v * NT < nv) finish(iv[v], V[v], f2[v], acc[v]);
@@ -1887,6 +1972,41 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
 template <int NT, int VPT, bool R2>
 __global__ void __launch_bounds__(NT, (R2 ? 3 : (VPT == 1 ? 4 : KG_PACKED_MINB)) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
     flux_regular_packed<NT, VPT, R2>(P, list[blockIdx.x]);
+}
+// the cells of packed_inner_ok, one CTA each
+template <int NT>
+__global__ void __launch_bounds__(NT, 3 * (BLOCK / NT)) flux_packed_inner_kernel(Dev P, const int32_t* list) {
+    flux_regular_packed<NT, 1, false, true>(P, list[blockIdx.x]);
+}
+
+// Per fluid-list entry: 1 when the packed kernel's INNER form takes the cell (not regular; every
+// incidence an inner face to a fluid cell on the same velocity grid, leaving through the side
+// its face points at; one or two sub-faces on each of the four sides), else 0.
+__global__ void packed_inner_ok_kernel(Dev P, int n, uint8_t* out) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    uint8_t ok = 0;
+    if (!P.fluid_reg[q]) {
+        const FluxCell& FC = P.fcrec[q];
+        int cnt[4] = {0, 0, 0, 0};
+        ok = FC.ninc > 0;
+        for (int e = 0; e < FC.ninc && ok; ++e) {
+            const Incidence& a = P.inc[FC.inc0 + e];
+            const int d = a.dir;
+            ok = a.kind == INC_INNER && a.pair < 0 && d >= 0 && d < 2 && a.orient_f * a.dxm_f[d] < 0.f;
+            if (ok) {
+                const int sd = 2 * d + (a.dxm_f[d] > 0.f ? 1 : 0);
+                ok = ++cnt[sd] <= 2;
+            }
+        }
+        for (int sd = 0; sd < 4 && ok; ++sd) ok = cnt[sd] >= 1;
+    }
+    out[q] = ok;
+}
+cudaError_t launch_packed_inner_ok(const Dev& P, int n, uint8_t* out, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    packed_inner_ok_kernel<<<(n + 255) / 256, 256, 0, s>>>(P, n, out);
+    return cudaGetLastError();
 }
 
 // update_macro_slope! (Flux/Slope.jl:1022-1036): sw[:, dir] = calc_w0(midpoint, sdf[:, :, dir],
@@ -2932,6 +3052,20 @@ struct Launch {
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;   // R2 lists exist only for the 2D mixed form
+    }
+    // the packed kernel's INNER form, one CTA per listed entry (2D mixed form)
+    static cudaError_t flux_inner_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+        if (n <= 0) return cudaSuccess;
+        if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
+            const size_t smem = packed_smem(max_nv, P.max_axis);
+            using RegFn = void (*)(Dev, const int32_t*);
+            RegFn fn = P.flux_nt == 128 ? flux_packed_inner_kernel<128> : flux_packed_inner_kernel<BLOCK>;
+            cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            fn<<<n, P.flux_nt == 128 ? 128 : BLOCK, smem, s>>>(P, list);
+            return cudaGetLastError();
+        }
+        return cudaErrorInvalidValue;   // inner lists exist only for the 2D mixed form
     }
     // persistent schedule: `grid` resident CTAs; the counter must be zero at launch
     static cudaError_t flux_persistent(const Dev& P, int n, int max_nv, int grid, int* counter, const int32_t* order,
