@@ -302,7 +302,8 @@ def accuracy_single(prob, topo, state, acc_steps, oracle_steps, threads, oracle_
     return out
 
 
-FLUX_KERNELS = ("flux_packed_kernel", "flux_packed_kernel_r2", "flux_packed_inner_kernel", "flux_regular_kernel",
+FLUX_KERNELS = ("flux_packed_kernel", "flux_packed_kernel_r2", "flux_packed_inner_kernel", "flux_packed_inner_kernel_paired",
+                "flux_regular_kernel",
                 "flux_collide_kernel")
 
 

@@ -415,7 +415,7 @@ int kg_device_flatten(kg_handle *h, int enable);
 /* Test support: copies the named array of the gather form the next step reads ("slope_ops",
  * "slope_nbr", "cell_slope_op", "pass_cells", "screc", "crit_ops", "crit_nbr", "inc_off",
  * "inc", "bc_prim", "bc_hl", "fluid_cells", "fluid_reg", "fcrec", "regrec", "r2rec",
- * "slope_items", "reg_list", "nonreg_list", "r2_list", "inner_list", "p_off", "p_j0", "p_cnt", "ib_nbr",
+ * "slope_items", "reg_list", "nonreg_list", "r2_list", "inner_list", "innerp_list", "p_off", "p_j0", "p_cnt", "ib_nbr",
  * "wall_ops", "solid_ops") into out, up to cap bytes; *bytes receives the array's size.
  * No counterpart in the reference (it exposes its Julia objects instead).               */
 int kg_layout_read(kg_handle *h, const char *name, void *out, int64_t cap, int64_t *bytes);

@@ -23,7 +23,7 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t);
     static cudaError_t flux_r2_list(const Dev&, const int32_t*, int, int, cudaStream_t);
-    static cudaError_t flux_inner_list(const Dev&, const int32_t*, int, int, cudaStream_t);
+    static cudaError_t flux_inner_list(const Dev&, const int32_t*, int, int, bool, cudaStream_t);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t cip(const Dev&, int, cudaStream_t);
     static cudaError_t conserve(const Dev&, const int32_t*, int, cudaStream_t);
@@ -170,8 +170,9 @@ struct kg_handle {
     const int32_t* d_nonreg = nullptr; // every other entry
     const int32_t* d_r2 = nullptr;     // regular cells whose slopes the packed kernel computes
     const int32_t* d_inner = nullptr;  // cells of the packed kernel's INNER form (2D mixed form)
-    int n_reg = 0, n_nonreg = 0, n_r2 = 0, n_inner = 0;
-    int64_t ph_reg = 0, ph_nonreg = 0, ph_r2 = 0, ph_inner = 0;   // their phase cells (profile units)
+    const int32_t* d_innerp = nullptr; // the same with a neighbour on another velocity grid
+    int n_reg = 0, n_nonreg = 0, n_r2 = 0, n_inner = 0, n_innerp = 0;
+    int64_t ph_reg = 0, ph_nonreg = 0, ph_r2 = 0, ph_inner = 0, ph_innerp = 0;   // their phase cells (profile units)
     std::string err;
     bool is_batch = false;
     bool have_state = false;       // single-problem API: state uploaded
@@ -611,7 +612,7 @@ int rebuild(kg_handle* h) {
         if (smax > (size_t)dev_smem) return fail(h, KG_ERR_TOPOLOGY, "velocity grid too large for one CTA's shared memory");
     }
     // the launch lists of the flux kernels are filled in below (their arena regions reserved)
-    std::vector<int32_t> order, reg, nonreg, r2, inner;
+    std::vector<int32_t> order, reg, nonreg, r2, inner, innerp;
     Dev& P = h->dev;
     P = Dev{};
     P.dim = h->prm.dim; P.ndf = h->prm.ndf; P.n_cells = M.n_cells; P.n_walls = M.n_walls;
@@ -632,13 +633,13 @@ int rebuild(kg_handle* h) {
         UP(solid_ops, solid_ops); UP(wall_ops, wall_ops); UP(ib_nbr, ib_nbr); UP(ib_dx, ib_dx);
         UP(cut_idx, cut_idx); UP(cut_gw, cut_gw); UP(cut_sw, cut_sw); UP(cvcw, cvcw);
 #undef UP
-        void* lr[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+        void* lr[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
         int r = KG_OK;
-        for (int k = 0; k < 5 && !r; ++k) r = arena_reserve(h, sizeof(int32_t) * std::max(M.n_fluid, 1), &lr[k]);
-        if (!r) r = arena_reserve(h, std::max(M.n_fluid, 1), &lr[5]);
+        for (int k = 0; k < 6 && !r; ++k) r = arena_reserve(h, sizeof(int32_t) * std::max(M.n_fluid, 1), &lr[k]);
+        if (!r) r = arena_reserve(h, std::max(M.n_fluid, 1), &lr[6]);
         h->d_order = (const int32_t*)lr[0]; h->d_reg = (const int32_t*)lr[1]; h->d_nonreg = (const int32_t*)lr[2];
-        h->d_r2 = (const int32_t*)lr[3]; h->d_inner = (const int32_t*)lr[4];
-        inner_flags = (uint8_t*)lr[5];
+        h->d_r2 = (const int32_t*)lr[3]; h->d_inner = (const int32_t*)lr[4]; h->d_innerp = (const int32_t*)lr[5];
+        inner_flags = (uint8_t*)lr[6];
         const int32_t* dlive = nullptr;
         if (!r) r = upload_vec(h, h->live, &dlive);
         h->d_live = const_cast<int32_t*>(dlive);
@@ -710,7 +711,8 @@ int rebuild(kg_handle* h) {
         }
         for (int q = 0; q < M.n_fluid; ++q) {
             if (!M.fluid_reg[q]) {
-                if (inner_ok[q]) inner.push_back(q);
+                if (inner_ok[q] == 1) inner.push_back(q);
+                else if (inner_ok[q] == 2) innerp.push_back(q);
                 else { nonreg.push_back(q); order.push_back(q); }
             } else if (M.fluid_r2[q]) r2.push_back(q);
             else reg.push_back(q);
@@ -722,6 +724,7 @@ int rebuild(kg_handle* h) {
         h->n_nonreg = (int)nonreg.size();
         h->n_r2 = (int)r2.size();
         h->n_inner = (int)inner.size();
+        h->n_innerp = (int)innerp.size();
         auto phase = [&](const std::vector<int32_t>& l) {
             int64_t n = 0;
             for (int32_t q : l) n += M.dnv[M.fluid_cells[q]];
@@ -731,9 +734,10 @@ int rebuild(kg_handle* h) {
         h->ph_nonreg = phase(nonreg);
         h->ph_r2 = phase(r2);
         h->ph_inner = phase(inner);
-        const std::vector<int32_t>* lists[5] = {&order, &reg, &nonreg, &r2, &inner};
-        const int32_t* dst[5] = {h->d_order, h->d_reg, h->d_nonreg, h->d_r2, h->d_inner};
-        for (int k = 0; k < 5; ++k)
+        h->ph_innerp = phase(innerp);
+        const std::vector<int32_t>* lists[6] = {&order, &reg, &nonreg, &r2, &inner, &innerp};
+        const int32_t* dst[6] = {h->d_order, h->d_reg, h->d_nonreg, h->d_r2, h->d_inner, h->d_innerp};
+        for (int k = 0; k < 6; ++k)
             if (!lists[k]->empty())
                 KG_CUDA(h, cudaMemcpyAsync(const_cast<int32_t*>(dst[k]), lists[k]->data(), sizeof(int32_t) * lists[k]->size(),
                                            cudaMemcpyHostToDevice, h->stream));
@@ -772,7 +776,8 @@ cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, in
     const Flat& F = h->M;
     if (part == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
     if (part == 1) return dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
-    if (part == 3) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_inner, h->n_inner, F.max_nv, s); });
+    if (part == 3) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_inner, h->n_inner, F.max_nv, false, s); });
+    if (part == 4) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_innerp, h->n_innerp, F.max_nv, true, s); });
     if (h->n_nonreg == 0) return cudaSuccess;
     if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, s); });
     int nsm = 0;
@@ -784,7 +789,7 @@ cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, in
 
 cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
     cudaError_t e = cudaSuccess;
-    for (int part = 0; part < 4 && e == cudaSuccess; ++part) e = launch_flux_part(h, P, part, sched, ctas, s);
+    for (int part = 0; part < 5 && e == cudaSuccess; ++part) e = launch_flux_part(h, P, part, sched, ctas, s);
     return e;
 }
 
@@ -939,7 +944,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         end("slope_kernel");
         ++*launches;
     }
-    const int n_main = (h->n_r2 > 0 ? h->n_r2 : h->n_reg) + h->n_inner;
+    const int n_main = (h->n_r2 > 0 ? h->n_r2 : h->n_reg) + h->n_inner + h->n_innerp;
     const int n_aux = h->n_nonreg + (h->n_r2 > 0 ? h->n_reg : 0);
     if (!timed && h->sched == 0 && n_main > 0 && n_aux > 0) {
         // two streams after the slopes: the regular cells whose slopes the flux kernel computes
@@ -972,10 +977,11 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
         // the cells of the packed kernel's INNER form read no IB output: the handle's stream
         e = launch_flux_part(h, P, 3, 0, 0, s);
+        if (e == cudaSuccess) e = launch_flux_part(h, P, 4, 0, 0, s);
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_inner_kernel");
         KG_CUDA(h, cudaEventRecord(h->ev_join, a));
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
-        *launches += (h->n_nonreg > 0) + (h->n_reg > 0) + (h->n_r2 > 0) + (h->n_inner > 0);
+        *launches += (h->n_nonreg > 0) + (h->n_reg > 0) + (h->n_r2 > 0) + (h->n_inner > 0) + (h->n_innerp > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
             if (e != cudaSuccess) return cuda_fail(h, e, "cip_kernel");
@@ -1006,18 +1012,18 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         // the 2D mixed form outside CIP marching), the R2 cells' and the other cells'
         const bool packed = h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED && !P.fst_global &&
                             h->prm.marching != KG_MARCH_CIP;
-        const char* names[4] = {packed ? "flux_packed_kernel" : "flux_regular_kernel", "flux_packed_kernel_r2",
-                                "flux_collide_kernel", "flux_packed_inner_kernel"};
-        const int counts[4] = {h->n_reg, h->n_r2, h->n_nonreg, h->n_inner};
-        const int64_t units[4] = {h->ph_reg, h->ph_r2, h->ph_nonreg, h->ph_inner};
-        for (int part = 0; part < 4; ++part) {
+        const char* names[5] = {packed ? "flux_packed_kernel" : "flux_regular_kernel", "flux_packed_kernel_r2",
+                                "flux_collide_kernel", "flux_packed_inner_kernel", "flux_packed_inner_kernel_paired"};
+        const int counts[5] = {h->n_reg, h->n_r2, h->n_nonreg, h->n_inner, h->n_innerp};
+        const int64_t units[5] = {h->ph_reg, h->ph_r2, h->ph_nonreg, h->ph_inner, h->ph_innerp};
+        for (int part = 0; part < 5; ++part) {
             if (counts[part] == 0) continue;
             begin();
             e = launch_flux_part(h, P, part, h->sched, h->sched_ctas, s);
             if (e != cudaSuccess) return cuda_fail(h, e, names[part]);
             end(names[part], units[part]);
         }
-        *launches += (h->n_reg > 0) + (h->n_nonreg > 0) + (h->n_r2 > 0) + (h->n_inner > 0);
+        *launches += (h->n_reg > 0) + (h->n_nonreg > 0) + (h->n_r2 > 0) + (h->n_inner > 0) + (h->n_innerp > 0);
         if (h->prm.marching == KG_MARCH_CIP) {
             begin();
             e = dispatch(h, [&](auto L) { return decltype(L)::cip(P, F.n_fluid, s); });
@@ -2286,6 +2292,7 @@ int kg_layout_read(kg_handle* h, const char* name, void* out, int64_t cap, int64
     if (!std::strcmp(name, "nonreg_list")) { ptr = h->d_nonreg; n = (int64_t)h->n_nonreg * 4; }
     if (!std::strcmp(name, "r2_list")) { ptr = h->d_r2; n = (int64_t)h->n_r2 * 4; }
     if (!std::strcmp(name, "inner_list")) { ptr = h->d_inner; n = (int64_t)h->n_inner * 4; }
+    if (!std::strcmp(name, "innerp_list")) { ptr = h->d_innerp; n = (int64_t)h->n_innerp * 4; }
     if (n < 0) return fail(h, KG_ERR_ARG, std::string("unknown layout array ") + name);
     *bytes = n;
     if (out && n > 0) {

@@ -1264,7 +1264,18 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
         if (reg) {
             // regular cell: per direction the velocity leaves through the face it points at
             // (own reconstruction there) and enters through the opposite face (the upwind
-            // neighbour's reconstruction) -- the generic loop below with its branches resolved
+            // neighbour's reconstruction) -- the generic loop below with its branches resolved;
+            // the own limiter factor (positivity_preserving_reconstruct, the same for every
+            // face) once per velocity
+            A thown[NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                A sabs = 0;
+#pragma unroll
+                for (int d = 0; d < D; ++d) sabs += myds[d] * fabs(sr[k][d]);
+                const A th = fabs(lim_div(fr[k] - (A)JL_EPS, (A)0.5 * sabs + (A)EPS_REF));
+                thown[k] = th < (A)1 ? th : (A)1;
+            }
 #pragma unroll
             for (int d = 0; d < D; ++d) {
                 const A ud = u[d];
@@ -1281,7 +1292,10 @@ __device__ __forceinline__ void flux_collide_cell(const Dev& P, const int fcx) {
                 other_micro<D, NDF, T, A>(fi_.of, fi_.os, nv, i, u, dxo, myds, adt, d, 0, mi);
 #pragma unroll
                 for (int k = 0; k < NDF; ++k) {
-                    const A mo = own_recon<D, A>(0, fr[k], sr[k], dx, myds) * ud;
+                    A sdx = 0;
+#pragma unroll
+                    for (int d2 = 0; d2 < D; ++d2) sdx += dx[d2] * sr[k][d2];
+                    const A mo = (fr[k] + thown[k] * sdx) * ud;
                     acc[k] += fo_.sarea * mo;
                     acc[k] += fi_.sarea * mi[k];
                 }
@@ -1589,15 +1603,19 @@ __device__ __forceinline__ float2 minmod2(float2 a, float2 b) { return make_floa
 __device__ __forceinline__ float2 dslope2(float2 f, float2 fn, float inv) { return mul2(fma2(fn, bc2(-1.f), f), bc2(inv)); }
 
 // R2: the cell's slopes and its upwind neighbours' are computed here from f (R2Rec), so no sdf is read.
-// INNER: a cell whose faces are all inner faces to fluid cells on its own velocity grid, at most
-// two sub-faces a side (hanging faces, neighbours of other sizes: packed_inner_ok); per velocity
-// and direction the sub-faces of the side it leaves through take its own reconstruction, those
-// of the side it enters through the neighbour's.
+// INNER: a cell whose faces are all inner faces to fluid cells, one or two sub-faces a side
+// (hanging faces, neighbours of other sizes or on other velocity grids: packed_inner_ok); per
+// velocity and direction the sub-faces of the side it leaves through take its own
+// reconstruction, those of the side it enters through the neighbour's (INNER = 2: through the
+// pairing runs from another grid, whose macro flux is then summed on that grid; INNER = 1: every
+// neighbour on the cell's own grid).
 struct PSub {                 // one sub-face of a side (INNER): the incidence's FP32 geometry
-    float dxm0, dxm1, dxo0, dxo1, ods0, ods1, sa, pad;
-    int64_t ofoff;
+    float dxm0, dxm1, dxo0, dxo1, ods0, ods1, sa;
+    int32_t pair;             // pairing (my grid <- the neighbour's), -1: the same grid
+    int64_t ofoff;            // the neighbour's f offset
+    int32_t onv, ogo;         // its velocity count and grid offset
 };
-template <int NT, int VPT, bool R2, bool INNER = false>
+template <int NT, int VPT, bool R2, int INNER = 0>
 __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx) {
     constexpr int D = 2;
     extern __shared__ __align__(16) unsigned char sh_raw[];
@@ -1638,7 +1656,8 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
                 const int k = cnt[sd] < 2 ? cnt[sd]++ : 1;
                 PSub q;
                 q.dxm0 = a.dxm_f[0]; q.dxm1 = a.dxm_f[1]; q.dxo0 = a.dxo_f[0]; q.dxo1 = a.dxo_f[1];
-                q.ods0 = a.ods_f[0]; q.ods1 = a.ods_f[1]; q.sa = a.sarea_f; q.pad = 0.f; q.ofoff = a.ofoff;
+                q.ods0 = a.ods_f[0]; q.ods1 = a.ods_f[1]; q.sa = a.sarea_f; q.pair = a.pair; q.ofoff = a.ofoff;
+                q.onv = a.onv; q.ogo = a.ogo;
                 psub[sd][k] = q;
             }
             for (int sd = 0; sd < 4; ++sd) pcnt[sd] = cnt[sd];
@@ -1775,7 +1794,36 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     };
     // INNER: the flux sum of velocity i through the sub-faces of the four sides (the loads of
     // the two sides it enters through first)
-    auto gather_inner = [&](int i, const float4& V, float2& f2, float2& acc) {
+    // the micro flux into this cell at velocity i through paired sub-face q: the neighbour's
+    // reconstructed micro fluxes at the velocities of its grid that overlap i (the pairing run),
+    // averaged onto i (a finer run) or copied (a coarser or equal one)
+    auto paired_micro = [&](const PSub& q, int i, int dir) {
+        const int64_t po = P.p_off[q.pair] + i;
+        const int j0 = P.p_j0[po], jc = P.p_cnt[po];
+        const int li = P.vlev[FC.goff + i];
+        const float* of = fbase + q.ofoff;
+        const float* os = sbase + q.ofoff * D;
+        const int onv = q.onv;
+        float2 mic = bc2(0.f);
+        for (int j = j0; j < j0 + jc; ++j) {
+            const float uj0 = P.vuf[q.ogo + j], uj1 = P.vuf[P.PG + q.ogo + j];
+            const float sc_ = merge_scale<D, float>(li, P.vlev[q.ogo + j]);
+            const float2 g = make_float2(of[j], of[onv + j]);
+            const float2 t0_ = make_float2(os[j], os[onv + j]);
+            const float2 t1_ = make_float2(os[2 * onv + j], os[3 * onv + j]);
+            const float ndx0 = q.dxo0 - uj0 * adt;
+            const float ndx1 = q.dxo1 - uj1 * adt;
+            const float2 nsdx = fma2(bc2(ndx1), t1_, mul2(bc2(ndx0), t0_));
+            const float2 thn = pp_theta2(g, t0_, t1_, q.ods0, q.ods1);
+            const float2 m = mul2(fma2(thn, nsdx, g), bc2(dir == 0 ? uj0 : uj1));
+            mic = fma2(m, bc2(sc_), mic);
+        }
+        return mic;
+    };
+    // accM: the part of acc whose moments are the macro flux on this cell's grid (all but the
+    // paired sub-faces' micro fluxes)
+    float2 accM_last[VPT];
+    auto gather_inner = [&](int i, const float4& V, float2& f2, float2& acc, float2& accM) {
         const float u0 = V.x, u1 = V.y;
         f2 = make_float2(fc[i], fc[nv + i]);
         const float2 s0 = make_float2(scl[i], scl[nv + i]);
@@ -1789,17 +1837,21 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
             si[d] = 2 * d + (pos ? 0 : 1);
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
-                // a side with one sub-face reads that one twice (in flight together; unused)
-                const int64_t no = psub[si[d]][k < pcnt[si[d]] ? k : 0].ofoff;
+                // a side with one sub-face reads that one twice (in flight together; unused); a
+                // paired sub-face's loads are its runs' (below)
+                const PSub& qq = psub[si[d]][k < pcnt[si[d]] ? k : 0];
+                const int64_t no = qq.ofoff;
+                const int ii = (INNER == 1 || qq.pair < 0) ? i : 0;
                 const float* of = fbase + no;
                 const float* os = sbase + no * D;
-                g2[d][k] = make_float2(of[i], of[nv + i]);
-                t0[d][k] = make_float2(os[i], os[nv + i]);
-                t1[d][k] = make_float2(os[2 * nv + i], os[3 * nv + i]);
+                g2[d][k] = make_float2(of[ii], of[nv + ii]);
+                t0[d][k] = make_float2(os[ii], os[nv + ii]);
+                t1[d][k] = make_float2(os[2 * nv + ii], os[3 * nv + ii]);
             }
         }
         const float2 th = pp_theta2(f2, s0, s1, ds0, ds1);
         acc = bc2(0.f);
+        accM = bc2(0.f);
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             const float ud = d == 0 ? u0 : u1;
@@ -1813,30 +1865,38 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
                 const float2 sdx = fma2(bc2(dx1), s1, mul2(bc2(dx0), s0));
                 const float2 mo = mul2(fma2(th, sdx, f2), bc2(ud));
                 acc = fma2(bc2(q.sa), mo, acc);
+                accM = fma2(bc2(q.sa), mo, accM);
             }
             // incoming through the opposite side: the neighbours' reconstructions
 #pragma unroll
             for (int k = 0; k < 2; ++k) {
                 if (k >= pcnt[si[d]]) break;
                 const PSub& q = psub[si[d]][k];
+                if constexpr (INNER == 2) {
+                    if (q.pair >= 0) {
+                        acc = fma2(bc2(q.sa), paired_micro(q, i, d), acc);
+                        continue;
+                    }
+                }
                 const float ndx0 = q.dxo0 - u0 * adt;
                 const float ndx1 = q.dxo1 - u1 * adt;
                 const float2 nsdx = fma2(bc2(ndx1), t1[d][k], mul2(bc2(ndx0), t0[d][k]));
                 const float2 thn = pp_theta2(g2[d][k], t0[d][k], t1[d][k], q.ods0, q.ods1);
                 const float2 mi = mul2(fma2(thn, nsdx, g2[d][k]), bc2(ud));
                 acc = fma2(bc2(q.sa), mi, acc);
+                accM = fma2(bc2(q.sa), mi, accM);
             }
         }
     };
     // the convected f, and the macro flux (CAIDVM) with the moments of the convected f (CAIDVM
     // marching) or of f (Euler) as the pairs (flux, f) in one set of packed sums
-    auto finish = [&](int i, const float4& V, const float2& f2, const float2& acc) {
+    auto finish = [&](int i, const float4& V, const float2& f2, const float2& acc, const float2& accM) {
         const float u0 = V.x, u1 = V.y, wi = V.z;
         const float2 fs = fma2(bc2(s_dt), acc, f2);
         fst[i] = fs;
         const float2 mf = march_caidvm ? fs : f2;
-        const float2 H = make_float2(caidvm ? acc.x : 0.f, mf.x);
-        const float2 B = make_float2(caidvm ? acc.y : 0.f, mf.y);
+        const float2 H = make_float2(caidvm ? accM.x : 0.f, mf.x);
+        const float2 B = make_float2(caidvm ? accM.y : 0.f, mf.y);
         float u2 = u0 * u0;
         u2 += u1 * u1;
         const float2 a0 = mul2(bc2(wi), H);
@@ -1857,12 +1917,51 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
         }
 #pragma unroll
         for (int v = 0; v < VPT; ++v) {
-            if constexpr (INNER) gather_inner(iv[v], V[v], f2[v], acc[v]);
-            else gather(iv[v], V[v], f2[v], acc[v]);
+            if constexpr (INNER) gather_inner(iv[v], V[v], f2[v], acc[v], accM_last[v]);
+            else { gather(iv[v], V[v], f2[v], acc[v]); accM_last[v] = acc[v]; }
         }
 #pragma unroll
         for (int v = 0; v < VPT; ++v)
-            if (v == 0 || i0 + v * NT < nv) finish(iv[v], V[v], f2[v], acc[v]);
+            if (v == 0 || i0 + v * NT < nv) finish(iv[v], V[v], f2[v], acc[v], accM_last[v]);
+    }
+    if constexpr (INNER == 2) {
+        // the macro flux of the paired sub-faces on the neighbour's grid: the moments of its
+        // micro fluxes at the velocities that leave it towards this cell, with its weights
+        if (caidvm) {
+#pragma unroll
+            for (int sd = 0; sd < 4; ++sd) {
+                const int d = sd >> 1;
+                const bool plus = sd & 1;
+                for (int k = 0; k < pcnt[sd]; ++k) {
+                    const PSub& q = psub[sd][k];
+                    if (q.pair < 0) continue;
+                    const float* of = fbase + q.ofoff;
+                    const float* os = sbase + q.ofoff * D;
+                    const int onv = q.onv;
+                    for (int j = threadIdx.x; j < onv; j += NT) {
+                        const float uj0 = P.vuf[q.ogo + j], uj1 = P.vuf[P.PG + q.ogo + j];
+                        const float ud = d == 0 ? uj0 : uj1;
+                        if (plus ? !(ud < 0.f) : !(ud > 0.f)) continue;   // not towards this cell
+                        const float2 g = make_float2(of[j], of[onv + j]);
+                        const float2 t0_ = make_float2(os[j], os[onv + j]);
+                        const float2 t1_ = make_float2(os[2 * onv + j], os[3 * onv + j]);
+                        const float ndx0 = q.dxo0 - uj0 * adt;
+                        const float ndx1 = q.dxo1 - uj1 * adt;
+                        const float2 nsdx = fma2(bc2(ndx1), t1_, mul2(bc2(ndx0), t0_));
+                        const float2 thn = pp_theta2(g, t0_, t1_, q.ods0, q.ods1);
+                        const float2 m = mul2(fma2(thn, nsdx, g), bc2(ud));
+                        const float wj = P.vwf[q.ogo + j] * q.sa;
+                        float u2 = uj0 * uj0;
+                        u2 += uj1 * uj1;
+                        const float a0 = wj * m.x;
+                        m0.x += a0;
+                        m1.x += uj0 * a0;
+                        m2.x += uj1 * a0;
+                        mE.x += 0.5f * wj * (u2 * m.x + m.y);
+                    }
+                }
+            }
+        }
     }
     double qv[D];
     {
@@ -1973,19 +2072,21 @@ template <int NT, int VPT, bool R2>
 __global__ void __launch_bounds__(NT, (R2 ? 3 : (VPT == 1 ? 4 : KG_PACKED_MINB)) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
     flux_regular_packed<NT, VPT, R2>(P, list[blockIdx.x]);
 }
-// the cells of packed_inner_ok, one CTA each
-template <int NT>
+// the cells of packed_inner_ok, one CTA each (PAIRED: some sub-face to another velocity grid)
+template <int NT, bool PAIRED>
 __global__ void __launch_bounds__(NT, 3 * (BLOCK / NT)) flux_packed_inner_kernel(Dev P, const int32_t* list) {
-    flux_regular_packed<NT, 1, false, true>(P, list[blockIdx.x]);
+    flux_regular_packed<NT, 1, false, PAIRED ? 2 : 1>(P, list[blockIdx.x]);
 }
 
 // Per fluid-list entry: 1 when the packed kernel's INNER form takes the cell (not regular; every
-// incidence an inner face to a fluid cell on the same velocity grid, leaving through the side
-// its face points at; one or two sub-faces on each of the four sides), else 0.
+// incidence an inner face to a fluid cell on its own velocity grid, leaving through the side its
+// face points at; one or two sub-faces on each of the four sides), 2 when it does so with some
+// neighbour on another grid, else 0.
 __global__ void packed_inner_ok_kernel(Dev P, int n, uint8_t* out) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
     uint8_t ok = 0;
+    bool paired = false;
     if (!P.fluid_reg[q]) {
         const FluxCell& FC = P.fcrec[q];
         int cnt[4] = {0, 0, 0, 0};
@@ -1993,7 +2094,8 @@ __global__ void packed_inner_ok_kernel(Dev P, int n, uint8_t* out) {
         for (int e = 0; e < FC.ninc && ok; ++e) {
             const Incidence& a = P.inc[FC.inc0 + e];
             const int d = a.dir;
-            ok = a.kind == INC_INNER && a.pair < 0 && d >= 0 && d < 2 && a.orient_f * a.dxm_f[d] < 0.f;
+            ok = a.kind == INC_INNER && d >= 0 && d < 2 && a.orient_f * a.dxm_f[d] < 0.f;
+            paired = paired || a.pair >= 0;
             if (ok) {
                 const int sd = 2 * d + (a.dxm_f[d] > 0.f ? 1 : 0);
                 ok = ++cnt[sd] <= 2;
@@ -2001,7 +2103,7 @@ __global__ void packed_inner_ok_kernel(Dev P, int n, uint8_t* out) {
         }
         for (int sd = 0; sd < 4 && ok; ++sd) ok = cnt[sd] >= 1;
     }
-    out[q] = ok;
+    out[q] = ok ? (paired ? 2 : 1) : 0;
 }
 cudaError_t launch_packed_inner_ok(const Dev& P, int n, uint8_t* out, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
@@ -3054,12 +3156,13 @@ struct Launch {
         return cudaErrorInvalidValue;   // R2 lists exist only for the 2D mixed form
     }
     // the packed kernel's INNER form, one CTA per listed entry (2D mixed form)
-    static cudaError_t flux_inner_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+    static cudaError_t flux_inner_list(const Dev& P, const int32_t* list, int n, int max_nv, bool paired, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             const size_t smem = packed_smem(max_nv, P.max_axis);
             using RegFn = void (*)(Dev, const int32_t*);
-            RegFn fn = P.flux_nt == 128 ? flux_packed_inner_kernel<128> : flux_packed_inner_kernel<BLOCK>;
+            RegFn fn = paired ? (P.flux_nt == 128 ? flux_packed_inner_kernel<128, true> : flux_packed_inner_kernel<BLOCK, true>)
+                              : (P.flux_nt == 128 ? flux_packed_inner_kernel<128, false> : flux_packed_inner_kernel<BLOCK, false>);
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
             fn<<<n, P.flux_nt == 128 ? 128 : BLOCK, smem, s>>>(P, list);

@@ -11,7 +11,7 @@ pytestmark = pytest.mark.gpu
 
 NAMES = ["slope_ops", "slope_nbr", "cell_slope_op", "pass_cells", "screc", "crit_ops", "crit_nbr", "inc_off",
          "inc", "bc_prim", "bc_hl", "fluid_cells", "fluid_reg", "fcrec", "regrec", "r2rec", "slope_items",
-         "reg_list", "nonreg_list", "r2_list", "inner_list", "p_off", "p_j0", "p_cnt", "ib_nbr", "wall_ops", "solid_ops"]
+         "reg_list", "nonreg_list", "r2_list", "inner_list", "innerp_list", "p_off", "p_j0", "p_cnt", "ib_nbr", "wall_ops", "solid_ops"]
 
 LAYOUTS = [
     ("sod_levels", lambda: cases.sod(scale=0.125, nv=16)),
