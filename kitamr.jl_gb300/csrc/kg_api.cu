@@ -694,6 +694,10 @@ int rebuild(kg_handle* h) {
         const double mean_nv = (double)M.phase_cells / (double)M.n_fluid;
         P.flux_nt = (!P.fst_global && (mean_nv < 1024.0 || M.dim == 2)) ? 128 : BLOCK;
         P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
+#ifndef KG_PACKED64_NV
+#define KG_PACKED64_NV 0.0
+#endif
+        P.packed_nt = mean_nv < KG_PACKED64_NV ? 64 : P.flux_nt;
     }
     {
         // the launch lists of the flux kernels: the regular fluid cells (the regular-cell kernel;

@@ -72,6 +72,8 @@ struct Dev {
     int flux_nt;                       // flux kernel threads per CTA: 256, or 128 for layouts of
                                        // small velocity grids (twice the cells in flight)
     int slope_nt;                      // slope kernel threads per CTA (the same choice)
+    int packed_nt;                     // packed kernels' threads per CTA: 64 for layouts of small
+                                       // velocity grids (more cells in flight), else flux_nt
     // ib
     const SolidOp* solid_ops;
     const WallOp* wall_ops;
@@ -157,7 +159,7 @@ template <int N, int NT = BLOCK>
 __device__ __forceinline__ void block_sum_ff(float (&hi)[N], float (&lo)[N], double (&out)[N], double* sred) {
     // sred: shared scratch of at least N * (NT/32) doubles; NT: threads of the block
     constexpr int NWARP = NT / 32;
-    static_assert(NWARP == 4 || NWARP == 8, "the warp-0 stage maps NWARP lanes per element");
+    static_assert(NWARP == 2 || NWARP == 4 || NWARP == 8, "the warp-0 stage maps NWARP lanes per element");
     static_assert(N <= 32, "at most 32 elements");
     constexpr int GROUPS = 32 / NWARP;            // elements per round of warp 0
     constexpr int K = Pow2<N>::K, P = 1 << K;

@@ -3127,16 +3127,20 @@ struct Launch {
         RegFn fn = P.fst_global ? flux_regular_kernel<D, NDF, T, true, BLOCK>
                                 : (P.flux_nt == 128 ? flux_regular_kernel<D, NDF, T, false, 128>
                                                     : flux_regular_kernel<D, NDF, T, false, BLOCK>);
+        int ntl = nt;
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
-            // the packed-FP32 kernel (its convected f always in shared memory)
+            // the packed-FP32 kernel (its convected f always in shared memory; 64 threads for
+            // layouts of small velocity grids)
             if (!P.fst_global && P.marching != KG_MARCH_CIP) {
-                fn = P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT, false> : flux_packed_kernel<BLOCK, PACKED_VPT, false>;
+                fn = P.packed_nt == 64 ? flux_packed_kernel<64, PACKED_VPT, false>
+                   : (P.flux_nt == 128 ? flux_packed_kernel<128, PACKED_VPT, false> : flux_packed_kernel<BLOCK, PACKED_VPT, false>);
+                ntl = P.packed_nt == 64 ? 64 : nt;
                 smem = packed_smem(max_nv, P.max_axis);
             }
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        fn<<<n, nt, smem, s>>>(P, list);
+        fn<<<n, ntl, smem, s>>>(P, list);
         return cudaGetLastError();
     }
     // the packed kernel of the R2 cells (slopes from f), one CTA per listed entry
@@ -3145,9 +3149,10 @@ struct Launch {
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             using A = typename Arith<T>::type;
             const size_t smem = packed_smem(max_nv, P.max_axis);
-            const int nt = P.flux_nt == 128 ? 128 : BLOCK;
+            const int nt = P.packed_nt == 64 ? 64 : (P.flux_nt == 128 ? 128 : BLOCK);
             using RegFn = void (*)(Dev, const int32_t*);
-            RegFn fn = nt == 128 ? flux_packed_kernel<128, R2_VPT, true> : flux_packed_kernel<BLOCK, R2_VPT, true>;
+            RegFn fn = nt == 64 ? flux_packed_kernel<64, R2_VPT, true>
+                     : (nt == 128 ? flux_packed_kernel<128, R2_VPT, true> : flux_packed_kernel<BLOCK, R2_VPT, true>);
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
             fn<<<n, nt, smem, s>>>(P, list);
@@ -3161,11 +3166,14 @@ struct Launch {
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             const size_t smem = packed_smem(max_nv, P.max_axis);
             using RegFn = void (*)(Dev, const int32_t*);
-            RegFn fn = paired ? (P.flux_nt == 128 ? flux_packed_inner_kernel<128, true> : flux_packed_inner_kernel<BLOCK, true>)
-                              : (P.flux_nt == 128 ? flux_packed_inner_kernel<128, false> : flux_packed_inner_kernel<BLOCK, false>);
+            const int nt = P.packed_nt == 64 ? 64 : (P.flux_nt == 128 ? 128 : BLOCK);
+            RegFn fn = paired ? (nt == 64 ? flux_packed_inner_kernel<64, true>
+                               : (nt == 128 ? flux_packed_inner_kernel<128, true> : flux_packed_inner_kernel<BLOCK, true>))
+                              : (nt == 64 ? flux_packed_inner_kernel<64, false>
+                               : (nt == 128 ? flux_packed_inner_kernel<128, false> : flux_packed_inner_kernel<BLOCK, false>));
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            fn<<<n, P.flux_nt == 128 ? 128 : BLOCK, smem, s>>>(P, list);
+            fn<<<n, nt, smem, s>>>(P, list);
             return cudaGetLastError();
         }
         return cudaErrorInvalidValue;   // inner lists exist only for the 2D mixed form
