@@ -694,10 +694,13 @@ int rebuild(kg_handle* h) {
         const double mean_nv = (double)M.phase_cells / (double)M.n_fluid;
         P.flux_nt = (!P.fst_global && (mean_nv < 1024.0 || M.dim == 2)) ? 128 : BLOCK;
         P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
-#ifndef KG_PACKED64_NV
-#define KG_PACKED64_NV 0.0
-#endif
-        P.packed_nt = mean_nv < KG_PACKED64_NV ? 64 : P.flux_nt;
+        // the packed kernels of a layout of many cells with small velocity grids (a batch): 64
+        // threads, twice the cells in flight per SM (batched workload, mean 700 velocity cells:
+        // 30.5 -> 35.1 G updates/s); with few cells (the 848-cell Sod tube: 9.1 -> 8.0) each
+        // cell's longer chain of passes costs more than the extra cells in flight bring
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, h->device);
+        P.packed_nt = (mean_nv < 1024.0 && (int64_t)M.n_fluid >= (int64_t)24 * std::max(nsm, 1)) ? 64 : P.flux_nt;
     }
     {
         // the launch lists of the flux kernels: the regular fluid cells (the regular-cell kernel;
