@@ -133,6 +133,13 @@ __device__ __forceinline__ void slope_side(int i, int li, const typename Arith<T
     for (int k = 0; k < NDF; ++k) s[k] = acc[k] * inv_cnt;
 }
 
+#ifndef KG_SLOPE_PPT
+#define KG_SLOPE_PPT 1
+#endif
+template <typename T> struct Vec2;
+template <> struct Vec2<float> { using type = float2; };
+template <> struct Vec2<double> { using type = double2; };
+
 // NT: threads per CTA (128 for layouts of small velocity grids, whose cells would leave half
 // of a 256-thread CTA idle)
 // One CTA per work item: a pass cell and a chunk of SLOPE_CHUNK of its velocity cells (every
@@ -166,6 +173,68 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
             fb[dir] = (const T*)P.f_in + SC.nfoff[2 * dir + 1];
             if constexpr (sizeof(A) == 4) { ia[dir] = SC.inv_f[2 * dir]; ib[dir] = SC.inv_f[2 * dir + 1]; }
             else { ia[dir] = SC.inv_d[2 * dir]; ib[dir] = SC.inv_d[2 * dir + 1]; }
+        }
+        // pairs of neighbouring velocity cells per thread and vector loads and stores (8 bytes in
+        // the mixed form, 16 in FP64) when every block the cell reads and writes starts at an even
+        // element: the cell's and its neighbours' f offsets and its velocity count even (chunks
+        // start at multiples of SLOPE_CHUNK); the same arithmetic per velocity cell
+        bool pairs = ((SC.foff | (int64_t)nv) & 1) == 0;
+#pragma unroll
+        for (int q = 0; q < 2 * D; ++q) pairs = pairs && (SC.nfoff[q] & 1) == 0;
+        if (pairs) {
+            using T2 = typename Vec2<T>::type;
+            constexpr int PPT = KG_SLOPE_PPT;   // pairs per thread and pass
+            const int q1 = v1 >> 1;
+            const T2* fc2[NDF];
+            const T2* fa2[D][NDF];
+            const T2* fb2[D][NDF];
+            T2* sc2[D][NDF];
+#pragma unroll
+            for (int k = 0; k < NDF; ++k) {
+                fc2[k] = reinterpret_cast<const T2*>(fcell + (int64_t)k * nv);
+#pragma unroll
+                for (int dir = 0; dir < D; ++dir) {
+                    fa2[dir][k] = reinterpret_cast<const T2*>(fa[dir] + (int64_t)k * nv);
+                    fb2[dir][k] = reinterpret_cast<const T2*>(fb[dir] + (int64_t)k * nv);
+                    sc2[dir][k] = reinterpret_cast<T2*>(scell + (int64_t)(dir * NDF + k) * nv);
+                }
+            }
+            for (int q0 = (v0 >> 1) + threadIdx.x; q0 < q1; q0 += PPT * NT) {
+                int iq[PPT], jq[PPT];
+#pragma unroll
+                for (int v = 0; v < PPT; ++v) {
+                    iq[v] = q0 + v * NT;
+                    jq[v] = iq[v] < q1 ? iq[v] : q0;
+                }
+                T2 fc[PPT][NDF], a[PPT][D][NDF], b[PPT][D][NDF];
+#pragma unroll
+                for (int v = 0; v < PPT; ++v) {
+#pragma unroll
+                    for (int k = 0; k < NDF; ++k) {
+                        fc[v][k] = fc2[k][jq[v]];
+#pragma unroll
+                        for (int dir = 0; dir < D; ++dir) {
+                            a[v][dir][k] = fa2[dir][k][jq[v]];
+                            b[v][dir][k] = fb2[dir][k][jq[v]];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int v = 0; v < PPT; ++v) {
+                    if (v > 0 && iq[v] >= q1) break;
+#pragma unroll
+                    for (int dir = 0; dir < D; ++dir) {
+#pragma unroll
+                        for (int k = 0; k < NDF; ++k) {
+                            T2 o;
+                            o.x = (T)minmod(((A)fc[v][k].x - (A)a[v][dir][k].x) * ia[dir], ((A)fc[v][k].x - (A)b[v][dir][k].x) * ib[dir]);
+                            o.y = (T)minmod(((A)fc[v][k].y - (A)a[v][dir][k].y) * ia[dir], ((A)fc[v][k].y - (A)b[v][dir][k].y) * ib[dir]);
+                            sc2[dir][k][iq[v]] = o;
+                        }
+                    }
+                }
+            }
+            return;
         }
         // velocity cells per thread and pass (measured on the 3D sphere, mixed form: 2 beats 3
         // and 4, whose registers cost resident CTAs)
