@@ -21,9 +21,9 @@ template <int D, int NDF, typename T> struct Launch {
     static cudaError_t wall_rows(const Dev&, int, double*, cudaStream_t);
     static cudaError_t flux_persistent(const Dev&, int, int, int, int*, const int32_t*, cudaStream_t);
     static cudaError_t flux_list(const Dev&, const int32_t*, int, int, cudaStream_t);
-    static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t);
+    static cudaError_t flux_reg_list(const Dev&, const int32_t*, int, int, cudaStream_t, bool = false);
     static cudaError_t flux_r2_list(const Dev&, const int32_t*, int, int, cudaStream_t);
-    static cudaError_t flux_inner_list(const Dev&, const int32_t*, int, int, bool, cudaStream_t);
+    static cudaError_t flux_inner_list(const Dev&, const int32_t*, int, int, bool, cudaStream_t, bool);
     static int flux_occupancy(const Dev&, int);
     static cudaError_t cip(const Dev&, int, cudaStream_t);
     static cudaError_t conserve(const Dev&, const int32_t*, int, cudaStream_t);
@@ -779,12 +779,13 @@ int rebuild(kg_handle* h) {
 // largest velocity grids first).
 // The flux of the fluid cells by list: 0 the regular cells, 1 the R2 cells, 2 the others
 // (under the schedule `sched`).
-cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, int ctas, cudaStream_t s) {
+// (pdl: parts 3 and 4 launched as programmatic dependents of the packed kernel before them)
+cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, int ctas, cudaStream_t s, bool pdl) {
     const Flat& F = h->M;
     if (part == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
     if (part == 1) return dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
-    if (part == 3) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_inner, h->n_inner, F.max_nv, false, s); });
-    if (part == 4) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_innerp, h->n_innerp, F.max_nv, true, s); });
+    if (part == 3) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_inner, h->n_inner, F.max_nv, false, s, pdl); });
+    if (part == 4) return dispatch(h, [&](auto L) { return decltype(L)::flux_inner_list(P, h->d_innerp, h->n_innerp, F.max_nv, true, s, pdl); });
     if (h->n_nonreg == 0) return cudaSuccess;
     if (sched == 0) return dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, s); });
     int nsm = 0;
@@ -794,9 +795,12 @@ cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, in
     return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, h->n_nonreg, F.max_nv, grid, h->d_counter, order, s); });
 }
 
+#ifndef KG_PDL
+#define KG_PDL 1
+#endif
 cudaError_t launch_flux(kg_handle* h, const Dev& P, int sched, int ctas, cudaStream_t s) {
     cudaError_t e = cudaSuccess;
-    for (int part = 0; part < 5 && e == cudaSuccess; ++part) e = launch_flux_part(h, P, part, sched, ctas, s);
+    for (int part = 0; part < 5 && e == cudaSuccess; ++part) e = launch_flux_part(h, P, part, sched, ctas, s, false);
     return e;
 }
 
@@ -974,18 +978,35 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         }
         e = dispatch(h, [&](auto L) { return decltype(L)::flux_list(P, h->d_nonreg, h->n_nonreg, F.max_nv, a); });
         if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
+        // the handle's stream: the packed forms (none reads an IB output), the costliest cells
+        // first -- the paired INNER form, the INNER form, then the regular cells, whose many short
+        // CTAs end the phase -- each after the first launched as a programmatic dependent of the
+        // one before, so that its CTAs start on the SMs the other's last wave frees
+        const bool chain = KG_PDL && h->n_r2 == 0 && h->prm.dim == 2 && h->prm.precision == KG_PREC_MIXED &&
+                           !P.fst_global && h->prm.marching != KG_MARCH_CIP;
         if (h->n_r2 > 0) {
             e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, a); });
             if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
             e = dispatch(h, [&](auto L) { return decltype(L)::flux_r2_list(P, h->d_r2, h->n_r2, F.max_nv, s); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_kernel_r2");
+            e = launch_flux_part(h, P, 3, 0, 0, s, false);
+            if (e == cudaSuccess) e = launch_flux_part(h, P, 4, 0, 0, s, false);
+            if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_inner_kernel");
         } else {
-            e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s); });
+            bool after = false;   // a packed-form kernel launched before on this stream
+            if (h->n_innerp > 0) {
+                e = launch_flux_part(h, P, 4, 0, 0, s, false);
+                if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_inner_kernel_paired");
+                after = true;
+            }
+            if (h->n_inner > 0) {
+                e = launch_flux_part(h, P, 3, 0, 0, s, chain && after);
+                if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_inner_kernel");
+                after = true;
+            }
+            e = dispatch(h, [&](auto L) { return decltype(L)::flux_reg_list(P, h->d_reg, h->n_reg, F.max_nv, s, chain && after); });
+            if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_kernel");
         }
-        if (e != cudaSuccess) return cuda_fail(h, e, "flux_collide_kernel");
-        // the cells of the packed kernel's INNER form read no IB output: the handle's stream
-        e = launch_flux_part(h, P, 3, 0, 0, s);
-        if (e == cudaSuccess) e = launch_flux_part(h, P, 4, 0, 0, s);
-        if (e != cudaSuccess) return cuda_fail(h, e, "flux_packed_inner_kernel");
         KG_CUDA(h, cudaEventRecord(h->ev_join, a));
         KG_CUDA(h, cudaStreamWaitEvent(s, h->ev_join, 0));
         *launches += (h->n_nonreg > 0) + (h->n_reg > 0) + (h->n_r2 > 0) + (h->n_inner > 0) + (h->n_innerp > 0);
@@ -1026,7 +1047,7 @@ int enqueue_step(kg_handle* h, bool timed, int64_t* launches) {
         for (int part = 0; part < 5; ++part) {
             if (counts[part] == 0) continue;
             begin();
-            e = launch_flux_part(h, P, part, h->sched, h->sched_ctas, s);
+            e = launch_flux_part(h, P, part, h->sched, h->sched_ctas, s, false);
             if (e != cudaSuccess) return cuda_fail(h, e, names[part]);
             end(names[part], units[part]);
         }

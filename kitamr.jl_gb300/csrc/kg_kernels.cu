@@ -2137,14 +2137,26 @@ __global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) f
 }
 // VPT velocity cells per thread and pass of the gather (their loads in flight together);
 // more registers, so fewer resident CTAs
+// Programmatic dependent launch (sm_90+) of the packed forms one after another on a stream: a
+// kernel launched with programmatic stream serialization may start once every CTA of the kernel
+// before it has executed launch_dependents (here at its start), so its CTAs fill the SMs the
+// other's last wave frees; the packed forms read nothing another writes, and each CTA waits at
+// its end until the kernel before has completed, so that the stream's next operation, ordered
+// after the last kernel, finds them all complete (both are no-ops under an ordinary launch).
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 template <int NT, int VPT, bool R2>
 __global__ void __launch_bounds__(NT, (R2 ? 3 : (VPT == 1 ? 4 : KG_PACKED_MINB)) * (BLOCK / NT)) flux_packed_kernel(Dev P, const int32_t* list) {
+    pdl_trigger();
     flux_regular_packed<NT, VPT, R2>(P, list[blockIdx.x]);
+    pdl_wait();
 }
 // the cells of packed_inner_ok, one CTA each (PAIRED: some sub-face to another velocity grid)
 template <int NT, bool PAIRED>
 __global__ void __launch_bounds__(NT, 3 * (BLOCK / NT)) flux_packed_inner_kernel(Dev P, const int32_t* list) {
+    pdl_trigger();
     flux_regular_packed<NT, 1, false, PAIRED ? 2 : 1>(P, list[blockIdx.x]);
+    pdl_wait();
 }
 
 // Per fluid-list entry: 1 when the packed kernel's INNER form takes the cell (not regular; every
@@ -3134,6 +3146,27 @@ __global__ void __launch_bounds__(BLOCK) wall_rows_kernel(Dev P, double* out) {
     }
 }
 
+// an ordinary launch, or one with programmatic stream serialization (pdl: a programmatic
+// dependent of the kernel before it on the stream)
+template <typename... Args>
+static cudaError_t launch_pdl(void (*fn)(Args...), int grid, int nt, size_t smem, cudaStream_t s, bool pdl, Args... args) {
+    if (!pdl) {
+        fn<<<grid, nt, smem, s>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)nt);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
 template <int D, int NDF, typename T>
 struct Launch {
     // the slope work items [item_base, item_base + n) of one pass
@@ -3185,7 +3218,10 @@ struct Launch {
         return cudaGetLastError();
     }
     // the regular-cell kernel, one CTA per listed fluid-list entry (every one regular)
-    static cudaError_t flux_reg_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
+    // (pdl: the packed kernel launched as a programmatic dependent of the packed-form kernel
+    // before it)
+    static cudaError_t flux_reg_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s,
+                                     bool pdl = false) {
         if (n <= 0) return cudaSuccess;
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
@@ -3209,8 +3245,7 @@ struct Launch {
         }
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        fn<<<n, ntl, smem, s>>>(P, list);
-        return cudaGetLastError();
+        return launch_pdl(fn, n, ntl, smem, s, pdl, P, list);
     }
     // the packed kernel of the R2 cells (slopes from f), one CTA per listed entry
     static cudaError_t flux_r2_list(const Dev& P, const int32_t* list, int n, int max_nv, cudaStream_t s) {
@@ -3230,7 +3265,9 @@ struct Launch {
         return cudaErrorInvalidValue;   // R2 lists exist only for the 2D mixed form
     }
     // the packed kernel's INNER form, one CTA per listed entry (2D mixed form)
-    static cudaError_t flux_inner_list(const Dev& P, const int32_t* list, int n, int max_nv, bool paired, cudaStream_t s) {
+    // (pdl: launched as a programmatic dependent of the packed-form kernel before it)
+    static cudaError_t flux_inner_list(const Dev& P, const int32_t* list, int n, int max_nv, bool paired, cudaStream_t s,
+                                       bool pdl) {
         if (n <= 0) return cudaSuccess;
         if constexpr (D == 2 && NDF == 2 && sizeof(T) == 4) {
             const size_t smem = packed_smem(max_nv, P.max_axis);
@@ -3242,8 +3279,7 @@ struct Launch {
                                : (nt == 128 ? flux_packed_inner_kernel<128, false> : flux_packed_inner_kernel<BLOCK, false>));
             cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            fn<<<n, nt, smem, s>>>(P, list);
-            return cudaGetLastError();
+            return launch_pdl(fn, n, nt, smem, s, pdl, P, list);
         }
         return cudaErrorInvalidValue;   // inner lists exist only for the 2D mixed form
     }
