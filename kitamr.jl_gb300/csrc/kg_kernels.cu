@@ -136,12 +136,13 @@ __device__ __forceinline__ void slope_side(int i, int li, const typename Arith<T
 #ifndef KG_SLOPE_PPT
 #define KG_SLOPE_PPT 1
 #endif
-#ifndef KG_SLOPE_SMALL_PASS
-#define KG_SLOPE_SMALL_PASS 0
-#endif
 template <typename T> struct Vec2;
 template <> struct Vec2<float> { using type = float2; };
 template <> struct Vec2<double> { using type = double2; };
+
+// neighbours a side of the slope kernel's loads-first path: every side's (2^(D-1)), but one in
+// the FP64 3D form, whose registers would cost resident CTAs
+template <int D, typename T> constexpr int SLOPE_SIMPLE_MC = (D == 3 && sizeof(T) == 8) ? 1 : 1 << (D - 1);
 
 // NT: threads per CTA (128 for layouts of small velocity grids, whose cells would leave half
 // of a 256-thread CTA idle)
@@ -288,7 +289,7 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
     __shared__ SlopeNbrA<A, T> snb[MAX_SLOPE_NBR];
     __shared__ int sbase[2 * MAXD + 1];
     __shared__ A sconst[4 * MAXD];   // inv_dsA, inv_dsB, 1/cntA, 1/cntB per direction
-    __shared__ int ssimple;          // every side at most one neighbour, on the cell's own grid
+    __shared__ int ssimple;          // every neighbour on the cell's own grid
     if (threadIdx.x < D) ops[threadIdx.x] = P.slope_ops[op0 + threadIdx.x];
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -299,7 +300,8 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
                 const int cnt = (op.kind == SLOPE_ONE || op.kind == SLOPE_TWO) ? (side == 0 ? op.cntA : (op.kind == SLOPE_TWO ? op.cntB : 0)) : 0;
                 sbase[2 * dir + side] = n;
                 n += cnt;
-                if (cnt > 1 || (cnt == 1 && P.slope_nbr[side == 0 ? op.listA : op.listB].pair >= 0)) simple = 0;
+                for (int e = 0; e < cnt; ++e)
+                    if (e >= SLOPE_SIMPLE_MC<D, T> || P.slope_nbr[(side == 0 ? op.listA : op.listB) + e].pair >= 0) simple = 0;
             }
             sconst[4 * dir + 0] = (A)op.inv_dsA;
             sconst[4 * dir + 1] = (A)op.inv_dsB;
@@ -348,34 +350,38 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
     __syncthreads();
     const int v1 = P.slope_split ? (int)min((int64_t)nv, (int64_t)v0 + P.slope_chunk) : nv;
     if (ssimple) {
-        // every side has at most one neighbour, on the cell's own grid (the cells beside a
-        // coarser one, whose side projects that neighbour with its transverse slopes, and
-        // the cells at domain boundaries): slope_side's arithmetic for one unpaired entry, with
-        // every side's loads issued before any is used
+        // every neighbour on the cell's own grid (the cells beside a coarser one, whose side
+        // projects that neighbour with its transverse slopes, those beside finer ones, and the
+        // cells at domain boundaries): slope_side's arithmetic for unpaired entries, in its
+        // order, with every entry's loads issued before any is used
+        constexpr int MC = SLOPE_SIMPLE_MC<D, T>;
         for (int i = v0 + threadIdx.x; i < v1; i += NT) {
             A fc[NDF];
 #pragma unroll
             for (int k = 0; k < NDF; ++k) fc[k] = (A)fcell[k * nv + i];
-            A pv[D][2][NDF];
+            A pv[D][2][MC][NDF];
 #pragma unroll
             for (int dir = 0; dir < D; ++dir) {
 #pragma unroll
                 for (int side = 0; side < 2; ++side) {
-                    const int cnt = side == 0 ? ops[dir].cntA : (ops[dir].kind == SLOPE_TWO ? ops[dir].cntB : 0);
-                    const bool used = (ops[dir].kind == SLOPE_ONE || ops[dir].kind == SLOPE_TWO) && cnt > 0;
-                    const SlopeNbrA<A, T>& r = snb[sbase[2 * dir + side]];
+                    const int cnt = (ops[dir].kind == SLOPE_ONE || ops[dir].kind == SLOPE_TWO)
+                                  ? (side == 0 ? ops[dir].cntA : (ops[dir].kind == SLOPE_TWO ? ops[dir].cntB : 0)) : 0;
 #pragma unroll
-                    for (int k = 0; k < NDF; ++k) {
-                        A p = 0;
-                        if (used) {
-                            p = (A)r.fn[k * r.nvn + i];
-                            if (r.any) {
+                    for (int e = 0; e < MC; ++e) {
+                        const SlopeNbrA<A, T>& r = snb[sbase[2 * dir + side] + (e < cnt ? e : 0)];
 #pragma unroll
-                                for (int t = 0; t < D; ++t)
-                                    if (r.dm[t] != (A)0) p += r.dm[t] * (A)r.sn[(t * NDF + k) * r.nvn + i];
+                        for (int k = 0; k < NDF; ++k) {
+                            A p = 0;
+                            if (e < cnt) {
+                                p = (A)r.fn[k * r.nvn + i];
+                                if (r.any) {
+#pragma unroll
+                                    for (int t = 0; t < D; ++t)
+                                        if (r.dm[t] != (A)0) p += r.dm[t] * (A)r.sn[(t * NDF + k) * r.nvn + i];
+                                }
                             }
+                            pv[dir][side][e][k] = p;
                         }
-                        pv[dir][side][k] = p;
                     }
                 }
             }
@@ -392,12 +398,16 @@ __global__ void __launch_bounds__(NT) slope_kernel(Dev P, int item_base) {
 #pragma unroll
                     for (int k = 0; k < NDF; ++k) {
                         A accA = 0, accB = 0;
-                        if (cA > 0) accA += (fc[k] - pv[dir][0][k]) * (A)1 * sconst[4 * dir];
+#pragma unroll
+                        for (int e = 0; e < MC; ++e)
+                            if (e < cA) accA += (fc[k] - pv[dir][0][e][k]) * (A)1 * sconst[4 * dir];
                         const A sA = accA * sconst[4 * dir + 2];
                         if (op.kind == SLOPE_ONE) {
                             out[k] = sA;
                         } else {
-                            if (cB > 0) accB += (fc[k] - pv[dir][1][k]) * (A)1 * sconst[4 * dir + 1];
+#pragma unroll
+                            for (int e = 0; e < MC; ++e)
+                                if (e < cB) accB += (fc[k] - pv[dir][1][e][k]) * (A)1 * sconst[4 * dir + 1];
                             out[k] = minmod(sA, accB * sconst[4 * dir + 3]);
                         }
                     }
@@ -3239,7 +3249,7 @@ struct Launch {
     // the slope work items [item_base, item_base + n) of one pass
     static cudaError_t slope(const Dev& P, int item_base, int n, cudaStream_t s) {
         if (n <= 0) return cudaSuccess;
-        if (P.slope_nt == 128 || n < KG_SLOPE_SMALL_PASS) slope_kernel<D, NDF, T, 128><<<n, 128, 0, s>>>(P, item_base);
+        if (P.slope_nt == 128) slope_kernel<D, NDF, T, 128><<<n, 128, 0, s>>>(P, item_base);
         else slope_kernel<D, NDF, T, BLOCK><<<n, BLOCK, 0, s>>>(P, item_base);
         return cudaGetLastError();
     }
