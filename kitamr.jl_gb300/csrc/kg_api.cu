@@ -693,7 +693,10 @@ int rebuild(kg_handle* h) {
         // half the instructions per velocity cell, so the per-cell fixed work weighs more)
         const double mean_nv = (double)M.phase_cells / (double)M.n_fluid;
         P.flux_nt = (!P.fst_global && (mean_nv < 1024.0 || M.dim == 2)) ? 128 : BLOCK;
-        P.slope_nt = mean_nv < 1024.0 ? 128 : BLOCK;
+        // (3D layouts: 128 threads at every grid size -- twice the work items in flight per SM;
+        // the sphere's slope passes 7.4 -> 7.0 ms per launch, while the 2D cylinder's grids of
+        // 2,304 velocity cells are faster at 256)
+        P.slope_nt = (mean_nv < 1024.0 || M.dim == 3) ? 128 : BLOCK;
         // the packed kernels of a layout of many cells with small velocity grids (a batch): 64
         // threads, twice the cells in flight per SM (batched workload, mean 700 velocity cells:
         // 30.5 -> 35.1 G updates/s); with few cells (the 848-cell Sod tube: 9.1 -> 8.0) each
