@@ -1758,6 +1758,7 @@ __device__ __forceinline__ float2 dslope2(float2 f, float2 fn, float inv) { retu
 struct PSub {                 // one sub-face of a side (INNER): the incidence's FP32 geometry
     float dxm0, dxm1, dxo0, dxo1, ods0, ods1, sa;
     int32_t pair;             // pairing (my grid <- the neighbour's), -1: the same grid
+    int64_t poff;             // that pairing's rows (p_off), read once per cell
     int64_t ofoff;            // the neighbour's f offset
     int32_t onv, ogo;         // its velocity count and grid offset
 };
@@ -1803,6 +1804,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
                 PSub q;
                 q.dxm0 = a.dxm_f[0]; q.dxm1 = a.dxm_f[1]; q.dxo0 = a.dxo_f[0]; q.dxo1 = a.dxo_f[1];
                 q.ods0 = a.ods_f[0]; q.ods1 = a.ods_f[1]; q.sa = a.sarea_f; q.pair = a.pair; q.ofoff = a.ofoff;
+                q.poff = a.pair >= 0 ? P.p_off[a.pair] : 0;
                 q.onv = a.onv; q.ogo = a.ogo;
                 psub[sd][k] = q;
             }
@@ -1944,7 +1946,7 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
     // reconstructed micro fluxes at the velocities of its grid that overlap i (the pairing run),
     // averaged onto i (a finer run) or copied (a coarser or equal one)
     auto paired_micro = [&](const PSub& q, int i, int dir) {
-        const int64_t po = P.p_off[q.pair] + i;
+        const int64_t po = q.poff + i;
         const int j0 = P.p_j0[po], jc = P.p_cnt[po];
         const int li = P.vlev[FC.goff + i];
         const float* of = fbase + q.ofoff;
