@@ -798,6 +798,7 @@ cudaError_t launch_flux_part(kg_handle* h, const Dev& P, int part, int sched, in
     return dispatch(h, [&](auto L) { return decltype(L)::flux_persistent(P, h->n_nonreg, F.max_nv, grid, h->d_counter, order, s); });
 }
 
+// the packed forms of a step chained by programmatic dependent launch (0: ordinary launches)
 #ifndef KG_PDL
 #define KG_PDL 1
 #endif
