@@ -234,6 +234,9 @@ def run_single(args, mode, scale, rank, world, dist, e2e=True, march="caidvm"):
             e2e_steps = max(1, args.steps)     # one request per timed step
             requests = [ins] * e2e_steps
             req_out = [outs[r % 2] for r in range(e2e_steps)]
+            # untimed warm-up requests: the handle's serving staging (three f blocks in FP64) and
+            # copy streams are made on first use
+            g.serve(requests[:2], dt, step, 1, outputs=req_out[:2])
             barrier()
             t0 = time.perf_counter()
             g.serve(requests, dt, step, 1, outputs=req_out)

@@ -2188,8 +2188,9 @@ __device__ __forceinline__ void flux_regular_packed(const Dev& P, const int fcx)
 //  * persistent: `gridDim.x` resident CTAs take cells from the work counter (in `order`,
 //    when given), so a batch of uneven problems keeps every SM busy to the end of the
 //    sub-step.  The counter must be zero at launch.
-template <int D, int NDF, typename T, bool FG, int NT, bool PPIB = false>
-__global__ void __launch_bounds__(NT, (sizeof(T) == 4 ? 4 : 2) * (BLOCK / NT)) flux_collide_kernel(Dev P, int* counter,
+// MB: resident 256-thread-CTA equivalents the registers allow (0: 4 in FP32, 2 in FP64)
+template <int D, int NDF, typename T, bool FG, int NT, bool PPIB = false, int MB = 0>
+__global__ void __launch_bounds__(NT, (MB ? MB : (sizeof(T) == 4 ? 4 : 2)) * (BLOCK / NT)) flux_collide_kernel(Dev P, int* counter,
                                                                                              const int32_t* order, int n) {
     __shared__ int item;
     int it = blockIdx.x;
@@ -3275,11 +3276,16 @@ struct Launch {
     }
     // the flux kernel of the layout's staging choice
     using FluxFn = void (*)(Dev, int*, const int32_t*, int);
-    static FluxFn flux_fn(const Dev& P) {
+    // (list: one CTA per cell, schedule 0; the 2D mixed form's variant then takes 80 registers
+    // and 6 resident 128-thread CTAs: beside the packed kernels on the other stream it shortened
+    // the cylinder's step 1.52 -> 1.47 ms, while the persistent schedule of a batch, whose
+    // autotuned grid counts on 8 resident CTAs, keeps 64; the same arithmetic either way)
+    static FluxFn flux_fn(const Dev& P, bool list = false) {
         // CIP marching on a layout with walls: the variant with positivity_preserving_ib!
         if (P.marching == KG_MARCH_CIP && P.n_walls > 0)
             return P.fst_global ? flux_collide_kernel<D, NDF, T, true, BLOCK, true> : flux_collide_kernel<D, NDF, T, false, BLOCK, true>;
         if (P.fst_global) return flux_collide_kernel<D, NDF, T, true, BLOCK>;
+        if (D == 2 && sizeof(T) == 4 && list && P.flux_nt == 128) return flux_collide_kernel<D, NDF, T, false, 128, false, 3>;
         return P.flux_nt == 128 ? flux_collide_kernel<D, NDF, T, false, 128> : flux_collide_kernel<D, NDF, T, false, BLOCK>;
     }
     static int flux_threads(const Dev& P) {
@@ -3290,7 +3296,7 @@ struct Launch {
         if (n <= 0) return cudaSuccess;
         using A = typename Arith<T>::type;
         size_t smem = flux_smem<D, NDF, A>(max_nv, P.max_axis, P.max_bcm, P.fst_global);
-        const FluxFn fn = flux_fn(P);
+        const FluxFn fn = flux_fn(P, true);
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         fn<<<n, flux_threads(P), smem, s>>>(P, nullptr, list, n);
